@@ -1,0 +1,283 @@
+/*
+ * seedgb.h -- C ABI of the GB300-native triplet seeding library.
+ *
+ * A drop-in for traccc's triplet seeding stage (spacepoint binning, doublet
+ * finding, triplet finding, seed filtering) and its track-parameter
+ * estimation, running on one GB300 (sm_103a).  Plain pointers and sizes only:
+ * every pointer marked "device" is a CUDA device address, streams are passed
+ * as void* holding a cudaStream_t.
+ *
+ * Reference interfaces replaced (paths in the traccc 1.6.0 tree):
+ *  - seedgb_seeding_*  <- traccc::cuda::triplet_seeding_algorithm
+ *      (device/cuda/include/traccc/cuda/seeding/triplet_seeding_algorithm.hpp:35-40,
+ *       operator() at device/common/include/traccc/seeding/device/
+ *       triplet_seeding_algorithm.hpp:68-69), with the results of
+ *      traccc::host::seeding_algorithm (core/include/traccc/seeding/
+ *       seeding_algorithm.hpp:40-52).
+ *  - seedgb_params_*   <- traccc::cuda::seed_parameter_estimation_algorithm
+ *      (device/cuda/include/traccc/cuda/seeding/
+ *       seed_parameter_estimation_algorithm.hpp:33-37, operator() at
+ *       device/common/include/traccc/seeding/device/
+ *       seed_parameter_estimation_algorithm.hpp:48-67) and
+ *      traccc::host::track_params_estimation (core/include/traccc/seeding/
+ *       track_params_estimation.hpp:31-67).
+ *
+ * Semantics: all work is enqueued on the caller's stream and the calls return
+ * before it finishes (as the reference's device algorithms do); no call of the
+ * run functions blocks on the device.  Errors are status codes, never
+ * exceptions.  A handle is not thread-safe: use one handle per host thread /
+ * stream, as the reference uses one algorithm object per thread.
+ */
+#ifndef SEEDGB_H
+#define SEEDGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SEEDGB_ABI_VERSION 1u
+#define SEEDGB_INVALID_MEASUREMENT_INDEX 0xFFFFFFFFu
+/* Largest number of seeds kept per middle spacepoint (maxSeedsPerSpM). */
+#define SEEDGB_MAX_SEEDS_PER_MIDDLE 8u
+
+typedef enum {
+    SEEDGB_OK = 0,
+    /* empty input: nothing was launched except writing size 0 (the reference
+     * returns an empty buffer, triplet_seeding_algorithm.cpp:75-77) */
+    SEEDGB_EMPTY = 1,
+    /* the configuration is rejected (the reference throws std::domain_error,
+     * spacepoint_binning_helper.hpp:33-38,77-81) */
+    SEEDGB_BAD_CONFIG = 2,
+    /* a CUDA runtime call failed (the reference throws std::runtime_error,
+     * device/cuda/src/utils/cuda_error_handling.hpp:14-21) */
+    SEEDGB_CUDA_ERROR = 3,
+    /* a device-side buffer was too small; the result is incomplete */
+    SEEDGB_CAPACITY_OVERFLOW = 4,
+    /* a bounded device-side wait ran out */
+    SEEDGB_TIMEOUT = 5,
+    SEEDGB_INVALID_ARGUMENT = 6,
+    SEEDGB_UNSUPPORTED = 7
+} seedgb_status;
+
+/* traccc::seedfinder_config (core/include/traccc/seeding/detail/
+ * seeding_config.hpp:17-139), same fields, same order, same units
+ * (mm, GeV, T = 0.000299792458 GeV/(e mm)). */
+typedef struct {
+    float zMin, zMax, rMax, rMin;
+    float collisionRegionMin, collisionRegionMax;
+    float phiMin, phiMax;
+    float minPt, cotThetaMax, deltaRMin, deltaRMax, deltaZMax;
+    float impactMax, sigmaScattering, maxPtScattering;
+    uint32_t maxSeedsPerSpM;
+    float bFieldInZ;
+    float beamPos[2];
+    float radLengthPerSeed, zAlign, rAlign, sigmaError;
+    float highland, maxScatteringAngle2, pTPerHelixRadius, minHelixDiameter2,
+        minHelixRadius, pT2perRadius;
+    int32_t phiBinDeflectionCoverage;
+    uint32_t neighbor_scope[2];
+} seedgb_seedfinder_config;
+
+/* traccc::spacepoint_grid_config (seeding_config.hpp:142-189). */
+typedef struct {
+    float bFieldInZ, minPt, rMax, zMax, zMin, deltaRMax, cotThetaMax, impactMax;
+    float phiMin, phiMax;
+    int32_t phiBinDeflectionCoverage;
+} seedgb_spacepoint_grid_config;
+
+/* traccc::seedfilter_config (seeding_config.hpp:191-219). */
+typedef struct {
+    float deltaInvHelixDiameter, impactWeightFactor, compatSeedWeight, deltaRMin;
+    uint64_t compatSeedLimit;
+    float good_spB_min_radius, good_spB_weight_increase;
+    float good_spT_max_radius, good_spT_weight_increase;
+    float good_spB_min_weight, seed_min_weight, spB_min_radius;
+} seedgb_seedfilter_config;
+
+/* traccc::track_params_estimation_config
+ * (core/include/traccc/seeding/detail/track_params_estimation_config.hpp:18-33) */
+typedef struct {
+    float initial_sigma[6];
+    float initial_sigma_qopt;
+    float initial_sigma_pt_rel;
+    float initial_inflation[6];
+} seedgb_track_params_estimation_config;
+
+/* The reference's config constructors: defaults + setup()
+ * (seeding_config.hpp:19,120-138,146-157,191-219). */
+void seedgb_seedfinder_config_default(seedgb_seedfinder_config* c);
+/* seedfinder_config::setup(): recompute the derived members after a change. */
+void seedgb_seedfinder_config_setup(seedgb_seedfinder_config* c);
+void seedgb_spacepoint_grid_config_from_finder(seedgb_spacepoint_grid_config* g,
+                                               const seedgb_seedfinder_config* f);
+void seedgb_seedfilter_config_default(seedgb_seedfilter_config* c);
+void seedgb_track_params_estimation_config_default(
+    seedgb_track_params_estimation_config* c);
+
+/* Grid axes from get_axes (core/include/traccc/seeding/
+ * spacepoint_binning_helper.hpp:22-110): circular phi axis, regular z axis. */
+typedef struct {
+    uint32_t phi_bins;
+    float phi_min, phi_max;
+    uint32_t z_bins;
+    float z_min, z_max;
+} seedgb_grid_axes;
+seedgb_status seedgb_get_axes(const seedgb_spacepoint_grid_config* g,
+                              seedgb_grid_axes* out);
+
+/* edm::spacepoint_collection view (core/include/traccc/edm/
+ * spacepoint_collection.hpp:222-234): five device columns; global holds x, y, z
+ * interleaved (std::array<float,3>, 12-byte stride). */
+typedef struct {
+    const uint32_t* measurement_index_1;
+    const uint32_t* measurement_index_2;
+    const float* global;
+    const float* z_variance;
+    const float* radius_variance;
+    uint32_t size;
+} seedgb_spacepoint_view;
+
+/* edm::seed_collection buffer (core/include/traccc/edm/seed_collection.hpp:
+ * 142-146): four device columns of `capacity` elements and a device-resident
+ * element count, like the reference's resizable buffer
+ * (triplet_seeding_algorithm.cpp:249-252).  Seed indices are spacepoint
+ * indices of the input view. */
+typedef struct {
+    uint32_t* bottom_index;
+    uint32_t* middle_index;
+    uint32_t* top_index;
+    float* quality;
+    uint32_t capacity;
+    uint32_t* size; /* device */
+} seedgb_seed_buffer;
+
+/* The measurement columns parameter estimation reads (edm::
+ * measurement_collection, core/include/traccc/edm/measurement_collection.hpp:
+ * 240-259): local_position (2 floats each) and surface_link (64-bit id). */
+typedef struct {
+    const float* local_position;
+    const uint64_t* surface_link;
+    uint32_t size;
+} seedgb_measurement_view;
+
+/* bound_track_parameters: surface link, {loc0, loc1, phi, theta, q/p, time},
+ * 6x6 covariance (row-major; the diagonal is set, the rest is zero). */
+typedef struct {
+    uint64_t surface_link;
+    float params[6];
+    float cov[36];
+} seedgb_bound_track_parameters;
+
+typedef struct {
+    seedgb_bound_track_parameters* data; /* device */
+    uint32_t capacity;
+    uint32_t* size; /* device */
+} seedgb_params_buffer;
+
+/* ------------------------------------------------------------------------ */
+/* Seeding                                                                   */
+/* ------------------------------------------------------------------------ */
+
+typedef struct seedgb_seeding seedgb_seeding;
+
+/* Replaces triplet_seeding_algorithm(finder, grid, filter, mr, copy, stream)
+ * (triplet_seeding_algorithm.hpp:35-40).  Validates the grid (get_axes) and
+ * returns SEEDGB_BAD_CONFIG where the reference throws.  Allocates nothing on
+ * the device until the first run or seedgb_seeding_reserve. */
+seedgb_status seedgb_seeding_create(const seedgb_seedfinder_config* finder,
+                                    const seedgb_spacepoint_grid_config* grid,
+                                    const seedgb_seedfilter_config* filter,
+                                    seedgb_seeding** out);
+seedgb_status seedgb_seeding_destroy(seedgb_seeding* h);
+
+/* Size the device work space for batches of up to max_events events holding up
+ * to max_total_spacepoints spacepoints together.  Runs that fit need no
+ * further allocation (which is what makes them capturable in a CUDA graph). */
+seedgb_status seedgb_seeding_reserve(seedgb_seeding* h, uint32_t max_events,
+                                     uint64_t max_total_spacepoints);
+
+/* Replaces edm::seed_collection::buffer operator()(spacepoint view)
+ * (device/common/include/traccc/seeding/device/triplet_seeding_algorithm.hpp:
+ * 68-69).  Seeds are written in the host seeding order (grid bin, then middle
+ * spacepoint index, then seed rank), identical to traccc::host::
+ * seeding_algorithm.  out->capacity must be >= maxSeedsPerSpM * sps->size to
+ * be safe; a smaller buffer is filled up to capacity and the status word
+ * reports SEEDGB_CAPACITY_OVERFLOW.  Asynchronous on `stream`. */
+seedgb_status seedgb_seeding_run(seedgb_seeding* h,
+                                 const seedgb_spacepoint_view* sps,
+                                 seedgb_seed_buffer* out, void* stream);
+
+/* Many events with uneven sizes in one launch sequence (the GB300 form of the
+ * reference's one-stream-per-thread event concurrency, examples/run/common/
+ * include/traccc/examples/impl/throughput_mt.ipp:171-179). */
+seedgb_status seedgb_seeding_run_batch(seedgb_seeding* h,
+                                       const seedgb_spacepoint_view* events,
+                                       uint32_t n_events,
+                                       seedgb_seed_buffer* outs, void* stream);
+
+/* Synchronise `stream` and return the device status of the last run
+ * (SEEDGB_OK, SEEDGB_CAPACITY_OVERFLOW, SEEDGB_TIMEOUT). */
+seedgb_status seedgb_seeding_last_status(seedgb_seeding* h, void* stream);
+
+/* Work counters of the last run (after seedgb_seeding_last_status):
+ * out[0] valid spacepoints, out[1] middles sent to the large-capacity path,
+ * out[2] middle-bottom doublets, out[3] middle-top doublets,
+ * out[4] triplets, out[5] seeds. */
+seedgb_status seedgb_seeding_counters(seedgb_seeding* h, uint64_t out[8]);
+
+/* Copy the phi-z grid of event `event` of the last run to host memory
+ * (synchronises `stream`): bin_offsets[nbins+1] (CSR) and bin_sps[n_valid] =
+ * spacepoint indices in grid order.  The same grid as
+ * traccc::host::details::spacepoint_binning::operator()
+ * (core/src/seeding/spacepoint_binning.cpp:27-53): bins in serial order
+ * phi + nphi * z, spacepoints of a bin in ascending index order.
+ * bin_sps_capacity must be >= the event's spacepoint count. */
+seedgb_status seedgb_seeding_copy_grid(seedgb_seeding* h, uint32_t event,
+                                       uint32_t* bin_offsets, uint32_t* bin_sps,
+                                       uint32_t bin_sps_capacity,
+                                       uint32_t* n_valid, void* stream);
+
+/* Behaviour options (not part of the reference interface). */
+typedef enum {
+    /* 1: test every middle-bottom x middle-top doublet pair for triplets
+     * instead of the cot(theta) window (verification of the window; the
+     * results are identical, only slower). */
+    SEEDGB_OPTION_EXHAUSTIVE_TRIPLETS = 1
+} seedgb_option;
+seedgb_status seedgb_seeding_set_option(seedgb_seeding* h, seedgb_option opt,
+                                        int64_t value);
+
+/* ------------------------------------------------------------------------ */
+/* Track parameter estimation                                                */
+/* ------------------------------------------------------------------------ */
+
+typedef struct seedgb_params seedgb_params;
+
+/* Replaces seed_parameter_estimation_algorithm(config, mr, copy, stream)
+ * (seed_parameter_estimation_algorithm.hpp:33-37). */
+seedgb_status seedgb_params_create(
+    const seedgb_track_params_estimation_config* cfg, seedgb_params** out);
+seedgb_status seedgb_params_destroy(seedgb_params* h);
+
+/* Replaces operator()(magnetic_field, measurements, spacepoints, seeds)
+ * (seed_parameter_estimation_algorithm.hpp:48-67) for a constant field
+ * bfield = {Bx, By, Bz} in GeV/(e mm).  One parameter set per seed, in seed
+ * order; reads the seed count from seeds->size on the device. */
+seedgb_status seedgb_params_run(seedgb_params* h, const float bfield[3],
+                                const seedgb_measurement_view* meas,
+                                const seedgb_spacepoint_view* sps,
+                                const seedgb_seed_buffer* seeds,
+                                seedgb_params_buffer* out, void* stream);
+
+/* ------------------------------------------------------------------------ */
+
+const char* seedgb_status_string(seedgb_status s);
+uint32_t seedgb_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

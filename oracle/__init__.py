@@ -1,0 +1,281 @@
+"""ctypes front-end of the CPU seeding oracle.
+
+TEST INFRASTRUCTURE ONLY.  The oracle is a plain-C restatement of traccc's
+host seeding (``core/src/seeding/*``) and host track-parameter estimation
+(``core/src/seeding/track_params_estimation.cpp``).  Only the tests, the smoke
+check and bench.py's CPU-baseline leg import this module; the product package
+``traccc_gb300`` never does.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_lib", "libseedoracle.so")
+
+PHI_LIBM = 0
+PHI_CR = 1
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle with gcc (-O2 -ffp-contract=off) into oracle/_lib."""
+    src = os.path.join(_HERE, "seeding_oracle.c")
+    if (not force and os.path.exists(_LIB_PATH)
+            and os.path.getmtime(_LIB_PATH) >= os.path.getmtime(src)):
+        return _LIB_PATH
+    os.makedirs(os.path.dirname(_LIB_PATH), exist_ok=True)
+    cmd = ["gcc", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fPIC",
+           "-std=c11", "-D_GNU_SOURCE", "-shared", "-o", _LIB_PATH, src, "-lm"]
+    subprocess.run(cmd, check=True)
+    return _LIB_PATH
+
+
+class FinderConfig(C.Structure):
+    _fields_ = [(n, C.c_float) for n in (
+        "zMin", "zMax", "rMax", "rMin", "collisionRegionMin",
+        "collisionRegionMax", "phiMin", "phiMax", "minPt", "cotThetaMax",
+        "deltaRMin", "deltaRMax", "deltaZMax", "impactMax", "sigmaScattering",
+        "maxPtScattering")] + [
+        ("maxSeedsPerSpM", C.c_uint32), ("bFieldInZ", C.c_float),
+        ("beamPos", C.c_float * 2)] + [(n, C.c_float) for n in (
+            "radLengthPerSeed", "zAlign", "rAlign", "sigmaError", "highland",
+            "maxScatteringAngle2", "pTPerHelixRadius", "minHelixDiameter2",
+            "minHelixRadius", "pT2perRadius")] + [
+        ("phiBinDeflectionCoverage", C.c_int32),
+        ("neighbor_scope", C.c_uint32 * 2)]
+
+
+class GridConfig(C.Structure):
+    _fields_ = [(n, C.c_float) for n in (
+        "bFieldInZ", "minPt", "rMax", "zMax", "zMin", "deltaRMax",
+        "cotThetaMax", "impactMax", "phiMin", "phiMax")] + [
+        ("phiBinDeflectionCoverage", C.c_int32)]
+
+
+class FilterConfig(C.Structure):
+    _fields_ = [(n, C.c_float) for n in (
+        "deltaInvHelixDiameter", "impactWeightFactor", "compatSeedWeight",
+        "deltaRMin")] + [("compatSeedLimit", C.c_uint64)] + [
+        (n, C.c_float) for n in (
+            "good_spB_min_radius", "good_spB_weight_increase",
+            "good_spT_max_radius", "good_spT_weight_increase",
+            "good_spB_min_weight", "seed_min_weight", "spB_min_radius")]
+
+
+class TPConfig(C.Structure):
+    _fields_ = [("initial_sigma", C.c_float * 6),
+                ("initial_sigma_qopt", C.c_float),
+                ("initial_sigma_pt_rel", C.c_float),
+                ("initial_inflation", C.c_float * 6)]
+
+
+class Axes(C.Structure):
+    _fields_ = [("phi_bins", C.c_uint32), ("phi_min", C.c_float),
+                ("phi_max", C.c_float), ("z_bins", C.c_uint32),
+                ("z_min", C.c_float), ("z_max", C.c_float)]
+
+
+class Spacepoints(C.Structure):
+    _fields_ = [("measurement_index_1", C.POINTER(C.c_uint32)),
+                ("measurement_index_2", C.POINTER(C.c_uint32)),
+                ("glob", C.POINTER(C.c_float)),
+                ("z_variance", C.POINTER(C.c_float)),
+                ("radius_variance", C.POINTER(C.c_float)),
+                ("size", C.c_uint32)]
+
+
+class Measurements(C.Structure):
+    _fields_ = [("local_position", C.POINTER(C.c_float)),
+                ("surface_link", C.POINTER(C.c_uint64)),
+                ("size", C.c_uint32)]
+
+
+SEED_DTYPE = np.dtype([("bottom", "<u4"), ("middle", "<u4"), ("top", "<u4"),
+                       ("quality", "<f4")])
+PARAMS_DTYPE = np.dtype([("surface_link", "<u8"), ("params", "<f4", (6,)),
+                         ("cov", "<f4", (36,))])
+
+_STATS_FIELDS = (
+    "n_sp", "n_valid", "n_pair_tests", "n_mb", "n_mt", "n_middles_with_mb",
+    "n_middles_both", "n_triplet_tests", "n_triplets", "n_triplets_after_cut",
+    "n_seeds", "max_mb_per_middle", "max_mt_per_middle",
+    "max_triplets_per_mb", "max_triplets_per_middle", "max_bin_size",
+    "max_neighbourhood", "near_doublet_cuts", "near_triplet_cuts",
+    "near_bin_edges", "phi_cr_undecided")
+
+
+class Stats(C.Structure):
+    _fields_ = [(n, C.c_uint64) for n in _STATS_FIELDS]
+
+    def as_dict(self):
+        return {n: int(getattr(self, n)) for n in _STATS_FIELDS}
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_LIB_PATH):
+            build()
+        L = C.CDLL(_LIB_PATH)
+        P = C.POINTER
+        L.or_finder_config_default.argtypes = [P(FinderConfig)]
+        L.or_finder_config_setup.argtypes = [P(FinderConfig)]
+        L.or_grid_config_from_finder.argtypes = [P(GridConfig), P(FinderConfig)]
+        L.or_filter_config_default.argtypes = [P(FilterConfig)]
+        L.or_tp_config_default.argtypes = [P(TPConfig)]
+        L.or_get_axes.argtypes = [P(GridConfig), P(Axes)]
+        L.or_get_axes.restype = C.c_int
+        for f in ("or_regular_bin", "or_circular_bin"):
+            getattr(L, f).argtypes = [C.c_uint32, C.c_float, C.c_float, C.c_float]
+            getattr(L, f).restype = C.c_uint32
+        for f in ("or_regular_range", "or_circular_range"):
+            getattr(L, f).argtypes = [C.c_uint32, C.c_float, C.c_float, C.c_float,
+                                      P(C.c_uint32), P(C.c_uint32)]
+        for f in ("or_regular_zone", "or_circular_zone"):
+            getattr(L, f).argtypes = [C.c_uint32, C.c_float, C.c_float, C.c_float,
+                                      P(C.c_uint32), P(C.c_uint32), C.c_uint32]
+            getattr(L, f).restype = C.c_uint32
+        L.or_circular_remap.argtypes = [C.c_uint32, C.c_uint32, C.c_int32]
+        L.or_circular_remap.restype = C.c_uint32
+        L.or_sp_phi.argtypes = [C.c_float, C.c_float, C.c_int, P(C.c_int)]
+        L.or_sp_phi.restype = C.c_float
+        L.or_is_valid_sp.argtypes = [P(FinderConfig), C.c_float, C.c_float,
+                                     C.c_float, C.c_int]
+        L.or_is_valid_sp.restype = C.c_int
+        L.or_binning.argtypes = [P(FinderConfig), P(Axes), P(Spacepoints), C.c_int,
+                                 P(C.c_uint32), P(C.c_uint32), P(C.c_uint32),
+                                 P(Stats)]
+        L.or_binning.restype = C.c_int
+        L.or_seeding.argtypes = [P(FinderConfig), P(GridConfig), P(FilterConfig),
+                                 P(Spacepoints), C.c_int, C.c_void_p, C.c_uint32,
+                                 P(C.c_uint32), P(Stats)]
+        L.or_seeding.restype = C.c_int
+        L.or_track_params.argtypes = [P(TPConfig), P(Measurements), P(Spacepoints),
+                                      C.c_void_p, C.c_uint32, P(C.c_float),
+                                      C.c_void_p]
+        L.or_track_params.restype = C.c_int
+        fa = P(C.c_float)
+        L.or_doublet_compatible.argtypes = [C.c_int, fa, fa, P(FinderConfig)]
+        L.or_doublet_compatible.restype = C.c_int
+        L.or_transform_coordinates.argtypes = [C.c_int, fa, fa, fa]
+        L.or_triplet_compatible.argtypes = [fa, fa, fa, P(FinderConfig), C.c_float,
+                                            C.c_float, fa, fa]
+        L.or_triplet_compatible.restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def default_configs():
+    """Reference default finder/grid/filter/params configs."""
+    L = lib()
+    f, g, fl, tp = FinderConfig(), GridConfig(), FilterConfig(), TPConfig()
+    L.or_finder_config_default(C.byref(f))
+    L.or_grid_config_from_finder(C.byref(g), C.byref(f))
+    L.or_filter_config_default(C.byref(fl))
+    L.or_tp_config_default(C.byref(tp))
+    return f, g, fl, tp
+
+
+def grid_from_finder(f):
+    g = GridConfig()
+    lib().or_grid_config_from_finder(C.byref(g), C.byref(f))
+    return g
+
+
+def get_axes(g):
+    a = Axes()
+    rc = lib().or_get_axes(C.byref(g), C.byref(a))
+    if rc:
+        raise ValueError(f"get_axes domain error {rc}")
+    return a
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _u32(a):
+    return np.ascontiguousarray(a, dtype=np.uint32)
+
+
+def sp_struct(ev):
+    """Build an oracle spacepoint view over a dict of numpy columns.
+    Keeps references alive on the returned tuple."""
+    keep = (_u32(ev["measurement_index_1"]), _u32(ev["measurement_index_2"]),
+            _f32(ev["global"]).reshape(-1), _f32(ev["z_variance"]),
+            _f32(ev["radius_variance"]))
+    s = Spacepoints(keep[0].ctypes.data_as(C.POINTER(C.c_uint32)),
+                    keep[1].ctypes.data_as(C.POINTER(C.c_uint32)),
+                    keep[2].ctypes.data_as(C.POINTER(C.c_float)),
+                    keep[3].ctypes.data_as(C.POINTER(C.c_float)),
+                    keep[4].ctypes.data_as(C.POINTER(C.c_float)),
+                    len(keep[0]))
+    return s, keep
+
+
+def binning(ev, f=None, g=None, phi_mode=PHI_CR):
+    """Returns (bin_offsets[nbins+1], bin_sps[n_valid], axes, stats)."""
+    if f is None:
+        f, g, _, _ = default_configs()
+    a = get_axes(g)
+    s, keep = sp_struct(ev)
+    nb = a.phi_bins * a.z_bins
+    off = np.zeros(nb + 1, np.uint32)
+    sps = np.zeros(max(1, s.size), np.uint32)
+    nv = C.c_uint32(0)
+    st = Stats()
+    rc = lib().or_binning(C.byref(f), C.byref(a), C.byref(s), phi_mode,
+                          off.ctypes.data_as(C.POINTER(C.c_uint32)),
+                          sps.ctypes.data_as(C.POINTER(C.c_uint32)),
+                          C.byref(nv), C.byref(st))
+    if rc:
+        raise RuntimeError(f"or_binning failed {rc}")
+    return off, sps[: nv.value].copy(), a, st.as_dict()
+
+
+def seeding(ev, f=None, g=None, fl=None, phi_mode=PHI_CR):
+    """Host seeding.  Returns (seeds structured array, stats dict)."""
+    if f is None:
+        f, g, fl, _ = default_configs()
+    s, keep = sp_struct(ev)
+    cap = max(16, 5 * s.size)
+    out = np.zeros(cap, SEED_DTYPE)
+    n = C.c_uint32(0)
+    st = Stats()
+    rc = lib().or_seeding(C.byref(f), C.byref(g), C.byref(fl), C.byref(s),
+                          phi_mode, out.ctypes.data, cap, C.byref(n), C.byref(st))
+    if rc == -1:
+        cap = n.value
+        out = np.zeros(cap, SEED_DTYPE)
+        st = Stats()
+        rc = lib().or_seeding(C.byref(f), C.byref(g), C.byref(fl), C.byref(s),
+                              phi_mode, out.ctypes.data, cap, C.byref(n),
+                              C.byref(st))
+    if rc:
+        raise RuntimeError(f"or_seeding failed {rc}")
+    return out[: n.value].copy(), st.as_dict()
+
+
+def track_params(ev, seeds, bfield, tp=None):
+    if tp is None:
+        _, _, _, tp = default_configs()
+    s, keep = sp_struct(ev)
+    lp = _f32(ev["local_position"]).reshape(-1)
+    sl = np.ascontiguousarray(ev["surface_link"], dtype=np.uint64)
+    m = Measurements(lp.ctypes.data_as(C.POINTER(C.c_float)),
+                     sl.ctypes.data_as(C.POINTER(C.c_uint64)), len(sl))
+    seeds = np.ascontiguousarray(seeds, dtype=SEED_DTYPE)
+    out = np.zeros(max(1, len(seeds)), PARAMS_DTYPE)
+    b = (C.c_float * 3)(*[float(v) for v in bfield])
+    rc = lib().or_track_params(C.byref(tp), C.byref(m), C.byref(s),
+                               seeds.ctypes.data, len(seeds), b, out.ctypes.data)
+    if rc:
+        raise RuntimeError(f"or_track_params failed {rc}")
+    return out[: len(seeds)].copy()

@@ -1,0 +1,208 @@
+/*
+ * seeding_oracle.h -- CPU restatement of traccc's host triplet seeding and
+ * track-parameter estimation.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the correctness checker for the
+ * GB300 seeding path.  Only the test-suite, the smoke check and the timed CPU
+ * baseline of bench.py may load it; the product library never links or calls
+ * it, and nothing in the product falls back to it.
+ *
+ * Every routine restates the reference algorithm in plain C, in the same
+ * floating-point operation order as the reference (float arithmetic, no FMA
+ * contraction: build with -O2 -ffp-contract=off).  Each function names the
+ * reference file:line it follows.  Paths are relative to the traccc source
+ * tree (traccc 1.6.0).
+ *
+ * Parity pins (tests/test_oracle_kat.py):
+ *   - tests/cpu/test_seeding.cpp:35-181 (two 5-spacepoint muon events, exactly
+ *     one seed each, with the same config tweaks);
+ *   - tests/cpu/test_track_params_estimation.cpp:34-144 (helix spacepoints,
+ *     |p - sqrt(2) GeV| < 2e-4 and the q/p sign);
+ *   - tests/cpu/test_axis.cpp:26-87 and the circular-axis cases that follow
+ *     (bin, range, zone and remap known answers).
+ */
+#ifndef SEEDING_ORACLE_H
+#define SEEDING_ORACLE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* traccc::seedfinder_config (core/include/traccc/seeding/detail/
+ * seeding_config.hpp:17-139), field for field. */
+typedef struct {
+    float zMin, zMax, rMax, rMin;
+    float collisionRegionMin, collisionRegionMax;
+    float phiMin, phiMax;
+    float minPt, cotThetaMax, deltaRMin, deltaRMax, deltaZMax;
+    float impactMax, sigmaScattering, maxPtScattering;
+    uint32_t maxSeedsPerSpM;
+    float bFieldInZ;
+    float beamPos[2];
+    float radLengthPerSeed, zAlign, rAlign, sigmaError;
+    /* derived by or_finder_config_setup() */
+    float highland, maxScatteringAngle2, pTPerHelixRadius, minHelixDiameter2,
+        minHelixRadius, pT2perRadius;
+    int32_t phiBinDeflectionCoverage;
+    uint32_t neighbor_scope[2];
+} or_finder_config;
+
+/* traccc::spacepoint_grid_config (seeding_config.hpp:142-189). */
+typedef struct {
+    float bFieldInZ, minPt, rMax, zMax, zMin, deltaRMax, cotThetaMax, impactMax;
+    float phiMin, phiMax;
+    int32_t phiBinDeflectionCoverage;
+} or_grid_config;
+
+/* traccc::seedfilter_config (seeding_config.hpp:191-219). */
+typedef struct {
+    float deltaInvHelixDiameter, impactWeightFactor, compatSeedWeight, deltaRMin;
+    uint64_t compatSeedLimit;
+    float good_spB_min_radius, good_spB_weight_increase;
+    float good_spT_max_radius, good_spT_weight_increase;
+    float good_spB_min_weight, seed_min_weight, spB_min_radius;
+} or_filter_config;
+
+/* traccc::track_params_estimation_config
+ * (core/include/traccc/seeding/detail/track_params_estimation_config.hpp:18-33) */
+typedef struct {
+    float initial_sigma[6];
+    float initial_sigma_qopt;
+    float initial_sigma_pt_rel;
+    float initial_inflation[6];
+} or_tp_config;
+
+/* The two axes of the phi-z grid (axis2::circular / axis2::regular). */
+typedef struct {
+    uint32_t phi_bins;
+    float phi_min, phi_max;
+    uint32_t z_bins;
+    float z_min, z_max;
+} or_axes;
+
+/* spacepoint_collection SoA (core/include/traccc/edm/spacepoint_collection.hpp:
+ * 222-234): global is xyz interleaved (std::array<float,3>). */
+typedef struct {
+    const uint32_t* measurement_index_1;
+    const uint32_t* measurement_index_2;
+    const float* global;
+    const float* z_variance;
+    const float* radius_variance;
+    uint32_t size;
+} or_spacepoints;
+
+/* The measurement columns that parameter estimation reads. */
+typedef struct {
+    const float* local_position; /* 2 floats per measurement */
+    const uint64_t* surface_link;
+    uint32_t size;
+} or_measurements;
+
+/* edm::seed (core/include/traccc/edm/seed_collection.hpp:28-146). */
+typedef struct {
+    uint32_t bottom, middle, top;
+    float quality;
+} or_seed;
+
+/* bound_track_parameters: vector {loc0, loc1, phi, theta, qop, time},
+ * diagonal-filled 6x6 covariance (row-major), surface link. */
+typedef struct {
+    uint64_t surface_link;
+    float params[6];
+    float cov[36];
+} or_bound_params;
+
+/* How the azimuth of a spacepoint is evaluated.
+ *  OR_PHI_LIBM: atan2f of the C library, as the reference host code does.
+ *  OR_PHI_CR  : the correctly rounded float atan2, i.e. the reference host code
+ *               on a C library whose atan2f is correctly rounded. */
+enum { OR_PHI_LIBM = 0, OR_PHI_CR = 1 };
+
+/* Work counters and near-threshold counts of one seeding call. */
+typedef struct {
+    uint64_t n_sp, n_valid;
+    uint64_t n_pair_tests;            /* (middle, neighbour) visits         */
+    uint64_t n_mb, n_mt;              /* doublets                            */
+    uint64_t n_middles_with_mb;       /* middles whose MT search ran         */
+    uint64_t n_middles_both;          /* middles with MB and MT doublets     */
+    uint64_t n_triplet_tests;         /* sum n_mb * n_mt                     */
+    uint64_t n_triplets;              /* compatible triplets                 */
+    uint64_t n_triplets_after_cut;    /* after the single-seed cut           */
+    uint64_t n_seeds;
+    uint64_t max_mb_per_middle, max_mt_per_middle, max_triplets_per_mb;
+    uint64_t max_triplets_per_middle;
+    uint64_t max_bin_size, max_neighbourhood;
+    /* decisions whose deciding quantity lies within 1e-6 relative of its cut */
+    uint64_t near_doublet_cuts, near_triplet_cuts, near_bin_edges;
+    uint64_t phi_cr_undecided;        /* CR atan2 too close to a float midpoint */
+} or_stats;
+
+/* Config construction: defaults and setup() (seeding_config.hpp:19,120-138). */
+void or_finder_config_default(or_finder_config* c);
+void or_finder_config_setup(or_finder_config* c);
+void or_grid_config_from_finder(or_grid_config* g, const or_finder_config* f);
+void or_filter_config_default(or_filter_config* c);
+void or_tp_config_default(or_tp_config* c);
+
+/* get_axes (core/include/traccc/seeding/spacepoint_binning_helper.hpp:22-110).
+ * Returns 0, or 1/2 for the two std::domain_error conditions. */
+int or_get_axes(const or_grid_config* g, or_axes* out);
+
+/* Axis primitives (core/include/traccc/seeding/grids/axis.hpp). */
+uint32_t or_regular_bin(uint32_t n, float mn, float mx, float v);
+void or_regular_range(uint32_t n, float mn, float mx, float v,
+                      const uint32_t nh[2], uint32_t out[2]);
+uint32_t or_regular_zone(uint32_t n, float mn, float mx, float v,
+                         const uint32_t nh[2], uint32_t* out, uint32_t cap);
+uint32_t or_circular_bin(uint32_t n, float mn, float mx, float v);
+uint32_t or_circular_remap(uint32_t n, uint32_t ibin, int32_t shood);
+void or_circular_range(uint32_t n, float mn, float mx, float v,
+                       const uint32_t nh[2], uint32_t out[2]);
+uint32_t or_circular_zone(uint32_t n, float mn, float mx, float v,
+                          const uint32_t nh[2], uint32_t* out, uint32_t cap);
+
+/* Spacepoint azimuth and validity (spacepoint_collection.ipp:52-63,
+ * spacepoint_binning_helper.hpp:112-127). */
+float or_sp_phi(float x, float y, int phi_mode, int* undecided);
+int or_is_valid_sp(const or_finder_config* c, float x, float y, float z,
+                   int phi_mode);
+
+/* Binning (core/src/seeding/spacepoint_binning.cpp:27-53).
+ * bin_offsets[nbins+1] (CSR), bin_sps[n_valid] = spacepoint indices. */
+int or_binning(const or_finder_config* c, const or_axes* axes,
+               const or_spacepoints* sps, int phi_mode, uint32_t* bin_offsets,
+               uint32_t* bin_sps, uint32_t* n_valid, or_stats* stats);
+
+/* Full host seeding (core/src/seeding/seeding_algorithm.cpp:24-28 ->
+ * seed_finding.cpp:58-121).  Returns 0 on success, -1 if cap is too small
+ * (n_out then holds the required size), >0 for config errors. */
+int or_seeding(const or_finder_config* fc, const or_grid_config* gc,
+               const or_filter_config* flt, const or_spacepoints* sps,
+               int phi_mode, or_seed* out, uint32_t cap, uint32_t* n_out,
+               or_stats* stats);
+
+/* Host track-parameter estimation (core/src/seeding/
+ * track_params_estimation.cpp:23-91). */
+int or_track_params(const or_tp_config* c, const or_measurements* meas,
+                    const or_spacepoints* sps, const or_seed* seeds,
+                    uint32_t n_seeds, const float bfield[3],
+                    or_bound_params* out);
+
+/* Doublet/triplet helpers, exposed for unit tests.
+ * m/o = {x, y, z, r, var_z, var_r}. */
+int or_doublet_compatible(int top, const float m[6], const float o[6],
+                          const or_finder_config* c);
+void or_transform_coordinates(int top, const float m[6], const float o[6],
+                              float lc[6] /* Zo,cot,iDR,Er,U,V */);
+int or_triplet_compatible(const float m[6], const float lb[6],
+                          const float lt[6], const or_finder_config* c,
+                          float iSinTheta2, float scatteringInRegion2,
+                          float* curvature, float* impact);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,442 @@
+// C-ABI layer of the seeding library: handles, the device work arena and the
+// launch sequence.  No call here blocks on the device except the explicit
+// status query and arena (re)allocation, which happens only when a batch is
+// larger than anything reserved before.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "seedgb.h"
+#include "seedgb_internal.h"
+
+using namespace seedgb;
+
+struct seedgb_seeding {
+    seedgb_seedfinder_config finder;
+    seedgb_spacepoint_grid_config grid;
+    seedgb_seedfilter_config filter;
+    seedgb_grid_axes axes;
+    DevConfig dc;
+    TuneParams tune;
+    int device = 0;
+    int num_sms = 0;
+    // arena
+    void* arena = nullptr;
+    size_t arena_bytes = 0;
+    uint32_t cap_events = 0;
+    uint64_t cap_sp = 0;
+    Arena a{};
+    // pinned staging of the event descriptors
+    EventDesc* h_desc = nullptr;
+    uint32_t h_desc_cap = 0;
+    cudaEvent_t staged = nullptr;
+    unsigned long long h_counters[kNumCounters] = {};
+};
+
+struct seedgb_params {
+    ParamsConfig pc;
+    int num_sms = 0;
+};
+
+namespace {
+
+seedgb_status cuda_status(cudaError_t e) {
+    return e == cudaSuccess ? SEEDGB_OK : SEEDGB_CUDA_ERROR;
+}
+
+size_t align_up(size_t v, size_t a = 256) { return (v + a - 1) / a * a; }
+
+DevConfig make_dev_config(const seedgb_seedfinder_config& f,
+                          const seedgb_seedfilter_config& fl,
+                          const seedgb_grid_axes& ax) {
+    DevConfig d{};
+    d.zMin = f.zMin;
+    d.zMax = f.zMax;
+    d.phiMin = f.phiMin;
+    d.phiMax = f.phiMax;
+    d.beam0 = f.beamPos[0];
+    d.beam1 = f.beamPos[1];
+    // seedfinder_config::get_num_rbins(), seeding_config.hpp:111-113
+    const float nr = f.rMax + std::sqrt(f.beamPos[0] * f.beamPos[0] +
+                                        f.beamPos[1] * f.beamPos[1]);
+    d.nrbins = (nr >= 0.f && nr < 1.8e19f) ? static_cast<unsigned long long>(nr) : 0ull;
+    d.deltaRMin = f.deltaRMin;
+    d.deltaRMax = f.deltaRMax;
+    d.cotThetaMax = f.cotThetaMax;
+    d.collisionRegionMin = f.collisionRegionMin;
+    d.collisionRegionMax = f.collisionRegionMax;
+    d.deltaZMax = f.deltaZMax;
+    d.impactMax = f.impactMax;
+    d.minHelixRadius = f.minHelixRadius;
+    d.maxScatteringAngle2 = f.maxScatteringAngle2;
+    d.sigmaScattering = f.sigmaScattering;
+    d.minHelixDiameter2 = f.minHelixDiameter2;
+    d.pT2perRadius = f.pT2perRadius;
+    d.pTPerHelixRadius = f.pTPerHelixRadius;
+    d.maxPtScattering = f.maxPtScattering;
+    d.highland = f.highland;
+    d.maxSeedsPerSpM = f.maxSeedsPerSpM;
+    d.scope0 = f.neighbor_scope[0];
+    d.scope1 = f.neighbor_scope[1];
+    d.deltaInvHelixDiameter = fl.deltaInvHelixDiameter;
+    d.impactWeightFactor = fl.impactWeightFactor;
+    d.compatSeedWeight = fl.compatSeedWeight;
+    d.filterDeltaRMin = fl.deltaRMin;
+    d.compatSeedLimit = static_cast<uint32_t>(fl.compatSeedLimit);
+    d.good_spB_min_radius = fl.good_spB_min_radius;
+    d.good_spB_weight_increase = fl.good_spB_weight_increase;
+    d.good_spT_max_radius = fl.good_spT_max_radius;
+    d.good_spT_weight_increase = fl.good_spT_weight_increase;
+    d.good_spB_min_weight = fl.good_spB_min_weight;
+    d.seed_min_weight = fl.seed_min_weight;
+    d.spB_min_radius = fl.spB_min_radius;
+    d.phi_bins = ax.phi_bins;
+    d.z_bins = ax.z_bins;
+    d.nbins = ax.phi_bins * ax.z_bins;
+    d.phi_min = ax.phi_min;
+    d.phi_max = ax.phi_max;
+    d.z_min = ax.z_min;
+    d.z_max = ax.z_max;
+    d.brute_force_triplets = 0;
+    return d;
+}
+
+// Longest phi zone over all phi bins (circular::zone_t semantics).
+uint32_t max_phi_zone(uint32_t n, uint32_t s0, uint32_t s1) {
+    auto remap = [n](uint32_t ibin, int sh) -> uint32_t {
+        const int opt = static_cast<int>(ibin) + sh;
+        if (opt >= 0 && opt < static_cast<int>(n)) return static_cast<uint32_t>(opt);
+        if (opt < 0) return static_cast<uint32_t>(static_cast<int>(n) + opt);
+        return static_cast<uint32_t>(opt) - n;
+    };
+    uint32_t mx = 0;
+    for (uint32_t b = 0; b < n; ++b) {
+        const uint32_t lo = remap(b, -static_cast<int>(s0)), hi = remap(b, static_cast<int>(s1));
+        const uint32_t len = lo < hi ? hi - lo + 1u : n - lo + hi + 1u;
+        mx = std::max(mx, len);
+    }
+    return mx;
+}
+
+uint32_t chunks_of(uint32_t n_sp) { return (n_sp + kBinChunk - 1) / kBinChunk; }
+
+seedgb_status ensure_arena(seedgb_seeding* h, uint32_t n_events, uint64_t total_sp,
+                           uint32_t total_chunks) {
+    const uint32_t nb = h->dc.nbins;
+    const uint32_t mpi = static_cast<uint32_t>(h->tune.middles_per_item);
+    if (h->arena && n_events <= h->cap_events && total_sp <= h->cap_sp) {
+        const uint32_t cap_chunks =
+            static_cast<uint32_t>(h->cap_sp / kBinChunk) + h->cap_events;
+        if (total_chunks <= cap_chunks) return SEEDGB_OK;
+    }
+    const uint32_t ce = std::max(n_events, h->cap_events);
+    const uint64_t cs = std::max<uint64_t>(std::max<uint64_t>(total_sp, h->cap_sp), 1);
+    if (cs > 0xF0000000ull) return SEEDGB_UNSUPPORTED;
+    const uint32_t cc = static_cast<uint32_t>(cs / kBinChunk) + ce;
+    const uint32_t ci = static_cast<uint32_t>(cs / mpi) + ce * nb + 1;
+    size_t off = 0;
+    auto take = [&off](size_t bytes) { const size_t o = off; off = align_up(off + bytes); return o; };
+    const size_t o_events = take(sizeof(EventDesc) * ce);
+    const size_t o_spbin = take(sizeof(int32_t) * cs);
+    const size_t o_whist = take(sizeof(uint32_t) * static_cast<size_t>(cc) * kBinWarps * nb);
+    const size_t o_bs = take(sizeof(uint32_t) * static_cast<size_t>(ce) * (nb + 1));
+    const size_t o_nv = take(sizeof(uint32_t) * ce);
+    const size_t o_xyzr = take(sizeof(float4) * cs);
+    const size_t o_var = take(sizeof(float2) * cs);
+    const size_t o_idx = take(sizeof(uint32_t) * cs);
+    const size_t o_items = take(sizeof(uint2) * ci);
+    const size_t o_cnt = take(sizeof(uint8_t) * cs);
+    const size_t o_slot = take(sizeof(SeedSlot) * cs * kMaxSeedsPerMiddle);
+    const size_t o_ovf = take(sizeof(uint32_t) * cs);
+    const size_t o_ctr = take(sizeof(unsigned long long) * kNumCounters);
+    if (h->arena) {
+        cudaFree(h->arena);
+        h->arena = nullptr;
+    }
+    void* p = nullptr;
+    if (cudaMalloc(&p, off) != cudaSuccess) {
+        h->cap_events = 0;
+        h->cap_sp = 0;
+        return SEEDGB_CUDA_ERROR;
+    }
+    h->arena = p;
+    h->arena_bytes = off;
+    h->cap_events = ce;
+    h->cap_sp = cs;
+    char* base = static_cast<char*>(p);
+    Arena& a = h->a;
+    a.events = reinterpret_cast<EventDesc*>(base + o_events);
+    a.sp_bin = reinterpret_cast<int32_t*>(base + o_spbin);
+    a.whist = reinterpret_cast<uint32_t*>(base + o_whist);
+    a.bin_start = reinterpret_cast<uint32_t*>(base + o_bs);
+    a.n_valid = reinterpret_cast<uint32_t*>(base + o_nv);
+    a.g_xyzr = reinterpret_cast<float4*>(base + o_xyzr);
+    a.g_var = reinterpret_cast<float2*>(base + o_var);
+    a.g_idx = reinterpret_cast<uint32_t*>(base + o_idx);
+    a.items = reinterpret_cast<uint2*>(base + o_items);
+    a.seed_cnt = reinterpret_cast<uint8_t*>(base + o_cnt);
+    a.seed_slot = reinterpret_cast<SeedSlot*>(base + o_slot);
+    a.ovf = reinterpret_cast<uint32_t*>(base + o_ovf);
+    a.counters = reinterpret_cast<unsigned long long*>(base + o_ctr);
+    a.max_items = ci;
+    if (h->h_desc_cap < ce) {
+        if (h->h_desc) cudaFreeHost(h->h_desc);
+        h->h_desc = nullptr;
+        if (cudaMallocHost(&h->h_desc, sizeof(EventDesc) * ce) != cudaSuccess) {
+            h->h_desc_cap = 0;
+            return SEEDGB_CUDA_ERROR;
+        }
+        h->h_desc_cap = ce;
+    }
+    return SEEDGB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+seedgb_status seedgb_seeding_create(const seedgb_seedfinder_config* finder,
+                                    const seedgb_spacepoint_grid_config* grid,
+                                    const seedgb_seedfilter_config* filter,
+                                    seedgb_seeding** out) {
+    if (!finder || !grid || !filter || !out) return SEEDGB_INVALID_ARGUMENT;
+    *out = nullptr;
+    seedgb_grid_axes ax;
+    const seedgb_status st = seedgb_get_axes(grid, &ax);
+    if (st != SEEDGB_OK) return st;
+    const uint64_t nbins = static_cast<uint64_t>(ax.phi_bins) * ax.z_bins;
+    if (ax.phi_bins == 0 || nbins > static_cast<uint64_t>(kMaxBins)) return SEEDGB_UNSUPPORTED;
+    if (finder->neighbor_scope[0] >= ax.phi_bins || finder->neighbor_scope[1] >= ax.phi_bins)
+        return SEEDGB_UNSUPPORTED;
+    const uint32_t zl = std::min<uint32_t>(ax.z_bins,
+                                           finder->neighbor_scope[0] + finder->neighbor_scope[1] + 1);
+    if (static_cast<uint64_t>(max_phi_zone(ax.phi_bins, finder->neighbor_scope[0],
+                                           finder->neighbor_scope[1])) * zl >
+        static_cast<uint64_t>(kMaxSegments))
+        return SEEDGB_UNSUPPORTED;
+    if (finder->maxSeedsPerSpM > kMaxSeedsPerMiddle) return SEEDGB_UNSUPPORTED;
+    if (filter->compatSeedLimit > 8) return SEEDGB_UNSUPPORTED;
+
+    seedgb_seeding* h = new (std::nothrow) seedgb_seeding();
+    if (!h) return SEEDGB_INVALID_ARGUMENT;
+    h->finder = *finder;
+    h->grid = *grid;
+    h->filter = *filter;
+    h->axes = ax;
+    h->dc = make_dev_config(*finder, *filter, ax);
+    if (cudaGetDevice(&h->device) != cudaSuccess ||
+        cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device) !=
+            cudaSuccess ||
+        cudaEventCreateWithFlags(&h->staged, cudaEventDisableTiming) != cudaSuccess) {
+        delete h;
+        return SEEDGB_CUDA_ERROR;
+    }
+    h->tune.fast_warps = 8;
+    h->tune.middles_per_item = 32;
+    h->tune.nb_cap = 3072;
+    h->tune.ctas_per_sm = 1;
+    if (const char* s = std::getenv("SEEDGB_TUNE")) {
+        int w, m, nb, c;
+        if (std::sscanf(s, "%d,%d,%d,%d", &w, &m, &nb, &c) == 4 && w >= 1 && w <= 8 &&
+            m >= 1 && m <= 4096 && nb >= 256 && nb <= 8192 && c >= 1 && c <= 8) {
+            h->tune = TuneParams{w, m, nb, c};
+        }
+    }
+    *out = h;
+    return SEEDGB_OK;
+}
+
+seedgb_status seedgb_seeding_destroy(seedgb_seeding* h) {
+    if (!h) return SEEDGB_INVALID_ARGUMENT;
+    if (h->arena) cudaFree(h->arena);
+    if (h->h_desc) cudaFreeHost(h->h_desc);
+    if (h->staged) cudaEventDestroy(h->staged);
+    delete h;
+    return SEEDGB_OK;
+}
+
+seedgb_status seedgb_seeding_reserve(seedgb_seeding* h, uint32_t max_events,
+                                     uint64_t max_total_spacepoints) {
+    if (!h || max_events == 0) return SEEDGB_INVALID_ARGUMENT;
+    const uint32_t chunks =
+        static_cast<uint32_t>(max_total_spacepoints / kBinChunk) + max_events;
+    return ensure_arena(h, max_events, max_total_spacepoints, chunks);
+}
+
+seedgb_status seedgb_seeding_run_batch(seedgb_seeding* h, const seedgb_spacepoint_view* events,
+                                       uint32_t n_events, seedgb_seed_buffer* outs,
+                                       void* stream) {
+    if (!h || !events || !outs || n_events == 0) return SEEDGB_INVALID_ARGUMENT;
+    if (n_events > kMaxEventsPerBatch) return SEEDGB_UNSUPPORTED;
+    uint64_t total_sp = 0;
+    uint32_t total_chunks = 0;
+    for (uint32_t e = 0; e < n_events; ++e) {
+        const seedgb_spacepoint_view& v = events[e];
+        if (v.size > 0 && !v.global) return SEEDGB_INVALID_ARGUMENT;
+        if (!outs[e].size || (outs[e].capacity > 0 &&
+                              (!outs[e].bottom_index || !outs[e].middle_index ||
+                               !outs[e].top_index || !outs[e].quality)))
+            return SEEDGB_INVALID_ARGUMENT;
+        total_sp += v.size;
+        total_chunks += chunks_of(v.size);
+    }
+    if (total_sp > 0xF0000000ull) return SEEDGB_UNSUPPORTED;
+    seedgb_status st = ensure_arena(h, n_events, total_sp, total_chunks);
+    if (st != SEEDGB_OK) return st;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    // the staging buffer may still feed the previous call's copy
+    if (cudaEventSynchronize(h->staged) != cudaSuccess) return SEEDGB_CUDA_ERROR;
+    uint32_t sp_base = 0, chunk_base = 0;
+    for (uint32_t e = 0; e < n_events; ++e) {
+        const seedgb_spacepoint_view& v = events[e];
+        EventDesc& d = h->h_desc[e];
+        d.mi1 = v.measurement_index_1;
+        d.mi2 = v.measurement_index_2;
+        d.global = v.global;
+        d.zvar = v.z_variance;
+        d.rvar = v.radius_variance;
+        d.n_sp = v.size;
+        d.sp_base = sp_base;
+        d.chunk_base = chunk_base;
+        d.n_chunks = chunks_of(v.size);
+        d.out_b = outs[e].bottom_index;
+        d.out_m = outs[e].middle_index;
+        d.out_t = outs[e].top_index;
+        d.out_q = outs[e].quality;
+        d.out_cap = outs[e].capacity;
+        d.pad = 0;
+        d.out_size = outs[e].size;
+        sp_base += v.size;
+        chunk_base += d.n_chunks;
+    }
+    Arena a = h->a;
+    a.n_events = n_events;
+    a.total_chunks = total_chunks;
+    a.total_sp = static_cast<uint32_t>(total_sp);
+    cudaError_t err = cudaMemcpyAsync(a.events, h->h_desc, sizeof(EventDesc) * n_events,
+                                      cudaMemcpyHostToDevice, s);
+    if (err == cudaSuccess) err = cudaEventRecord(h->staged, s);
+    if (err == cudaSuccess)
+        err = cudaMemsetAsync(a.counters, 0, sizeof(unsigned long long) * kNumCounters, s);
+    if (err == cudaSuccess) err = launch_seeding(h->dc, a, h->tune, h->num_sms, s);
+    return cuda_status(err);
+}
+
+seedgb_status seedgb_seeding_run(seedgb_seeding* h, const seedgb_spacepoint_view* sps,
+                                 seedgb_seed_buffer* out, void* stream) {
+    return seedgb_seeding_run_batch(h, sps, 1, out, stream);
+}
+
+seedgb_status seedgb_seeding_last_status(seedgb_seeding* h, void* stream) {
+    if (!h) return SEEDGB_INVALID_ARGUMENT;
+    if (!h->arena) return SEEDGB_OK;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    cudaError_t err = cudaMemcpyAsync(h->h_counters, h->a.counters,
+                                      sizeof(unsigned long long) * kNumCounters,
+                                      cudaMemcpyDeviceToHost, s);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(s);
+    if (err != cudaSuccess) return SEEDGB_CUDA_ERROR;
+    const unsigned long long bits = h->h_counters[kStatus];
+    if (bits & (1ull << SEEDGB_CAPACITY_OVERFLOW)) return SEEDGB_CAPACITY_OVERFLOW;
+    if (bits & (1ull << SEEDGB_TIMEOUT)) return SEEDGB_TIMEOUT;
+    if (bits & (1ull << SEEDGB_BAD_CONFIG)) return SEEDGB_BAD_CONFIG;
+    return SEEDGB_OK;
+}
+
+seedgb_status seedgb_seeding_counters(seedgb_seeding* h, uint64_t out[8]) {
+    if (!h || !out) return SEEDGB_INVALID_ARGUMENT;
+    out[0] = h->h_counters[kNumValid];
+    out[1] = h->h_counters[kOvfCount];
+    out[2] = h->h_counters[kNumMB];
+    out[3] = h->h_counters[kNumMT];
+    out[4] = h->h_counters[kNumTriplets];
+    out[5] = h->h_counters[kNumSeeds];
+    out[6] = h->h_counters[kPhiUndecided];
+    out[7] = h->h_counters[kItemTotal];
+    return SEEDGB_OK;
+}
+
+seedgb_status seedgb_seeding_copy_grid(seedgb_seeding* h, uint32_t event,
+                                       uint32_t* bin_offsets, uint32_t* bin_sps,
+                                       uint32_t bin_sps_capacity, uint32_t* n_valid,
+                                       void* stream) {
+    if (!h || !bin_offsets || !n_valid) return SEEDGB_INVALID_ARGUMENT;
+    if (!h->arena || event >= h->cap_events) return SEEDGB_INVALID_ARGUMENT;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const uint32_t nb = h->dc.nbins;
+    std::vector<uint32_t> bs(nb + 1);
+    EventDesc d;
+    cudaError_t err = cudaMemcpyAsync(bs.data(), h->a.bin_start + static_cast<size_t>(event) * (nb + 1),
+                                      sizeof(uint32_t) * (nb + 1), cudaMemcpyDeviceToHost, s);
+    if (err == cudaSuccess)
+        err = cudaMemcpyAsync(&d, h->a.events + event, sizeof(EventDesc), cudaMemcpyDeviceToHost, s);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(s);
+    if (err != cudaSuccess) return SEEDGB_CUDA_ERROR;
+    const uint32_t nv = bs[nb] - bs[0];
+    *n_valid = nv;
+    for (uint32_t b = 0; b <= nb; ++b) bin_offsets[b] = bs[b] - bs[0];
+    if (nv > 0) {
+        if (!bin_sps || bin_sps_capacity < nv) return SEEDGB_INVALID_ARGUMENT;
+        err = cudaMemcpyAsync(bin_sps, h->a.g_idx + bs[0], sizeof(uint32_t) * nv,
+                              cudaMemcpyDeviceToHost, s);
+        if (err == cudaSuccess) err = cudaStreamSynchronize(s);
+    }
+    return cuda_status(err);
+}
+
+seedgb_status seedgb_seeding_set_option(seedgb_seeding* h, seedgb_option opt, int64_t value) {
+    if (!h) return SEEDGB_INVALID_ARGUMENT;
+    switch (opt) {
+        case SEEDGB_OPTION_EXHAUSTIVE_TRIPLETS:
+            h->dc.brute_force_triplets = value ? 1u : 0u;
+            return SEEDGB_OK;
+    }
+    return SEEDGB_INVALID_ARGUMENT;
+}
+
+seedgb_status seedgb_params_create(const seedgb_track_params_estimation_config* cfg,
+                                   seedgb_params** out) {
+    if (!cfg || !out) return SEEDGB_INVALID_ARGUMENT;
+    seedgb_params* h = new (std::nothrow) seedgb_params();
+    if (!h) return SEEDGB_INVALID_ARGUMENT;
+    for (int i = 0; i < 6; ++i) {
+        h->pc.initial_sigma[i] = cfg->initial_sigma[i];
+        h->pc.initial_inflation[i] = cfg->initial_inflation[i];
+    }
+    h->pc.initial_sigma_qopt = cfg->initial_sigma_qopt;
+    h->pc.initial_sigma_pt_rel = cfg->initial_sigma_pt_rel;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, dev) !=
+            cudaSuccess) {
+        delete h;
+        return SEEDGB_CUDA_ERROR;
+    }
+    *out = h;
+    return SEEDGB_OK;
+}
+
+seedgb_status seedgb_params_destroy(seedgb_params* h) {
+    if (!h) return SEEDGB_INVALID_ARGUMENT;
+    delete h;
+    return SEEDGB_OK;
+}
+
+seedgb_status seedgb_params_run(seedgb_params* h, const float bfield[3],
+                                const seedgb_measurement_view* meas,
+                                const seedgb_spacepoint_view* sps,
+                                const seedgb_seed_buffer* seeds, seedgb_params_buffer* out,
+                                void* stream) {
+    if (!h || !bfield || !meas || !sps || !seeds || !out || !seeds->size || !out->size)
+        return SEEDGB_INVALID_ARGUMENT;
+    return cuda_status(launch_params(h->pc, bfield, *meas, *sps, *seeds, *out, h->num_sms,
+                                     static_cast<cudaStream_t>(stream)));
+}
+
+}  // extern "C"

@@ -1,0 +1,154 @@
+// Internal structures shared by the seeding kernels and the C-ABI layer.
+//
+// Device data layout of one batch (all arrays live in one arena owned by the
+// seeding handle; "grid position" = position in the binned spacepoint grid of
+// the whole batch, event e owning [sp_base[e], sp_base[e] + n_valid[e])):
+//
+//   sp_bin      int32 [total_sp]            grid bin of each input spacepoint or -1
+//   whist       uint32[chunks][NWB][nbins]  per-warp bin histograms -> offsets
+//   bin_start   uint32[E][nbins+1]          grid-position range of each bin
+//   g_xyzr      float4[total_sp]            binned x, y, z, r (r = sqrt(x^2+y^2))
+//   g_var       float2[total_sp]            binned z / radius variances
+//   g_idx       uint32[total_sp]            binned spacepoint index within its event
+//   items       uint2 [max_items]           (event, bin | chunk<<16) work items
+//   seed_cnt    uint8 [total_sp]            seeds per middle spacepoint
+//   seed_slot   SeedSlot[total_sp][KMAX]    seeds per middle, in final order
+//   ovf         uint32[total_sp]            middles for the large-capacity path
+//   counters    uint64[kNumCounters]
+#pragma once
+
+#include <cstdint>
+
+#include "seedgb.h"
+
+namespace seedgb {
+
+constexpr int kMaxSeedsPerMiddle = SEEDGB_MAX_SEEDS_PER_MIDDLE;
+constexpr int kMaxSegments = 64;      // neighbourhood bins per middle
+constexpr int kMaxBins = 4096;        // phi x z bins
+constexpr uint32_t kMaxEventsPerBatch = 65535;
+
+// Binning chunk geometry: NWB warps x RB rounds x 32 spacepoints, each warp a
+// contiguous run of spacepoints (stable order inside a bin).
+constexpr int kBinWarps = 8;
+constexpr int kBinRounds = 8;
+constexpr int kBinChunk = kBinWarps * kBinRounds * 32;  // 2048
+
+enum Counter : int {
+    kStatus = 0,        // bit mask of seedgb_status values (1 << status)
+    kItemFetch = 1,     // work-item counter of the fast seeding kernel
+    kItemTotal = 2,     // number of work items
+    kOvfCount = 3,      // middles queued for the large-capacity path
+    kOvfFetch = 4,
+    kNumMB = 5,
+    kNumMT = 6,
+    kNumTriplets = 7,
+    kNumSeeds = 8,
+    kNumValid = 9,
+    kAnyVariance = 10,  // nonzero if any spacepoint has a nonzero variance
+    kPhiUndecided = 11, // correctly rounded phi not decidable from double
+    kNumCounters = 16
+};
+
+// Kernel-side copy of the configuration (host-derived, passed by value).
+struct DevConfig {
+    // seedfinder_config
+    float zMin, zMax, phiMin, phiMax;
+    float beam0, beam1;
+    unsigned long long nrbins;  // (size_t)(rMax + |beamPos|)
+    float deltaRMin, deltaRMax, cotThetaMax, collisionRegionMin,
+        collisionRegionMax, deltaZMax, impactMax, minHelixRadius;
+    float maxScatteringAngle2, sigmaScattering, minHelixDiameter2, pT2perRadius,
+        pTPerHelixRadius, maxPtScattering, highland;
+    uint32_t maxSeedsPerSpM;
+    uint32_t scope0, scope1;
+    // seedfilter_config
+    float deltaInvHelixDiameter, impactWeightFactor, compatSeedWeight,
+        filterDeltaRMin;
+    uint32_t compatSeedLimit;
+    float good_spB_min_radius, good_spB_weight_increase, good_spT_max_radius,
+        good_spT_weight_increase, good_spB_min_weight, seed_min_weight,
+        spB_min_radius;
+    // axes
+    uint32_t phi_bins, z_bins, nbins;
+    float phi_min, phi_max, z_min, z_max;
+    // behaviour switches (tests)
+    uint32_t brute_force_triplets;  // 1: test every MB x MT pair (no cot window)
+};
+
+// One event of a batch, as the kernels see it.
+struct EventDesc {
+    const uint32_t* mi1;
+    const uint32_t* mi2;
+    const float* global;
+    const float* zvar;
+    const float* rvar;
+    uint32_t n_sp;
+    uint32_t sp_base;     // first grid position / internal index of the event
+    uint32_t chunk_base;  // first binning chunk of the event
+    uint32_t n_chunks;
+    uint32_t* out_b;
+    uint32_t* out_m;
+    uint32_t* out_t;
+    float* out_q;
+    uint32_t out_cap;
+    uint32_t pad;
+    uint32_t* out_size;
+};
+
+struct SeedSlot {
+    uint32_t b, m, t;
+    float q;
+};
+
+// Pointers into the work arena.
+struct Arena {
+    EventDesc* events;      // [E]
+    uint32_t* chunk_event;  // [total_chunks]
+    int32_t* sp_bin;
+    uint32_t* whist;
+    uint32_t* bin_start;
+    uint32_t* n_valid;      // [E]
+    float4* g_xyzr;
+    float2* g_var;
+    uint32_t* g_idx;
+    uint2* items;
+    uint8_t* seed_cnt;
+    SeedSlot* seed_slot;
+    uint32_t* ovf;
+    unsigned long long* counters;
+    uint32_t n_events;
+    uint32_t total_chunks;
+    uint32_t total_sp;
+    uint32_t max_items;
+};
+
+// Launch shapes picked by the autotuner (see seedgb_api.cu).
+struct TuneParams {
+    int fast_warps;        // warps per CTA of the fast seeding kernel
+    int middles_per_item;  // middles per work item
+    int nb_cap;            // neighbourhood spacepoints staged in shared memory
+    int ctas_per_sm;
+};
+
+// Kernel launchers (seedgb_kernels.cu).  All asynchronous on `stream`.
+cudaError_t launch_seeding(const DevConfig& cfg, const Arena& a,
+                           const TuneParams& tp, int num_sms,
+                           cudaStream_t stream);
+
+struct ParamsConfig {
+    float initial_sigma[6];
+    float initial_sigma_qopt, initial_sigma_pt_rel;
+    float initial_inflation[6];
+};
+
+cudaError_t launch_params(const ParamsConfig& cfg, const float bfield[3],
+                          const seedgb_measurement_view& meas,
+                          const seedgb_spacepoint_view& sps,
+                          const seedgb_seed_buffer& seeds,
+                          const seedgb_params_buffer& out, int num_sms,
+                          cudaStream_t stream);
+
+size_t fast_kernel_smem(const TuneParams& tp);
+
+}  // namespace seedgb

@@ -1,0 +1,471 @@
+"""Python host mirror of traccc's seeding call surface over the C ABI.
+
+Names and call shapes follow the reference:
+
+* ``TripletSeedingAlgorithm(finder, grid, filter)(spacepoints) -> SeedBuffer``
+  mirrors ``traccc::cuda::triplet_seeding_algorithm``
+  (device/cuda/include/traccc/cuda/seeding/triplet_seeding_algorithm.hpp:35-40,
+  ``operator()`` at device/common/include/traccc/seeding/device/
+  triplet_seeding_algorithm.hpp:68-69).
+* ``SeedParameterEstimationAlgorithm(config)(bfield, measurements, spacepoints,
+  seeds) -> ParamsBuffer`` mirrors ``traccc::cuda::
+  seed_parameter_estimation_algorithm`` (device/common/include/traccc/seeding/
+  device/seed_parameter_estimation_algorithm.hpp:48-67).
+* Config objects mirror ``seedfinder_config``, ``spacepoint_grid_config``,
+  ``seedfilter_config`` and ``track_params_estimation_config``; invalid grids
+  raise ``ValueError`` where the reference throws ``std::domain_error``.
+
+Device memory is held in torch CUDA tensors; the work runs in the native
+library ``_lib/libseedgb.so``.  There is no CPU fallback: without the library
+or without a GPU, the calls raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import _build
+
+# ---------------------------------------------------------------------------
+# C structures (include/seedgb.h)
+# ---------------------------------------------------------------------------
+
+
+class SeedfinderConfig(C.Structure):
+    _fields_ = [(n, C.c_float) for n in (
+        "zMin", "zMax", "rMax", "rMin", "collisionRegionMin",
+        "collisionRegionMax", "phiMin", "phiMax", "minPt", "cotThetaMax",
+        "deltaRMin", "deltaRMax", "deltaZMax", "impactMax", "sigmaScattering",
+        "maxPtScattering")] + [
+        ("maxSeedsPerSpM", C.c_uint32), ("bFieldInZ", C.c_float),
+        ("beamPos", C.c_float * 2)] + [(n, C.c_float) for n in (
+            "radLengthPerSeed", "zAlign", "rAlign", "sigmaError", "highland",
+            "maxScatteringAngle2", "pTPerHelixRadius", "minHelixDiameter2",
+            "minHelixRadius", "pT2perRadius")] + [
+        ("phiBinDeflectionCoverage", C.c_int32),
+        ("neighbor_scope", C.c_uint32 * 2)]
+
+    def setup(self):
+        """seedfinder_config::setup(): recompute the derived members."""
+        lib().seedgb_seedfinder_config_setup(C.byref(self))
+        return self
+
+
+class SpacepointGridConfig(C.Structure):
+    _fields_ = [(n, C.c_float) for n in (
+        "bFieldInZ", "minPt", "rMax", "zMax", "zMin", "deltaRMax",
+        "cotThetaMax", "impactMax", "phiMin", "phiMax")] + [
+        ("phiBinDeflectionCoverage", C.c_int32)]
+
+
+class SeedfilterConfig(C.Structure):
+    _fields_ = [(n, C.c_float) for n in (
+        "deltaInvHelixDiameter", "impactWeightFactor", "compatSeedWeight",
+        "deltaRMin")] + [("compatSeedLimit", C.c_uint64)] + [
+        (n, C.c_float) for n in (
+            "good_spB_min_radius", "good_spB_weight_increase",
+            "good_spT_max_radius", "good_spT_weight_increase",
+            "good_spB_min_weight", "seed_min_weight", "spB_min_radius")]
+
+
+class TrackParamsEstimationConfig(C.Structure):
+    _fields_ = [("initial_sigma", C.c_float * 6),
+                ("initial_sigma_qopt", C.c_float),
+                ("initial_sigma_pt_rel", C.c_float),
+                ("initial_inflation", C.c_float * 6)]
+
+
+class GridAxes(C.Structure):
+    _fields_ = [("phi_bins", C.c_uint32), ("phi_min", C.c_float),
+                ("phi_max", C.c_float), ("z_bins", C.c_uint32),
+                ("z_min", C.c_float), ("z_max", C.c_float)]
+
+
+class _SpacepointView(C.Structure):
+    _fields_ = [("measurement_index_1", C.c_void_p),
+                ("measurement_index_2", C.c_void_p), ("glob", C.c_void_p),
+                ("z_variance", C.c_void_p), ("radius_variance", C.c_void_p),
+                ("size", C.c_uint32)]
+
+
+class _SeedBuffer(C.Structure):
+    _fields_ = [("bottom_index", C.c_void_p), ("middle_index", C.c_void_p),
+                ("top_index", C.c_void_p), ("quality", C.c_void_p),
+                ("capacity", C.c_uint32), ("size", C.c_void_p)]
+
+
+class _MeasurementView(C.Structure):
+    _fields_ = [("local_position", C.c_void_p), ("surface_link", C.c_void_p),
+                ("size", C.c_uint32)]
+
+
+class _ParamsBuffer(C.Structure):
+    _fields_ = [("data", C.c_void_p), ("capacity", C.c_uint32),
+                ("size", C.c_void_p)]
+
+
+STATUS = {0: "ok", 1: "empty input", 2: "bad configuration", 3: "CUDA error",
+          4: "device buffer capacity exceeded", 5: "device wait timed out",
+          6: "invalid argument", 7: "unsupported configuration"}
+OK, EMPTY, BAD_CONFIG, CUDA_ERROR, CAPACITY_OVERFLOW, TIMEOUT = 0, 1, 2, 3, 4, 5
+OPTION_EXHAUSTIVE_TRIPLETS = 1
+
+PARAMS_DTYPE = np.dtype([("surface_link", "<u8"), ("params", "<f4", (6,)),
+                         ("cov", "<f4", (36,))])
+SEED_DTYPE = np.dtype([("bottom", "<u4"), ("middle", "<u4"), ("top", "<u4"),
+                       ("quality", "<f4")])
+
+
+class SeedingError(RuntimeError):
+    def __init__(self, status, what=""):
+        super().__init__(f"{what}: {STATUS.get(status, status)} (status {status})")
+        self.status = status
+
+
+_lib = None
+
+
+def library_path() -> str:
+    return os.path.join(_build.LIBDIR, "libseedgb.so")
+
+
+def lib():
+    """Load the native library.  It must have been built (``build()``)."""
+    global _lib
+    if _lib is None:
+        path = library_path()
+        if not os.path.exists(path):
+            raise RuntimeError(
+                f"native seeding library missing ({path}); run "
+                "traccc_gb300._build.build_all() first -- there is no CPU fallback")
+        L = C.CDLL(path)
+        P = C.POINTER
+        vp = C.c_void_p
+        L.seedgb_seedfinder_config_default.argtypes = [P(SeedfinderConfig)]
+        L.seedgb_seedfinder_config_setup.argtypes = [P(SeedfinderConfig)]
+        L.seedgb_spacepoint_grid_config_from_finder.argtypes = [
+            P(SpacepointGridConfig), P(SeedfinderConfig)]
+        L.seedgb_seedfilter_config_default.argtypes = [P(SeedfilterConfig)]
+        L.seedgb_track_params_estimation_config_default.argtypes = [
+            P(TrackParamsEstimationConfig)]
+        L.seedgb_get_axes.argtypes = [P(SpacepointGridConfig), P(GridAxes)]
+        L.seedgb_get_axes.restype = C.c_int
+        L.seedgb_seeding_create.argtypes = [P(SeedfinderConfig), P(SpacepointGridConfig),
+                                            P(SeedfilterConfig), P(vp)]
+        L.seedgb_seeding_create.restype = C.c_int
+        L.seedgb_seeding_destroy.argtypes = [vp]
+        L.seedgb_seeding_destroy.restype = C.c_int
+        L.seedgb_seeding_reserve.argtypes = [vp, C.c_uint32, C.c_uint64]
+        L.seedgb_seeding_reserve.restype = C.c_int
+        L.seedgb_seeding_run.argtypes = [vp, P(_SpacepointView), P(_SeedBuffer), vp]
+        L.seedgb_seeding_run.restype = C.c_int
+        L.seedgb_seeding_run_batch.argtypes = [vp, P(_SpacepointView), C.c_uint32,
+                                               P(_SeedBuffer), vp]
+        L.seedgb_seeding_run_batch.restype = C.c_int
+        L.seedgb_seeding_last_status.argtypes = [vp, vp]
+        L.seedgb_seeding_last_status.restype = C.c_int
+        L.seedgb_seeding_counters.argtypes = [vp, P(C.c_uint64)]
+        L.seedgb_seeding_counters.restype = C.c_int
+        L.seedgb_seeding_copy_grid.argtypes = [vp, C.c_uint32, P(C.c_uint32),
+                                               P(C.c_uint32), C.c_uint32,
+                                               P(C.c_uint32), vp]
+        L.seedgb_seeding_copy_grid.restype = C.c_int
+        L.seedgb_seeding_set_option.argtypes = [vp, C.c_int, C.c_int64]
+        L.seedgb_seeding_set_option.restype = C.c_int
+        L.seedgb_params_create.argtypes = [P(TrackParamsEstimationConfig), P(vp)]
+        L.seedgb_params_create.restype = C.c_int
+        L.seedgb_params_destroy.argtypes = [vp]
+        L.seedgb_params_destroy.restype = C.c_int
+        L.seedgb_params_run.argtypes = [vp, P(C.c_float), P(_MeasurementView),
+                                        P(_SpacepointView), P(_SeedBuffer),
+                                        P(_ParamsBuffer), vp]
+        L.seedgb_params_run.restype = C.c_int
+        L.seedgb_status_string.argtypes = [C.c_int]
+        L.seedgb_status_string.restype = C.c_char_p
+        L.seedgb_abi_version.restype = C.c_uint32
+        _lib = L
+    return _lib
+
+
+def _check(status, what):
+    if status != OK:
+        raise SeedingError(status, what)
+
+
+def default_configs():
+    """Reference defaults: (seedfinder, spacepoint_grid, seedfilter,
+    track_params_estimation) configs."""
+    L = lib()
+    f, g, fl, tp = (SeedfinderConfig(), SpacepointGridConfig(), SeedfilterConfig(),
+                    TrackParamsEstimationConfig())
+    L.seedgb_seedfinder_config_default(C.byref(f))
+    L.seedgb_spacepoint_grid_config_from_finder(C.byref(g), C.byref(f))
+    L.seedgb_seedfilter_config_default(C.byref(fl))
+    L.seedgb_track_params_estimation_config_default(C.byref(tp))
+    return f, g, fl, tp
+
+
+def grid_config_from_finder(f: SeedfinderConfig) -> SpacepointGridConfig:
+    g = SpacepointGridConfig()
+    lib().seedgb_spacepoint_grid_config_from_finder(C.byref(g), C.byref(f))
+    return g
+
+
+def get_axes(g: SpacepointGridConfig) -> GridAxes:
+    a = GridAxes()
+    st = lib().seedgb_get_axes(C.byref(g), C.byref(a))
+    if st == BAD_CONFIG:
+        raise ValueError("invalid spacepoint grid configuration")
+    _check(st, "get_axes")
+    return a
+
+
+# ---------------------------------------------------------------------------
+# Device collections (torch tensors)
+# ---------------------------------------------------------------------------
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def _stream_ptr(stream):
+    torch = _torch()
+    if stream is None:
+        stream = torch.cuda.current_stream()
+    return C.c_void_p(stream.cuda_stream)
+
+
+class SpacepointCollection:
+    """Device SoA of edm::spacepoint_collection (spacepoint_collection.hpp:
+    222-234): measurement_index_1/2 (u32, stored as int32), global (N, 3 f32,
+    xyz interleaved), z_variance, radius_variance (f32)."""
+
+    def __init__(self, measurement_index_1, measurement_index_2, global_,
+                 z_variance, radius_variance):
+        self.measurement_index_1 = measurement_index_1
+        self.measurement_index_2 = measurement_index_2
+        self.global_ = global_
+        self.z_variance = z_variance
+        self.radius_variance = radius_variance
+
+    @classmethod
+    def from_numpy(cls, ev, device="cuda"):
+        torch = _torch()
+        t = lambda a, dt: torch.from_numpy(np.ascontiguousarray(a).view(dt)).to(device)
+        return cls(t(ev["measurement_index_1"].astype(np.uint32), np.int32),
+                   t(ev["measurement_index_2"].astype(np.uint32), np.int32),
+                   t(np.asarray(ev["global"], np.float32).reshape(-1, 3), np.float32),
+                   t(np.asarray(ev["z_variance"], np.float32), np.float32),
+                   t(np.asarray(ev["radius_variance"], np.float32), np.float32))
+
+    def __len__(self):
+        return int(self.global_.shape[0])
+
+    def view(self) -> _SpacepointView:
+        n = len(self)
+        return _SpacepointView(self.measurement_index_1.data_ptr(),
+                               self.measurement_index_2.data_ptr(),
+                               self.global_.data_ptr(), self.z_variance.data_ptr(),
+                               self.radius_variance.data_ptr(), n)
+
+
+class MeasurementCollection:
+    """The measurement columns parameter estimation reads: local_position
+    (M, 2 f32) and surface_link (u64, stored as int64)."""
+
+    def __init__(self, local_position, surface_link):
+        self.local_position = local_position
+        self.surface_link = surface_link
+
+    @classmethod
+    def from_numpy(cls, ev, device="cuda"):
+        torch = _torch()
+        lp = torch.from_numpy(np.ascontiguousarray(ev["local_position"], np.float32)
+                              .reshape(-1, 2)).to(device)
+        sl = torch.from_numpy(np.ascontiguousarray(ev["surface_link"], np.uint64)
+                              .view(np.int64)).to(device)
+        return cls(lp, sl)
+
+    def view(self) -> _MeasurementView:
+        return _MeasurementView(self.local_position.data_ptr(),
+                                self.surface_link.data_ptr(),
+                                int(self.surface_link.shape[0]))
+
+
+class SeedBuffer:
+    """Device edm::seed_collection buffer: four columns of `capacity` and a
+    device-resident size (seed_collection.hpp:142-146)."""
+
+    def __init__(self, capacity, device="cuda"):
+        torch = _torch()
+        cap = max(1, int(capacity))
+        self.capacity = int(capacity)
+        self.bottom_index = torch.empty(cap, dtype=torch.int32, device=device)
+        self.middle_index = torch.empty(cap, dtype=torch.int32, device=device)
+        self.top_index = torch.empty(cap, dtype=torch.int32, device=device)
+        self.quality = torch.empty(cap, dtype=torch.float32, device=device)
+        self.size = torch.zeros(1, dtype=torch.int32, device=device)
+
+    def buf(self) -> _SeedBuffer:
+        return _SeedBuffer(self.bottom_index.data_ptr(), self.middle_index.data_ptr(),
+                           self.top_index.data_ptr(), self.quality.data_ptr(),
+                           self.capacity, self.size.data_ptr())
+
+    def __len__(self):
+        return int(self.size.item())
+
+    def to_numpy(self):
+        n = len(self)
+        out = np.zeros(n, SEED_DTYPE)
+        out["bottom"] = self.bottom_index[:n].cpu().numpy().view(np.uint32)
+        out["middle"] = self.middle_index[:n].cpu().numpy().view(np.uint32)
+        out["top"] = self.top_index[:n].cpu().numpy().view(np.uint32)
+        out["quality"] = self.quality[:n].cpu().numpy()
+        return out
+
+
+class ParamsBuffer:
+    """Device bound_track_parameters collection (176-byte records)."""
+
+    def __init__(self, capacity, device="cuda"):
+        torch = _torch()
+        self.capacity = int(capacity)
+        self.data = torch.empty(max(1, self.capacity) * PARAMS_DTYPE.itemsize,
+                                dtype=torch.uint8, device=device)
+        self.size = torch.zeros(1, dtype=torch.int32, device=device)
+
+    def buf(self) -> _ParamsBuffer:
+        return _ParamsBuffer(self.data.data_ptr(), self.capacity, self.size.data_ptr())
+
+    def __len__(self):
+        return int(self.size.item())
+
+    def to_numpy(self):
+        n = len(self)
+        raw = self.data[: n * PARAMS_DTYPE.itemsize].cpu().numpy()
+        return raw.view(PARAMS_DTYPE).copy()
+
+
+# ---------------------------------------------------------------------------
+# Algorithms
+# ---------------------------------------------------------------------------
+
+
+class TripletSeedingAlgorithm:
+    """traccc::cuda::triplet_seeding_algorithm on one GB300."""
+
+    def __init__(self, finder_config=None, grid_config=None, filter_config=None):
+        if finder_config is None:
+            finder_config, g0, f0, _ = default_configs()
+            grid_config = grid_config or g0
+            filter_config = filter_config or f0
+        if grid_config is None:
+            grid_config = grid_config_from_finder(finder_config)
+        if filter_config is None:
+            filter_config = default_configs()[2]
+        self.finder_config = finder_config
+        self.grid_config = grid_config
+        self.filter_config = filter_config
+        self._h = C.c_void_p()
+        st = lib().seedgb_seeding_create(C.byref(finder_config), C.byref(grid_config),
+                                         C.byref(filter_config), C.byref(self._h))
+        if st == BAD_CONFIG:
+            raise ValueError("invalid seeding configuration (get_axes domain error)")
+        _check(st, "seedgb_seeding_create")
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and h.value and _lib is not None:
+            _lib.seedgb_seeding_destroy(h)
+            self._h = C.c_void_p()
+
+    def max_seeds(self, n_sp: int) -> int:
+        return max(1, int(self.finder_config.maxSeedsPerSpM) * int(n_sp))
+
+    def reserve(self, max_events: int, max_total_spacepoints: int):
+        _check(lib().seedgb_seeding_reserve(self._h, max_events, max_total_spacepoints),
+               "seedgb_seeding_reserve")
+
+    def set_option(self, option: int, value: int):
+        _check(lib().seedgb_seeding_set_option(self._h, option, value),
+               "seedgb_seeding_set_option")
+
+    def __call__(self, spacepoints: SpacepointCollection, out: SeedBuffer | None = None,
+                 stream=None) -> SeedBuffer:
+        if out is None:
+            out = SeedBuffer(self.max_seeds(len(spacepoints)),
+                             device=spacepoints.global_.device)
+        v = spacepoints.view()
+        b = out.buf()
+        _check(lib().seedgb_seeding_run(self._h, C.byref(v), C.byref(b),
+                                        _stream_ptr(stream)), "seedgb_seeding_run")
+        return out
+
+    def run_batch(self, events, outs=None, stream=None):
+        n = len(events)
+        if outs is None:
+            outs = [SeedBuffer(self.max_seeds(len(e)), device=e.global_.device)
+                    for e in events]
+        views = (_SpacepointView * n)(*[e.view() for e in events])
+        bufs = (_SeedBuffer * n)(*[o.buf() for o in outs])
+        _check(lib().seedgb_seeding_run_batch(self._h, views, n, bufs,
+                                              _stream_ptr(stream)),
+               "seedgb_seeding_run_batch")
+        return outs
+
+    def last_status(self, stream=None) -> int:
+        return int(lib().seedgb_seeding_last_status(self._h, _stream_ptr(stream)))
+
+    def counters(self) -> dict:
+        arr = (C.c_uint64 * 8)()
+        _check(lib().seedgb_seeding_counters(self._h, arr), "seedgb_seeding_counters")
+        keys = ("n_valid", "n_overflow_middles", "n_mb", "n_mt", "n_triplets",
+                "n_seeds", "phi_undecided", "n_items")
+        return {k: int(v) for k, v in zip(keys, arr)}
+
+    def grid(self, event: int = 0, n_sp: int = 0, stream=None):
+        """(bin_offsets, bin_sps) of the last run's event (host copy)."""
+        ax = get_axes(self.grid_config)
+        nb = ax.phi_bins * ax.z_bins
+        off = np.zeros(nb + 1, np.uint32)
+        sps = np.zeros(max(1, n_sp), np.uint32)
+        nv = C.c_uint32(0)
+        _check(lib().seedgb_seeding_copy_grid(
+            self._h, event, off.ctypes.data_as(C.POINTER(C.c_uint32)),
+            sps.ctypes.data_as(C.POINTER(C.c_uint32)), len(sps), C.byref(nv),
+            _stream_ptr(stream)), "seedgb_seeding_copy_grid")
+        return off, sps[: nv.value].copy()
+
+
+class SeedParameterEstimationAlgorithm:
+    """traccc::cuda::seed_parameter_estimation_algorithm (constant field)."""
+
+    def __init__(self, config: TrackParamsEstimationConfig | None = None):
+        if config is None:
+            config = default_configs()[3]
+        self.config = config
+        self._h = C.c_void_p()
+        _check(lib().seedgb_params_create(C.byref(config), C.byref(self._h)),
+               "seedgb_params_create")
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and h.value and _lib is not None:
+            _lib.seedgb_params_destroy(h)
+            self._h = C.c_void_p()
+
+    def __call__(self, bfield, measurements: MeasurementCollection,
+                 spacepoints: SpacepointCollection, seeds: SeedBuffer,
+                 out: ParamsBuffer | None = None, stream=None) -> ParamsBuffer:
+        if out is None:
+            out = ParamsBuffer(seeds.capacity, device=spacepoints.global_.device)
+        bf = (C.c_float * 3)(*[float(x) for x in bfield])
+        mv, sv, sb, pb = measurements.view(), spacepoints.view(), seeds.buf(), out.buf()
+        _check(lib().seedgb_params_run(self._h, bf, C.byref(mv), C.byref(sv),
+                                       C.byref(sb), C.byref(pb), _stream_ptr(stream)),
+               "seedgb_params_run")
+        return out
