@@ -1,0 +1,460 @@
+#!/usr/bin/env python
+"""Seeding throughput: events/s of traccc-style triplet seeding on one GB300.
+
+Workload (the ~100k-spacepoint configuration the metric is quoted on): 20
+synthetic events from seeds 0-19, each 9000 helices with pT ~ exp(mean
+0.6 GeV) truncated at 0.1 GeV, |eta| < 1.5, plus 12 % noise spacepoints
+(~88k spacepoints per event) in a 10-layer barrel, 2 T field.  The seeding
+config is the reference default.
+
+One step = the whole stage for all 20 events: spacepoint binning, doublets,
+triplets, seed filtering (one batched launch sequence) and track-parameter
+estimation (one launch per event).
+
+  value : events/s with inputs resident in HBM (device time, CUDA events on
+          the launching stream, L2 flushed between steps by a 256 MiB write)
+  e2e   : events/s through the public API from pinned host buffers: the
+          spacepoint columns are copied in, seeds and parameters copied out
+          every step
+  cpu_baseline : the oracle (restated reference host seeding, libm phi) on a
+          bounded sample of the same events, one event per host thread
+
+``--impl reference`` times the reference's CPU seeding path (the oracle port;
+the reference itself cannot be built here) with all host
+threads on the same workload and metric.
+
+Multi-GPU (``torchrun --nproc-per-node N``): replicas only -- every rank seeds
+its own copy of the 20 events, no collective on the data path; value = events
+of all ranks / max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import concurrent.futures as cf
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "events/s seeding @100k SP/event, plain vs learned-pruned at >=99.5% seed recall"
+WORKLOAD = ("cfg2: 20 synthetic events (seeds 0-19), 9000 helices + 12% noise, "
+            "~88k spacepoints/event, reference default seeding config")
+N_EVENTS = 20
+L2_FLUSH_BYTES = 256 << 20
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="seedgb", choices=["seedgb", "reference"])
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--events", type=int, default=N_EVENTS)
+    return p.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def make_events(n):
+    from traccc_gb300 import synth
+    return [synth.workload_event("cfg2", s) for s in range(n)]
+
+
+# ---------------------------------------------------------------------------
+# CPU side (oracle): baseline and the reference arm
+# ---------------------------------------------------------------------------
+
+def cpu_seed_event(ev):
+    import oracle
+    f, g, fl, tp = oracle.default_configs()
+    seeds, _ = oracle.seeding(ev, f, g, fl, phi_mode=oracle.PHI_LIBM)
+    oracle.track_params(ev, seeds, (0.0, 0.0, float(f.bFieldInZ)), tp)
+    return len(seeds)
+
+
+def cpu_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+def cpu_run(events, threads):
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+        n_seeds = sum(ex.map(cpu_seed_event, events))
+    return time.perf_counter() - t0, n_seeds
+
+
+def cpu_model():
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    return "unknown"
+
+
+def cpu_baseline(events):
+    threads = cpu_threads()
+    sample = [events[i % len(events)] for i in range(min(threads, 2 * len(events)))]
+    dt, _ = cpu_run(sample, threads)
+    return {"value": len(sample) / dt, "unit": "events/s", "cores": threads,
+            "kind": "port",
+            "sample": f"{len(sample)} cfg2 events (seeds 0-{min(len(events), len(sample)) - 1}), "
+                      f"one per thread on {threads} threads ({cpu_model()}), oracle with libm "
+                      f"phi, seeding + params, {dt:.1f} s"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    threads = cpu_threads()
+    from traccc_gb300 import synth
+    warm = [synth.workload_event("cfg0", s) for s in range(threads)]
+    events = make_events(min(threads, args.events))
+    sample = [events[i % len(events)] for i in range(threads)]
+    for _ in range(args.warmup):
+        cpu_run(warm, threads)
+    times = []
+    for _ in range(args.steps):
+        dt, _ = cpu_run(sample, threads)
+        times.append(dt)
+    tot = sum(times)
+    value = len(sample) * args.steps / tot
+    line = {
+        "metric": METRIC, "value": value, "unit": "events/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * tot / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "impl": "reference",
+        "config": {"workload": WORKLOAD, "step": f"{len(sample)} events, one per host thread",
+                   "l2": "n/a (CPU)"},
+        "cpu_baseline": {"value": value, "unit": "events/s", "cores": threads,
+                         "kind": "port",
+                         "sample": f"{len(sample)} cfg2 events per step on {threads} threads "
+                                   f"({cpu_model()}); warm-up steps on cfg0 events"},
+        "e2e": {"value": value, "unit": "events/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index):
+        self.idx = device_index
+        self.samples = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.samples.append(parts)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        s = self.samples
+        if not s:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(x[1]) for x in s if x[1].replace(".", "").isdigit()]
+        mx = [float(x[2]) for x in s if x[2].replace(".", "").isdigit()]
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        reasons = sorted({n for x in s for n, v in zip(names, x[5:9]) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(s)}
+
+
+def load_profile_traffic(kernel):
+    """DRAM bytes per launch of `kernel` on this workload from the committed
+    ncu summary (profiles/traffic.json), or None."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(p) as fh:
+            return json.load(fh).get(kernel)
+    except Exception:
+        return None
+
+
+def run_gpu(args):
+    import torch
+    import torch.distributed as dist
+
+    from traccc_gb300 import seeding
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    events = make_events(args.events)
+    n_ev = len(events)
+    sizes = [len(e["layer"]) for e in events]
+    offs = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+    total = int(offs[-1])
+
+    def cat(key, dt, shape=()):
+        return np.ascontiguousarray(np.concatenate([np.asarray(e[key]).reshape((-1,) + shape)
+                                                    for e in events]).astype(dt))
+
+    host_cols = {
+        "mi1": cat("measurement_index_1", np.uint32).view(np.int32),
+        "mi2": cat("measurement_index_2", np.uint32).view(np.int32),
+        "glob": cat("global", np.float32, (3,)),
+        "zvar": cat("z_variance", np.float32),
+        "rvar": cat("radius_variance", np.float32),
+        "lp": cat("local_position", np.float32, (2,)),
+        "sl": cat("surface_link", np.uint64).view(np.int64),
+    }
+    dev = torch.device("cuda", local)
+    pinned = {k: torch.from_numpy(v).pin_memory() for k, v in host_cols.items()}
+    dcols = {k: torch.empty_like(v, device=dev) for k, v in pinned.items()}
+    for k in dcols:
+        dcols[k].copy_(pinned[k])
+    f, g, fl, tp = seeding.default_configs()
+    bfield = (0.0, 0.0, float(f.bFieldInZ))
+    alg = seeding.TripletSeedingAlgorithm(f, g, fl)
+    est = seeding.SeedParameterEstimationAlgorithm(tp)
+    alg.reserve(n_ev, total)
+    alg.set_option(seeding.OPTION_KERNEL_TIMING, 1)
+
+    sps, meas, souts, pouts = [], [], [], []
+    size_all = torch.zeros(2 * n_ev, dtype=torch.int32, device=dev)
+    for e in range(n_ev):
+        a, b = int(offs[e]), int(offs[e + 1])
+        sps.append(seeding.SpacepointCollection(dcols["mi1"][a:b], dcols["mi2"][a:b],
+                                                dcols["glob"][a:b], dcols["zvar"][a:b],
+                                                dcols["rvar"][a:b]))
+        meas.append(seeding.MeasurementCollection(dcols["lp"][a:b], dcols["sl"][a:b]))
+        so = seeding.SeedBuffer(alg.max_seeds(b - a), device=dev)
+        so.size = size_all[e:e + 1]
+        po = seeding.ParamsBuffer(so.capacity, device=dev)
+        po.size = size_all[n_ev + e:n_ev + e + 1]
+        souts.append(so)
+        pouts.append(po)
+    stream = torch.cuda.current_stream()
+    flush_buf = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device=dev)
+
+    def step_device():
+        alg.run_batch(sps, souts, stream=stream)
+        for e in range(n_ev):
+            est(bfield, meas[e], sps[e], souts[e], pouts[e], stream=stream)
+
+    # host-side result buffers for the end-to-end path
+    h_sizes = torch.zeros(2 * n_ev, dtype=torch.int32).pin_memory()
+    h_seeds = [torch.empty((4, max(1, s.capacity)), dtype=torch.int32).pin_memory()
+               for s in souts]
+    h_params = [torch.empty(p.data.numel(), dtype=torch.uint8).pin_memory() for p in pouts]
+    h2d_bytes = sum(v.numel() * v.element_size() for v in pinned.values())
+
+    def step_e2e():
+        for k in dcols:
+            dcols[k].copy_(pinned[k], non_blocking=True)
+        step_device()
+        h_sizes.copy_(size_all, non_blocking=True)
+        stream.synchronize()
+        d2h = h_sizes.numel() * 4
+        for e in range(n_ev):
+            ns, npar = int(h_sizes[e]), int(h_sizes[n_ev + e])
+            so = souts[e]
+            for j, col in enumerate((so.bottom_index, so.middle_index, so.top_index)):
+                h_seeds[e][j, :ns].copy_(col[:ns], non_blocking=True)
+            h_seeds[e][3, :ns].copy_(so.quality[:ns].view(torch.int32), non_blocking=True)
+            nb = npar * seeding.PARAMS_DTYPE.itemsize
+            h_params[e][:nb].copy_(pouts[e].data[:nb], non_blocking=True)
+            d2h += 16 * ns + nb
+        return d2h
+
+    # -- warm-up (also checks the device status once)
+    for _ in range(max(3, args.warmup)):
+        step_device()
+    torch.cuda.synchronize()
+    st = alg.last_status(stream)
+    if st != seeding.OK:
+        raise RuntimeError(f"seeding status {st}")
+    counters = alg.counters()
+
+    # -- timed: device-resident inputs
+    sampler = ClockSampler(local)
+    kt_sum = {k: 0.0 for k in seeding.KERNEL_NAMES}
+    step_ms = []
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    torch.cuda.synchronize()
+    sampler.start()
+    wall0 = time.perf_counter()
+    for _ in range(args.steps):
+        flush_buf.fill_(1)
+        e0.record(stream)
+        step_device()
+        e1.record(stream)
+        e1.synchronize()
+        step_ms.append(e0.elapsed_time(e1))
+        for k, v in alg.kernel_times().items():
+            kt_sum[k] += v
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    barrier()
+    clocks = sampler.stop()
+    dev_s = sum(step_ms) / 1e3
+
+    # -- timed: end to end through the API from host buffers
+    e2e_ms, d2h_bytes = [], 0
+    for _ in range(max(1, args.warmup)):
+        step_e2e()
+    torch.cuda.synchronize()
+    barrier()
+    for _ in range(args.steps):
+        flush_buf.fill_(1)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e0.record(stream)
+        d2h_bytes = step_e2e()
+        e1.record(stream)
+        e1.synchronize()
+        e2e_ms.append(1e3 * (time.perf_counter() - t0))
+    barrier()
+    e2e_s = sum(e2e_ms) / 1e3
+
+    if world > 1:
+        t = torch.tensor([dev_s, e2e_s], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dev_s, e2e_s = float(t[0]), float(t[1])
+
+    value = world * n_ev * args.steps / dev_s
+    e2e_value = world * n_ev * args.steps / e2e_s
+
+    # roofline of the dominant kernel
+    dom = max(kt_sum, key=kt_sum.get)
+    dom_ms = kt_sum[dom] / args.steps
+    n_valid, n_seeds = counters["n_valid"], counters["n_seeds"]
+    # algorithmic bytes of seed_fast per launch: every valid spacepoint read
+    # once as a middle (x,y,z,r 16 B + its index 4 B), its seed count written
+    # (1 B), and per seed the slot (16 B) plus the two partner indices (8 B)
+    alg_bytes = {"seed_fast": 21 * n_valid + 24 * n_seeds,
+                 "bin_count": 20 * total + 4 * total,
+                 "bin_scatter": 20 * total + 4 * total + 28 * n_valid}
+    ab = alg_bytes.get(dom, 21 * n_valid + 24 * n_seeds)
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            peaks = json.load(fh)
+    except Exception:
+        pass
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    achieved = ab / (dom_ms * 1e-3) / 1e9
+    prof = load_profile_traffic(dom) or {}
+    roofline = {
+        "bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak,
+        "unit": "GB/s", "frac": achieved / hbm_peak,
+        "traffic": prof.get("dram_bytes_per_launch"),
+        "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else
+                       "fallback 6800 GB/s",
+        "avg_launch_ms": dom_ms,
+        "share": kt_sum[dom] / max(1e-12, sum(step_ms)),
+        "note": "seed_fast is issue-bound, not HBM-bound: see issue_roofline",
+    }
+    if prof.get("inst_issued_per_launch"):
+        sm_mhz = clocks.get("sm_mhz") or 1900.0
+        n_sm = torch.cuda.get_device_properties(dev).multi_processor_count
+        peak_issue = n_sm * 4 * sm_mhz * 1e6
+        ach_issue = prof["inst_issued_per_launch"] / (dom_ms * 1e-3)
+        roofline["issue_roofline"] = {
+            "achieved_warp_inst_per_s": ach_issue, "peak_warp_inst_per_s": peak_issue,
+            "frac": ach_issue / peak_issue,
+            "source": "warp instructions issued per launch from the ncu capture in "
+                      "profiles/, launch duration measured live, peak = SMs x 4 "
+                      "schedulers x median SM clock"}
+
+    kernels = {k: v / args.steps for k, v in kt_sum.items()}
+    line = {
+        "metric": METRIC, "value": value, "unit": "events/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * dev_s / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "impl": "seedgb",
+        "config": {"workload": WORKLOAD, "events_per_step": n_ev,
+                   "spacepoints_per_step": total, "parallelism": f"replicas{world}",
+                   "l2": "flushed between steps (256 MiB write)",
+                   "path": "plain (no learned filter)"},
+        "e2e": {"value": e2e_value, "unit": "events/s", "h2d_bytes_per_step": int(h2d_bytes),
+                "d2h_bytes_per_step": int(d2h_bytes),
+                "ms_per_step": e2e_s * 1e3 / args.steps},
+        "gpu_launches": len(seeding.KERNEL_NAMES) + n_ev,
+        "kernel_ms_per_step": kernels,
+        "wall_s_timed": wall,
+        "roofline": roofline,
+        "clocks": clocks,
+        "work": {"valid_spacepoints": n_valid, "seeds": n_seeds,
+                 "triplets": counters["n_triplets"],
+                 "overflow_middles": counters["n_overflow_middles"]},
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(events)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

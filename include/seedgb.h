@@ -245,10 +245,19 @@ typedef enum {
     /* 1: test every middle-bottom x middle-top doublet pair for triplets
      * instead of the cot(theta) window (verification of the window; the
      * results are identical, only slower). */
-    SEEDGB_OPTION_EXHAUSTIVE_TRIPLETS = 1
+    SEEDGB_OPTION_EXHAUSTIVE_TRIPLETS = 1,
+    /* 1: record CUDA events around every kernel of a run on the run's stream
+     * (read back with seedgb_seeding_kernel_times) */
+    SEEDGB_OPTION_KERNEL_TIMING = 2
 } seedgb_option;
 seedgb_status seedgb_seeding_set_option(seedgb_seeding* h, seedgb_option opt,
                                         int64_t value);
+
+/* Device durations (ms) of the kernels of the last run with
+ * SEEDGB_OPTION_KERNEL_TIMING on, in launch order: bin_count, bin_scan,
+ * bin_scatter, bin_rsort, seed_fast, seed_slow, seed_compact.  Waits for the
+ * last recorded event.  Returns SEEDGB_INVALID_ARGUMENT if timing was off. */
+seedgb_status seedgb_seeding_kernel_times(seedgb_seeding* h, float ms[7]);
 
 /* ------------------------------------------------------------------------ */
 /* Track parameter estimation                                                */

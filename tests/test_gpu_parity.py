@@ -88,8 +88,12 @@ def test_cfg2_event_matches_oracle():
     assert c["n_valid"] == stats["n_valid"]
 
 
-def test_window_equals_exhaustive():
-    ev = synth.workload_event("cfg1", 7)
-    _, _, a, _ = run_gpu(ev)
-    _, _, b, _ = run_gpu(ev, exhaustive=True)
+@pytest.mark.parametrize("name,seed", [("cfg1", 7), ("cfg2", 3), ("cfg2", 11)])
+def test_fast_paths_equal_exhaustive(name, seed):
+    """The cot(theta) window and the fast helix pre-check give exactly the
+    results of evaluating every pair with the reference arithmetic."""
+    ev = synth.workload_event(name, seed, n_tracks=12000 if name == "cfg2" else None)
+    _, _, a, sa = run_gpu(ev)
+    _, _, b, sb = run_gpu(ev, exhaustive=True)
+    assert sa == sb == seeding.OK
     assert np.array_equal(a.to_numpy(), b.to_numpy())

@@ -37,6 +37,9 @@ struct seedgb_seeding {
     uint32_t h_desc_cap = 0;
     cudaEvent_t staged = nullptr;
     unsigned long long h_counters[kNumCounters] = {};
+    bool timing = false;
+    bool timed_run = false;
+    cudaEvent_t tev[kNumKernels + 1] = {};
 };
 
 struct seedgb_params {
@@ -150,6 +153,9 @@ seedgb_status ensure_arena(seedgb_seeding* h, uint32_t n_events, uint64_t total_
     const size_t o_xyzr = take(sizeof(float4) * cs);
     const size_t o_var = take(sizeof(float2) * cs);
     const size_t o_idx = take(sizeof(uint32_t) * cs);
+    const size_t o_rs = take(sizeof(float4) * cs);
+    const size_t o_rsgp = take(sizeof(uint32_t) * cs);
+    const size_t o_uns = take(sizeof(uint8_t) * static_cast<size_t>(ce) * nb);
     const size_t o_items = take(sizeof(uint2) * ci);
     const size_t o_cnt = take(sizeof(uint8_t) * cs);
     const size_t o_slot = take(sizeof(SeedSlot) * cs * kMaxSeedsPerMiddle);
@@ -179,6 +185,9 @@ seedgb_status ensure_arena(seedgb_seeding* h, uint32_t n_events, uint64_t total_
     a.g_xyzr = reinterpret_cast<float4*>(base + o_xyzr);
     a.g_var = reinterpret_cast<float2*>(base + o_var);
     a.g_idx = reinterpret_cast<uint32_t*>(base + o_idx);
+    a.g_rs = reinterpret_cast<float4*>(base + o_rs);
+    a.g_rs_gp = reinterpret_cast<uint32_t*>(base + o_rsgp);
+    a.bin_unsorted = reinterpret_cast<uint8_t*>(base + o_uns);
     a.items = reinterpret_cast<uint2*>(base + o_items);
     a.seed_cnt = reinterpret_cast<uint8_t*>(base + o_cnt);
     a.seed_slot = reinterpret_cast<SeedSlot*>(base + o_slot);
@@ -237,17 +246,23 @@ seedgb_status seedgb_seeding_create(const seedgb_seedfinder_config* finder,
         delete h;
         return SEEDGB_CUDA_ERROR;
     }
-    h->tune.fast_warps = 8;
-    h->tune.middles_per_item = 32;
-    h->tune.nb_cap = 3072;
+    h->tune.fast_warps = 12;
+    h->tune.middles_per_item = 128;
+    h->tune.nb_cap = 2560;
     h->tune.ctas_per_sm = 1;
     if (const char* s = std::getenv("SEEDGB_TUNE")) {
         int w, m, nb, c;
-        if (std::sscanf(s, "%d,%d,%d,%d", &w, &m, &nb, &c) == 4 && w >= 1 && w <= 8 &&
+        if (std::sscanf(s, "%d,%d,%d,%d", &w, &m, &nb, &c) == 4 && w >= 1 && w <= 16 &&
             m >= 1 && m <= 4096 && nb >= 256 && nb <= 8192 && c >= 1 && c <= 8) {
             h->tune = TuneParams{w, m, nb, c};
         }
     }
+    const int mw = fast_kernel_max_warps(h->tune.nb_cap);
+    if (mw < 1) {
+        seedgb_seeding_destroy(h);
+        return SEEDGB_UNSUPPORTED;
+    }
+    h->tune.fast_warps = std::min(h->tune.fast_warps, mw);
     *out = h;
     return SEEDGB_OK;
 }
@@ -257,6 +272,8 @@ seedgb_status seedgb_seeding_destroy(seedgb_seeding* h) {
     if (h->arena) cudaFree(h->arena);
     if (h->h_desc) cudaFreeHost(h->h_desc);
     if (h->staged) cudaEventDestroy(h->staged);
+    for (auto& e : h->tev)
+        if (e) cudaEventDestroy(e);
     delete h;
     return SEEDGB_OK;
 }
@@ -324,7 +341,9 @@ seedgb_status seedgb_seeding_run_batch(seedgb_seeding* h, const seedgb_spacepoin
     if (err == cudaSuccess) err = cudaEventRecord(h->staged, s);
     if (err == cudaSuccess)
         err = cudaMemsetAsync(a.counters, 0, sizeof(unsigned long long) * kNumCounters, s);
-    if (err == cudaSuccess) err = launch_seeding(h->dc, a, h->tune, h->num_sms, s);
+    if (err == cudaSuccess)
+        err = launch_seeding(h->dc, a, h->tune, h->num_sms, s, h->timing ? h->tev : nullptr);
+    h->timed_run = h->timing && err == cudaSuccess;
     return cuda_status(err);
 }
 
@@ -396,8 +415,25 @@ seedgb_status seedgb_seeding_set_option(seedgb_seeding* h, seedgb_option opt, in
         case SEEDGB_OPTION_EXHAUSTIVE_TRIPLETS:
             h->dc.brute_force_triplets = value ? 1u : 0u;
             return SEEDGB_OK;
+        case SEEDGB_OPTION_KERNEL_TIMING:
+            if (value && !h->tev[0]) {
+                for (auto& e : h->tev)
+                    if (cudaEventCreate(&e) != cudaSuccess) return SEEDGB_CUDA_ERROR;
+            }
+            h->timing = value != 0;
+            return SEEDGB_OK;
     }
     return SEEDGB_INVALID_ARGUMENT;
+}
+
+seedgb_status seedgb_seeding_kernel_times(seedgb_seeding* h, float ms[7]) {
+    if (!h || !ms || !h->timed_run) return SEEDGB_INVALID_ARGUMENT;
+    if (cudaEventSynchronize(h->tev[kNumKernels]) != cudaSuccess) return SEEDGB_CUDA_ERROR;
+    for (int i = 0; i < kNumKernels; ++i) {
+        if (cudaEventElapsedTime(&ms[i], h->tev[i], h->tev[i + 1]) != cudaSuccess)
+            return SEEDGB_CUDA_ERROR;
+    }
+    return SEEDGB_OK;
 }
 
 seedgb_status seedgb_params_create(const seedgb_track_params_estimation_config* cfg,

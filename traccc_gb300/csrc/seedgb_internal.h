@@ -10,6 +10,9 @@
 //   g_xyzr      float4[total_sp]            binned x, y, z, r (r = sqrt(x^2+y^2))
 //   g_var       float2[total_sp]            binned z / radius variances
 //   g_idx       uint32[total_sp]            binned spacepoint index within its event
+//   g_rs        float4[total_sp]            each bin's spacepoints sorted by radius
+//   g_rs_gp     uint32[total_sp]            grid position of each g_rs entry
+//   bin_unsorted uint8[E][nbins]            bin too large to sort in shared memory
 //   items       uint2 [max_items]           (event, bin | chunk<<16) work items
 //   seed_cnt    uint8 [total_sp]            seeds per middle spacepoint
 //   seed_slot   SeedSlot[total_sp][KMAX]    seeds per middle, in final order
@@ -112,6 +115,9 @@ struct Arena {
     float4* g_xyzr;
     float2* g_var;
     uint32_t* g_idx;
+    float4* g_rs;           // [total_sp] every bin sorted by radius
+    uint32_t* g_rs_gp;      // [total_sp] grid position of each g_rs entry
+    uint8_t* bin_unsorted;  // [E][nbins] bin too large to sort
     uint2* items;
     uint8_t* seed_cnt;
     SeedSlot* seed_slot;
@@ -132,9 +138,11 @@ struct TuneParams {
 };
 
 // Kernel launchers (seedgb_kernels.cu).  All asynchronous on `stream`.
+// timing: nullptr, or kNumKernels+1 events recorded around the kernels.
+constexpr int kNumKernels = 7;
 cudaError_t launch_seeding(const DevConfig& cfg, const Arena& a,
                            const TuneParams& tp, int num_sms,
-                           cudaStream_t stream);
+                           cudaStream_t stream, cudaEvent_t* timing = nullptr);
 
 struct ParamsConfig {
     float initial_sigma[6];
@@ -150,5 +158,7 @@ cudaError_t launch_params(const ParamsConfig& cfg, const float bfield[3],
                           cudaStream_t stream);
 
 size_t fast_kernel_smem(const TuneParams& tp);
+// Most warps per CTA whose scratch fits next to an nb_cap staging buffer.
+int fast_kernel_max_warps(int nb_cap);
 
 }  // namespace seedgb

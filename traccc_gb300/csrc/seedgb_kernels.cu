@@ -20,6 +20,7 @@
 // bit-identical to the reference's host seeding.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cfloat>
 #include <cstdint>
 
@@ -110,7 +111,7 @@ __device__ __forceinline__ void z_range(const DevConfig& c, float z,
 __device__ uint32_t build_segments(const DevConfig& c, const uint32_t* bs,
                                    uint32_t pbin, uint32_t zlo, uint32_t zhi,
                                    uint32_t* seg_pos, uint32_t* seg_g,
-                                   uint32_t* nseg_out) {
+                                   uint32_t* nseg_out, uint32_t* seg_bin) {
     uint32_t phis[kMaxSegments];
     const uint32_t np = phi_zone(c, pbin, phis, kMaxSegments);
     const uint32_t nzz = zhi + 1u - zlo;  // zone length (may be 0)
@@ -121,6 +122,7 @@ __device__ uint32_t build_segments(const DevConfig& c, const uint32_t* bs,
             const uint32_t bin = phis[ip] + (zlo + iz) * c.phi_bins;
             seg_pos[ns] = pos;
             seg_g[ns] = bs[bin];
+            if (seg_bin) seg_bin[ns] = bin;
             pos += bs[bin + 1] - bs[bin];
             ++ns;
         }
@@ -384,11 +386,13 @@ __device__ __forceinline__ bool window_bottom(const DevConfig& c, const float4 m
     const float deltaR = m.w - o.w;
     const float cotTheta = m.z - o.z;
     const float zOrigin = m.z * deltaR - m.w * cotTheta;
-    return !((deltaR >= c.deltaRMax) || (deltaR <= c.deltaRMin) ||
-             (fabsf(cotTheta) >= c.cotThetaMax * deltaR) ||
-             (zOrigin <= c.collisionRegionMin * deltaR) ||
-             (zOrigin >= c.collisionRegionMax * deltaR) ||
-             fabsf(cotTheta) >= c.deltaZMax);
+    // the reference's short-circuit || over side-effect-free comparisons,
+    // evaluated without branches
+    return !((deltaR >= c.deltaRMax) | (deltaR <= c.deltaRMin) |
+             (fabsf(cotTheta) >= c.cotThetaMax * deltaR) |
+             (zOrigin <= c.collisionRegionMin * deltaR) |
+             (zOrigin >= c.collisionRegionMax * deltaR) |
+             (fabsf(cotTheta) >= c.deltaZMax));
 }
 
 // Same for isCompatible<top> (doublet_finding_helper.hpp:67-74).
@@ -397,11 +401,13 @@ __device__ __forceinline__ bool window_top(const DevConfig& c, const float4 m,
     const float deltaR = o.w - m.w;
     const float cotTheta = (o.z - m.z);
     const float zOrigin = m.z * deltaR - m.w * cotTheta;
-    return !((deltaR >= c.deltaRMax) || (deltaR <= c.deltaRMin) ||
-             (fabsf(cotTheta) >= c.cotThetaMax * deltaR) ||
-             (zOrigin <= c.collisionRegionMin * deltaR) ||
-             (zOrigin >= c.collisionRegionMax * deltaR) ||
-             fabsf(cotTheta) >= c.deltaZMax);
+    // the reference's short-circuit || over side-effect-free comparisons,
+    // evaluated without branches
+    return !((deltaR >= c.deltaRMax) | (deltaR <= c.deltaRMin) |
+             (fabsf(cotTheta) >= c.cotThetaMax * deltaR) |
+             (zOrigin <= c.collisionRegionMin * deltaR) |
+             (zOrigin >= c.collisionRegionMax * deltaR) |
+             (fabsf(cotTheta) >= c.deltaZMax));
 }
 
 // Second part of isCompatible: the minimum-helix-radius circle test
@@ -432,13 +438,50 @@ __device__ __forceinline__ bool helix_ok(const DevConfig& c, const float4 m,
                     (c.minHelixRadius - c.impactMax)));
 }
 
+// Fast evaluation of the same test.  The two circle centres are
+// mid +- sagitta * n with n = (|dy|, -sign(dy) dx) / |d| (the reference's
+// (cosCentralAngle, sinCentralAngle) written without the slope), so the
+// squared distances are evaluated with approximate reciprocal square roots.
+// Returns 1 (passes) or 0 (rejected) when the smaller squared distance is more
+// than 2e-4 relative away from the cut -- more than ten times the combined
+// rounding error of either evaluation (about 15 operations of 2^-22 relative
+// error each, amplified at most 2 (|mid| + R)^2 / (R - impactMax)^2 < 8 while
+// the chord midpoint lies inside the helix circle) -- and -1 when only the
+// exact evaluation can decide: near the cut, for a chord midpoint outside the
+// helix radius, and for degenerate chords (dx or dy zero or negligible,
+// sagitta undefined), where the reference's own arithmetic produces inf/NaN.
+__device__ __forceinline__ int helix_fast(const DevConfig& c, const float4 m,
+                                          const float4 o) {
+    const float dX = o.x - m.x, dY = o.y - m.y;
+    const float aX = fabsf(dX), aY = fabsf(dY);
+    const float d2 = dX * dX + dY * dY;
+    const float R2 = c.minHelixRadius * c.minHelixRadius;
+    const float s2 = R2 - 0.25f * d2;
+    if (!(aX > 1e-6f * aY) || !(aY > 1e-6f * aX) || !(s2 > 1e-3f * R2) ||
+        !(d2 > 1e-20f) || !(d2 < 1e30f))
+        return -1;
+    const float inv = rsqrtf(d2);
+    const float sag = s2 * rsqrtf(s2);
+    const float nX = aY * inv;
+    const float nY = (dY > 0.f ? -dX : dX) * inv;
+    const float midX = 0.5f * (m.x + o.x), midY = 0.5f * (m.y + o.y);
+    if (!(midX * midX + midY * midY < R2)) return -1;
+    const float p1X = midX + sag * nX, p1Y = midY + sag * nY;
+    const float p2X = midX - sag * nX, p2Y = midY - sag * nY;
+    const float mn = fminf(p1X * p1X + p1Y * p1Y, p2X * p2X + p2Y * p2Y);
+    const float lim = (c.minHelixRadius - c.impactMax) * (c.minHelixRadius - c.impactMax);
+    if (mn > lim * 1.0002f) return 1;
+    if (mn < lim * 0.9998f) return 0;
+    return -1;
+}
+
 // doublet_finding_helper::transform_coordinates, doublet_finding_helper.hpp:
-// 218-272.  vm/vo = (z_variance, radius_variance).
-__device__ __forceinline__ LinCircle lin_circle(bool top, const float4 m,
-                                                const float2 vm, const float4 o,
-                                                const float2 vo) {
-    const float cosPhiM = m.x / m.w;
-    const float sinPhiM = m.y / m.w;
+// 218-272, with the middle's cos/sin(phi) (x/r, y/r) computed once per middle
+// spacepoint.  vm/vo = (z_variance, radius_variance).
+__device__ __forceinline__ LinCircle lin_circle_cs(bool top, const float4 m,
+                                                   const float cosPhiM, const float sinPhiM,
+                                                   const float2 vm, const float4 o,
+                                                   const float2 vo) {
     const float deltaX = o.x - m.x;
     const float deltaY = o.y - m.y;
     const float deltaZ = o.z - m.z;
@@ -458,26 +501,33 @@ __device__ __forceinline__ LinCircle lin_circle(bool top, const float4 m,
     return l;
 }
 
-// triplet_finding_helper::isCompatible, triplet_finding_helper.hpp:42-133.
-__device__ __forceinline__ bool triplet_ok(const DevConfig& c, const float rM,
-                                           const float2 vm, const LinCircle& lb,
-                                           const float ltCot, const float ltIdr,
-                                           const float ltEr, const float ltU,
-                                           const float ltV, const float iSinTheta2,
-                                           const float scatteringInRegion2,
-                                           float& curvature, float& impact) {
-    const float error2 =
-        ltEr + lb.er + 2.f * (lb.cot * ltCot * vm.y + vm.x) * lb.idr * ltIdr;
-    float deltaCotTheta = lb.cot - ltCot;
+// triplet_finding_helper::isCompatible (triplet_finding_helper.hpp:42-133),
+// split in two exact stages, so that the candidates the
+// minimum-helix-diameter cut rejects (most of them) are dropped before the
+// costly remainder.  Stage 1 runs triplet_finding_helper.hpp:42-90 and returns
+// A and B; stage 2 runs the rest (:92-130) from A and B.  Together they make
+// the same decisions and produce the same curvature and impact parameter.
+__device__ __forceinline__ float triplet_error2(const float2 vm, const LinCircle& lb,
+                                                const float ltCot, const float ltIdr,
+                                                const float ltEr) {
+    return ltEr + lb.er + 2.f * (lb.cot * ltCot * vm.y + vm.x) * lb.idr * ltIdr;
+}
+
+__device__ __forceinline__ bool triplet_stage1(const DevConfig& c, const float2 vm,
+                                               const LinCircle& lb, const float ltCot,
+                                               const float ltIdr, const float ltEr,
+                                               const float ltU, const float ltV,
+                                               const float scatteringInRegion2,
+                                               float& A_out, float& B_out) {
+    const float error2 = triplet_error2(vm, lb, ltCot, ltIdr, ltEr);
+    const float deltaCotTheta = lb.cot - ltCot;
     const float deltaCotTheta2 = deltaCotTheta * deltaCotTheta;
-    float error = 0.f;
-    float dCotThetaMinusError2 = 0.f;
     if (deltaCotTheta2 - error2 > 0) {
-        deltaCotTheta = fabsf(deltaCotTheta);
-        error = sqrtf(error2);
-        dCotThetaMinusError2 =
-            deltaCotTheta2 + error2 - 2.f * deltaCotTheta * error;
-        if (dCotThetaMinusError2 > scatteringInRegion2) return false;
+        const float adct = fabsf(deltaCotTheta);
+        // sqrtf(+-0) = +-0: skip the square root of a zero error term
+        const float error = (error2 == 0.f) ? error2 : sqrtf(error2);
+        const float d = deltaCotTheta2 + error2 - 2.f * adct * error;
+        if (d > scatteringInRegion2) return false;
     }
     const float dU = ltU - lb.u;
     if (dU == 0.f) return false;
@@ -486,6 +536,19 @@ __device__ __forceinline__ bool triplet_ok(const DevConfig& c, const float rM,
     const float B = lb.v - A * lb.u;
     const float B2 = B * B;
     if (S2 < B2 * c.minHelixDiameter2) return false;
+    A_out = A;
+    B_out = B;
+    return true;
+}
+
+__device__ __forceinline__ bool triplet_stage2(const DevConfig& c, const float rM,
+                                               const float2 vm, const LinCircle& lb,
+                                               const float ltCot, const float ltIdr,
+                                               const float ltEr, const float iSinTheta2,
+                                               const float A, const float B,
+                                               float& curvature, float& impact) {
+    const float S2 = 1.f + A * A;
+    const float B2 = B * B;
     const float iHelixDiameter2 = B2 / S2;
     float pT2scatter = 4.f * iHelixDiameter2 * c.pT2perRadius;
     const float pT = c.pTPerHelixRadius * sqrtf(S2 / B2) / 2.f;
@@ -494,10 +557,15 @@ __device__ __forceinline__ bool triplet_ok(const DevConfig& c, const float rM,
         pT2scatter = pTscatter * pTscatter;
     }
     const float p2scatter = pT2scatter * iSinTheta2;
-    if ((deltaCotTheta2 - error2 > 0.f) &&
-        (dCotThetaMinusError2 >
-         p2scatter * c.sigmaScattering * c.sigmaScattering))
-        return false;
+    const float error2 = triplet_error2(vm, lb, ltCot, ltIdr, ltEr);
+    const float deltaCotTheta = lb.cot - ltCot;
+    const float deltaCotTheta2 = deltaCotTheta * deltaCotTheta;
+    if (deltaCotTheta2 - error2 > 0.f) {
+        const float adct = fabsf(deltaCotTheta);
+        const float error = (error2 == 0.f) ? error2 : sqrtf(error2);
+        const float d = deltaCotTheta2 + error2 - 2.f * adct * error;
+        if (d > p2scatter * c.sigmaScattering * c.sigmaScattering) return false;
+    }
     curvature = B / sqrtf(S2);
     impact = fabsf((A - B * rM) * rM);
     if (impact > c.impactMax) return false;
@@ -515,62 +583,171 @@ __device__ __forceinline__ bool better(float wa, float sa, uint32_t ka, float wb
 }
 
 // ---------------------------------------------------------------------------
+// Radius-sorted copy of every grid bin
+// ---------------------------------------------------------------------------
+
+constexpr int kSortCap = 4096;  // largest bin sorted in shared memory
+
+// One CTA per (event, bin): the bin's spacepoints sorted by radius (ties in
+// any order), with the grid position of each.  A bin larger than kSortCap is
+// flagged; middles whose neighbourhood holds such a bin take the
+// large-capacity path, which scans in host order.
+__global__ void __launch_bounds__(256) k_bin_rsort(DevConfig c, Arena a) {
+    __shared__ uint32_t key[kSortCap];
+    __shared__ uint32_t val[kSortCap];
+    const uint32_t e = blockIdx.x / c.nbins, b = blockIdx.x % c.nbins;
+    if (e >= a.n_events) return;
+    const uint32_t* bs = a.bin_start + static_cast<size_t>(e) * (c.nbins + 1);
+    const uint32_t g0 = bs[b], n = bs[b + 1] - g0;
+    if (threadIdx.x == 0) a.bin_unsorted[static_cast<size_t>(e) * c.nbins + b] = n > kSortCap;
+    if (n == 0 || n > kSortCap) return;
+    uint32_t P = 1;
+    while (P < n) P <<= 1;
+    for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) {
+        key[i] = i < n ? __float_as_uint(a.g_xyzr[g0 + i].w) : 0xffffffffu;
+        val[i] = g0 + i;
+    }
+    __syncthreads();
+    for (uint32_t k = 2; k <= P; k <<= 1) {
+        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+            for (uint32_t t = threadIdx.x; t < P / 2; t += blockDim.x) {
+                const uint32_t i = 2 * t - (t & (j - 1));
+                const uint32_t l = i + j;
+                const bool up = (i & k) == 0;
+                const uint32_t ki = key[i], kl = key[l];
+                if (up ? (ki > kl) : (ki < kl)) {
+                    key[i] = kl;
+                    key[l] = ki;
+                    const uint32_t v = val[i];
+                    val[i] = val[l];
+                    val[l] = v;
+                }
+            }
+            __syncthreads();
+        }
+    }
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+        a.g_rs[g0 + i] = a.g_xyzr[val[i]];
+        a.g_rs_gp[g0 + i] = val[i];
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Per-middle seeding routine
 // ---------------------------------------------------------------------------
 
-// Neighbourhood of a middle spacepoint: a concatenation of grid bins, either
-// staged in shared memory or read from the binned grid in global memory.
+constexpr uint32_t kFastSegs = 16;  // neighbourhood bins on the fast path
+
+// Neighbourhood of a middle spacepoint: the concatenation of its grid bins in
+// host order (phi zone outer, z zone inner).  "Host position" = position in
+// that concatenation.  The fast path stages every bin as a radius-sorted run
+// in shared memory (staged / staged_hp give the spacepoint and its host
+// position); the large-capacity path reads the grid in host order.
 struct NbView {
-    const float4* staged;    // nullptr: read from g_xyzr
+    const float4* staged;       // nullptr: host order from g_xyzr
+    const uint16_t* staged_hp;  // host position of each staged spacepoint
     const float4* g_xyzr;
-    const uint32_t* seg_pos; // [nseg + 1]
-    const uint32_t* seg_g;   // [nseg]
+    const uint32_t* seg_pos;    // [nseg + 1] host-position prefix
+    const uint32_t* seg_g;      // [nseg] first grid position of each bin
     uint32_t nseg;
     uint32_t size;
 
-    __device__ __forceinline__ uint32_t gpos(uint32_t p) const {
+    // host position -> grid position
+    __device__ __forceinline__ uint32_t gpos(uint32_t hp) const {
         uint32_t s = 0;
-        while (s + 1 < nseg && seg_pos[s + 1] <= p) ++s;
-        return seg_g[s] + (p - seg_pos[s]);
+        while (s + 1 < nseg && seg_pos[s + 1] <= hp) ++s;
+        return seg_g[s] + (hp - seg_pos[s]);
     }
     __device__ __forceinline__ float4 get(uint32_t p) const {
         return staged ? staged[p] : g_xyzr[gpos(p)];
     }
+    __device__ __forceinline__ uint32_t hpos(uint32_t p) const {
+        return staged ? staged_hp[p] : p;
+    }
 };
 
-template <int CAPB, int CAPT, int CAPLC>
+constexpr int kBuckets = 128;  // cot(theta) buckets of the middle-top doublets
+
+// A triplet of the middle spacepoint (before the compatible-seed weights).
+struct TripCand {
+    uint16_t tp;  // middle-top list index
+    uint16_t ib;  // middle-bottom list index
+    float curv;   // curvature
+    float w;      // weight: -impact * impactWeightFactor
+};
+
+// A candidate inside its doublet's cot window, with the doublet's lin_circle.
+struct Stage0Cand {
+    uint16_t tp, ib;  // middle-top / middle-bottom list indices
+    float cot, idr, er, u, v;
+};
+
+// A triplet candidate that passed stage 1, with what stage 2 needs of its
+// middle-bottom doublet.
+struct Stage1Cand {
+    uint16_t tp, ib;
+    float A, B;
+    float cot, idr, er, is2;  // lin_circle of the doublet, 1 + cot^2
+};
+
+template <int CAPB, int CAPT, int CAPLC, int CAPCT>
 struct WarpScratch {
-    float key[CAPLC];  // cot theta of the middle-top doublets, sorted
-    float idr[CAPLC], er[CAPLC], u[CAPLC], v[CAPLC];  // in list order
-    uint16_t perm[CAPLC];                              // sorted -> list index
+    // middle-top doublets in list order
+    float key[CAPLC];  // cot(theta)
+    float idr[CAPLC], er[CAPLC], u[CAPLC], v[CAPLC];
+    uint16_t hpt[CAPLC];  // host position of the top
+    uint16_t ppt[CAPLC];  // neighbourhood position of the top
+    uint16_t perm[CAPLC]; // bucket-sorted slot -> list index
+    uint32_t bstart[kBuckets + 1];
+    uint32_t bcur[kBuckets];
     uint16_t qb[CAPB];  // middle-bottom doublets (neighbourhood positions)
-    uint16_t qt[CAPT];  // middle-top doublets
+    union {
+        uint16_t qt[CAPT];  // middle-top doublets, until their lin_circles exist
+        struct {
+            Stage0Cand q0[96];  // in-window candidates awaiting stage 1
+            Stage1Cand q1[96];  // stage-1 survivors awaiting stage 2
+        } q;
+    };
+    TripCand ct[CAPCT];   // triplets of the middle
+    uint32_t skey[CAPCT]; // host-order sort key of the triplets
+    uint16_t sidx[CAPCT]; // sorted -> ct index
+    float wf[CAPCT];      // final weight in sorted order, -inf when cut
+    float ts[CAPCT];      // tie sum of the sort, sorted order
+    uint32_t bnd[4 * kFastSegs];        // radius windows per bin
+    uint32_t pre[2 * (kFastSegs + 1)];  // candidate prefix per bin
 };
 
-using FastScratch = WarpScratch<1024, 512, 256>;
-constexpr int kFastTcap = 8;
-using SlowScratch = WarpScratch<8192, 8192, 4096>;
-constexpr int kSlowTcap = 64;
+// shared memory per warp: fast ~20 KB, slow ~190 KB
+using FastScratch = WarpScratch<1024, 1024, 256, 256>;
+using SlowScratch = WarpScratch<8192, 8192, 4096, 2048>;
 
-// Keep the positions that pass `pred` (in order) in q[0..n).
-template <bool TOP>
+// Keep the positions whose doublet passes the minimum-helix-radius test, in
+// order, in q[0..n).  Two doublets per lane per iteration.
 __device__ __forceinline__ uint32_t helix_compact(const DevConfig& c, const NbView& nb,
                                                   const float4 m, uint16_t* q,
                                                   uint32_t n, uint32_t lane,
                                                   uint32_t lt) {
+    const bool exact = c.brute_force_triplets != 0;
     uint32_t w = 0;
-    for (uint32_t base = 0; base < n; base += 32) {
-        const uint32_t i = base + lane;
-        bool ok = false;
-        uint16_t p = 0;
-        if (i < n) {
-            p = q[i];
-            ok = helix_ok(c, m, nb.get(p));
-        }
+    for (uint32_t base = 0; base < n; base += 64) {
+        const uint32_t i0 = base + lane, i1 = base + 32 + lane;
+        bool ok0 = false, ok1 = false;
+        uint16_t p0 = 0, p1 = 0;
+        int f0 = 0, f1 = 0;
+        float4 o0 = m, o1 = m;
+        if (i0 < n) { p0 = q[i0]; o0 = nb.get(p0); f0 = exact ? -1 : helix_fast(c, m, o0); }
+        if (i1 < n) { p1 = q[i1]; o1 = nb.get(p1); f1 = exact ? -1 : helix_fast(c, m, o1); }
+        ok0 = f0 == 1;
+        ok1 = f1 == 1;
+        if (i0 < n && f0 < 0) ok0 = helix_ok(c, m, o0);
+        if (i1 < n && f1 < 0) ok1 = helix_ok(c, m, o1);
         __syncwarp();
-        const uint32_t mask = __ballot_sync(0xffffffffu, ok);
-        if (ok) q[w + __popc(mask & lt)] = p;
-        w += __popc(mask);
+        const uint32_t m0 = __ballot_sync(0xffffffffu, ok0);
+        const uint32_t m1 = __ballot_sync(0xffffffffu, ok1);
+        if (ok0) q[w + __popc(m0 & lt)] = p0;
+        w += __popc(m0);
+        if (ok1) q[w + __popc(m1 & lt)] = p1;
+        w += __popc(m1);
         __syncwarp();
     }
     return w;
@@ -581,17 +758,60 @@ struct MiddleResult {
     int status;  // 0 done, 1 needs the large-capacity path
 };
 
+// Append the positions passing the window cuts of one role to q (in order of
+// the flattened per-bin ranges).  Two candidates per lane per iteration.
+template <bool TOP>
+__device__ __forceinline__ uint32_t scan_runs(const DevConfig& c, const NbView& nb,
+                                              const float4 M, const uint32_t* bnd,
+                                              const uint32_t* pre, uint32_t ns,
+                                              uint16_t* q, uint32_t cap, uint32_t lane,
+                                              uint32_t lt) {
+    const uint32_t total = pre[ns];
+    uint32_t nq = 0;
+    for (uint32_t base = 0; base < total; base += 64) {
+        bool ok[2] = {false, false};
+        uint32_t p[2] = {0, 0};
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const uint32_t f = base + 32 * h + lane;
+            if (f < total) {
+                uint32_t s = 0;
+                while (s + 1 < ns && pre[s + 1] <= f) ++s;
+                p[h] = bnd[4 * s + (TOP ? 2 : 0)] + (f - pre[s]);
+                const float4 o = nb.staged[p[h]];
+                ok[h] = TOP ? window_top(c, M, o) : window_bottom(c, M, o);
+            }
+        }
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const uint32_t mask = __ballot_sync(0xffffffffu, ok[h]);
+            if (ok[h]) {
+                const uint32_t k = nq + __popc(mask & lt);
+                if (k < cap) q[k] = static_cast<uint16_t>(p[h]);
+            }
+            nq += __popc(mask);
+        }
+    }
+    return nq;
+}
+
+__device__ __forceinline__ uint32_t cot_bucket(float x, float cmin, float scale) {
+    const int b = static_cast<int>((x - cmin) * scale);
+    return static_cast<uint32_t>(b < 0 ? 0 : (b >= kBuckets ? kBuckets - 1 : b));
+}
+
 // Seeds of one middle spacepoint, following host seed_finding::operator()
 // (core/src/seeding/seed_finding.cpp:69-118) with triplet_finding
 // (triplet_finding.hpp:60-183) and seed_filtering (seed_filtering.cpp:28-123).
-// Executed by one full warp.
-template <int CAPB, int CAPT, int CAPLC, int TCAP>
+// Executed by one full warp.  The order-dependent steps (compatible-seed
+// weights, ties of the final sort) use host positions, so the result does not
+// depend on the order in which doublets are found.
+template <bool RSORTED, int CAPB, int CAPT, int CAPLC, int CAPCT>
 __device__ MiddleResult process_middle(const DevConfig& c, const Arena& a,
                                        const NbView& nb, const uint32_t gm,
                                        const bool any_var, const bool check_r,
                                        const float nb_minr, const float nb_maxr,
-                                       WarpScratch<CAPB, CAPT, CAPLC>& ws) {
-    constexpr int kUnroll = TCAP <= 8 ? TCAP : 1;
+                                       WarpScratch<CAPB, CAPT, CAPLC, CAPCT>& ws) {
     MiddleResult res{0, 0, 0, 0};
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t lt = lanemask_lt();
@@ -611,34 +831,79 @@ __device__ MiddleResult process_middle(const DevConfig& c, const Arena& a,
         }
     }
 
-    // -- doublets: window cuts with ballot compaction, in neighbourhood order
+    // -- doublets: window cuts with ballot compaction
     uint32_t nqb = 0, nqt = 0;
-    for (uint32_t base = 0; base < nb.size; base += 32) {
-        const uint32_t p = base + lane;
-        bool pb = false, pt = false;
-        if (p < nb.size) {
-            const float4 o = nb.get(p);
-            pb = window_bottom(c, M, o);
-            pt = window_top(c, M, o);
+    if constexpr (RSORTED) {
+        // Exact radial windows per radius-sorted bin: deltaR = fl(rM - r)
+        // (bottom) is non-increasing and fl(r - rM) (top) non-decreasing in r,
+        // so the spacepoints with deltaRMin < deltaR < deltaRMax form one
+        // contiguous range of each run, found by binary search on the same
+        // float expressions the cut evaluates.
+        const uint32_t ns = nb.nseg;
+        for (uint32_t i = lane; i < 4 * ns; i += 32) {
+            const uint32_t s = i >> 2, k = i & 3;
+            uint32_t lo = nb.seg_pos[s], hi = nb.seg_pos[s + 1];
+            while (lo < hi) {
+                const uint32_t mid = (lo + hi) >> 1;
+                const float r = nb.staged[mid].w;
+                const float d = (k < 2) ? (M.w - r) : (r - M.w);
+                const bool pr = (k == 0) ? (d < c.deltaRMax)
+                              : (k == 1) ? (d <= c.deltaRMin)
+                              : (k == 2) ? (d > c.deltaRMin)
+                                         : (d >= c.deltaRMax);
+                if (pr) hi = mid; else lo = mid + 1;
+            }
+            ws.bnd[i] = lo;
         }
-        const uint32_t mb = __ballot_sync(0xffffffffu, pb);
-        const uint32_t mt = __ballot_sync(0xffffffffu, pt);
-        if (pb) {
-            const uint32_t k = nqb + __popc(mb & lt);
-            if (k < CAPB) ws.qb[k] = static_cast<uint16_t>(p);
+        __syncwarp();
+        if (lane == 0) {
+            uint32_t ab = 0, at = 0;
+            for (uint32_t s = 0; s < ns; ++s) {
+                ws.pre[s] = ab;
+                ws.pre[kFastSegs + 1 + s] = at;
+                const uint32_t b0 = ws.bnd[4 * s], b1 = ws.bnd[4 * s + 1];
+                const uint32_t t0 = ws.bnd[4 * s + 2], t1 = ws.bnd[4 * s + 3];
+                ab += b1 > b0 ? b1 - b0 : 0u;
+                at += t1 > t0 ? t1 - t0 : 0u;
+            }
+            ws.pre[ns] = ab;
+            ws.pre[kFastSegs + 1 + ns] = at;
         }
-        if (pt) {
-            const uint32_t k = nqt + __popc(mt & lt);
-            if (k < CAPT) ws.qt[k] = static_cast<uint16_t>(p);
+        __syncwarp();
+        if (ws.pre[ns] == 0 || ws.pre[kFastSegs + 1 + ns] == 0) {
+            if (lane == 0) a.seed_cnt[gm] = 0;
+            return res;
         }
-        nqb += __popc(mb);
-        nqt += __popc(mt);
+        nqb = scan_runs<false>(c, nb, M, ws.bnd, ws.pre, ns, ws.qb, CAPB, lane, lt);
+        nqt = scan_runs<true>(c, nb, M, ws.bnd, ws.pre + kFastSegs + 1, ns, ws.qt, CAPT,
+                              lane, lt);
+    } else {
+        for (uint32_t base = 0; base < nb.size; base += 32) {
+            const uint32_t p = base + lane;
+            bool pb = false, pt = false;
+            if (p < nb.size) {
+                const float4 o = nb.get(p);
+                pb = window_bottom(c, M, o);
+                pt = window_top(c, M, o);
+            }
+            const uint32_t mb = __ballot_sync(0xffffffffu, pb);
+            const uint32_t mt = __ballot_sync(0xffffffffu, pt);
+            if (pb) {
+                const uint32_t k = nqb + __popc(mb & lt);
+                if (k < CAPB) ws.qb[k] = static_cast<uint16_t>(p);
+            }
+            if (pt) {
+                const uint32_t k = nqt + __popc(mt & lt);
+                if (k < CAPT) ws.qt[k] = static_cast<uint16_t>(p);
+            }
+            nqb += __popc(mb);
+            nqt += __popc(mt);
+        }
     }
     if (nqb > CAPB || nqt > CAPT) { res.status = 1; return res; }
     __syncwarp();
-    const uint32_t n_mb = nqb ? helix_compact<false>(c, nb, M, ws.qb, nqb, lane, lt) : 0u;
-    const uint32_t n_mt =
-        (n_mb && nqt) ? helix_compact<true>(c, nb, M, ws.qt, nqt, lane, lt) : 0u;
+    const uint32_t n_mb = nqb ? helix_compact(c, nb, M, ws.qb, nqb, lane, lt) : 0u;
+    const uint32_t n_mt = (n_mb && nqt) ? helix_compact(c, nb, M, ws.qt, nqt, lane, lt) : 0u;
     res.n_mb = n_mb;
     res.n_mt = n_mt;
     if (n_mb == 0 || n_mt == 0) {
@@ -647,275 +912,380 @@ __device__ MiddleResult process_middle(const DevConfig& c, const Arena& a,
     }
     if (n_mt > CAPLC) { res.status = 1; return res; }
 
-    // -- middle-top lin_circles, sorted by cot(theta)
+    // -- middle-top lin_circles (list order) and a counting sort by cot(theta)
+    const float cosPhiM = M.x / M.w, sinPhiM = M.y / M.w;
     float maxEr = 0.f, minEr = 0.f, maxCot = 0.f, maxIdr = 0.f;
+    float cmin = __int_as_float(0x7f800000), cmax = -__int_as_float(0x7f800000);
     for (uint32_t i = lane; i < n_mt; i += 32) {
         const uint32_t p = ws.qt[i];
-        const float2 vo = any_var ? a.g_var[nb.gpos(p)] : make_float2(0.f, 0.f);
-        const LinCircle l = lin_circle(true, M, vM, nb.get(p), vo);
+        const uint32_t hp = nb.hpos(p);
+        const float2 vo = any_var ? a.g_var[nb.gpos(hp)] : make_float2(0.f, 0.f);
+        const LinCircle l = lin_circle_cs(true, M, cosPhiM, sinPhiM, vM, nb.get(p), vo);
         ws.key[i] = l.cot;
         ws.idr[i] = l.idr;
         ws.er[i] = l.er;
         ws.u[i] = l.u;
         ws.v[i] = l.v;
-        ws.perm[i] = static_cast<uint16_t>(i);
+        ws.hpt[i] = static_cast<uint16_t>(hp);
+        ws.ppt[i] = static_cast<uint16_t>(p);
         maxEr = fmaxf(maxEr, l.er);
         minEr = fminf(minEr, l.er);
         maxCot = fmaxf(maxCot, fabsf(l.cot));
         maxIdr = fmaxf(maxIdr, l.idr);
+        cmin = fminf(cmin, l.cot);
+        cmax = fmaxf(cmax, l.cot);
         if (!(l.er == l.er)) minEr = -1.f;  // NaN error term: no window
     }
-    uint32_t P = 1;
-    while (P < n_mt) P <<= 1;
-    for (uint32_t i = n_mt + lane; i < P; i += 32) {
-        ws.key[i] = __int_as_float(0x7f800000);
-        ws.perm[i] = 0xffff;
-    }
-    __syncwarp();
-    for (uint32_t k = 2; k <= P; k <<= 1) {
-        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
-            for (uint32_t t = lane; t < P / 2; t += 32) {
-                const uint32_t i = 2 * t - (t & (j - 1));
-                const uint32_t l = i + j;
-                const bool up = (i & k) == 0;
-                const float ki = ws.key[i], kl = ws.key[l];
-                if (up ? (ki > kl) : (ki < kl)) {
-                    ws.key[i] = kl;
-                    ws.key[l] = ki;
-                    const uint16_t pi = ws.perm[i];
-                    ws.perm[i] = ws.perm[l];
-                    ws.perm[l] = pi;
-                }
-            }
-            __syncwarp();
-        }
-    }
-    if (any_var) {
-        for (int o = 16; o > 0; o >>= 1) {
+    for (uint32_t b = lane; b <= kBuckets; b += 32) ws.bstart[b] = 0;
+    for (int o = 16; o > 0; o >>= 1) {
+        cmin = fminf(cmin, __shfl_xor_sync(0xffffffffu, cmin, o));
+        cmax = fmaxf(cmax, __shfl_xor_sync(0xffffffffu, cmax, o));
+        if (any_var) {
             maxEr = fmaxf(maxEr, __shfl_xor_sync(0xffffffffu, maxEr, o));
             minEr = fminf(minEr, __shfl_xor_sync(0xffffffffu, minEr, o));
             maxCot = fmaxf(maxCot, __shfl_xor_sync(0xffffffffu, maxCot, o));
             maxIdr = fmaxf(maxIdr, __shfl_xor_sync(0xffffffffu, maxIdr, o));
         }
     }
-
-    // -- triplets per middle-bottom doublet, weights, lane-local best seeds
-    const uint32_t K = min(c.maxSeedsPerSpM, static_cast<uint32_t>(kMaxSeedsPerMiddle));
-    float bw[kMaxSeedsPerMiddle], bs[kMaxSeedsPerMiddle];
-    uint32_t bk[kMaxSeedsPerMiddle], bp[kMaxSeedsPerMiddle];
+    const float scale = (cmax > cmin) ? static_cast<float>(kBuckets) / (cmax - cmin) : 0.f;
+    __syncwarp();
+    for (uint32_t i = lane; i < n_mt; i += 32)
+        atomicAdd(&ws.bstart[cot_bucket(ws.key[i], cmin, scale) + 1], 1u);
+    __syncwarp();
+    {
+        // exclusive prefix over the buckets, four per lane
+        constexpr int kPer = kBuckets / 32;
+        uint32_t v[kPer], sum = 0;
 #pragma unroll
-    for (int k = 0; k < kMaxSeedsPerMiddle; ++k) {
-        bw[k] = -__int_as_float(0x7f800000);
-        bs[k] = 0.f;
-        bk[k] = 0xffffffffu;
-        bp[k] = 0;
+        for (int j = 0; j < kPer; ++j) { v[j] = ws.bstart[kPer * lane + j + 1]; sum += v[j]; }
+        uint32_t incl = sum;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= static_cast<uint32_t>(o)) incl += t;
+        }
+        __syncwarp();
+        uint32_t run = incl - sum;
+#pragma unroll
+        for (int j = 0; j < kPer; ++j) {
+            ws.bcur[kPer * lane + j] = run;
+            run += v[j];
+            ws.bstart[kPer * lane + j + 1] = run;
+        }
     }
-    uint32_t bn = 0;
-    bool lane_ovf = false;
-    uint32_t n_trip = 0;
+    __syncwarp();
+    for (uint32_t i = lane; i < n_mt; i += 32) {
+        const uint32_t slot = atomicAdd(&ws.bcur[cot_bucket(ws.key[i], cmin, scale)], 1u);
+        ws.perm[slot] = static_cast<uint16_t>(i);
+    }
+    __syncwarp();
+
+    // -- triplets.  The middle-bottom doublets are set up 32 at a time (one
+    //    per lane); each lane walks the middle-top doublets of its cot
+    //    buckets and queues those inside its exact cot window (q0, with the
+    //    doublet's lin_circle); stage 1 runs on 64 queued candidates at a
+    //    time, stage 2 on 32 stage-1 survivors at a time, so both run with
+    //    full lanes across doublets and chunks.
     const float sig2 = c.sigmaScattering * c.sigmaScattering;
+    uint32_t n_ct = 0, n0 = 0, n1 = 0;
+    uint32_t c0 = 0, it = 0, maxc = 0;
+    bool have_chunk = false;
+    LinCircle lbm;
+    lbm.Zo = 0.f;
+    float klo = 0.f, khi = 0.f;
+    uint32_t lo = 0, cnt = 0;
+    for (;;) {
+        if (!have_chunk && c0 < n_mb) {
+            const uint32_t ib = c0 + lane;
+            cnt = 0;
+            if (ib < n_mb) {
+                const uint32_t pB = ws.qb[ib];
+                const float4 B = nb.get(pB);
+                const float2 vB =
+                    any_var ? a.g_var[nb.gpos(nb.hpos(pB))] : make_float2(0.f, 0.f);
+                lbm = lin_circle_cs(false, M, cosPhiM, sinPhiM, vM, B, vB);
+                // triplet_finding.hpp:82-88
+                const float iSinTheta2 = 1.f + lbm.cot * lbm.cot;
+                float scatteringInRegion2 = c.maxScatteringAngle2 * iSinTheta2;
+                scatteringInRegion2 *= sig2;
+                // Window in cot(theta): a middle-top doublet outside it fails
+                // the reference's first scattering test for any rounding (1 %
+                // relative and 1e-5 absolute margins), so only doublets inside
+                // are tested.
+                float W;
+                if (c.brute_force_triplets) {
+                    W = __int_as_float(0x7f800000);
+                } else if (!any_var) {
+                    W = sqrtf(scatteringInRegion2) * 1.01f + 1e-5f * (1.f + fabsf(lbm.cot));
+                } else {
+                    const float e2 =
+                        (maxEr + lbm.er +
+                         2.f * (fabsf(lbm.cot) * maxCot * fabsf(vM.y) + fabsf(vM.x)) *
+                             lbm.idr * maxIdr) * 1.001f;
+                    const bool ok = (minEr >= 0.f) && (lbm.er >= 0.f) && (vM.x >= 0.f) &&
+                                    (vM.y >= 0.f) && (e2 >= 0.f) && (e2 < 3.0e38f);
+                    W = ok ? (sqrtf(scatteringInRegion2) + sqrtf(e2)) * 1.01f +
+                                 1e-5f * (1.f + fabsf(lbm.cot))
+                           : __int_as_float(0x7f800000);
+                }
+                klo = lbm.cot - W;
+                khi = lbm.cot + W;
+                lo = ws.bstart[cot_bucket(klo, cmin, scale)];
+                cnt = ws.bstart[cot_bucket(khi, cmin, scale) + 1] - lo;
+            }
+            maxc = cnt;
+            for (int o = 16; o > 0; o >>= 1) maxc = max(maxc, __shfl_xor_sync(0xffffffffu, maxc, o));
+            it = 0;
+            have_chunk = true;
+        }
+        if (have_chunk) {
+            while (it < maxc && n0 < 64) {
+                bool ok = false;
+                uint32_t tp = 0;
+                if (it < cnt) {
+                    tp = ws.perm[lo + it];
+                    const float kt = ws.key[tp];
+                    ok = kt >= klo && kt <= khi;
+                }
+                const uint32_t mask = __ballot_sync(0xffffffffu, ok);
+                if (ok) {
+                    Stage0Cand e;
+                    e.tp = static_cast<uint16_t>(tp);
+                    e.ib = static_cast<uint16_t>(c0 + lane);
+                    e.cot = lbm.cot;
+                    e.idr = lbm.idr;
+                    e.er = lbm.er;
+                    e.u = lbm.u;
+                    e.v = lbm.v;
+                    ws.q.q0[n0 + __popc(mask & lt)] = e;
+                }
+                n0 += __popc(mask);
+                ++it;
+            }
+            if (it >= maxc) {
+                have_chunk = false;
+                c0 += 32;
+            }
+        }
+        __syncwarp();
+        const bool more = have_chunk || c0 < n_mb;
+        if (n0 >= 64 || (!more && n0 > 0)) {
+            // stage 1 on q0[0..k), survivors to q1
+            const uint32_t k1 = min(n0, 64u);
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const uint32_t i = lane + 32 * h;
+                bool ok = false;
+                Stage1Cand s1;
+                if (i < k1) {
+                    const Stage0Cand e = ws.q.q0[i];
+                    LinCircle lb;
+                    lb.cot = e.cot;
+                    lb.idr = e.idr;
+                    lb.er = e.er;
+                    lb.u = e.u;
+                    lb.v = e.v;
+                    lb.Zo = 0.f;
+                    const float iSinTheta2 = 1.f + lb.cot * lb.cot;
+                    float scatteringInRegion2 = c.maxScatteringAngle2 * iSinTheta2;
+                    scatteringInRegion2 *= sig2;
+                    ok = triplet_stage1(c, vM, lb, ws.key[e.tp], ws.idr[e.tp], ws.er[e.tp],
+                                        ws.u[e.tp], ws.v[e.tp], scatteringInRegion2, s1.A,
+                                        s1.B);
+                    s1.tp = e.tp;
+                    s1.ib = e.ib;
+                    s1.cot = e.cot;
+                    s1.idr = e.idr;
+                    s1.er = e.er;
+                    s1.is2 = iSinTheta2;
+                }
+                const uint32_t mask = __ballot_sync(0xffffffffu, ok);
+                if (ok) ws.q.q1[n1 + __popc(mask & lt)] = s1;
+                n1 += __popc(mask);
+            }
+            // move the unprocessed tail of q0 (< 32 entries) to the front
+            const uint32_t rest = n0 - k1;
+            Stage0Cand t;
+            if (lane < rest) t = ws.q.q0[k1 + lane];
+            __syncwarp();
+            if (lane < rest) ws.q.q0[lane] = t;
+            n0 = rest;
+            __syncwarp();
+        }
+        while (n1 >= 32 || (!more && n0 == 0 && n1 > 0)) {
+            // stage 2 on q1[0..k), triplets to ct
+            const uint32_t k2 = min(n1, 32u);
+            bool ok = false;
+            TripCand t;
+            if (lane < k2) {
+                const Stage1Cand e = ws.q.q1[lane];
+                LinCircle lb;
+                lb.cot = e.cot;
+                lb.idr = e.idr;
+                lb.er = e.er;
+                lb.u = lb.v = lb.Zo = 0.f;
+                float curv = 0.f, imp = 0.f;
+                ok = triplet_stage2(c, M.w, vM, lb, ws.key[e.tp], ws.idr[e.tp], ws.er[e.tp],
+                                    e.is2, e.A, e.B, curv, imp);
+                t.tp = e.tp;
+                t.ib = e.ib;
+                t.curv = curv;
+                t.w = -imp * c.impactWeightFactor;
+            }
+            const uint32_t mask = __ballot_sync(0xffffffffu, ok);
+            if (ok) {
+                const uint32_t k = n_ct + __popc(mask & lt);
+                if (k < CAPCT) ws.ct[k] = t;
+            }
+            n_ct += __popc(mask);
+            const uint32_t rest = n1 - k2;
+            Stage1Cand t0, t1;
+            if (lane < rest) t0 = ws.q.q1[k2 + lane];
+            if (lane + 32 < rest) t1 = ws.q.q1[k2 + lane + 32];
+            __syncwarp();
+            if (lane < rest) ws.q.q1[lane] = t0;
+            if (lane + 32 < rest) ws.q.q1[lane + 32] = t1;
+            n1 = rest;
+            __syncwarp();
+        }
+        if (!more && n0 == 0 && n1 == 0) break;
+    }
+    if (n_ct > CAPCT) { res.status = 1; return res; }
+    res.n_trip = n_ct;
 
-    for (uint32_t ib = lane; ib < n_mb && !lane_ovf; ib += 32) {
-        const uint32_t pB = ws.qb[ib];
-        const float4 B = nb.get(pB);
-        const float2 vB = any_var ? a.g_var[nb.gpos(pB)] : make_float2(0.f, 0.f);
-        const LinCircle lb = lin_circle(false, M, vM, B, vB);
-        // triplet_finding.hpp:82-88
-        const float iSinTheta2 = 1.f + lb.cot * lb.cot;
-        float scatteringInRegion2 = c.maxScatteringAngle2 * iSinTheta2;
-        scatteringInRegion2 *= sig2;
-
-        // Window in cot(theta): a middle-top doublet outside it fails the
-        // reference's first scattering test for any rounding (1 % relative
-        // and 1e-5 absolute margins), so only doublets inside are tested.
-        float W;
-        if (c.brute_force_triplets) {
-            W = __int_as_float(0x7f800000);
-        } else if (!any_var) {
-            W = sqrtf(scatteringInRegion2) * 1.01f + 1e-5f * (1.f + fabsf(lb.cot));
-        } else {
-            const float e2 = (maxEr + lb.er +
-                              2.f * (fabsf(lb.cot) * maxCot * fabsf(vM.y) + fabsf(vM.x)) *
-                                  lb.idr * maxIdr) * 1.001f;
-            const bool ok = (minEr >= 0.f) && (lb.er >= 0.f) && (vM.x >= 0.f) &&
-                            (vM.y >= 0.f) && (e2 >= 0.f) && (e2 < 3.0e38f);
-            W = ok ? (sqrtf(scatteringInRegion2) + sqrtf(e2)) * 1.01f +
-                         1e-5f * (1.f + fabsf(lb.cot))
-                   : __int_as_float(0x7f800000);
+    // -- the middle's triplets in host order: (bottom host position, top
+    //    host position) ascending, so the triplets of one middle-bottom
+    //    doublet form a run ordered as triplet_finding.hpp:109-179 visits them
+    {
+        uint32_t P = 1;
+        while (P < n_ct) P <<= 1;
+        for (uint32_t i = lane; i < P; i += 32) {
+            ws.skey[i] = i < n_ct ? ((static_cast<uint32_t>(ws.ct[i].ib) << 16) |
+                                     ws.hpt[ws.ct[i].tp])
+                                  : 0xffffffffu;
+            ws.sidx[i] = static_cast<uint16_t>(i);
         }
-        const float klo = lb.cot - W, khi = lb.cot + W;
-        uint32_t lo = 0, hi = n_mt;
-        while (lo < hi) {
-            const uint32_t mid = (lo + hi) >> 1;
-            if (ws.key[mid] < klo) lo = mid + 1; else hi = mid;
-        }
-        // candidate triplets of this middle-bottom doublet (list order later)
-        uint32_t tt[TCAP];
-        float tcv[TCAP], twt[TCAP];
-        uint32_t nt = 0;
-        for (uint32_t s = lo; s < n_mt && ws.key[s] <= khi; ++s) {
-            const uint32_t tp = ws.perm[s];
-            float curvature, impact;
-            if (!triplet_ok(c, M.w, vM, lb, ws.key[s], ws.idr[tp], ws.er[tp],
-                            ws.u[tp], ws.v[tp], iSinTheta2, scatteringInRegion2,
-                            curvature, impact))
-                continue;
-            if (nt == TCAP) { lane_ovf = true; break; }
-#pragma unroll kUnroll
-            for (int k = 0; k < TCAP; ++k) {
-                if (k == static_cast<int>(nt)) {
-                    tt[k] = tp;
-                    tcv[k] = curvature;
-                    twt[k] = -impact * c.impactWeightFactor;
-                }
-            }
-            ++nt;
-        }
-        if (lane_ovf || nt == 0) continue;
-        n_trip += nt;
-        // host order of the triplets of this doublet: middle-top list order
-        if (nt > 1) {
-#pragma unroll kUnroll
-            for (int pass = 0; pass < TCAP - 1; ++pass) {
-#pragma unroll kUnroll
-                for (int k = 0; k + 1 < TCAP; ++k) {
-                    if (k + 1 < static_cast<int>(nt) && tt[k] > tt[k + 1]) {
-                        const uint32_t a0 = tt[k]; tt[k] = tt[k + 1]; tt[k + 1] = a0;
-                        const float c0 = tcv[k]; tcv[k] = tcv[k + 1]; tcv[k + 1] = c0;
-                        const float w0 = twt[k]; twt[k] = twt[k + 1]; twt[k + 1] = w0;
+        __syncwarp();
+        for (uint32_t k = 2; k <= P; k <<= 1) {
+            for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+                for (uint32_t t = lane; t < P / 2; t += 32) {
+                    const uint32_t i = 2 * t - (t & (j - 1));
+                    const uint32_t l = i + j;
+                    const bool up = (i & k) == 0;
+                    const uint32_t ki = ws.skey[i], kl = ws.skey[l];
+                    if (up ? (ki > kl) : (ki < kl)) {
+                        ws.skey[i] = kl;
+                        ws.skey[l] = ki;
+                        const uint16_t x = ws.sidx[i];
+                        ws.sidx[i] = ws.sidx[l];
+                        ws.sidx[l] = x;
                     }
                 }
-            }
-        }
-        float trT[TCAP];
-#pragma unroll kUnroll
-        for (int k = 0; k < TCAP; ++k)
-            trT[k] = (k < static_cast<int>(nt)) ? nb.get(ws.qt[tt[k]]).w : 0.f;
-        // compatible-seed weights, triplet_finding.hpp:107-179
-        if (nt > 1) {
-#pragma unroll kUnroll
-            for (int i = 0; i < TCAP; ++i) {
-                if (i >= static_cast<int>(nt)) break;
-                const float currentTop_r = trT[i];
-                const float lowerLimitCurv = tcv[i] - c.deltaInvHelixDiameter;
-                const float upperLimitCurv = tcv[i] + c.deltaInvHelixDiameter;
-                float compR[8];
-                uint32_t ncr = 0;
-                float w = twt[i];
-                for (int j = 0; j < TCAP; ++j) {
-                    if (j >= static_cast<int>(nt)) break;
-                    if (i == j) continue;
-                    const float otherTop_r = trT[j];
-                    const float deltaR = currentTop_r - otherTop_r;
-                    if (fabsf(deltaR) < c.filterDeltaRMin) continue;
-                    if (tcv[j] < lowerLimitCurv) continue;
-                    if (tcv[j] > upperLimitCurv) continue;
-                    bool newCompSeed = true;
-                    for (uint32_t q = 0; q < ncr; ++q) {
-                        if (fabsf(compR[q] - otherTop_r) < c.filterDeltaRMin) {
-                            newCompSeed = false;
-                            break;
-                        }
-                    }
-                    if (newCompSeed) {
-                        if (ncr < 8) compR[ncr] = otherTop_r;
-                        ++ncr;
-                        w += c.compatSeedWeight;
-                    }
-                    if (ncr >= c.compatSeedLimit) break;
-                }
-                twt[i] = w;
-            }
-        }
-        // seed_selecting_helper::seed_weight / single_seed_cut
-        // (seed_selecting_helper.hpp:27-62), then the per-lane best list
-#pragma unroll kUnroll
-        for (int i = 0; i < TCAP; ++i) {
-            if (i >= static_cast<int>(nt)) break;
-            float weight = 0;
-            if (B.w > c.good_spB_min_radius) weight = c.good_spB_weight_increase;
-            if (trT[i] < c.good_spT_max_radius) weight = c.good_spT_weight_increase;
-            const float w = twt[i] + weight;
-            if (B.w > c.good_spB_min_radius && w < c.good_spB_min_weight) continue;
-            const float4 T = nb.get(ws.qt[tt[i]]);
-            const float s = B.y * B.y + B.z * B.z + T.y * T.y + T.z * T.z;
-            const uint32_t key = (ib << 16) | tt[i];
-            // insertion into the sorted best-K list
-            uint32_t pos = 0;
-#pragma unroll
-            for (int k = 0; k < kMaxSeedsPerMiddle; ++k)
-                if (k < static_cast<int>(bn) && better(bw[k], bs[k], bk[k], w, s, key)) ++pos;
-            if (pos < K) {
-#pragma unroll
-                for (int k = kMaxSeedsPerMiddle - 1; k > 0; --k) {
-                    if (k > static_cast<int>(pos)) {
-                        bw[k] = bw[k - 1]; bs[k] = bs[k - 1];
-                        bk[k] = bk[k - 1]; bp[k] = bp[k - 1];
-                    }
-                }
-#pragma unroll
-                for (int k = 0; k < kMaxSeedsPerMiddle; ++k) {
-                    if (k == static_cast<int>(pos)) {
-                        bw[k] = w; bs[k] = s; bk[k] = key;
-                        bp[k] = (static_cast<uint32_t>(pB) << 16) | ws.qt[tt[i]];
-                    }
-                }
-                bn = min(bn + 1, K);
+                __syncwarp();
             }
         }
     }
-    if (__any_sync(0xffffffffu, lane_ovf)) { res.status = 1; return res; }
 
-    // -- warp merge of the lane-local lists: the global best K in order
+    // -- weights, one lane per triplet: compatible-seed weights over its
+    //    doublet's run (triplet_finding.hpp:107-179), seed_weight and
+    //    single_seed_cut (seed_selecting_helper.hpp:27-62)
+    for (uint32_t k = lane; k < n_ct; k += 32) {
+        const TripCand T = ws.ct[ws.sidx[k]];
+        uint32_t b = k, e = k + 1;
+        while (b > 0 && (ws.skey[b - 1] >> 16) == T.ib) --b;
+        while (e < n_ct && (ws.skey[e] >> 16) == T.ib) ++e;
+        const float4 Tp = nb.get(ws.ppt[T.tp]);
+        float w = T.w;
+        if (e - b > 1) {
+            const float currentTop_r = Tp.w;
+            const float lowerLimitCurv = T.curv - c.deltaInvHelixDiameter;
+            const float upperLimitCurv = T.curv + c.deltaInvHelixDiameter;
+            float compR[8];
+            uint32_t ncr = 0;
+            for (uint32_t j = b; j < e; ++j) {
+                if (j == k) continue;
+                const TripCand Tj = ws.ct[ws.sidx[j]];
+                const float otherTop_r = nb.get(ws.ppt[Tj.tp]).w;
+                const float deltaR = currentTop_r - otherTop_r;
+                if (fabsf(deltaR) < c.filterDeltaRMin) continue;
+                if (Tj.curv < lowerLimitCurv) continue;
+                if (Tj.curv > upperLimitCurv) continue;
+                bool newCompSeed = true;
+                for (uint32_t q = 0; q < ncr && q < 8; ++q) {
+                    if (fabsf(compR[q] - otherTop_r) < c.filterDeltaRMin) {
+                        newCompSeed = false;
+                        break;
+                    }
+                }
+                if (newCompSeed) {
+                    if (ncr < 8) compR[ncr] = otherTop_r;
+                    ++ncr;
+                    w += c.compatSeedWeight;
+                }
+                if (ncr >= c.compatSeedLimit) break;
+            }
+        }
+        const float4 B = nb.get(ws.qb[T.ib]);
+        float weight = 0;
+        if (B.w > c.good_spB_min_radius) weight = c.good_spB_weight_increase;
+        if (Tp.w < c.good_spT_max_radius) weight = c.good_spT_weight_increase;
+        w += weight;
+        const bool cut = B.w > c.good_spB_min_radius && w < c.good_spB_min_weight;
+        ws.wf[k] = cut ? -__int_as_float(0x7f800000) : w;
+        ws.ts[k] = B.y * B.y + B.z * B.z + Tp.y * Tp.y + Tp.z * Tp.z;
+    }
+    __syncwarp();
+
+    // -- the best K triplets in triplet_sorter order (K warp argmax rounds),
+    //    then the final selection (seed_filtering.cpp:87-122).  Index k of
+    //    the sorted triplets is their host order (the tie-break).
+    const uint32_t K = min(c.maxSeedsPerSpM, static_cast<uint32_t>(kMaxSeedsPerMiddle));
     float my_w = 0.f;
-    uint32_t my_p = 0;
-    uint32_t n_sel = 0;
+    uint32_t my_p = 0, n_sel = 0;
     for (uint32_t r = 0; r < K; ++r) {
-        float cw = bn > 0 ? bw[0] : -__int_as_float(0x7f800000);
-        float cs = bn > 0 ? bs[0] : 0.f;
-        uint32_t ck = bn > 0 ? bk[0] : 0xffffffffu;
-        uint32_t cl = lane;
+        float cw = -__int_as_float(0x7f800000), cs = 0.f;
+        uint32_t ck = 0xffffffffu;
+        for (uint32_t k = lane; k < n_ct; k += 32) {
+            const float wk = ws.wf[k];
+            if (wk == -__int_as_float(0x7f800000)) continue;
+            if (ck == 0xffffffffu || better(wk, ws.ts[k], k, cw, cs, ck)) {
+                cw = wk; cs = ws.ts[k]; ck = k;
+            }
+        }
         for (int o = 16; o > 0; o >>= 1) {
             const float ow = __shfl_xor_sync(0xffffffffu, cw, o);
             const float os = __shfl_xor_sync(0xffffffffu, cs, o);
             const uint32_t ok = __shfl_xor_sync(0xffffffffu, ck, o);
-            const uint32_t ol = __shfl_xor_sync(0xffffffffu, cl, o);
-            if (better(ow, os, ok, cw, cs, ck)) { cw = ow; cs = os; ck = ok; cl = ol; }
+            if (ok != 0xffffffffu && (ck == 0xffffffffu || better(ow, os, ok, cw, cs, ck))) {
+                cw = ow; cs = os; ck = ok;
+            }
         }
         if (ck == 0xffffffffu) break;
-        const uint32_t wp = __shfl_sync(0xffffffffu, bp[0], cl);
-        if (lane == cl) {
-#pragma unroll
-            for (int k = 0; k + 1 < kMaxSeedsPerMiddle; ++k) {
-                bw[k] = bw[k + 1]; bs[k] = bs[k + 1]; bk[k] = bk[k + 1]; bp[k] = bp[k + 1];
-            }
-            --bn;
+        if (lane == r) {
+            const TripCand T = ws.ct[ws.sidx[ck]];
+            my_w = cw;
+            my_p = (static_cast<uint32_t>(ws.qb[T.ib]) << 16) | ws.ppt[T.tp];
         }
-        if (lane == r) { my_w = cw; my_p = wp; }
+        __syncwarp();
+        if (lane == 0) ws.wf[ck] = -__int_as_float(0x7f800000);  // taken
+        __syncwarp();
         ++n_sel;
     }
-    // -- final selection (seed_filtering.cpp:87-122): the first is always
-    //    accepted, the next ones if cut_per_middle_sp holds
     bool acc = false;
-    float4 Bsel = make_float4(0.f, 0.f, 0.f, 0.f);
     if (lane < n_sel) {
-        Bsel = nb.get(my_p >> 16);
+        const float4 Bsel = nb.get(my_p >> 16);
         acc = (lane == 0) || (my_w > c.seed_min_weight) || (Bsel.w > c.spB_min_radius);
     }
     const uint32_t amask = __ballot_sync(0xffffffffu, acc);
     if (acc) {
         const uint32_t k = __popc(amask & lt);
         SeedSlot s;
-        s.b = a.g_idx[nb.gpos(my_p >> 16)];
+        s.b = a.g_idx[nb.gpos(nb.hpos(my_p >> 16))];
         s.m = a.g_idx[gm];
-        s.t = a.g_idx[nb.gpos(my_p & 0xffffu)];
+        s.t = a.g_idx[nb.gpos(nb.hpos(my_p & 0xffffu))];
         s.q = my_w;
         a.seed_slot[static_cast<size_t>(gm) * kMaxSeedsPerMiddle + k] = s;
     }
     if (lane == 0) a.seed_cnt[gm] = static_cast<uint8_t>(__popc(amask));
-    uint32_t tsum = n_trip;
-    for (int o = 16; o > 0; o >>= 1) tsum += __shfl_xor_sync(0xffffffffu, tsum, o);
-    res.n_trip = tsum;
     return res;
 }
 
@@ -931,28 +1301,33 @@ __device__ __forceinline__ void count_middle(const Arena& a, const MiddleResult&
     if (r.n_trip) atomicAdd(&a.counters[kNumTriplets], static_cast<unsigned long long>(r.n_trip));
 }
 
-// Persistent kernel over work items (event, bin, chunk of middles).
-__global__ void __launch_bounds__(256) k_seed_fast(DevConfig c, Arena a, uint32_t mpi,
+// Persistent kernel over work items (event, bin, chunk of middles).  The CTA
+// stages the bin's neighbourhood (radius-sorted runs) once per item; its warps
+// then take middles of the item one at a time.
+__global__ void __launch_bounds__(512) k_seed_fast(DevConfig c, Arena a, uint32_t mpi,
                                                     uint32_t nb_cap) {
     extern __shared__ __align__(16) uint8_t smem[];
     float4* nb_xyzr = reinterpret_cast<float4*>(smem);
-    uint32_t* seg_pos = reinterpret_cast<uint32_t*>(nb_xyzr + nb_cap);  // [kMaxSegments+1]
-    uint32_t* seg_g = seg_pos + kMaxSegments + 1;                        // [kMaxSegments]
-    uint32_t* misc = seg_g + kMaxSegments;                               // [16]
+    uint16_t* nb_hp = reinterpret_cast<uint16_t*>(nb_xyzr + nb_cap);      // [nb_cap]
+    uint32_t* seg_pos = reinterpret_cast<uint32_t*>(nb_hp + nb_cap);      // [kMaxSegments+1]
+    uint32_t* seg_g = seg_pos + kMaxSegments + 1;                          // [kMaxSegments]
+    uint32_t* seg_bin = seg_g + kMaxSegments;                              // [kMaxSegments]
+    uint32_t* misc = seg_bin + kMaxSegments;                               // [16]
     FastScratch* wsb = reinterpret_cast<FastScratch*>(
         reinterpret_cast<uint8_t*>(misc) + 16 * sizeof(uint32_t));
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t nwarps = blockDim.x >> 5;
     FastScratch& ws = wsb[warp];
     const bool any_var = a.counters[kAnyVariance] != 0;
-    const uint32_t total_items =
-        static_cast<uint32_t>(min(a.counters[kItemTotal], static_cast<unsigned long long>(a.max_items)));
+    const uint32_t total_items = static_cast<uint32_t>(
+        min(a.counters[kItemTotal], static_cast<unsigned long long>(a.max_items)));
 
     for (;;) {
         if (threadIdx.x == 0) {
             misc[0] = static_cast<uint32_t>(atomicAdd(&a.counters[kItemFetch], 1ull));
             misc[3] = 0x7f800000u;  // min r (as bits, r >= 0)
             misc[4] = 0u;           // max r
+            misc[5] = 0u;           // next middle of the item
+            misc[6] = 0u;           // any unsorted bin
         }
         __syncthreads();
         const uint32_t item = misc[0];
@@ -970,19 +1345,24 @@ __global__ void __launch_bounds__(256) k_seed_fast(DevConfig c, Arena a, uint32_
         }
         if (threadIdx.x == 0) {
             uint32_t ns;
-            misc[2] = build_segments(c, bs, pbin, zlo, zhi, seg_pos, seg_g, &ns);
+            misc[2] = build_segments(c, bs, pbin, zlo, zhi, seg_pos, seg_g, &ns, seg_bin);
             misc[1] = ns;
         }
         __syncthreads();
         const uint32_t nseg = misc[1], size = misc[2];
-        const bool staged = size <= nb_cap && size <= 65535u;
+        if (threadIdx.x < nseg &&
+            a.bin_unsorted[static_cast<size_t>(e) * c.nbins + seg_bin[threadIdx.x]])
+            misc[6] = 1u;
+        __syncthreads();
+        const bool staged = size <= nb_cap && size <= 65535u && nseg <= kFastSegs && !misc[6];
         if (staged) {
             float lmin = __int_as_float(0x7f800000), lmax = 0.f;
             for (uint32_t s = 0; s < nseg; ++s) {
                 const uint32_t p0 = seg_pos[s], len = seg_pos[s + 1] - p0, g0 = seg_g[s];
                 for (uint32_t k = threadIdx.x; k < len; k += blockDim.x) {
-                    const float4 v = a.g_xyzr[g0 + k];
+                    const float4 v = a.g_rs[g0 + k];
                     nb_xyzr[p0 + k] = v;
+                    nb_hp[p0 + k] = static_cast<uint16_t>(p0 + (a.g_rs_gp[g0 + k] - g0));
                     lmin = fminf(lmin, v.w);
                     lmax = fmaxf(lmax, v.w);
                 }
@@ -998,10 +1378,15 @@ __global__ void __launch_bounds__(256) k_seed_fast(DevConfig c, Arena a, uint32_
         }
         __syncthreads();
         const float nb_minr = __uint_as_float(misc[3]), nb_maxr = __uint_as_float(misc[4]);
-        NbView nb{staged ? nb_xyzr : nullptr, a.g_xyzr, seg_pos, seg_g, nseg, size};
+        NbView nb{staged ? nb_xyzr : nullptr, nb_hp, a.g_xyzr, seg_pos, seg_g, nseg, size};
         const uint32_t m0 = bs[bin] + ch * mpi;
         const uint32_t m1 = min(m0 + mpi, bs[bin + 1]);
-        for (uint32_t gm = m0 + warp; gm < m1; gm += nwarps) {
+        for (;;) {
+            uint32_t k = 0;
+            if (lane == 0) k = atomicAdd(&misc[5], 1u);
+            k = __shfl_sync(0xffffffffu, k, 0);
+            const uint32_t gm = m0 + k;
+            if (gm >= m1) break;
             bool standard = staged;
             if (standard && c.z_bins > 1) {
                 uint32_t l2, h2;
@@ -1012,7 +1397,7 @@ __global__ void __launch_bounds__(256) k_seed_fast(DevConfig c, Arena a, uint32_
                 if (lane == 0) push_overflow(a, gm);
                 continue;
             }
-            const MiddleResult r = process_middle<1024, 512, 256, kFastTcap>(
+            const MiddleResult r = process_middle<true, 1024, 1024, 256, 256>(
                 c, a, nb, gm, any_var, true, nb_minr, nb_maxr, ws);
             if (lane == 0) {
                 if (r.status) push_overflow(a, gm);
@@ -1024,11 +1409,12 @@ __global__ void __launch_bounds__(256) k_seed_fast(DevConfig c, Arena a, uint32_
 }
 
 // Large-capacity path: one warp per CTA, neighbourhood read from global
-// memory, per-middle z neighbourhood.
+// memory in host order, per-middle z neighbourhood.
 __global__ void __launch_bounds__(32) k_seed_slow(DevConfig c, Arena a) {
     extern __shared__ __align__(16) uint8_t smem[];
     uint32_t* seg_pos = reinterpret_cast<uint32_t*>(smem);     // [kMaxSegments+1]
     uint32_t* seg_g = seg_pos + kMaxSegments + 1;              // [kMaxSegments]
+    uint32_t* misc = seg_g + kMaxSegments;                     // [2]
     SlowScratch& ws = *reinterpret_cast<SlowScratch*>(smem + 1024);
     const uint32_t lane = threadIdx.x & 31;
     const bool any_var = a.counters[kAnyVariance] != 0;
@@ -1053,26 +1439,21 @@ __global__ void __launch_bounds__(32) k_seed_slow(DevConfig c, Arena a) {
             const uint32_t mid = (b0 + b1) >> 1;
             if (bs[mid] <= gm) b0 = mid; else b1 = mid;
         }
-        const uint32_t bin = b0;
         uint32_t zlo, zhi;
         z_range(c, a.g_xyzr[gm].z, zlo, zhi);
         if (lane == 0) {
             uint32_t ns;
-            seg_g[kMaxSegments - 1] = 0;
-            const uint32_t size = build_segments(c, bs, bin % c.phi_bins, zlo, zhi,
-                                                 seg_pos, seg_g, &ns);
-            seg_pos[kMaxSegments] = size;
-            ws.qb[0] = 0;
-            reinterpret_cast<uint32_t*>(smem)[2 * kMaxSegments + 1] = ns;
+            build_segments(c, bs, b0 % c.phi_bins, zlo, zhi, seg_pos, seg_g, &ns, nullptr);
+            misc[0] = ns;
         }
         __syncwarp();
-        const uint32_t nseg = reinterpret_cast<uint32_t*>(smem)[2 * kMaxSegments + 1];
+        const uint32_t nseg = misc[0];
         const uint32_t size = seg_pos[nseg];
         MiddleResult r{0, 0, 0, 1};
         if (size <= 65535u) {
-            NbView nb{nullptr, a.g_xyzr, seg_pos, seg_g, nseg, size};
-            r = process_middle<8192, 8192, 4096, kSlowTcap>(c, a, nb, gm, any_var, false,
-                                                            0.f, 0.f, ws);
+            NbView nb{nullptr, nullptr, a.g_xyzr, seg_pos, seg_g, nseg, size};
+            r = process_middle<false, 8192, 8192, 4096, 2048>(c, a, nb, gm, any_var,
+                                                                   false, 0.f, 0.f, ws);
         }
         if (lane == 0) {
             if (r.status) {
@@ -1236,15 +1617,26 @@ k_params(ParamsConfig c, float bx, float by, float bz, seedgb_measurement_view m
 // ---------------------------------------------------------------------------
 
 size_t fast_kernel_smem(const TuneParams& tp) {
-    return static_cast<size_t>(tp.nb_cap) * sizeof(float4) +
-           (2 * kMaxSegments + 1 + 16) * sizeof(uint32_t) +
+    const size_t nb = static_cast<size_t>(tp.nb_cap) * (sizeof(float4) + sizeof(uint16_t));
+    return ((nb + 3) & ~size_t(3)) + (3 * kMaxSegments + 1 + 16) * sizeof(uint32_t) +
            static_cast<size_t>(tp.fast_warps) * sizeof(FastScratch) + 16;
+}
+
+int fast_kernel_max_warps(int nb_cap) {
+    TuneParams t{0, 1, nb_cap, 1};
+    const size_t fixed = fast_kernel_smem(t);
+    const size_t limit = 227 * 1024;
+    if (fixed >= limit) return 0;
+    return static_cast<int>(std::min<size_t>(16, (limit - fixed) / sizeof(FastScratch)));
 }
 
 static size_t slow_kernel_smem() { return 1024 + sizeof(SlowScratch); }
 
 cudaError_t launch_seeding(const DevConfig& cfg, const Arena& a, const TuneParams& tp,
-                           int num_sms, cudaStream_t stream) {
+                           int num_sms, cudaStream_t stream, cudaEvent_t* timing) {
+    auto mark = [&](int i) {
+        if (timing) cudaEventRecord(timing[i], stream);
+    };
     static bool attrs_set = false;
     const size_t fsm = fast_kernel_smem(tp);
     const size_t ssm = slow_kernel_smem();
@@ -1258,9 +1650,11 @@ cudaError_t launch_seeding(const DevConfig& cfg, const Arena& a, const TuneParam
         attrs_set = true;
     }
     const size_t hsm = static_cast<size_t>(kBinWarps) * cfg.nbins * sizeof(uint32_t);
+    mark(0);
     if (a.total_chunks > 0) {
         k_bin_count<<<a.total_chunks, kBinWarps * 32, hsm, stream>>>(cfg, a);
     }
+    mark(1);
     {
         const uint32_t nb = cfg.nbins;
         const uint32_t G = std::max(1u, 1024u / nb);
@@ -1268,13 +1662,20 @@ cudaError_t launch_seeding(const DevConfig& cfg, const Arena& a, const TuneParam
         k_bin_scan<<<a.n_events, 1024, ssz, stream>>>(cfg, a,
                                                       static_cast<uint32_t>(tp.middles_per_item));
     }
+    mark(2);
     if (a.total_chunks > 0) {
         k_bin_scatter<<<a.total_chunks, kBinWarps * 32, hsm, stream>>>(cfg, a);
     }
+    mark(3);
+    k_bin_rsort<<<a.n_events * cfg.nbins, 256, 0, stream>>>(cfg, a);
+    mark(4);
     k_seed_fast<<<num_sms * tp.ctas_per_sm, tp.fast_warps * 32, fsm, stream>>>(
         cfg, a, static_cast<uint32_t>(tp.middles_per_item), static_cast<uint32_t>(tp.nb_cap));
+    mark(5);
     k_seed_slow<<<num_sms, 32, ssm, stream>>>(cfg, a);
+    mark(6);
     k_seed_compact<<<a.n_events, 1024, 0, stream>>>(a);
+    mark(7);
     return cudaGetLastError();
 }
 

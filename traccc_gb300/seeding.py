@@ -111,6 +111,9 @@ STATUS = {0: "ok", 1: "empty input", 2: "bad configuration", 3: "CUDA error",
           6: "invalid argument", 7: "unsupported configuration"}
 OK, EMPTY, BAD_CONFIG, CUDA_ERROR, CAPACITY_OVERFLOW, TIMEOUT = 0, 1, 2, 3, 4, 5
 OPTION_EXHAUSTIVE_TRIPLETS = 1
+OPTION_KERNEL_TIMING = 2
+KERNEL_NAMES = ("bin_count", "bin_scan", "bin_scatter", "bin_rsort", "seed_fast",
+                "seed_slow", "seed_compact")
 
 PARAMS_DTYPE = np.dtype([("surface_link", "<u8"), ("params", "<f4", (6,)),
                          ("cov", "<f4", (36,))])
@@ -174,6 +177,8 @@ def lib():
         L.seedgb_seeding_copy_grid.restype = C.c_int
         L.seedgb_seeding_set_option.argtypes = [vp, C.c_int, C.c_int64]
         L.seedgb_seeding_set_option.restype = C.c_int
+        L.seedgb_seeding_kernel_times.argtypes = [vp, P(C.c_float)]
+        L.seedgb_seeding_kernel_times.restype = C.c_int
         L.seedgb_params_create.argtypes = [P(TrackParamsEstimationConfig), P(vp)]
         L.seedgb_params_create.restype = C.c_int
         L.seedgb_params_destroy.argtypes = [vp]
@@ -426,6 +431,12 @@ class TripletSeedingAlgorithm:
         keys = ("n_valid", "n_overflow_middles", "n_mb", "n_mt", "n_triplets",
                 "n_seeds", "phi_undecided", "n_items")
         return {k: int(v) for k, v in zip(keys, arr)}
+
+    def kernel_times(self) -> dict:
+        """Per-kernel device ms of the last run (OPTION_KERNEL_TIMING on)."""
+        arr = (C.c_float * 7)()
+        _check(lib().seedgb_seeding_kernel_times(self._h, arr), "seedgb_seeding_kernel_times")
+        return {k: float(v) for k, v in zip(KERNEL_NAMES, arr)}
 
     def grid(self, event: int = 0, n_sp: int = 0, stream=None):
         """(bin_offsets, bin_sps) of the last run's event (host copy)."""
