@@ -666,7 +666,7 @@ struct NbView {
     }
 };
 
-constexpr int kBuckets = 128;  // cot(theta) buckets of the middle-top doublets
+constexpr int kBuckets = 256;  // cot(theta) buckets of the middle-top doublets
 
 // A triplet of the middle spacepoint (before the compatible-seed weights).
 struct TripCand {
@@ -692,9 +692,9 @@ struct Stage1Cand {
 
 template <int CAPB, int CAPT, int CAPLC, int CAPCT>
 struct WarpScratch {
-    // middle-top doublets in list order
-    float key[CAPLC];  // cot(theta)
-    float idr[CAPLC], er[CAPLC], u[CAPLC], v[CAPLC];
+    // middle-top doublets in list order: {cot(theta), iDeltaR, U, V}, Er
+    float4 mtd[CAPLC];
+    float er[CAPLC];
     uint16_t hpt[CAPLC];  // host position of the top
     uint16_t ppt[CAPLC];  // neighbourhood position of the top
     uint16_t perm[CAPLC]; // bucket-sorted slot -> list index
@@ -704,8 +704,8 @@ struct WarpScratch {
     union {
         uint16_t qt[CAPT];  // middle-top doublets, until their lin_circles exist
         struct {
-            Stage0Cand q0[96];  // in-window candidates awaiting stage 1
-            Stage1Cand q1[96];  // stage-1 survivors awaiting stage 2
+            Stage0Cand q0[96];  // in-window candidates awaiting stage 1 (< 32 + 64)
+            Stage1Cand q1[64];  // stage-1 survivors awaiting stage 2 (< 32 + 32)
         } q;
     };
     TripCand ct[CAPCT];   // triplets of the middle
@@ -717,8 +717,8 @@ struct WarpScratch {
     uint32_t pre[2 * (kFastSegs + 1)];  // candidate prefix per bin
 };
 
-// shared memory per warp: fast ~20 KB, slow ~190 KB
-using FastScratch = WarpScratch<1024, 1024, 256, 256>;
+// shared memory per warp: fast ~15 KB, slow ~190 KB
+using FastScratch = WarpScratch<1024, 1024, 256, 128>;
 using SlowScratch = WarpScratch<8192, 8192, 4096, 2048>;
 
 // Keep the positions whose doublet passes the minimum-helix-radius test, in
@@ -921,11 +921,8 @@ __device__ MiddleResult process_middle(const DevConfig& c, const Arena& a,
         const uint32_t hp = nb.hpos(p);
         const float2 vo = any_var ? a.g_var[nb.gpos(hp)] : make_float2(0.f, 0.f);
         const LinCircle l = lin_circle_cs(true, M, cosPhiM, sinPhiM, vM, nb.get(p), vo);
-        ws.key[i] = l.cot;
-        ws.idr[i] = l.idr;
+        ws.mtd[i] = make_float4(l.cot, l.idr, l.u, l.v);
         ws.er[i] = l.er;
-        ws.u[i] = l.u;
-        ws.v[i] = l.v;
         ws.hpt[i] = static_cast<uint16_t>(hp);
         ws.ppt[i] = static_cast<uint16_t>(p);
         maxEr = fmaxf(maxEr, l.er);
@@ -950,10 +947,10 @@ __device__ MiddleResult process_middle(const DevConfig& c, const Arena& a,
     const float scale = (cmax > cmin) ? static_cast<float>(kBuckets) / (cmax - cmin) : 0.f;
     __syncwarp();
     for (uint32_t i = lane; i < n_mt; i += 32)
-        atomicAdd(&ws.bstart[cot_bucket(ws.key[i], cmin, scale) + 1], 1u);
+        atomicAdd(&ws.bstart[cot_bucket(ws.mtd[i].x, cmin, scale) + 1], 1u);
     __syncwarp();
     {
-        // exclusive prefix over the buckets, four per lane
+        // exclusive prefix over the buckets, kBuckets / 32 per lane
         constexpr int kPer = kBuckets / 32;
         uint32_t v[kPer], sum = 0;
 #pragma unroll
@@ -974,7 +971,7 @@ __device__ MiddleResult process_middle(const DevConfig& c, const Arena& a,
     }
     __syncwarp();
     for (uint32_t i = lane; i < n_mt; i += 32) {
-        const uint32_t slot = atomicAdd(&ws.bcur[cot_bucket(ws.key[i], cmin, scale)], 1u);
+        const uint32_t slot = atomicAdd(&ws.bcur[cot_bucket(ws.mtd[i].x, cmin, scale)], 1u);
         ws.perm[slot] = static_cast<uint16_t>(i);
     }
     __syncwarp();
@@ -1015,7 +1012,12 @@ __device__ MiddleResult process_middle(const DevConfig& c, const Arena& a,
                 if (c.brute_force_triplets) {
                     W = __int_as_float(0x7f800000);
                 } else if (!any_var) {
-                    W = sqrtf(scatteringInRegion2) * 1.01f + 1e-5f * (1.f + fabsf(lbm.cot));
+                    // approximate square root: its ~1e-6 relative error is far
+                    // inside the 1 % margin
+                    const float sq = scatteringInRegion2 > 1e-30f
+                                         ? scatteringInRegion2 * rsqrtf(scatteringInRegion2)
+                                         : sqrtf(scatteringInRegion2);
+                    W = sq * 1.01f + 1e-5f * (1.f + fabsf(lbm.cot));
                 } else {
                     const float e2 =
                         (maxEr + lbm.er +
@@ -1038,28 +1040,32 @@ __device__ MiddleResult process_middle(const DevConfig& c, const Arena& a,
             have_chunk = true;
         }
         if (have_chunk) {
-            while (it < maxc && n0 < 64) {
-                bool ok = false;
-                uint32_t tp = 0;
-                if (it < cnt) {
-                    tp = ws.perm[lo + it];
-                    const float kt = ws.key[tp];
-                    ok = kt >= klo && kt <= khi;
+            while (it < maxc && n0 < 32) {
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const uint32_t j = it + h;
+                    bool ok = false;
+                    uint32_t tp = 0;
+                    if (j < cnt) {
+                        tp = ws.perm[lo + j];
+                        const float kt = ws.mtd[tp].x;
+                        ok = kt >= klo && kt <= khi;
+                    }
+                    const uint32_t mask = __ballot_sync(0xffffffffu, ok);
+                    if (ok) {
+                        Stage0Cand e;
+                        e.tp = static_cast<uint16_t>(tp);
+                        e.ib = static_cast<uint16_t>(c0 + lane);
+                        e.cot = lbm.cot;
+                        e.idr = lbm.idr;
+                        e.er = lbm.er;
+                        e.u = lbm.u;
+                        e.v = lbm.v;
+                        ws.q.q0[n0 + __popc(mask & lt)] = e;
+                    }
+                    n0 += __popc(mask);
                 }
-                const uint32_t mask = __ballot_sync(0xffffffffu, ok);
-                if (ok) {
-                    Stage0Cand e;
-                    e.tp = static_cast<uint16_t>(tp);
-                    e.ib = static_cast<uint16_t>(c0 + lane);
-                    e.cot = lbm.cot;
-                    e.idr = lbm.idr;
-                    e.er = lbm.er;
-                    e.u = lbm.u;
-                    e.v = lbm.v;
-                    ws.q.q0[n0 + __popc(mask & lt)] = e;
-                }
-                n0 += __popc(mask);
-                ++it;
+                it += 2;
             }
             if (it >= maxc) {
                 have_chunk = false;
@@ -1068,12 +1074,11 @@ __device__ MiddleResult process_middle(const DevConfig& c, const Arena& a,
         }
         __syncwarp();
         const bool more = have_chunk || c0 < n_mb;
-        if (n0 >= 64 || (!more && n0 > 0)) {
+        if (n0 >= 32 || (!more && n0 > 0)) {
             // stage 1 on q0[0..k), survivors to q1
-            const uint32_t k1 = min(n0, 64u);
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                const uint32_t i = lane + 32 * h;
+            const uint32_t k1 = min(n0, 32u);
+            {
+                const uint32_t i = lane;
                 bool ok = false;
                 Stage1Cand s1;
                 if (i < k1) {
@@ -1088,9 +1093,12 @@ __device__ MiddleResult process_middle(const DevConfig& c, const Arena& a,
                     const float iSinTheta2 = 1.f + lb.cot * lb.cot;
                     float scatteringInRegion2 = c.maxScatteringAngle2 * iSinTheta2;
                     scatteringInRegion2 *= sig2;
-                    ok = triplet_stage1(c, vM, lb, ws.key[e.tp], ws.idr[e.tp], ws.er[e.tp],
-                                        ws.u[e.tp], ws.v[e.tp], scatteringInRegion2, s1.A,
-                                        s1.B);
+                    const float4 mt = ws.mtd[e.tp];
+                    // with no variance anywhere every Er is +0 (transform_
+                    // coordinates multiplies (0 + 0) + cot^2 (0 + 0) by iDeltaR2)
+                    const float ter = any_var ? ws.er[e.tp] : 0.f;
+                    ok = triplet_stage1(c, vM, lb, mt.x, mt.y, ter, mt.z, mt.w,
+                                        scatteringInRegion2, s1.A, s1.B);
                     s1.tp = e.tp;
                     s1.ib = e.ib;
                     s1.cot = e.cot;
@@ -1102,12 +1110,14 @@ __device__ MiddleResult process_middle(const DevConfig& c, const Arena& a,
                 if (ok) ws.q.q1[n1 + __popc(mask & lt)] = s1;
                 n1 += __popc(mask);
             }
-            // move the unprocessed tail of q0 (< 32 entries) to the front
+            // move the unprocessed tail of q0 (< 64 entries) to the front
             const uint32_t rest = n0 - k1;
-            Stage0Cand t;
-            if (lane < rest) t = ws.q.q0[k1 + lane];
+            Stage0Cand t0, t1;
+            if (lane < rest) t0 = ws.q.q0[k1 + lane];
+            if (lane + 32 < rest) t1 = ws.q.q0[k1 + lane + 32];
             __syncwarp();
-            if (lane < rest) ws.q.q0[lane] = t;
+            if (lane < rest) ws.q.q0[lane] = t0;
+            if (lane + 32 < rest) ws.q.q0[lane + 32] = t1;
             n0 = rest;
             __syncwarp();
         }
@@ -1124,8 +1134,10 @@ __device__ MiddleResult process_middle(const DevConfig& c, const Arena& a,
                 lb.er = e.er;
                 lb.u = lb.v = lb.Zo = 0.f;
                 float curv = 0.f, imp = 0.f;
-                ok = triplet_stage2(c, M.w, vM, lb, ws.key[e.tp], ws.idr[e.tp], ws.er[e.tp],
-                                    e.is2, e.A, e.B, curv, imp);
+                const float4 mt = ws.mtd[e.tp];
+                const float ter = any_var ? ws.er[e.tp] : 0.f;
+                ok = triplet_stage2(c, M.w, vM, lb, mt.x, mt.y, ter, e.is2, e.A, e.B, curv,
+                                    imp);
                 t.tp = e.tp;
                 t.ib = e.ib;
                 t.curv = curv;
@@ -1138,12 +1150,10 @@ __device__ MiddleResult process_middle(const DevConfig& c, const Arena& a,
             }
             n_ct += __popc(mask);
             const uint32_t rest = n1 - k2;
-            Stage1Cand t0, t1;
+            Stage1Cand t0;
             if (lane < rest) t0 = ws.q.q1[k2 + lane];
-            if (lane + 32 < rest) t1 = ws.q.q1[k2 + lane + 32];
             __syncwarp();
             if (lane < rest) ws.q.q1[lane] = t0;
-            if (lane + 32 < rest) ws.q.q1[lane + 32] = t1;
             n1 = rest;
             __syncwarp();
         }
@@ -1301,20 +1311,33 @@ __device__ __forceinline__ void count_middle(const Arena& a, const MiddleResult&
     if (r.n_trip) atomicAdd(&a.counters[kNumTriplets], static_cast<unsigned long long>(r.n_trip));
 }
 
+// Shared-memory layout of k_seed_fast: the staged neighbourhood (float4 and
+// host position), the segment tables, then one scratch per warp at a
+// 128-byte boundary (the scratch holds float4 arrays).
+static_assert(alignof(FastScratch) <= 128, "scratch alignment");
+static_assert(sizeof(FastScratch) % 16 == 0, "scratch size");
+__host__ __device__ constexpr size_t fast_seg_offset(uint32_t nb_cap) {
+    return (static_cast<size_t>(nb_cap) * (sizeof(float4) + sizeof(uint16_t)) + 15) &
+           ~static_cast<size_t>(15);
+}
+__host__ __device__ constexpr size_t fast_scratch_offset(uint32_t nb_cap) {
+    return (fast_seg_offset(nb_cap) + (3 * kMaxSegments + 1 + 16) * sizeof(uint32_t) + 127) &
+           ~static_cast<size_t>(127);
+}
+
 // Persistent kernel over work items (event, bin, chunk of middles).  The CTA
 // stages the bin's neighbourhood (radius-sorted runs) once per item; its warps
 // then take middles of the item one at a time.
 __global__ void __launch_bounds__(512) k_seed_fast(DevConfig c, Arena a, uint32_t mpi,
                                                     uint32_t nb_cap) {
-    extern __shared__ __align__(16) uint8_t smem[];
+    extern __shared__ __align__(128) uint8_t smem[];
     float4* nb_xyzr = reinterpret_cast<float4*>(smem);
     uint16_t* nb_hp = reinterpret_cast<uint16_t*>(nb_xyzr + nb_cap);      // [nb_cap]
-    uint32_t* seg_pos = reinterpret_cast<uint32_t*>(nb_hp + nb_cap);      // [kMaxSegments+1]
+    uint32_t* seg_pos = reinterpret_cast<uint32_t*>(smem + fast_seg_offset(nb_cap));
     uint32_t* seg_g = seg_pos + kMaxSegments + 1;                          // [kMaxSegments]
     uint32_t* seg_bin = seg_g + kMaxSegments;                              // [kMaxSegments]
     uint32_t* misc = seg_bin + kMaxSegments;                               // [16]
-    FastScratch* wsb = reinterpret_cast<FastScratch*>(
-        reinterpret_cast<uint8_t*>(misc) + 16 * sizeof(uint32_t));
+    FastScratch* wsb = reinterpret_cast<FastScratch*>(smem + fast_scratch_offset(nb_cap));
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     FastScratch& ws = wsb[warp];
     const bool any_var = a.counters[kAnyVariance] != 0;
@@ -1397,7 +1420,7 @@ __global__ void __launch_bounds__(512) k_seed_fast(DevConfig c, Arena a, uint32_
                 if (lane == 0) push_overflow(a, gm);
                 continue;
             }
-            const MiddleResult r = process_middle<true, 1024, 1024, 256, 256>(
+            const MiddleResult r = process_middle<true, 1024, 1024, 256, 128>(
                 c, a, nb, gm, any_var, true, nb_minr, nb_maxr, ws);
             if (lane == 0) {
                 if (r.status) push_overflow(a, gm);
@@ -1411,10 +1434,11 @@ __global__ void __launch_bounds__(512) k_seed_fast(DevConfig c, Arena a, uint32_
 // Large-capacity path: one warp per CTA, neighbourhood read from global
 // memory in host order, per-middle z neighbourhood.
 __global__ void __launch_bounds__(32) k_seed_slow(DevConfig c, Arena a) {
-    extern __shared__ __align__(16) uint8_t smem[];
+    extern __shared__ __align__(128) uint8_t smem[];
     uint32_t* seg_pos = reinterpret_cast<uint32_t*>(smem);     // [kMaxSegments+1]
     uint32_t* seg_g = seg_pos + kMaxSegments + 1;              // [kMaxSegments]
     uint32_t* misc = seg_g + kMaxSegments;                     // [2]
+    static_assert(sizeof(uint32_t) * (2 * kMaxSegments + 3) <= 1024, "slow layout");
     SlowScratch& ws = *reinterpret_cast<SlowScratch*>(smem + 1024);
     const uint32_t lane = threadIdx.x & 31;
     const bool any_var = a.counters[kAnyVariance] != 0;
@@ -1617,9 +1641,8 @@ k_params(ParamsConfig c, float bx, float by, float bz, seedgb_measurement_view m
 // ---------------------------------------------------------------------------
 
 size_t fast_kernel_smem(const TuneParams& tp) {
-    const size_t nb = static_cast<size_t>(tp.nb_cap) * (sizeof(float4) + sizeof(uint16_t));
-    return ((nb + 3) & ~size_t(3)) + (3 * kMaxSegments + 1 + 16) * sizeof(uint32_t) +
-           static_cast<size_t>(tp.fast_warps) * sizeof(FastScratch) + 16;
+    return fast_scratch_offset(static_cast<uint32_t>(tp.nb_cap)) +
+           static_cast<size_t>(tp.fast_warps) * sizeof(FastScratch);
 }
 
 int fast_kernel_max_warps(int nb_cap) {
