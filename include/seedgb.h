@@ -59,7 +59,9 @@ typedef enum {
     /* a bounded device-side wait ran out */
     SEEDGB_TIMEOUT = 5,
     SEEDGB_INVALID_ARGUMENT = 6,
-    SEEDGB_UNSUPPORTED = 7
+    SEEDGB_UNSUPPORTED = 7,
+    /* the input exceeds the fixed capacity of an allocation-free entry point */
+    SEEDGB_SIZE_LIMIT = 8
 } seedgb_status;
 
 /* traccc::seedfinder_config (core/include/traccc/seeding/detail/
@@ -282,6 +284,44 @@ seedgb_status seedgb_params_run(seedgb_params* h, const float bfield[3],
                                 seedgb_params_buffer* out, void* stream);
 
 /* ------------------------------------------------------------------------ */
+
+/* ------------------------------------------------------------------------ */
+/* Binning without device allocation                                         */
+/* ------------------------------------------------------------------------ */
+
+/* Largest event and fixed device scratch of seedgb_spacepoint_binning_noalloc.
+ * The scratch is a static array in the library's device image: every GPU that
+ * loads the library holds SEEDGB_NOALLOC_SCRATCH_BYTES (768.25 KiB) until the
+ * process exits. */
+#define SEEDGB_NOALLOC_MAX_SPACEPOINTS 65536u
+#define SEEDGB_NOALLOC_SCRATCH_BYTES (256u + 4u * 65536u + 4u * 32u * 4096u)
+
+/* No counterpart in the reference.  Bins one event into the phi-z grid like
+ * the reference's spacepoint binning and this library's seeding path
+ * (seedgb_seeding_copy_grid gives the same grid), without allocating device
+ * memory: for callers that cannot call cudaMalloc on their event path -- code
+ * running during stream capture, trigger processes that reserve all memory
+ * at start-up, plugins of frameworks that own every device allocation.
+ *
+ *   sps          device spacepoint columns, at most
+ *                SEEDGB_NOALLOC_MAX_SPACEPOINTS (else SEEDGB_SIZE_LIMIT)
+ *   bin_offsets  device, nbins + 1 entries (nbins = phi bins x z bins of
+ *                get_axes, at most 4096, else SEEDGB_SIZE_LIMIT): CSR offsets
+ *   bin_sps      device, >= sps->size entries: spacepoint indices, bins in
+ *                serial order, ascending index inside a bin
+ *
+ * Asynchronous on `stream`.  The kernel's scratch is one static device array
+ * shared by every call, which keeps the last call's contents (the kernel
+ * clears what must start at zero): calls that overlap on the GPU -- on two
+ * streams, or from two host threads -- race and corrupt each other's result;
+ * serialise them.  The first call on each device looks up the array's device
+ * address (cudaGetSymbolAddress) with that device current; make that first
+ * call before any stream capture.  Allocates nothing: no cudaMalloc, no
+ * cudaFree. */
+seedgb_status seedgb_spacepoint_binning_noalloc(
+    const seedgb_seedfinder_config* finder, const seedgb_spacepoint_grid_config* grid,
+    const seedgb_spacepoint_view* sps, uint32_t* bin_offsets, uint32_t* bin_sps,
+    void* stream);
 
 const char* seedgb_status_string(seedgb_status s);
 uint32_t seedgb_abi_version(void);

@@ -1,0 +1,68 @@
+"""The allocation-free binning entry point.
+
+seedgb_spacepoint_binning_noalloc exists for callers that cannot allocate
+device memory on their event path (code running during stream capture,
+trigger processes that reserve all memory at start-up, plugins of frameworks
+that own every allocation).  Its scratch is a fixed array in the library's
+device image that every call shares.  These tests call it through the C ABI
+and compare its grid with the one the handle-based seeding path builds
+(integer output: identical), for two calls in a row on different events, so a
+call that inherits the previous call's scratch contents is covered.  The file
+is collected last so that a run stopping at the first failure has already run
+every other test; it also passes on its own in a fresh process.
+"""
+import numpy as np
+import pytest
+
+from traccc_gb300 import seeding, synth
+
+pytestmark = pytest.mark.gpu
+
+
+def _noalloc_grid(f, g, ev):
+    import torch
+    ax = seeding.get_axes(g)
+    nb = ax.phi_bins * ax.z_bins
+    sps = seeding.SpacepointCollection.from_numpy(ev)
+    off = torch.full((nb + 1,), -1, dtype=torch.int32, device="cuda")
+    bsp = torch.full((max(1, len(sps)),), -1, dtype=torch.int32, device="cuda")
+    st = seeding.spacepoint_binning_noalloc(f, g, sps, off, bsp)
+    assert st == seeding.OK, seeding.STATUS.get(st, st)
+    torch.cuda.synchronize()
+    o = off.cpu().numpy().view(np.uint32)
+    return o, bsp.cpu().numpy().view(np.uint32)[: int(o[-1])]
+
+
+def _handle_grid(f, g, fl, ev):
+    import torch
+    alg = seeding.TripletSeedingAlgorithm(f, g, fl)
+    alg(seeding.SpacepointCollection.from_numpy(ev))
+    torch.cuda.synchronize()
+    return alg.grid(0, len(ev["layer"]))
+
+
+def test_noalloc_binning_equals_seeding_grid_two_calls():
+    f, g, fl, _ = seeding.default_configs()
+    events = [synth.workload_event("cfg1", 21), synth.workload_event("cfg2", 22, 5000)]
+    # two calls in a row on the shared scratch, then the reference grids
+    got = [_noalloc_grid(f, g, ev) for ev in events]
+    for ev, (off, bsp) in zip(events, got):
+        roff, rbsp = _handle_grid(f, g, fl, ev)
+        assert np.array_equal(off, roff)
+        assert np.array_equal(bsp, rbsp)
+        assert off[-1] > 0
+
+
+def test_noalloc_rejects_events_above_its_capacity():
+    import torch
+    f, g, _, _ = seeding.default_configs()
+    n = seeding.NOALLOC_MAX_SPACEPOINTS + 1
+    ev = {"measurement_index_1": np.arange(n, dtype=np.uint32),
+          "measurement_index_2": np.full(n, 0xFFFFFFFF, np.uint32),
+          "global": np.ones((n, 3), np.float32),
+          "z_variance": np.zeros(n, np.float32),
+          "radius_variance": np.zeros(n, np.float32)}
+    sps = seeding.SpacepointCollection.from_numpy(ev)
+    off = torch.zeros(1024, dtype=torch.int32, device="cuda")
+    bsp = torch.zeros(n, dtype=torch.int32, device="cuda")
+    assert seeding.spacepoint_binning_noalloc(f, g, sps, off, bsp) == seeding.SIZE_LIMIT

@@ -19,7 +19,7 @@ LIBDIR = os.path.join(HERE, "_lib")
 REPO = os.path.dirname(HERE)
 INCLUDE = os.path.join(REPO, "include")
 
-CUDA_SOURCES = ["seedgb_kernels.cu", "seedgb_api.cu"]
+CUDA_SOURCES = ["seedgb_kernels.cu", "seedgb_api.cu", "seedgb_noalloc.cu"]
 HOST_SOURCES = ["seedgb_config.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -96,7 +96,7 @@ def cuda_library(force: bool = False, verbose: bool = False) -> str:
             if log.strip():
                 print(log)
     objs = [o for o, _ in results]
-    cmd = [nvcc] + ARCH + ["-shared", "-o", out] + objs + ["-lcuda"]
+    cmd = [nvcc] + ARCH + ["-shared", "-o", out] + objs
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")

@@ -47,13 +47,7 @@ struct seedgb_params {
     int num_sms = 0;
 };
 
-namespace {
-
-seedgb_status cuda_status(cudaError_t e) {
-    return e == cudaSuccess ? SEEDGB_OK : SEEDGB_CUDA_ERROR;
-}
-
-size_t align_up(size_t v, size_t a = 256) { return (v + a - 1) / a * a; }
+namespace seedgb {
 
 DevConfig make_dev_config(const seedgb_seedfinder_config& f,
                           const seedgb_seedfilter_config& fl,
@@ -109,6 +103,16 @@ DevConfig make_dev_config(const seedgb_seedfinder_config& f,
     d.brute_force_triplets = 0;
     return d;
 }
+
+}  // namespace seedgb
+
+namespace {
+
+seedgb_status cuda_status(cudaError_t e) {
+    return e == cudaSuccess ? SEEDGB_OK : SEEDGB_CUDA_ERROR;
+}
+
+size_t align_up(size_t v, size_t a = 256) { return (v + a - 1) / a * a; }
 
 // Longest phi zone over all phi bins (circular::zone_t semantics).
 uint32_t max_phi_zone(uint32_t n, uint32_t s0, uint32_t s1) {

@@ -173,6 +173,7 @@ const char* seedgb_status_string(seedgb_status s) {
         case SEEDGB_TIMEOUT: return "device wait timed out";
         case SEEDGB_INVALID_ARGUMENT: return "invalid argument";
         case SEEDGB_UNSUPPORTED: return "unsupported configuration";
+        case SEEDGB_SIZE_LIMIT: return "input larger than the fixed capacity of this entry point";
     }
     return "unknown status";
 }

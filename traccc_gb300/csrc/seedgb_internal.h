@@ -137,6 +137,11 @@ struct TuneParams {
     int ctas_per_sm;
 };
 
+// Kernel-side config from the reference config structs and the grid axes.
+DevConfig make_dev_config(const seedgb_seedfinder_config& f,
+                          const seedgb_seedfilter_config& fl,
+                          const seedgb_grid_axes& ax);
+
 // Kernel launchers (seedgb_kernels.cu).  All asynchronous on `stream`.
 // timing: nullptr, or kNumKernels+1 events recorded around the kernels.
 constexpr int kNumKernels = 7;

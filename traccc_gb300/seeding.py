@@ -108,8 +108,11 @@ class _ParamsBuffer(C.Structure):
 
 STATUS = {0: "ok", 1: "empty input", 2: "bad configuration", 3: "CUDA error",
           4: "device buffer capacity exceeded", 5: "device wait timed out",
-          6: "invalid argument", 7: "unsupported configuration"}
+          6: "invalid argument", 7: "unsupported configuration",
+          8: "input larger than the fixed capacity of this entry point"}
 OK, EMPTY, BAD_CONFIG, CUDA_ERROR, CAPACITY_OVERFLOW, TIMEOUT = 0, 1, 2, 3, 4, 5
+INVALID_ARGUMENT, UNSUPPORTED, SIZE_LIMIT = 6, 7, 8
+NOALLOC_MAX_SPACEPOINTS = 65536
 OPTION_EXHAUSTIVE_TRIPLETS = 1
 OPTION_KERNEL_TIMING = 2
 KERNEL_NAMES = ("bin_count", "bin_scan", "bin_scatter", "bin_rsort", "seed_fast",
@@ -187,6 +190,9 @@ def lib():
                                         P(_SpacepointView), P(_SeedBuffer),
                                         P(_ParamsBuffer), vp]
         L.seedgb_params_run.restype = C.c_int
+        L.seedgb_spacepoint_binning_noalloc.argtypes = [
+            P(SeedfinderConfig), P(SpacepointGridConfig), P(_SpacepointView), vp, vp, vp]
+        L.seedgb_spacepoint_binning_noalloc.restype = C.c_int
         L.seedgb_status_string.argtypes = [C.c_int]
         L.seedgb_status_string.restype = C.c_char_p
         L.seedgb_abi_version.restype = C.c_uint32
@@ -358,6 +364,21 @@ class ParamsBuffer:
 # ---------------------------------------------------------------------------
 # Algorithms
 # ---------------------------------------------------------------------------
+
+
+def spacepoint_binning_noalloc(finder_config, grid_config, spacepoints, bin_offsets,
+                               bin_sps, stream=None) -> int:
+    """Bin one event into the phi-z grid without any device allocation by the
+    library (seedgb_spacepoint_binning_noalloc): for callers that must not
+    allocate on their event path.  bin_offsets (nbins + 1) and bin_sps (>= the
+    spacepoint count) are caller-owned int32 CUDA tensors.  Returns the status
+    code (SIZE_LIMIT above NOALLOC_MAX_SPACEPOINTS spacepoints)."""
+    v = spacepoints.view()
+    return int(lib().seedgb_spacepoint_binning_noalloc(
+        C.byref(finder_config), C.byref(grid_config), C.byref(v),
+        C.c_void_p(bin_offsets.data_ptr()),
+        C.c_void_p(bin_sps.data_ptr() if bin_sps is not None else 0),
+        _stream_ptr(stream)))
 
 
 class TripletSeedingAlgorithm:
