@@ -70,6 +70,22 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(values, device):
+    """Element-wise maximum of per-rank timings over all ranks (the slowest
+    replica sets the job's time)."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor(values, dtype=torch.float64, device=device)
+    if dist.is_available() and dist.is_initialized() and dist.get_world_size() > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(x) for x in t.tolist()]
+
+
+def job_throughput(events_per_rank_step, steps, world, seconds):
+    """Events of all ranks per second of the slowest rank."""
+    return world * events_per_rank_step * steps / seconds
+
+
 def make_events(n):
     from traccc_gb300 import synth
     return [synth.workload_event("cfg2", s) for s in range(n)]
@@ -367,13 +383,9 @@ def run_gpu(args):
     barrier()
     e2e_s = sum(e2e_ms) / 1e3
 
-    if world > 1:
-        t = torch.tensor([dev_s, e2e_s], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dev_s, e2e_s = float(t[0]), float(t[1])
-
-    value = world * n_ev * args.steps / dev_s
-    e2e_value = world * n_ev * args.steps / e2e_s
+    dev_s, e2e_s = max_over_ranks([dev_s, e2e_s], dev)
+    value = job_throughput(n_ev, args.steps, world, dev_s)
+    e2e_value = job_throughput(n_ev, args.steps, world, e2e_s)
 
     # roofline of the dominant kernel
     dom = max(kt_sum, key=kt_sum.get)

@@ -1,0 +1,90 @@
+"""The C ABI without a GPU: the library loads, exports every function
+include/seedgb.h declares, derives the reference's configs bit for bit like
+the oracle, and reports errors as status codes (no exceptions, no crashes)."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+
+import oracle as O
+from traccc_gb300 import seeding
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    text = open(os.path.join(ROOT, "include", "seedgb.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"^\s*[A-Za-z_][\w\s\*]*?\b(seedgb_\w+)\s*\(", text, re.M)))
+
+
+def test_library_exports_every_declared_function():
+    names = declared_functions()
+    assert len(names) >= 20
+    lib = C.CDLL(seeding.library_path())
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def _fields(s):
+    out = {}
+    for name, _ in s._fields_:
+        v = getattr(s, name)
+        out[name] = list(v) if hasattr(v, "__len__") else v
+    return out
+
+
+def _bits(d):
+    return {k: (np.asarray(v, np.float32).view(np.uint32).tolist()
+                if isinstance(v, (float, list)) else v) for k, v in d.items()}
+
+
+def test_configs_match_the_oracle_bit_for_bit():
+    f, g, fl, tp = seeding.default_configs()
+    of, og, ofl, otp = O.default_configs()
+    for ours, theirs in ((f, of), (g, og), (fl, ofl), (tp, otp)):
+        a, b = _fields(ours), _fields(theirs)
+        assert a.keys() == b.keys()
+        assert _bits(a) == _bits(b)
+
+
+def test_axes_match_the_oracle():
+    f, g, _, _ = seeding.default_configs()
+    a = seeding.get_axes(g)
+    b = O.get_axes(O.default_configs()[1])
+    assert (a.phi_bins, a.z_bins, a.phi_min, a.phi_max, a.z_min, a.z_max) == \
+        (b.phi_bins, b.z_bins, b.phi_min, b.phi_max, b.z_min, b.z_max)
+    # a modified config follows setup() identically
+    f.minPt = 0.9
+    f.setup()
+    of = O.default_configs()[0]
+    of.minPt = 0.9
+    O.lib().or_finder_config_setup(C.byref(of))
+    assert _bits(_fields(f)) == _bits(_fields(of))
+
+
+def test_bad_config_is_a_status_not_an_exception():
+    f, g, fl, _ = seeding.default_configs()
+    g.minPt = 0.01
+    a = seeding.GridAxes()
+    assert seeding.lib().seedgb_get_axes(C.byref(g), C.byref(a)) == seeding.BAD_CONFIG
+
+
+def test_status_strings():
+    L = seeding.lib()
+    for s in range(9):
+        assert L.seedgb_status_string(s)
+    assert L.seedgb_status_string(99) == b"unknown status"
+    assert L.seedgb_abi_version() == 1
+
+
+def test_invalid_arguments_are_rejected_before_device_work():
+    L = seeding.lib()
+    assert L.seedgb_seeding_run(None, None, None, None) == seeding.INVALID_ARGUMENT
+    assert L.seedgb_seeding_destroy(None) == seeding.INVALID_ARGUMENT
+    f, g, _, _ = seeding.default_configs()
+    v = seeding._SpacepointView(0, 0, 1, 0, 0, seeding.NOALLOC_MAX_SPACEPOINTS + 1)
+    st = L.seedgb_spacepoint_binning_noalloc(C.byref(f), C.byref(g), C.byref(v),
+                                             C.c_void_p(1), C.c_void_p(1), None)
+    assert st == seeding.SIZE_LIMIT
