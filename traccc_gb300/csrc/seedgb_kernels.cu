@@ -1083,12 +1083,16 @@ __device__ MiddleResult process_middle(const DevConfig& c, const Arena& a,
 
     // -- the middle's triplets in host order: (bottom host position, top
     //    host position) ascending, so the triplets of one middle-bottom
-    //    doublet form a run ordered as triplet_finding.hpp:109-179 visits them
+    //    doublet form a run ordered as triplet_finding.hpp:109-179 visits them,
+    //    and the position in this order breaks exact ties of the final sort
+    //    as the reference's triplet list order does
     {
         uint32_t P = 1;
         while (P < n_ct) P <<= 1;
         for (uint32_t i = lane; i < P; i += 32) {
-            ws.skey[i] = i < n_ct ? ((static_cast<uint32_t>(ws.ct[i].ib) << 16) |
+            // host order: the bottom's host position (the middle-bottom list
+            // itself is in radius order), then the top's
+            ws.skey[i] = i < n_ct ? ((nb.hpos(ws.qb[ws.ct[i].ib]) << 16) |
                                      ws.hpt[ws.ct[i].tp])
                                   : 0xffffffffu;
             ws.sidx[i] = static_cast<uint16_t>(i);
@@ -1119,9 +1123,10 @@ __device__ MiddleResult process_middle(const DevConfig& c, const Arena& a,
     //    single_seed_cut (seed_selecting_helper.hpp:27-62)
     for (uint32_t k = lane; k < n_ct; k += 32) {
         const TripCand T = ws.ct[ws.sidx[k]];
+        const uint32_t hB = ws.skey[k] >> 16;
         uint32_t b = k, e = k + 1;
-        while (b > 0 && (ws.skey[b - 1] >> 16) == T.ib) --b;
-        while (e < n_ct && (ws.skey[e] >> 16) == T.ib) ++e;
+        while (b > 0 && (ws.skey[b - 1] >> 16) == hB) --b;
+        while (e < n_ct && (ws.skey[e] >> 16) == hB) ++e;
         const float4 Tp = nb.get(ws.ppt[T.tp]);
         float w = T.w;
         if (e - b > 1) {
