@@ -55,11 +55,15 @@ L2_FLUSH_BYTES = 256 << 20
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--steps", type=int, default=30)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="seedgb", choices=["seedgb", "reference"])
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--events", type=int, default=N_EVENTS)
+    p.add_argument("--no-batched", action="store_true",
+                   help="skip the 64-event graph-launched batch")
+    p.add_argument("--retune", action="store_true",
+                   help="search launch shapes even if the tuning table has an entry")
     return p.parse_args()
 
 
@@ -89,6 +93,145 @@ def job_throughput(events_per_rank_step, steps, world, seconds):
 def make_events(n):
     from traccc_gb300 import synth
     return [synth.workload_event("cfg2", s) for s in range(n)]
+
+
+BATCH_EVENTS = 64
+BATCH_SEED = 3
+BATCH_WORKLOAD = ("cfg3: 64 synthetic events (batch seed 3) with U(500, 12000) helices each "
+                  "+ 12% noise, cfg2 pT/eta/z0 statistics, one graph launch per batch")
+
+
+def quantile(xs, q):
+    xs = sorted(xs)
+    if not xs:
+        return None
+    k = (len(xs) - 1) * q
+    lo, hi = int(np.floor(k)), int(np.ceil(k))
+    return xs[lo] + (xs[hi] - xs[lo]) * (k - lo)
+
+
+def tune_table_path():
+    return os.environ.get("SEEDGB_TUNE_TABLE",
+                          os.path.join(ROOT, "traccc_gb300", "_lib", "tune_table.json"))
+
+
+def run_batched(args, dev, stream, flush_buf):
+    """The uneven 64-event batch through the captured graph: autotuned launch
+    shape, events/s over K batches, p50/p99 per-batch latency (device time of
+    one graph launch, L2 flushed before each), and the same end to end (pinned
+    host columns in, seeds out, wall clock)."""
+    import torch
+
+    from traccc_gb300 import autotune, seeding, synth
+    events = synth.batch_events(BATCH_EVENTS, BATCH_SEED)
+    sizes = [len(e["layer"]) for e in events]
+    offs = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+    total = int(offs[-1])
+
+    def cat(key, dt, shape=()):
+        return np.ascontiguousarray(np.concatenate(
+            [np.asarray(e[key]).reshape((-1,) + shape) for e in events]).astype(dt))
+
+    host = {"mi1": cat("measurement_index_1", np.uint32).view(np.int32),
+            "mi2": cat("measurement_index_2", np.uint32).view(np.int32),
+            "glob": cat("global", np.float32, (3,)),
+            "zvar": cat("z_variance", np.float32),
+            "rvar": cat("radius_variance", np.float32)}
+    pinned = {k: torch.from_numpy(v).pin_memory() for k, v in host.items()}
+    dcols = {k: v.to(dev) for k, v in pinned.items()}
+    alg = seeding.TripletSeedingAlgorithm()
+    sps, outs = [], []
+    size_all = torch.zeros(BATCH_EVENTS, dtype=torch.int32, device=dev)
+    for e in range(BATCH_EVENTS):
+        a, b = int(offs[e]), int(offs[e + 1])
+        sps.append(seeding.SpacepointCollection(dcols["mi1"][a:b], dcols["mi2"][a:b],
+                                                dcols["glob"][a:b], dcols["zvar"][a:b],
+                                                dcols["rvar"][a:b]))
+        so = seeding.SeedBuffer(alg.max_seeds(b - a), device=dev)
+        so.size = size_all[e:e + 1]
+        outs.append(so)
+    mean_sp = total / BATCH_EVENTS
+    path = tune_table_path()
+    table = autotune.load(path)
+    shape = None if args.retune else autotune.lookup(table, mean_sp)
+    t0 = time.perf_counter()
+    if shape is None:
+        shape, report = autotune.tune(alg, sps, outs, stream=stream)
+        try:
+            os.makedirs(os.path.dirname(path), exist_ok=True)
+            autotune.store(path, mean_sp, shape, report)
+        except OSError:
+            pass
+        tuned = {"shape": list(shape), "source": "searched", "measured": len(report),
+                 "search_s": time.perf_counter() - t0,
+                 "top3": report[:3], "default_ms": next(
+                     (r["ms"] for r in report if r["shape"][1:] == [128, 2560, 1]), None)}
+    else:
+        alg.set_tune(*shape)
+        alg.graph_create(BATCH_EVENTS, total)
+        tuned = {"shape": list(alg.get_tune()), "source": "table " + os.path.basename(path)}
+    sptr = stream.cuda_stream
+    for _ in range(max(3, args.warmup)):
+        alg.graph_launch(sps, outs, stream=sptr)
+    torch.cuda.synchronize()
+    st = alg.last_status(sptr)
+    if st != seeding.OK:
+        raise RuntimeError(f"batched seeding status {st}")
+    n_seeds = int(size_all.sum().item())
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2 * args.steps)]
+    for k in range(args.steps):
+        flush_buf.fill_(1)
+        ev[2 * k].record(stream)
+        alg.graph_launch(sps, outs, stream=sptr)
+        ev[2 * k + 1].record(stream)
+    torch.cuda.synchronize()
+    lat = [ev[2 * k].elapsed_time(ev[2 * k + 1]) for k in range(args.steps)]
+    # end to end: columns in from pinned memory, seeds out, per batch
+    h_size = torch.zeros(BATCH_EVENTS, dtype=torch.int32).pin_memory()
+    h_seeds = torch.empty((4, sum(o.capacity for o in outs)), dtype=torch.int32).pin_memory()
+    h2d = sum(v.numel() * v.element_size() for v in pinned.values())
+
+    def e2e_batch():
+        for k in dcols:
+            dcols[k].copy_(pinned[k], non_blocking=True)
+        alg.graph_launch(sps, outs, stream=sptr)
+        h_size.copy_(size_all, non_blocking=True)
+        stream.synchronize()
+        o, d2h = 0, 4 * BATCH_EVENTS
+        for e in range(BATCH_EVENTS):
+            ns = int(h_size[e])
+            so = outs[e]
+            for j, col in enumerate((so.bottom_index, so.middle_index, so.top_index)):
+                h_seeds[j, o:o + ns].copy_(col[:ns], non_blocking=True)
+            h_seeds[3, o:o + ns].copy_(so.quality[:ns].view(torch.int32), non_blocking=True)
+            o += ns
+            d2h += 16 * ns
+        stream.synchronize()
+        return d2h
+
+    for _ in range(max(1, args.warmup)):
+        e2e_batch()
+    e2e_lat, d2h = [], 0
+    for _ in range(args.steps):
+        flush_buf.fill_(1)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        d2h = e2e_batch()
+        e2e_lat.append(1e3 * (time.perf_counter() - t0))
+    return {
+        "workload": BATCH_WORKLOAD, "events_per_batch": BATCH_EVENTS,
+        "spacepoints_per_batch": total, "min_max_spacepoints": [min(sizes), max(sizes)],
+        "seeds_per_batch": n_seeds,
+        "value": BATCH_EVENTS * args.steps / (sum(lat) / 1e3), "unit": "events/s",
+        "latency_ms": {"p50": quantile(lat, 0.5), "p99": quantile(lat, 0.99),
+                       "max": max(lat), "batches": len(lat)},
+        "e2e": {"value": BATCH_EVENTS * args.steps / (sum(e2e_lat) / 1e3), "unit": "events/s",
+                "latency_ms": {"p50": quantile(e2e_lat, 0.5), "p99": quantile(e2e_lat, 0.99)},
+                "h2d_bytes_per_batch": int(h2d), "d2h_bytes_per_batch": int(d2h)},
+        "autotune": tuned,
+        "gpu_launches_per_batch": len(seeding.KERNEL_NAMES),
+        "l2": "flushed before each batch (256 MiB write)",
+    }
 
 
 # ---------------------------------------------------------------------------
@@ -362,7 +505,6 @@ def run_gpu(args):
     torch.cuda.synchronize()
     wall = time.perf_counter() - wall0
     barrier()
-    clocks = sampler.stop()
     dev_s = sum(step_ms) / 1e3
 
     # -- timed: end to end through the API from host buffers
@@ -382,6 +524,10 @@ def run_gpu(args):
         e2e_ms.append(1e3 * (time.perf_counter() - t0))
     barrier()
     e2e_s = sum(e2e_ms) / 1e3
+    batched = None
+    if not args.no_batched and world == 1:
+        batched = run_batched(args, dev, stream, flush_buf)
+    clocks = sampler.stop()
 
     dev_s, e2e_s = max_over_ranks([dev_s, e2e_s], dev)
     value = job_throughput(n_ev, args.steps, world, dev_s)
@@ -452,6 +598,8 @@ def run_gpu(args):
                  "triplets": counters["n_triplets"],
                  "overflow_middles": counters["n_overflow_middles"]},
     }
+    if batched is not None:
+        line["batched"] = batched
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(events)
     if rank == 0:

@@ -262,6 +262,45 @@ seedgb_status seedgb_seeding_set_option(seedgb_seeding* h, seedgb_option opt,
 seedgb_status seedgb_seeding_kernel_times(seedgb_seeding* h, float ms[7]);
 
 /* ------------------------------------------------------------------------ */
+/* Batched, graph-captured launches.  No counterpart in the reference, which */
+/* overlaps events with one CUDA stream per host thread (throughput_mt.ipp:  */
+/* 171-179); here a whole batch of uneven events runs as one captured launch */
+/* sequence whose persistent seeding kernel load-balances across events.     */
+/* ------------------------------------------------------------------------ */
+
+/* Capture the launch sequence (descriptor copy, counter reset, the seven
+ * kernels) for batches of up to max_events events with up to
+ * max_total_spacepoints spacepoints together.  Grids are sized for that
+ * capacity; the kernels read the batch's actual sizes from device memory, so
+ * one captured graph serves every batch within it.  Allocates the arena for
+ * the capacity; later runs within it allocate nothing. */
+seedgb_status seedgb_seeding_graph_create(seedgb_seeding* h, uint32_t max_events,
+                                          uint64_t max_total_spacepoints);
+
+/* Same contract and output as seedgb_seeding_run_batch, through the captured
+ * graph: one cudaGraphLaunch per batch.  SEEDGB_SIZE_LIMIT when the batch
+ * exceeds the captured capacity.  Two graph slots alternate, so the host
+ * prepares batch k+1 while batch k runs; it waits only for batch k-1.
+ * Changing the options or the tuning re-captures on the next launch. */
+seedgb_status seedgb_seeding_graph_launch(seedgb_seeding* h,
+                                          const seedgb_spacepoint_view* events,
+                                          uint32_t n_events, seedgb_seed_buffer* outs,
+                                          void* stream);
+
+/* Launch shape of the seeding kernel (the autotuner's search space).  No
+ * counterpart in the reference.  warps_per_cta is clamped to what fits in
+ * shared memory with the given neighbourhood capacity (read it back with
+ * seedgb_seeding_get_tune).  Results do not depend on the tuning. */
+typedef struct {
+    int32_t warps_per_cta;          /* 1..16: warps (middle spacepoints in flight) per CTA */
+    int32_t middles_per_item;       /* 1..4096: middle spacepoints per work item */
+    int32_t neighbourhood_capacity; /* 256..8192: spacepoints staged in shared memory */
+    int32_t ctas_per_sm;            /* 1..8: resident CTAs per SM of the persistent grid */
+} seedgb_tune;
+seedgb_status seedgb_seeding_set_tune(seedgb_seeding* h, const seedgb_tune* t);
+seedgb_status seedgb_seeding_get_tune(seedgb_seeding* h, seedgb_tune* t);
+
+/* ------------------------------------------------------------------------ */
 /* Track parameter estimation                                                */
 /* ------------------------------------------------------------------------ */
 

@@ -17,6 +17,19 @@
 
 using namespace seedgb;
 
+// Pinned host copy of what a launch sequence reads first: the batch header
+// (kHdrBytes) followed by the event descriptors, copied to the device in one
+// transfer.  `done` is recorded after the transfer that reads it.
+constexpr size_t kHdrBytes = 256;
+
+struct Staging {
+    uint8_t* host = nullptr;
+    uint32_t cap = 0;
+    cudaEvent_t done = nullptr;
+    BatchHeader* hdr() { return reinterpret_cast<BatchHeader*>(host); }
+    EventDesc* desc() { return reinterpret_cast<EventDesc*>(host + kHdrBytes); }
+};
+
 struct seedgb_seeding {
     seedgb_seedfinder_config finder;
     seedgb_spacepoint_grid_config grid;
@@ -31,11 +44,18 @@ struct seedgb_seeding {
     size_t arena_bytes = 0;
     uint32_t cap_events = 0;
     uint64_t cap_sp = 0;
+    uint32_t cap_chunks = 0;
     Arena a{};
-    // pinned staging of the event descriptors
-    EventDesc* h_desc = nullptr;
-    uint32_t h_desc_cap = 0;
-    cudaEvent_t staged = nullptr;
+    // staging[0]: direct runs; staging[1], staging[2]: the two graph slots
+    Staging staging[3];
+    // captured launch sequences (two, alternating, so that the host fills one
+    // slot's descriptors while the other slot's graph runs)
+    cudaGraphExec_t gexec[2] = {nullptr, nullptr};
+    uint32_t g_events = 0;      // capacity the graphs were captured for
+    uint64_t g_sp = 0;
+    bool g_valid = false;
+    int g_next = 0;
+    cudaStream_t cap_stream = nullptr;
     unsigned long long h_counters[kNumCounters] = {};
     bool timing = false;
     bool timed_run = false;
@@ -133,22 +153,57 @@ uint32_t max_phi_zone(uint32_t n, uint32_t s0, uint32_t s1) {
 
 uint32_t chunks_of(uint32_t n_sp) { return (n_sp + kBinChunk - 1) / kBinChunk; }
 
+uint32_t chunk_capacity(uint32_t events, uint64_t sp) {
+    return static_cast<uint32_t>(sp / kBinChunk) + events;
+}
+
+uint32_t item_capacity(uint32_t events, uint64_t sp, uint32_t nb, uint32_t mpi) {
+    return static_cast<uint32_t>(sp / mpi) + events * nb + 1;
+}
+
+void drop_graphs(seedgb_seeding* h) {
+    for (auto& g : h->gexec) {
+        if (g) cudaGraphExecDestroy(g);
+        g = nullptr;
+    }
+    h->g_valid = false;
+}
+
+seedgb_status ensure_staging(Staging& st, uint32_t events) {
+    if (!st.done && cudaEventCreateWithFlags(&st.done, cudaEventDisableTiming) != cudaSuccess)
+        return SEEDGB_CUDA_ERROR;
+    if (st.cap >= events) return SEEDGB_OK;
+    if (cudaEventSynchronize(st.done) != cudaSuccess) return SEEDGB_CUDA_ERROR;
+    if (st.host) cudaFreeHost(st.host);
+    st.host = nullptr;
+    st.cap = 0;
+    const size_t bytes = kHdrBytes + sizeof(EventDesc) * events;
+    void* p = nullptr;
+    if (cudaMallocHost(&p, bytes) != cudaSuccess) return SEEDGB_CUDA_ERROR;
+    std::memset(p, 0, bytes);
+    st.host = static_cast<uint8_t*>(p);
+    st.cap = events;
+    return SEEDGB_OK;
+}
+
+// Size the arena for a batch; reallocation (which drops the captured graphs)
+// only when the batch does not fit what is there.
 seedgb_status ensure_arena(seedgb_seeding* h, uint32_t n_events, uint64_t total_sp,
                            uint32_t total_chunks) {
     const uint32_t nb = h->dc.nbins;
     const uint32_t mpi = static_cast<uint32_t>(h->tune.middles_per_item);
-    if (h->arena && n_events <= h->cap_events && total_sp <= h->cap_sp) {
-        const uint32_t cap_chunks =
-            static_cast<uint32_t>(h->cap_sp / kBinChunk) + h->cap_events;
-        if (total_chunks <= cap_chunks) return SEEDGB_OK;
-    }
+    if (h->arena && n_events <= h->cap_events && total_sp <= h->cap_sp &&
+        total_chunks <= h->cap_chunks &&
+        item_capacity(h->cap_events, h->cap_sp, nb, mpi) <= h->a.max_items)
+        return ensure_staging(h->staging[0], h->cap_events);
     const uint32_t ce = std::max(n_events, h->cap_events);
     const uint64_t cs = std::max<uint64_t>(std::max<uint64_t>(total_sp, h->cap_sp), 1);
     if (cs > 0xF0000000ull) return SEEDGB_UNSUPPORTED;
-    const uint32_t cc = static_cast<uint32_t>(cs / kBinChunk) + ce;
-    const uint32_t ci = static_cast<uint32_t>(cs / mpi) + ce * nb + 1;
+    const uint32_t cc = std::max(chunk_capacity(ce, cs), total_chunks);
+    const uint32_t ci = item_capacity(ce, cs, nb, mpi);
     size_t off = 0;
     auto take = [&off](size_t bytes) { const size_t o = off; off = align_up(off + bytes); return o; };
+    const size_t o_hdr = take(kHdrBytes);
     const size_t o_events = take(sizeof(EventDesc) * ce);
     const size_t o_spbin = take(sizeof(int32_t) * cs);
     const size_t o_whist = take(sizeof(uint32_t) * static_cast<size_t>(cc) * kBinWarps * nb);
@@ -165,7 +220,12 @@ seedgb_status ensure_arena(seedgb_seeding* h, uint32_t n_events, uint64_t total_
     const size_t o_slot = take(sizeof(SeedSlot) * cs * kMaxSeedsPerMiddle);
     const size_t o_ovf = take(sizeof(uint32_t) * cs);
     const size_t o_ctr = take(sizeof(unsigned long long) * kNumCounters);
+    static_assert(kHdrBytes >= sizeof(BatchHeader) && kHdrBytes % 256 == 0,
+                  "the descriptors follow the header directly");
+    drop_graphs(h);
     if (h->arena) {
+        // in-flight work of this handle may still use the old arena
+        if (cudaDeviceSynchronize() != cudaSuccess) return SEEDGB_CUDA_ERROR;
         cudaFree(h->arena);
         h->arena = nullptr;
     }
@@ -173,14 +233,17 @@ seedgb_status ensure_arena(seedgb_seeding* h, uint32_t n_events, uint64_t total_
     if (cudaMalloc(&p, off) != cudaSuccess) {
         h->cap_events = 0;
         h->cap_sp = 0;
+        h->cap_chunks = 0;
         return SEEDGB_CUDA_ERROR;
     }
     h->arena = p;
     h->arena_bytes = off;
     h->cap_events = ce;
     h->cap_sp = cs;
+    h->cap_chunks = cc;
     char* base = static_cast<char*>(p);
     Arena& a = h->a;
+    a.hdr = reinterpret_cast<BatchHeader*>(base + o_hdr);
     a.events = reinterpret_cast<EventDesc*>(base + o_events);
     a.sp_bin = reinterpret_cast<int32_t*>(base + o_spbin);
     a.whist = reinterpret_cast<uint32_t*>(base + o_whist);
@@ -197,16 +260,120 @@ seedgb_status ensure_arena(seedgb_seeding* h, uint32_t n_events, uint64_t total_
     a.seed_slot = reinterpret_cast<SeedSlot*>(base + o_slot);
     a.ovf = reinterpret_cast<uint32_t*>(base + o_ovf);
     a.counters = reinterpret_cast<unsigned long long*>(base + o_ctr);
+    a.cap_events = ce;
+    a.cap_chunks = cc;
+    a.cap_sp = static_cast<uint32_t>(cs);
     a.max_items = ci;
-    if (h->h_desc_cap < ce) {
-        if (h->h_desc) cudaFreeHost(h->h_desc);
-        h->h_desc = nullptr;
-        if (cudaMallocHost(&h->h_desc, sizeof(EventDesc) * ce) != cudaSuccess) {
-            h->h_desc_cap = 0;
+    return ensure_staging(h->staging[0], ce);
+}
+
+// Validates a batch and writes its header and descriptors into `st`
+// (which the caller has waited for).
+seedgb_status stage_batch(Staging& st, const seedgb_spacepoint_view* events, uint32_t n_events,
+                          const seedgb_seed_buffer* outs) {
+    uint32_t sp_base = 0, chunk_base = 0;
+    for (uint32_t e = 0; e < n_events; ++e) {
+        const seedgb_spacepoint_view& v = events[e];
+        EventDesc& d = st.desc()[e];
+        d.mi1 = v.measurement_index_1;
+        d.mi2 = v.measurement_index_2;
+        d.global = v.global;
+        d.zvar = v.z_variance;
+        d.rvar = v.radius_variance;
+        d.n_sp = v.size;
+        d.sp_base = sp_base;
+        d.chunk_base = chunk_base;
+        d.n_chunks = chunks_of(v.size);
+        d.out_b = outs[e].bottom_index;
+        d.out_m = outs[e].middle_index;
+        d.out_t = outs[e].top_index;
+        d.out_q = outs[e].quality;
+        d.out_cap = outs[e].capacity;
+        d.pad = 0;
+        d.out_size = outs[e].size;
+        sp_base += v.size;
+        chunk_base += d.n_chunks;
+    }
+    BatchHeader& hb = *st.hdr();
+    hb.n_events = n_events;
+    hb.total_chunks = chunk_base;
+    hb.total_sp = sp_base;
+    hb.pad = 0;
+    return SEEDGB_OK;
+}
+
+// Checks the arguments of a batch and sums its sizes.
+seedgb_status check_batch(const seedgb_spacepoint_view* events, uint32_t n_events,
+                          const seedgb_seed_buffer* outs, uint64_t* total_sp,
+                          uint32_t* total_chunks) {
+    if (!events || !outs || n_events == 0) return SEEDGB_INVALID_ARGUMENT;
+    if (n_events > kMaxEventsPerBatch) return SEEDGB_UNSUPPORTED;
+    uint64_t sp = 0;
+    uint64_t chunks = 0;
+    for (uint32_t e = 0; e < n_events; ++e) {
+        const seedgb_spacepoint_view& v = events[e];
+        if (v.size > 0 && !v.global) return SEEDGB_INVALID_ARGUMENT;
+        if (!outs[e].size || (outs[e].capacity > 0 &&
+                              (!outs[e].bottom_index || !outs[e].middle_index ||
+                               !outs[e].top_index || !outs[e].quality)))
+            return SEEDGB_INVALID_ARGUMENT;
+        sp += v.size;
+        chunks += chunks_of(v.size);
+    }
+    if (sp > 0xF0000000ull) return SEEDGB_UNSUPPORTED;
+    *total_sp = sp;
+    *total_chunks = static_cast<uint32_t>(chunks);
+    return SEEDGB_OK;
+}
+
+// Enqueues header + descriptor copy, counter reset and the kernels.
+// copied: recorded once the staging buffer has been read (nullptr: none).
+cudaError_t enqueue_batch(seedgb_seeding* h, Staging& st, uint32_t staged_events,
+                          const BatchHeader& grid, cudaStream_t s, cudaEvent_t copied,
+                          cudaEvent_t* timing) {
+    cudaError_t err = cudaMemcpyAsync(h->a.hdr, st.host,
+                                      kHdrBytes + sizeof(EventDesc) * staged_events,
+                                      cudaMemcpyHostToDevice, s);
+    if (err == cudaSuccess && copied) err = cudaEventRecord(copied, s);
+    if (err == cudaSuccess)
+        err = cudaMemsetAsync(h->a.counters, 0, sizeof(unsigned long long) * kNumCounters, s);
+    if (err == cudaSuccess)
+        err = launch_seeding(h->dc, h->a, grid, h->tune, h->num_sms, s, timing);
+    return err;
+}
+
+// Captures the two graph slots for batches up to h->g_events / h->g_sp.
+seedgb_status capture_graphs(seedgb_seeding* h) {
+    drop_graphs(h);
+    const uint32_t ce = h->g_events;
+    const uint64_t cs = h->g_sp;
+    seedgb_status st = ensure_arena(h, ce, cs, chunk_capacity(ce, cs));
+    if (st != SEEDGB_OK) return st;
+    if (!h->cap_stream &&
+        cudaStreamCreateWithFlags(&h->cap_stream, cudaStreamNonBlocking) != cudaSuccess)
+        return SEEDGB_CUDA_ERROR;
+    if (prepare_kernels() != cudaSuccess) return SEEDGB_CUDA_ERROR;
+    const BatchHeader grid{ce, chunk_capacity(ce, cs), static_cast<uint32_t>(cs), 0};
+    for (int k = 0; k < 2; ++k) {
+        Staging& sg = h->staging[1 + k];
+        st = ensure_staging(sg, ce);
+        if (st != SEEDGB_OK) return st;
+        cudaGraph_t g = nullptr;
+        cudaError_t err = cudaStreamBeginCapture(h->cap_stream, cudaStreamCaptureModeThreadLocal);
+        if (err == cudaSuccess) {
+            const cudaError_t e1 = enqueue_batch(h, sg, ce, grid, h->cap_stream, nullptr, nullptr);
+            err = cudaStreamEndCapture(h->cap_stream, &g);
+            if (e1 != cudaSuccess) err = e1;
+        }
+        if (err == cudaSuccess) err = cudaGraphInstantiate(&h->gexec[k], g, 0);
+        if (g) cudaGraphDestroy(g);
+        if (err != cudaSuccess) {
+            drop_graphs(h);
             return SEEDGB_CUDA_ERROR;
         }
-        h->h_desc_cap = ce;
     }
+    h->g_valid = true;
+    h->g_next = 0;
     return SEEDGB_OK;
 }
 
@@ -246,8 +413,8 @@ seedgb_status seedgb_seeding_create(const seedgb_seedfinder_config* finder,
     if (cudaGetDevice(&h->device) != cudaSuccess ||
         cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device) !=
             cudaSuccess ||
-        cudaEventCreateWithFlags(&h->staged, cudaEventDisableTiming) != cudaSuccess) {
-        delete h;
+        ensure_staging(h->staging[0], 1) != SEEDGB_OK) {
+        seedgb_seeding_destroy(h);
         return SEEDGB_CUDA_ERROR;
     }
     h->tune.fast_warps = 16;  // clamped below to what fits in shared memory
@@ -261,7 +428,7 @@ seedgb_status seedgb_seeding_create(const seedgb_seedfinder_config* finder,
             h->tune = TuneParams{w, m, nb, c};
         }
     }
-    const int mw = fast_kernel_max_warps(h->tune.nb_cap);
+    const int mw = fast_kernel_max_warps(h->tune.nb_cap, h->tune.ctas_per_sm);
     if (mw < 1) {
         seedgb_seeding_destroy(h);
         return SEEDGB_UNSUPPORTED;
@@ -273,9 +440,19 @@ seedgb_status seedgb_seeding_create(const seedgb_seedfinder_config* finder,
 
 seedgb_status seedgb_seeding_destroy(seedgb_seeding* h) {
     if (!h) return SEEDGB_INVALID_ARGUMENT;
-    if (h->arena) cudaFree(h->arena);
-    if (h->h_desc) cudaFreeHost(h->h_desc);
-    if (h->staged) cudaEventDestroy(h->staged);
+    drop_graphs(h);
+    if (h->arena) {
+        cudaDeviceSynchronize();
+        cudaFree(h->arena);
+    }
+    for (auto& st : h->staging) {
+        if (st.done) {
+            cudaEventSynchronize(st.done);
+            cudaEventDestroy(st.done);
+        }
+        if (st.host) cudaFreeHost(st.host);
+    }
+    if (h->cap_stream) cudaStreamDestroy(h->cap_stream);
     for (auto& e : h->tev)
         if (e) cudaEventDestroy(e);
     delete h;
@@ -285,70 +462,93 @@ seedgb_status seedgb_seeding_destroy(seedgb_seeding* h) {
 seedgb_status seedgb_seeding_reserve(seedgb_seeding* h, uint32_t max_events,
                                      uint64_t max_total_spacepoints) {
     if (!h || max_events == 0) return SEEDGB_INVALID_ARGUMENT;
-    const uint32_t chunks =
-        static_cast<uint32_t>(max_total_spacepoints / kBinChunk) + max_events;
-    return ensure_arena(h, max_events, max_total_spacepoints, chunks);
+    if (max_total_spacepoints > 0xF0000000ull) return SEEDGB_UNSUPPORTED;
+    return ensure_arena(h, max_events, max_total_spacepoints,
+                        chunk_capacity(max_events, max_total_spacepoints));
 }
 
 seedgb_status seedgb_seeding_run_batch(seedgb_seeding* h, const seedgb_spacepoint_view* events,
                                        uint32_t n_events, seedgb_seed_buffer* outs,
                                        void* stream) {
-    if (!h || !events || !outs || n_events == 0) return SEEDGB_INVALID_ARGUMENT;
-    if (n_events > kMaxEventsPerBatch) return SEEDGB_UNSUPPORTED;
+    if (!h) return SEEDGB_INVALID_ARGUMENT;
     uint64_t total_sp = 0;
     uint32_t total_chunks = 0;
-    for (uint32_t e = 0; e < n_events; ++e) {
-        const seedgb_spacepoint_view& v = events[e];
-        if (v.size > 0 && !v.global) return SEEDGB_INVALID_ARGUMENT;
-        if (!outs[e].size || (outs[e].capacity > 0 &&
-                              (!outs[e].bottom_index || !outs[e].middle_index ||
-                               !outs[e].top_index || !outs[e].quality)))
-            return SEEDGB_INVALID_ARGUMENT;
-        total_sp += v.size;
-        total_chunks += chunks_of(v.size);
-    }
-    if (total_sp > 0xF0000000ull) return SEEDGB_UNSUPPORTED;
-    seedgb_status st = ensure_arena(h, n_events, total_sp, total_chunks);
+    seedgb_status st = check_batch(events, n_events, outs, &total_sp, &total_chunks);
+    if (st != SEEDGB_OK) return st;
+    st = ensure_arena(h, n_events, total_sp, total_chunks);
     if (st != SEEDGB_OK) return st;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
+    Staging& sg = h->staging[0];
     // the staging buffer may still feed the previous call's copy
-    if (cudaEventSynchronize(h->staged) != cudaSuccess) return SEEDGB_CUDA_ERROR;
-    uint32_t sp_base = 0, chunk_base = 0;
-    for (uint32_t e = 0; e < n_events; ++e) {
-        const seedgb_spacepoint_view& v = events[e];
-        EventDesc& d = h->h_desc[e];
-        d.mi1 = v.measurement_index_1;
-        d.mi2 = v.measurement_index_2;
-        d.global = v.global;
-        d.zvar = v.z_variance;
-        d.rvar = v.radius_variance;
-        d.n_sp = v.size;
-        d.sp_base = sp_base;
-        d.chunk_base = chunk_base;
-        d.n_chunks = chunks_of(v.size);
-        d.out_b = outs[e].bottom_index;
-        d.out_m = outs[e].middle_index;
-        d.out_t = outs[e].top_index;
-        d.out_q = outs[e].quality;
-        d.out_cap = outs[e].capacity;
-        d.pad = 0;
-        d.out_size = outs[e].size;
-        sp_base += v.size;
-        chunk_base += d.n_chunks;
-    }
-    Arena a = h->a;
-    a.n_events = n_events;
-    a.total_chunks = total_chunks;
-    a.total_sp = static_cast<uint32_t>(total_sp);
-    cudaError_t err = cudaMemcpyAsync(a.events, h->h_desc, sizeof(EventDesc) * n_events,
-                                      cudaMemcpyHostToDevice, s);
-    if (err == cudaSuccess) err = cudaEventRecord(h->staged, s);
-    if (err == cudaSuccess)
-        err = cudaMemsetAsync(a.counters, 0, sizeof(unsigned long long) * kNumCounters, s);
-    if (err == cudaSuccess)
-        err = launch_seeding(h->dc, a, h->tune, h->num_sms, s, h->timing ? h->tev : nullptr);
+    if (cudaEventSynchronize(sg.done) != cudaSuccess) return SEEDGB_CUDA_ERROR;
+    stage_batch(sg, events, n_events, outs);
+    const BatchHeader grid = *sg.hdr();
+    const cudaError_t err =
+        enqueue_batch(h, sg, n_events, grid, s, sg.done, h->timing ? h->tev : nullptr);
     h->timed_run = h->timing && err == cudaSuccess;
     return cuda_status(err);
+}
+
+seedgb_status seedgb_seeding_graph_create(seedgb_seeding* h, uint32_t max_events,
+                                          uint64_t max_total_spacepoints) {
+    if (!h || max_events == 0 || max_events > kMaxEventsPerBatch)
+        return SEEDGB_INVALID_ARGUMENT;
+    if (max_total_spacepoints > 0xF0000000ull) return SEEDGB_UNSUPPORTED;
+    h->g_events = max_events;
+    h->g_sp = std::max<uint64_t>(max_total_spacepoints, 1);
+    return capture_graphs(h);
+}
+
+seedgb_status seedgb_seeding_graph_launch(seedgb_seeding* h,
+                                          const seedgb_spacepoint_view* events,
+                                          uint32_t n_events, seedgb_seed_buffer* outs,
+                                          void* stream) {
+    if (!h || h->g_events == 0) return SEEDGB_INVALID_ARGUMENT;
+    uint64_t total_sp = 0;
+    uint32_t total_chunks = 0;
+    seedgb_status st = check_batch(events, n_events, outs, &total_sp, &total_chunks);
+    if (st != SEEDGB_OK) return st;
+    if (n_events > h->g_events || total_sp > h->g_sp) return SEEDGB_SIZE_LIMIT;
+    if (!h->g_valid) {
+        // a configuration change or a larger direct run replaced the arena
+        st = capture_graphs(h);
+        if (st != SEEDGB_OK) return st;
+    }
+    const int k = h->g_next;
+    Staging& sg = h->staging[1 + k];
+    if (cudaEventSynchronize(sg.done) != cudaSuccess) return SEEDGB_CUDA_ERROR;
+    stage_batch(sg, events, n_events, outs);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    cudaError_t err = cudaGraphLaunch(h->gexec[k], s);
+    if (err == cudaSuccess) err = cudaEventRecord(sg.done, s);
+    h->g_next = k ^ 1;
+    h->timed_run = false;
+    return cuda_status(err);
+}
+
+seedgb_status seedgb_seeding_set_tune(seedgb_seeding* h, const seedgb_tune* t) {
+    if (!h || !t) return SEEDGB_INVALID_ARGUMENT;
+    if (t->warps_per_cta < 1 || t->warps_per_cta > 16 || t->middles_per_item < 1 ||
+        t->middles_per_item > 4096 || t->neighbourhood_capacity < 256 ||
+        t->neighbourhood_capacity > 8192 || t->ctas_per_sm < 1 || t->ctas_per_sm > 8)
+        return SEEDGB_INVALID_ARGUMENT;
+    const int mw = fast_kernel_max_warps(t->neighbourhood_capacity, t->ctas_per_sm);
+    if (mw < 1) return SEEDGB_UNSUPPORTED;
+    const TuneParams tp{std::min(t->warps_per_cta, mw), t->middles_per_item,
+                        t->neighbourhood_capacity, t->ctas_per_sm};
+    if (h->arena && cudaDeviceSynchronize() != cudaSuccess) return SEEDGB_CUDA_ERROR;
+    h->tune = tp;
+    h->g_valid = false;
+    return SEEDGB_OK;
+}
+
+seedgb_status seedgb_seeding_get_tune(seedgb_seeding* h, seedgb_tune* t) {
+    if (!h || !t) return SEEDGB_INVALID_ARGUMENT;
+    t->warps_per_cta = h->tune.fast_warps;
+    t->middles_per_item = h->tune.middles_per_item;
+    t->neighbourhood_capacity = h->tune.nb_cap;
+    t->ctas_per_sm = h->tune.ctas_per_sm;
+    return SEEDGB_OK;
 }
 
 seedgb_status seedgb_seeding_run(seedgb_seeding* h, const seedgb_spacepoint_view* sps,
@@ -418,6 +618,7 @@ seedgb_status seedgb_seeding_set_option(seedgb_seeding* h, seedgb_option opt, in
     switch (opt) {
         case SEEDGB_OPTION_EXHAUSTIVE_TRIPLETS:
             h->dc.brute_force_triplets = value ? 1u : 0u;
+            h->g_valid = false;  // the configuration is baked into the graphs
             return SEEDGB_OK;
         case SEEDGB_OPTION_KERNEL_TIMING:
             if (value && !h->tev[0]) {

@@ -99,6 +99,15 @@ struct EventDesc {
     uint32_t* out_size;
 };
 
+// Sizes of the batch in flight, device-resident so that a CUDA graph captured
+// with capacity-sized grids serves any batch up to its capacity.
+struct BatchHeader {
+    uint32_t n_events;
+    uint32_t total_chunks;
+    uint32_t total_sp;
+    uint32_t pad;
+};
+
 struct SeedSlot {
     uint32_t b, m, t;
     float q;
@@ -106,6 +115,7 @@ struct SeedSlot {
 
 // Pointers into the work arena.
 struct Arena {
+    BatchHeader* hdr;       // sizes of the batch (device)
     EventDesc* events;      // [E]
     uint32_t* chunk_event;  // [total_chunks]
     int32_t* sp_bin;
@@ -123,9 +133,9 @@ struct Arena {
     SeedSlot* seed_slot;
     uint32_t* ovf;
     unsigned long long* counters;
-    uint32_t n_events;
-    uint32_t total_chunks;
-    uint32_t total_sp;
+    uint32_t cap_events;    // capacities of the arena (launch grids of a graph)
+    uint32_t cap_chunks;
+    uint32_t cap_sp;
     uint32_t max_items;
 };
 
@@ -144,8 +154,13 @@ DevConfig make_dev_config(const seedgb_seedfinder_config& f,
 
 // Kernel launchers (seedgb_kernels.cu).  All asynchronous on `stream`.
 // timing: nullptr, or kNumKernels+1 events recorded around the kernels.
+// grid: the batch sizes that size the launch grids (the actual batch, or the
+// arena capacities when capturing a graph); the kernels read the actual
+// sizes from a.hdr.
 constexpr int kNumKernels = 7;
-cudaError_t launch_seeding(const DevConfig& cfg, const Arena& a,
+// Sets the kernels' shared-memory attributes on the current device (once).
+cudaError_t prepare_kernels();
+cudaError_t launch_seeding(const DevConfig& cfg, const Arena& a, const BatchHeader& grid,
                            const TuneParams& tp, int num_sms,
                            cudaStream_t stream, cudaEvent_t* timing = nullptr);
 
@@ -163,7 +178,8 @@ cudaError_t launch_params(const ParamsConfig& cfg, const float bfield[3],
                           cudaStream_t stream);
 
 size_t fast_kernel_smem(const TuneParams& tp);
-// Most warps per CTA whose scratch fits next to an nb_cap staging buffer.
-int fast_kernel_max_warps(int nb_cap);
+// Most warps per CTA whose scratch fits next to an nb_cap staging buffer with
+// ctas_per_sm CTAs resident on one SM.
+int fast_kernel_max_warps(int nb_cap, int ctas_per_sm = 1);
 
 }  // namespace seedgb

@@ -101,8 +101,9 @@ __device__ uint32_t build_segments(const DevConfig& c, const uint32_t* bs,
     return pos;
 }
 
-__device__ __forceinline__ uint32_t event_of_chunk(const Arena& a, uint32_t chunk) {
-    uint32_t lo = 0, hi = a.n_events;  // last event with chunk_base <= chunk
+__device__ __forceinline__ uint32_t event_of_chunk(const Arena& a, uint32_t n_events,
+                                                   uint32_t chunk) {
+    uint32_t lo = 0, hi = n_events;  // last event with chunk_base <= chunk
     while (hi - lo > 1) {
         const uint32_t mid = (lo + hi) >> 1;
         if (a.events[mid].chunk_base <= chunk) lo = mid; else hi = mid;
@@ -118,8 +119,9 @@ __global__ void __launch_bounds__(kBinWarps * 32)
 k_bin_count(DevConfig c, Arena a) {
     extern __shared__ uint32_t hist[];  // [kBinWarps][nbins]
     const uint32_t chunk = blockIdx.x;
-    if (chunk >= a.total_chunks) return;
-    const uint32_t e = event_of_chunk(a, chunk);
+    const BatchHeader hb = *a.hdr;
+    if (chunk >= hb.total_chunks) return;
+    const uint32_t e = event_of_chunk(a, hb.n_events, chunk);
     const EventDesc ev = a.events[e];
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (uint32_t i = threadIdx.x; i < kBinWarps * c.nbins; i += blockDim.x) hist[i] = 0;
@@ -191,7 +193,7 @@ __device__ uint32_t block_exclusive_scan(uint32_t* data, uint32_t n, uint32_t* t
 __global__ void __launch_bounds__(1024) k_bin_scan(DevConfig c, Arena a, uint32_t mpi) {
     extern __shared__ uint32_t sh[];
     const uint32_t e = blockIdx.x;
-    if (e >= a.n_events) return;
+    if (e >= a.hdr->n_events) return;
     const EventDesc ev = a.events[e];
     const uint32_t nb = c.nbins;
     const uint32_t nslots = ev.n_chunks * kBinWarps;
@@ -260,8 +262,9 @@ __global__ void __launch_bounds__(1024) k_bin_scan(DevConfig c, Arena a, uint32_
 __global__ void __launch_bounds__(kBinWarps * 32) k_bin_scatter(DevConfig c, Arena a) {
     extern __shared__ uint32_t base[];  // [kBinWarps][nbins]
     const uint32_t chunk = blockIdx.x;
-    if (chunk >= a.total_chunks) return;
-    const uint32_t e = event_of_chunk(a, chunk);
+    const BatchHeader hb = *a.hdr;
+    if (chunk >= hb.total_chunks) return;
+    const uint32_t e = event_of_chunk(a, hb.n_events, chunk);
     const EventDesc ev = a.events[e];
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t* src = a.whist + static_cast<size_t>(chunk) * kBinWarps * c.nbins;
@@ -515,7 +518,7 @@ __global__ void __launch_bounds__(256) k_bin_rsort(DevConfig c, Arena a) {
     __shared__ uint32_t key[kSortCap];
     __shared__ uint32_t val[kSortCap];
     const uint32_t e = blockIdx.x / c.nbins, b = blockIdx.x % c.nbins;
-    if (e >= a.n_events) return;
+    if (e >= a.hdr->n_events) return;
     const uint32_t* bs = a.bin_start + static_cast<size_t>(e) * (c.nbins + 1);
     const uint32_t g0 = bs[b], n = bs[b + 1] - g0;
     if (threadIdx.x == 0) a.bin_unsorted[static_cast<size_t>(e) * c.nbins + b] = n > kSortCap;
@@ -1225,7 +1228,7 @@ __device__ MiddleResult process_middle(const DevConfig& c, const Arena& a,
 
 __device__ __forceinline__ void push_overflow(const Arena& a, uint32_t gm) {
     const unsigned long long k = atomicAdd(&a.counters[kOvfCount], 1ull);
-    if (k < a.total_sp) a.ovf[k] = gm;
+    if (k < a.cap_sp) a.ovf[k] = gm;
     a.seed_cnt[gm] = 0;
 }
 
@@ -1367,7 +1370,8 @@ __global__ void __launch_bounds__(32) k_seed_slow(DevConfig c, Arena a) {
     const uint32_t lane = threadIdx.x & 31;
     const bool any_var = a.counters[kAnyVariance] != 0;
     const uint32_t n = static_cast<uint32_t>(
-        min(a.counters[kOvfCount], static_cast<unsigned long long>(a.total_sp)));
+        min(a.counters[kOvfCount], static_cast<unsigned long long>(a.cap_sp)));
+    const uint32_t n_events = a.hdr->n_events;
     for (;;) {
         uint32_t idx = 0;
         if (lane == 0) idx = static_cast<uint32_t>(atomicAdd(&a.counters[kOvfFetch], 1ull));
@@ -1375,7 +1379,7 @@ __global__ void __launch_bounds__(32) k_seed_slow(DevConfig c, Arena a) {
         if (idx >= n) break;
         const uint32_t gm = a.ovf[idx];
         // event: last with sp_base <= gm
-        uint32_t lo = 0, hi = a.n_events;
+        uint32_t lo = 0, hi = n_events;
         while (hi - lo > 1) {
             const uint32_t mid = (lo + hi) >> 1;
             if (a.events[mid].sp_base <= gm) lo = mid; else hi = mid;
@@ -1419,7 +1423,7 @@ __global__ void __launch_bounds__(32) k_seed_slow(DevConfig c, Arena a) {
 __global__ void __launch_bounds__(1024) k_seed_compact(Arena a) {
     __shared__ uint32_t tmp[33];
     const uint32_t e = blockIdx.x;
-    if (e >= a.n_events) return;
+    if (e >= a.hdr->n_events) return;
     const EventDesc ev = a.events[e];
     const uint32_t nv = a.n_valid[e];
     const uint32_t t = threadIdx.x, nt = blockDim.x;
@@ -1569,59 +1573,69 @@ size_t fast_kernel_smem(const TuneParams& tp) {
            static_cast<size_t>(tp.fast_warps) * sizeof(FastScratch);
 }
 
-int fast_kernel_max_warps(int nb_cap) {
+int fast_kernel_max_warps(int nb_cap, int ctas_per_sm) {
     TuneParams t{0, 1, nb_cap, 1};
     const size_t fixed = fast_kernel_smem(t);
-    const size_t limit = 227 * 1024;
+    // 228 KiB per SM, of which 1 KiB per resident CTA is reserved; 227 KiB per CTA
+    const size_t per_sm = 228 * 1024 / static_cast<size_t>(std::max(1, ctas_per_sm));
+    const size_t limit = std::min<size_t>(227 * 1024, per_sm - 1024);
     if (fixed >= limit) return 0;
     return static_cast<int>(std::min<size_t>(16, (limit - fixed) / sizeof(FastScratch)));
 }
 
 static size_t slow_kernel_smem() { return 1024 + sizeof(SlowScratch); }
 
-cudaError_t launch_seeding(const DevConfig& cfg, const Arena& a, const TuneParams& tp,
-                           int num_sms, cudaStream_t stream, cudaEvent_t* timing) {
+cudaError_t prepare_kernels() {
+    // per device: the attribute belongs to the current context
+    static thread_local int done_for = -1;
+    int dev = -1;
+    cudaError_t err = cudaGetDevice(&dev);
+    if (err != cudaSuccess || dev == done_for) return err;
+    err = cudaFuncSetAttribute(k_seed_fast, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               227 * 1024);
+    if (err == cudaSuccess)
+        err = cudaFuncSetAttribute(k_seed_slow, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   static_cast<int>(slow_kernel_smem()));
+    if (err == cudaSuccess) done_for = dev;
+    return err;
+}
+
+cudaError_t launch_seeding(const DevConfig& cfg, const Arena& a, const BatchHeader& grid,
+                           const TuneParams& tp, int num_sms, cudaStream_t stream,
+                           cudaEvent_t* timing) {
     auto mark = [&](int i) {
         if (timing) cudaEventRecord(timing[i], stream);
     };
-    static bool attrs_set = false;
     const size_t fsm = fast_kernel_smem(tp);
     const size_t ssm = slow_kernel_smem();
-    if (!attrs_set) {
-        cudaError_t err = cudaFuncSetAttribute(
-            k_seed_fast, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-        if (err != cudaSuccess) return err;
-        err = cudaFuncSetAttribute(k_seed_slow, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   static_cast<int>(ssm));
-        if (err != cudaSuccess) return err;
-        attrs_set = true;
-    }
+    cudaError_t err = prepare_kernels();
+    if (err != cudaSuccess) return err;
     const size_t hsm = static_cast<size_t>(kBinWarps) * cfg.nbins * sizeof(uint32_t);
     mark(0);
-    if (a.total_chunks > 0) {
-        k_bin_count<<<a.total_chunks, kBinWarps * 32, hsm, stream>>>(cfg, a);
+    if (grid.total_chunks > 0) {
+        k_bin_count<<<grid.total_chunks, kBinWarps * 32, hsm, stream>>>(cfg, a);
     }
     mark(1);
     {
         const uint32_t nb = cfg.nbins;
         const uint32_t G = std::max(1u, 1024u / nb);
         const size_t ssz = (static_cast<size_t>(G) * nb + 2 * nb + 40) * sizeof(uint32_t);
-        k_bin_scan<<<a.n_events, 1024, ssz, stream>>>(cfg, a,
+        k_bin_scan<<<grid.n_events, 1024, ssz, stream>>>(cfg, a,
                                                       static_cast<uint32_t>(tp.middles_per_item));
     }
     mark(2);
-    if (a.total_chunks > 0) {
-        k_bin_scatter<<<a.total_chunks, kBinWarps * 32, hsm, stream>>>(cfg, a);
+    if (grid.total_chunks > 0) {
+        k_bin_scatter<<<grid.total_chunks, kBinWarps * 32, hsm, stream>>>(cfg, a);
     }
     mark(3);
-    k_bin_rsort<<<a.n_events * cfg.nbins, 256, 0, stream>>>(cfg, a);
+    k_bin_rsort<<<grid.n_events * cfg.nbins, 256, 0, stream>>>(cfg, a);
     mark(4);
     k_seed_fast<<<num_sms * tp.ctas_per_sm, tp.fast_warps * 32, fsm, stream>>>(
         cfg, a, static_cast<uint32_t>(tp.middles_per_item), static_cast<uint32_t>(tp.nb_cap));
     mark(5);
     k_seed_slow<<<num_sms, 32, ssm, stream>>>(cfg, a);
     mark(6);
-    k_seed_compact<<<a.n_events, 1024, 0, stream>>>(a);
+    k_seed_compact<<<grid.n_events, 1024, 0, stream>>>(a);
     mark(7);
     return cudaGetLastError();
 }

@@ -101,6 +101,16 @@ class _MeasurementView(C.Structure):
                 ("size", C.c_uint32)]
 
 
+class Tune(C.Structure):
+    """seedgb_tune: launch shape of the seeding kernel."""
+    _fields_ = [("warps_per_cta", C.c_int32), ("middles_per_item", C.c_int32),
+                ("neighbourhood_capacity", C.c_int32), ("ctas_per_sm", C.c_int32)]
+
+    def astuple(self):
+        return (self.warps_per_cta, self.middles_per_item, self.neighbourhood_capacity,
+                self.ctas_per_sm)
+
+
 class _ParamsBuffer(C.Structure):
     _fields_ = [("data", C.c_void_p), ("capacity", C.c_uint32),
                 ("size", C.c_void_p)]
@@ -182,6 +192,15 @@ def lib():
         L.seedgb_seeding_set_option.restype = C.c_int
         L.seedgb_seeding_kernel_times.argtypes = [vp, P(C.c_float)]
         L.seedgb_seeding_kernel_times.restype = C.c_int
+        L.seedgb_seeding_graph_create.argtypes = [vp, C.c_uint32, C.c_uint64]
+        L.seedgb_seeding_graph_create.restype = C.c_int
+        L.seedgb_seeding_graph_launch.argtypes = [vp, P(_SpacepointView), C.c_uint32,
+                                                  P(_SeedBuffer), vp]
+        L.seedgb_seeding_graph_launch.restype = C.c_int
+        L.seedgb_seeding_set_tune.argtypes = [vp, P(Tune)]
+        L.seedgb_seeding_set_tune.restype = C.c_int
+        L.seedgb_seeding_get_tune.argtypes = [vp, P(Tune)]
+        L.seedgb_seeding_get_tune.restype = C.c_int
         L.seedgb_params_create.argtypes = [P(TrackParamsEstimationConfig), P(vp)]
         L.seedgb_params_create.restype = C.c_int
         L.seedgb_params_destroy.argtypes = [vp]
@@ -244,9 +263,11 @@ def _torch():
 
 
 def _stream_ptr(stream):
-    torch = _torch()
+    """A torch.cuda.Stream, a raw cudaStream_t (int) or None (current stream)."""
+    if isinstance(stream, int):
+        return C.c_void_p(stream)
     if stream is None:
-        stream = torch.cuda.current_stream()
+        stream = _torch().cuda.current_stream()
     return C.c_void_p(stream.cuda_stream)
 
 
@@ -442,6 +463,34 @@ class TripletSeedingAlgorithm:
                                               _stream_ptr(stream)),
                "seedgb_seeding_run_batch")
         return outs
+
+    def graph_create(self, max_events: int, max_total_spacepoints: int):
+        """Capture the batched launch sequence for batches up to this size."""
+        _check(lib().seedgb_seeding_graph_create(self._h, max_events, max_total_spacepoints),
+               "seedgb_seeding_graph_create")
+
+    def graph_launch(self, events, outs=None, stream=None):
+        """run_batch through the captured graph (graph_create first)."""
+        n = len(events)
+        if outs is None:
+            outs = [SeedBuffer(self.max_seeds(len(e)), device=e.global_.device)
+                    for e in events]
+        views = (_SpacepointView * n)(*[e.view() for e in events])
+        bufs = (_SeedBuffer * n)(*[o.buf() for o in outs])
+        _check(lib().seedgb_seeding_graph_launch(self._h, views, n, bufs,
+                                                 _stream_ptr(stream)),
+               "seedgb_seeding_graph_launch")
+        return outs
+
+    def set_tune(self, warps_per_cta, middles_per_item, neighbourhood_capacity, ctas_per_sm):
+        t = Tune(warps_per_cta, middles_per_item, neighbourhood_capacity, ctas_per_sm)
+        _check(lib().seedgb_seeding_set_tune(self._h, C.byref(t)), "seedgb_seeding_set_tune")
+        return self.get_tune()
+
+    def get_tune(self) -> tuple:
+        t = Tune()
+        _check(lib().seedgb_seeding_get_tune(self._h, C.byref(t)), "seedgb_seeding_get_tune")
+        return t.astuple()
 
     def last_status(self, stream=None) -> int:
         return int(lib().seedgb_seeding_last_status(self._h, _stream_ptr(stream)))
