@@ -64,6 +64,9 @@ def parse():
                    help="skip the 64-event graph-launched batch")
     p.add_argument("--retune", action="store_true",
                    help="search launch shapes even if the tuning table has an entry")
+    p.add_argument("--no-learned", action="store_true",
+                   help="skip training and timing the learned doublet filter")
+    p.add_argument("--filter-events", type=int, default=FILTER_TRAIN_EVENTS)
     return p.parse_args()
 
 
@@ -115,43 +118,63 @@ def tune_table_path():
                           os.path.join(ROOT, "traccc_gb300", "_lib", "tune_table.json"))
 
 
-def run_batched(args, dev, stream, flush_buf):
-    """The uneven 64-event batch through the captured graph: autotuned launch
-    shape, events/s over K batches, p50/p99 per-batch latency (device time of
-    one graph launch, L2 flushed before each), and the same end to end (pinned
-    host columns in, seeds out, wall clock)."""
+class BatchInputs:
+    """The uneven 64-event batch, resident on the device and pinned on the
+    host (for the end-to-end timing)."""
+
+    def __init__(self, dev):
+        import torch
+
+        from traccc_gb300 import seeding, synth
+        events = synth.batch_events(BATCH_EVENTS, BATCH_SEED)
+        self.sizes = [len(e["layer"]) for e in events]
+        offs = np.concatenate([[0], np.cumsum(self.sizes)]).astype(np.int64)
+        self.total = int(offs[-1])
+
+        def cat(key, dt, shape=()):
+            return np.ascontiguousarray(np.concatenate(
+                [np.asarray(e[key]).reshape((-1,) + shape) for e in events]).astype(dt))
+
+        host = {"mi1": cat("measurement_index_1", np.uint32).view(np.int32),
+                "mi2": cat("measurement_index_2", np.uint32).view(np.int32),
+                "glob": cat("global", np.float32, (3,)),
+                "zvar": cat("z_variance", np.float32),
+                "rvar": cat("radius_variance", np.float32)}
+        self.pinned = {k: torch.from_numpy(v).pin_memory() for k, v in host.items()}
+        self.dcols = {k: v.to(dev) for k, v in self.pinned.items()}
+        self.sps = []
+        for e in range(BATCH_EVENTS):
+            a, b = int(offs[e]), int(offs[e + 1])
+            d = self.dcols
+            self.sps.append(seeding.SpacepointCollection(d["mi1"][a:b], d["mi2"][a:b],
+                                                         d["glob"][a:b], d["zvar"][a:b],
+                                                         d["rvar"][a:b]))
+
+
+def run_batched(args, dev, stream, flush_buf, inputs, model=None):
+    """The uneven 64-event batch through the captured graph (with the learned
+    filter when `model` is given): autotuned launch shape, events/s over K
+    batches, p50/p99 per-batch latency (device time of one graph launch, L2
+    flushed before each), and the same end to end (pinned host columns in,
+    seeds out, wall clock).  Returns (report, seed buffers of the last
+    batch)."""
     import torch
 
-    from traccc_gb300 import autotune, seeding, synth
-    events = synth.batch_events(BATCH_EVENTS, BATCH_SEED)
-    sizes = [len(e["layer"]) for e in events]
-    offs = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
-    total = int(offs[-1])
-
-    def cat(key, dt, shape=()):
-        return np.ascontiguousarray(np.concatenate(
-            [np.asarray(e[key]).reshape((-1,) + shape) for e in events]).astype(dt))
-
-    host = {"mi1": cat("measurement_index_1", np.uint32).view(np.int32),
-            "mi2": cat("measurement_index_2", np.uint32).view(np.int32),
-            "glob": cat("global", np.float32, (3,)),
-            "zvar": cat("z_variance", np.float32),
-            "rvar": cat("radius_variance", np.float32)}
-    pinned = {k: torch.from_numpy(v).pin_memory() for k, v in host.items()}
-    dcols = {k: v.to(dev) for k, v in pinned.items()}
+    from traccc_gb300 import autotune, seeding
     alg = seeding.TripletSeedingAlgorithm()
-    sps, outs = [], []
+    if model is not None:
+        alg.set_filter(model.struct())
+    sps, total = inputs.sps, inputs.total
+    outs = []
     size_all = torch.zeros(BATCH_EVENTS, dtype=torch.int32, device=dev)
     for e in range(BATCH_EVENTS):
-        a, b = int(offs[e]), int(offs[e + 1])
-        sps.append(seeding.SpacepointCollection(dcols["mi1"][a:b], dcols["mi2"][a:b],
-                                                dcols["glob"][a:b], dcols["zvar"][a:b],
-                                                dcols["rvar"][a:b]))
-        so = seeding.SeedBuffer(alg.max_seeds(b - a), device=dev)
+        so = seeding.SeedBuffer(alg.max_seeds(len(sps[e])), device=dev)
         so.size = size_all[e:e + 1]
         outs.append(so)
     mean_sp = total / BATCH_EVENTS
     path = tune_table_path()
+    if model is not None:
+        path = path.replace(".json", "_learned.json")
     table = autotune.load(path)
     shape = None if args.retune else autotune.lookup(table, mean_sp)
     t0 = time.perf_counter()
@@ -189,11 +212,11 @@ def run_batched(args, dev, stream, flush_buf):
     # end to end: columns in from pinned memory, seeds out, per batch
     h_size = torch.zeros(BATCH_EVENTS, dtype=torch.int32).pin_memory()
     h_seeds = torch.empty((4, sum(o.capacity for o in outs)), dtype=torch.int32).pin_memory()
-    h2d = sum(v.numel() * v.element_size() for v in pinned.values())
+    h2d = sum(v.numel() * v.element_size() for v in inputs.pinned.values())
 
     def e2e_batch():
-        for k in dcols:
-            dcols[k].copy_(pinned[k], non_blocking=True)
+        for k in inputs.dcols:
+            inputs.dcols[k].copy_(inputs.pinned[k], non_blocking=True)
         alg.graph_launch(sps, outs, stream=sptr)
         h_size.copy_(size_all, non_blocking=True)
         stream.synchronize()
@@ -218,9 +241,10 @@ def run_batched(args, dev, stream, flush_buf):
         t0 = time.perf_counter()
         d2h = e2e_batch()
         e2e_lat.append(1e3 * (time.perf_counter() - t0))
-    return {
+    rep = {
         "workload": BATCH_WORKLOAD, "events_per_batch": BATCH_EVENTS,
-        "spacepoints_per_batch": total, "min_max_spacepoints": [min(sizes), max(sizes)],
+        "spacepoints_per_batch": total,
+        "min_max_spacepoints": [min(inputs.sizes), max(inputs.sizes)],
         "seeds_per_batch": n_seeds,
         "value": BATCH_EVENTS * args.steps / (sum(lat) / 1e3), "unit": "events/s",
         "latency_ms": {"p50": quantile(lat, 0.5), "p99": quantile(lat, 0.99),
@@ -229,9 +253,52 @@ def run_batched(args, dev, stream, flush_buf):
                 "latency_ms": {"p50": quantile(e2e_lat, 0.5), "p99": quantile(e2e_lat, 0.99)},
                 "h2d_bytes_per_batch": int(h2d), "d2h_bytes_per_batch": int(d2h)},
         "autotune": tuned,
-        "gpu_launches_per_batch": len(seeding.KERNEL_NAMES),
+        "gpu_launches_per_batch": len(seeding.KERNEL_NAMES) + (3 if model is not None else 0),
         "l2": "flushed before each batch (256 MiB write)",
     }
+    if model is not None:
+        per, fb, _ = alg.filter_stats(BATCH_EVENTS)
+        frac = (per[:, 1] + per[:, 3]) / np.maximum(per[:, 0] + per[:, 2], 1)
+        rep["pruned_fraction"] = {"mean": float(frac.mean()), "min": float(frac.min()),
+                                  "max": float(frac.max())}
+        rep["fallback_events"] = int(fb.sum())
+    return rep, outs
+
+
+FILTER_TRAIN_EVENTS = 200
+FILTER_CALIB_EVENTS = 20
+
+
+def train_filter(args):
+    """Learned doublet filter: 200 training events with cfg2's per-track
+    statistics and U(500, 12000) tracks each (batch seed 10, so that the
+    filter sees the densities of the uneven batch), labels from the plain
+    seeder, trained with the library's kernels; thresholds and band
+    calibrated on 20 held-out events of the same kind (batch seed 20) for
+    >= 99.5 % seed recall on every one of them."""
+    from traccc_gb300 import learned, seeding, synth
+    t0 = time.perf_counter()
+    train_ev = synth.batch_events(args.filter_events, 10)
+    calib_ev = synth.batch_events(FILTER_CALIB_EVENTS, 20)
+    gen_s = time.perf_counter() - t0
+    alg = seeding.TripletSeedingAlgorithm()
+    model, rep = learned.build_filter(
+        alg, train_ev, calib_ev, epochs=4, target=0.995,
+        quantiles=(0.02, 0.015, 0.01, 0.008, 0.006, 0.005, 0.004, 0.003, 0.0025, 0.002,
+                   0.0015, 0.001, 0.0005, 0.0))
+    rep["generate_s"] = gen_s
+    rep.pop("candidates", None)
+    return model, rep
+
+
+def recall_report(plain, learned_keys):
+    from traccc_gb300 import learned
+    rec, out = learned.compare(plain, learned_keys)
+    n_plain = sum(len(p) for p in plain)
+    return {"min": float(rec.min()), "mean": float(rec.mean()),
+            "per_event_ge_0.995": int((rec >= 0.995).sum()), "events": len(rec),
+            "outside_plain_set": int(out.sum()),
+            "outside_fraction": float(out.sum() / max(n_plain, 1))}
 
 
 # ---------------------------------------------------------------------------
@@ -524,9 +591,60 @@ def run_gpu(args):
         e2e_ms.append(1e3 * (time.perf_counter() - t0))
     barrier()
     e2e_s = sum(e2e_ms) / 1e3
+
+    learned_line = None
     batched = None
+    if world == 1 and not args.no_learned:
+        from traccc_gb300 import learned
+        # plain seeds of the 20 events (the last step's output)
+        step_device()
+        torch.cuda.synchronize()
+        plain_keys = learned.seed_keys(souts)
+        model, train_rep = train_filter(args)
+        alg.set_filter(model.struct())
+        for _ in range(max(3, args.warmup)):
+            step_device()
+        torch.cuda.synchronize()
+        if alg.last_status(stream) != seeding.OK:
+            raise RuntimeError("learned seeding failed")
+        lkeys = learned.seed_keys(souts)
+        per, fb, _ = alg.filter_stats(n_ev)
+        lms = []
+        for _ in range(args.steps):
+            flush_buf.fill_(1)
+            e0.record(stream)
+            step_device()
+            e1.record(stream)
+            e1.synchronize()
+            lms.append(e0.elapsed_time(e1))
+        alg.set_filter(None)
+        frac = (per[:, 1] + per[:, 3]) / np.maximum(per[:, 0] + per[:, 2], 1)
+        l_value = n_ev * args.steps / (sum(lms) / 1e3)
+        learned_line = {
+            "value": l_value, "unit": "events/s", "workload": WORKLOAD,
+            "ms_per_step": sum(lms) / args.steps,
+            "speedup_vs_plain": l_value / job_throughput(n_ev, args.steps, 1, dev_s),
+            "recall": recall_report(plain_keys, lkeys),
+            "pruned_fraction": {"mean": float(frac.mean()), "min": float(frac.min()),
+                                "max": float(frac.max())},
+            "fallback_events": int(fb.sum()),
+            "threshold": [float(v) for v in model.threshold],
+            "band": [float(v) for v in model.band],
+            "training": train_rep,
+        }
     if not args.no_batched and world == 1:
-        batched = run_batched(args, dev, stream, flush_buf)
+        inputs = BatchInputs(dev)
+        b_plain, outs_plain = run_batched(args, dev, stream, flush_buf, inputs)
+        batched = {"plain": b_plain}
+        if learned_line is not None:
+            from traccc_gb300 import learned
+            pk = learned.seed_keys(outs_plain)
+            b_learn, outs_learn = run_batched(args, dev, stream, flush_buf, inputs, model)
+            b_learn["recall"] = recall_report(pk, learned.seed_keys(outs_learn))
+            b_learn["speedup_vs_plain_batched"] = b_learn["value"] / b_plain["value"]
+            b_learn["speedup_vs_plain_cfg2"] = (
+                b_learn["value"] / job_throughput(n_ev, args.steps, 1, dev_s))
+            batched["learned"] = b_learn
     clocks = sampler.stop()
 
     dev_s, e2e_s = max_over_ranks([dev_s, e2e_s], dev)
@@ -598,6 +716,8 @@ def run_gpu(args):
                  "triplets": counters["n_triplets"],
                  "overflow_middles": counters["n_overflow_middles"]},
     }
+    if learned_line is not None:
+        line["learned"] = learned_line
     if batched is not None:
         line["batched"] = batched
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

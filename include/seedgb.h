@@ -301,6 +301,93 @@ seedgb_status seedgb_seeding_set_tune(seedgb_seeding* h, const seedgb_tune* t);
 seedgb_status seedgb_seeding_get_tune(seedgb_seeding* h, seedgb_tune* t);
 
 /* ------------------------------------------------------------------------ */
+/* Learned doublet filter.  No counterpart in the reference.                 */
+/*                                                                          */
+/* For every middle spacepoint with both middle-bottom and middle-top       */
+/* doublets (after all doublet cuts), each doublet is described by 8        */
+/* features, computed in float arithmetic without contraction:             */
+/*   0 r_m  1 z_m  2 r_o - r_m  3 z_o - z_m  4 cot(theta) of the doublet's  */
+/*   lin_circle  5 y / |dxy| in the lin_circle's frame (the sine of the     */
+/*   doublet's azimuthal angle to the middle spacepoint's radial direction) */
+/*   6 the lin_circle's z-intercept Zo  7 layer-pair id = band(r_m) *       */
+/*   (n_edges + 1) + band(r_o), band(r) = number of edges <= r              */
+/* and scored by an MLP 8 -> 32 -> 32 -> 1 on the tensor cores: inputs     */
+/* (f - mu) * isd rounded to bf16, bf16 weights, fp32 biases and            */
+/* accumulation, ReLU, bf16 hidden activations, a logit out.  Doublets of   */
+/* a role the filter may prune are dropped when logit < threshold[role]     */
+/* (role 0 middle-bottom, 1 middle-top); the unchanged triplet finding and  */
+/* seed filtering run on the survivors.  Per event, when the pruned         */
+/* fraction of the scored doublets lies outside [band[0], band[1]], the     */
+/* event is seeded again without the filter inside the same launch          */
+/* sequence (fallback).                                                      */
+/* ------------------------------------------------------------------------ */
+typedef struct {
+    float mu[8], isd[8];
+    float w1[8 * 32];   /* [input][output], rounded to bf16 when loaded */
+    float b1[32];
+    float w2[32 * 32];  /* [input][output] */
+    float b2[32];
+    float w3[32];
+    float b3;
+    float threshold[2];
+    uint32_t n_edges;   /* <= 15 */
+    float edges[15];    /* ascending radial band edges (mm) */
+    uint32_t prune_bottom, prune_top;
+    float band[2];
+} seedgb_doublet_filter;
+
+/* Install (copy) a filter on the handle, or remove it with f == NULL. */
+seedgb_status seedgb_seeding_set_filter(seedgb_seeding* h, const seedgb_doublet_filter* f);
+
+/* Record every scored doublet of the following runs into `records` (device
+ * memory, `capacity` records of 48 bytes: uint32 middle, uint32 other,
+ * uint32 role | event << 1, float features[8], float logit; indices are the
+ * event's spacepoint indices).  Scoring needs an installed filter (with
+ * prune flags 0 the seeds stay those of plain seeding).  records == NULL
+ * stops recording.  Records are written in no particular order. */
+seedgb_status seedgb_seeding_set_doublet_dump(seedgb_seeding* h, void* records,
+                                              uint64_t capacity);
+
+/* Record every triplet (before seed filtering) of the middles the filter
+ * scores into `records` (device memory, `capacity` records of 16 bytes:
+ * uint32 middle, bottom, top, event; the event's spacepoint indices).  With
+ * an installed filter that prunes nothing, these are the triplets of plain
+ * seeding: a doublet in none of them can change no seed (the training
+ * label).  records == NULL stops recording. */
+seedgb_status seedgb_seeding_set_triplet_dump(seedgb_seeding* h, void* records,
+                                              uint64_t capacity);
+
+/* After a run (synchronises `stream`): per event {scored middle-bottom,
+ * pruned middle-bottom, scored middle-top, pruned middle-top} into
+ * per_event[4 * n_events], 1 in fell_back[e] if event e was re-seeded
+ * without the filter (either may be NULL), and the numbers of doublet and
+ * triplet records the run produced (may exceed the dump capacities). */
+seedgb_status seedgb_seeding_filter_stats(seedgb_seeding* h, uint32_t n_events,
+                                          uint32_t* per_event, uint8_t* fell_back,
+                                          uint64_t* n_records, uint64_t* n_triplet_records,
+                                          void* stream);
+
+/* Training and stand-alone inference of the network on the tensor cores.
+ * params: device fp32 block of seedgb_mlp_num_params() values laid out as
+ * w1[8][32], b1[32], w2[32][32], b2[32], w3[32], b3 (bf16-rounded when
+ * used); norm: device {mu[8], isd[8]}; features: device n x 8 floats
+ * (16-byte aligned); labels: device n floats in {0, 1}. */
+uint32_t seedgb_mlp_num_params(void);
+seedgb_status seedgb_mlp_forward(const float* params, const float* norm,
+                                 const float* features, uint32_t n, float* logits,
+                                 void* stream);
+/* grad (device, num_params floats) and loss (device, 1 float) are
+ * overwritten with the gradient and value of the mean weighted logistic loss
+ * -(p y log s(z) + (1 - y) log(1 - s(z))), p = pos_weight. */
+seedgb_status seedgb_mlp_grad(const float* params, const float* norm,
+                              const float* features, const float* labels, uint32_t n,
+                              float pos_weight, float* grad, float* loss, void* stream);
+/* One Adam step (bias-corrected, step >= 1) on n parameters. */
+seedgb_status seedgb_mlp_adam(float* params, const float* grad, float* m, float* v,
+                              uint32_t n, uint32_t step, float lr, float beta1,
+                              float beta2, float eps, void* stream);
+
+/* ------------------------------------------------------------------------ */
 /* Track parameter estimation                                                */
 /* ------------------------------------------------------------------------ */
 

@@ -105,7 +105,8 @@ _STATS_FIELDS = (
     "n_seeds", "max_mb_per_middle", "max_mt_per_middle",
     "max_triplets_per_mb", "max_triplets_per_middle", "max_bin_size",
     "max_neighbourhood", "near_doublet_cuts", "near_triplet_cuts",
-    "near_bin_edges", "phi_cr_undecided")
+    "near_bin_edges", "phi_cr_undecided", "n_scored_mb", "n_scored_mt",
+    "n_pruned_mb", "n_pruned_mt")
 
 
 class Stats(C.Structure):
@@ -157,6 +158,16 @@ def lib():
                                  P(Spacepoints), C.c_int, C.c_void_p, C.c_uint32,
                                  P(C.c_uint32), P(Stats)]
         L.or_seeding.restype = C.c_int
+        L.or_seeding_ex.argtypes = [P(FinderConfig), P(GridConfig), P(FilterConfig),
+                                    P(Spacepoints), C.c_int, P(DoubletFilter), C.c_void_p,
+                                    C.c_uint64, P(C.c_uint64), C.c_void_p, C.c_uint64,
+                                    P(C.c_uint64), C.c_void_p, C.c_uint32,
+                                    P(C.c_uint32), P(Stats)]
+        L.or_seeding_ex.restype = C.c_int
+        L.or_mlp_logit.argtypes = [P(DoubletFilter), P(C.c_float)]
+        L.or_mlp_logit.restype = C.c_float
+        L.or_bf16_round.argtypes = [C.c_float]
+        L.or_bf16_round.restype = C.c_float
         L.or_track_params.argtypes = [P(TPConfig), P(Measurements), P(Spacepoints),
                                       C.c_void_p, C.c_uint32, P(C.c_float),
                                       C.c_void_p]
@@ -261,6 +272,94 @@ def seeding(ev, f=None, g=None, fl=None, phi_mode=PHI_CR):
     if rc:
         raise RuntimeError(f"or_seeding failed {rc}")
     return out[: n.value].copy(), st.as_dict()
+
+
+MLP_IN, MLP_H, MAX_BAND_EDGES = 8, 32, 15
+
+DOUBLET_DTYPE = np.dtype([("middle", "<u4"), ("other", "<u4"), ("top", "<u4"),
+                          ("feat", "<f4", (MLP_IN,)), ("logit", "<f4")])
+
+
+class DoubletFilter(C.Structure):
+    """or_doublet_filter: the learned doublet filter's network, input
+    standardisation, threshold and radial band edges."""
+    _fields_ = [("mu", C.c_float * MLP_IN), ("isd", C.c_float * MLP_IN),
+                ("w1", C.c_float * (MLP_IN * MLP_H)), ("b1", C.c_float * MLP_H),
+                ("w2", C.c_float * (MLP_H * MLP_H)), ("b2", C.c_float * MLP_H),
+                ("w3", C.c_float * MLP_H), ("b3", C.c_float),
+                ("threshold", C.c_float * 2), ("n_edges", C.c_uint32),
+                ("edges", C.c_float * MAX_BAND_EDGES),
+                ("prune_bottom", C.c_uint32), ("prune_top", C.c_uint32)]
+
+
+def doublet_filter(model: dict, threshold, prune_bottom=True, prune_top=True):
+    """A DoubletFilter from a model dict with numpy arrays mu, isd, w1 (8x32),
+    b1, w2 (32x32), b2, w3 (32), b3 and edges; threshold = (middle-bottom,
+    middle-top) logit thresholds (or one for both)."""
+    f = DoubletFilter()
+    def put(name, arr):
+        arr = np.asarray(arr, np.float32).reshape(-1)
+        getattr(f, name)[:] = arr.tolist()
+    for k in ("mu", "isd", "w1", "b1", "w2", "b2", "w3"):
+        put(k, model[k])
+    f.b3 = float(np.float32(model["b3"]))
+    th = np.broadcast_to(np.asarray(threshold, np.float32), (2,))
+    f.threshold[0] = float(th[0])
+    f.threshold[1] = float(th[1])
+    edges = np.asarray(model["edges"], np.float32)
+    f.n_edges = len(edges)
+    f.edges[: len(edges)] = edges.tolist()
+    f.prune_bottom = 1 if prune_bottom else 0
+    f.prune_top = 1 if prune_top else 0
+    return f
+
+
+def bf16_round(x):
+    """Round float32 values to bf16 (nearest even), returned as float32."""
+    u = np.ascontiguousarray(x, np.float32).view(np.uint32).astype(np.uint64)
+    nan = ((u & 0x7f800000) == 0x7f800000) & ((u & 0x007fffff) != 0)
+    r = ((u + 0x7fff + ((u >> 16) & 1)) & 0xffff0000)
+    r = np.where(nan, (u | 0x00400000) & 0xffff0000, r)
+    return r.astype(np.uint32).view(np.float32).reshape(np.shape(x))
+
+
+TRIPLET_DTYPE = np.dtype([("middle", "<u4"), ("bottom", "<u4"), ("top", "<u4"),
+                          ("event", "<u4")])
+
+
+def seeding_ex(ev, f=None, g=None, fl=None, phi_mode=PHI_CR, filt=None, dump=False,
+               triplets=False):
+    """Host seeding with the learned doublet filter (filt: DoubletFilter or
+    None) and/or dumps of every scored doublet and every triplet of the
+    scored middles.  Returns (seeds, stats, doublets or None[, triplets])."""
+    if f is None:
+        f, g, fl, _ = default_configs()
+    s, keep = sp_struct(ev)
+    cap = max(16, 5 * s.size)
+    dcap = tcap = 0
+    for _ in range(3):
+        out = np.zeros(cap, SEED_DTYPE)
+        drec = np.zeros(max(1, dcap), DOUBLET_DTYPE)
+        trec = np.zeros(max(1, tcap), TRIPLET_DTYPE)
+        n = C.c_uint32(0)
+        nd = C.c_uint64(0)
+        nt = C.c_uint64(0)
+        st = Stats()
+        rc = lib().or_seeding_ex(
+            C.byref(f), C.byref(g), C.byref(fl), C.byref(s), phi_mode,
+            C.byref(filt) if filt is not None else None,
+            drec.ctypes.data if dump else None, dcap, C.byref(nd),
+            trec.ctypes.data if triplets else None, tcap, C.byref(nt),
+            out.ctypes.data, cap, C.byref(n), C.byref(st))
+        if rc not in (0, -1):
+            raise RuntimeError(f"or_seeding_ex failed {rc}")
+        if rc == 0 and (not dump or nd.value <= dcap) and (not triplets or nt.value <= tcap):
+            break
+        cap = max(cap, n.value)
+        dcap = nd.value
+        tcap = nt.value
+    res = (out[: n.value].copy(), st.as_dict(), (drec[: nd.value].copy() if dump else None))
+    return res + (trec[: nt.value].copy(),) if triplets else res
 
 
 def track_params(ev, seeds, bfield, tp=None):

@@ -616,10 +616,127 @@ static int find_doublets(const seed_ctx_t* x, uint32_t spM, const float m[6],
  * core/src/seeding/triplet_finding.hpp:60-183,
  * core/src/seeding/seed_filtering.cpp:28-123,
  * core/include/traccc/seeding/seed_selecting_helper.hpp:27-80. */
+/* ------------------------------------------------------------------------ */
+/* Learned doublet filter                                                    */
+/* ------------------------------------------------------------------------ */
+
+/* float -> bf16 -> float, round to nearest even (NaN stays NaN). */
+float or_bf16_round(float x) {
+    uint32_t u;
+    memcpy(&u, &x, 4);
+    if ((u & 0x7f800000u) == 0x7f800000u && (u & 0x007fffffu)) {
+        u |= 0x00400000u;
+        u &= 0xffff0000u;
+    } else {
+        u += 0x7fffu + ((u >> 16) & 1u);
+        u &= 0xffff0000u;
+    }
+    memcpy(&x, &u, 4);
+    return x;
+}
+
+static uint32_t band_of(const or_doublet_filter* f, float r) {
+    uint32_t b = 0;
+    for (uint32_t i = 0; i < f->n_edges; ++i)
+        if (f->edges[i] <= r) ++b;
+    return b;
+}
+
+void or_doublet_features(int top, const float m[6], const float o[6],
+                         const float lc[6], const or_doublet_filter* f,
+                         float feat[OR_MLP_IN]) {
+    (void)top;
+    feat[0] = m[3];
+    feat[1] = m[2];
+    feat[2] = o[3] - m[3];
+    feat[3] = o[2] - m[2];
+    feat[4] = lc[1];
+    /* y * iDeltaR with the operations of or_transform_coordinates */
+    const float cosPhiM = m[0] / m[3], sinPhiM = m[1] / m[3];
+    const float deltaX = o[0] - m[0], deltaY = o[1] - m[1];
+    const float y = deltaY * cosPhiM - deltaX * sinPhiM;
+    const float iDeltaR2 = 1.f / (deltaX * deltaX + deltaY * deltaY);
+    feat[5] = y * sqrtf(iDeltaR2);
+    feat[6] = lc[0];
+    const uint32_t nb = f ? f->n_edges + 1 : 1;
+    feat[7] = f ? (float)(band_of(f, m[3]) * nb + band_of(f, o[3])) : 0.f;
+}
+
+float or_mlp_logit(const or_doublet_filter* f, const float feat[OR_MLP_IN]) {
+    float x[OR_MLP_IN], h1[OR_MLP_H], h2[OR_MLP_H];
+    for (int i = 0; i < OR_MLP_IN; ++i) x[i] = or_bf16_round((feat[i] - f->mu[i]) * f->isd[i]);
+    for (int j = 0; j < OR_MLP_H; ++j) {
+        float a = f->b1[j];
+        for (int i = 0; i < OR_MLP_IN; ++i) a += x[i] * or_bf16_round(f->w1[i * OR_MLP_H + j]);
+        h1[j] = or_bf16_round(a > 0.f ? a : 0.f);
+    }
+    for (int j = 0; j < OR_MLP_H; ++j) {
+        float a = f->b2[j];
+        for (int i = 0; i < OR_MLP_H; ++i) a += h1[i] * or_bf16_round(f->w2[i * OR_MLP_H + j]);
+        h2[j] = or_bf16_round(a > 0.f ? a : 0.f);
+    }
+    float a = f->b3;
+    for (int i = 0; i < OR_MLP_H; ++i) a += h2[i] * or_bf16_round(f->w3[i]);
+    return a;
+}
+
+/* Scores the doublets of one role, dumps them, and (if the filter may prune
+ * this role) keeps those with logit >= threshold, in order. */
+static int score_role(const or_doublet_filter* filt, int top, uint32_t spM,
+                      const float m[6], const or_spacepoints* sps, vec_t* v,
+                      or_doublet_rec* dump, uint64_t dump_cap, uint64_t* n_dump,
+                      uint64_t* n_scored, uint64_t* n_pruned) {
+    dbl_t* D = (dbl_t*)v->p;
+    size_t w = 0;
+    const int may_prune = filt && (top ? filt->prune_top : filt->prune_bottom);
+    for (size_t k = 0; k < v->n; ++k) {
+        float ov[6], feat[OR_MLP_IN];
+        load_sp(sps, D[k].sp, ov);
+        or_doublet_features(top, m, ov, D[k].lc, filt, feat);
+        const float logit = filt ? or_mlp_logit(filt, feat) : 0.f;
+        if (dump && n_dump) {
+            if (*n_dump < dump_cap) {
+                or_doublet_rec* r = &dump[*n_dump];
+                r->middle = spM;
+                r->other = D[k].sp;
+                r->top = (uint32_t)top;
+                memcpy(r->feat, feat, sizeof feat);
+                r->logit = logit;
+            }
+            ++*n_dump;
+        }
+        (*n_scored)++;
+        if (may_prune && !(logit >= filt->threshold[top ? 1 : 0])) {
+            (*n_pruned)++;
+            continue;
+        }
+        D[w++] = D[k];
+    }
+    v->n = w;
+    return 0;
+}
+
 int or_seeding(const or_finder_config* fc, const or_grid_config* gc,
                const or_filter_config* flt, const or_spacepoints* sps,
                int phi_mode, or_seed* out, uint32_t cap, uint32_t* n_out,
                or_stats* st) {
+    return or_seeding_ex(fc, gc, flt, sps, phi_mode, NULL, NULL, 0, NULL, NULL, 0, NULL,
+                         out, cap, n_out, st);
+}
+
+int or_seeding_ex(const or_finder_config* fc, const or_grid_config* gc,
+                  const or_filter_config* flt, const or_spacepoints* sps,
+                  int phi_mode, const or_doublet_filter* filt,
+                  or_doublet_rec* dump, uint64_t dump_cap, uint64_t* n_dump,
+                  or_triplet_rec* tdump, uint64_t tdump_cap, uint64_t* n_tdump,
+                  or_seed* out, uint32_t cap, uint32_t* n_out, or_stats* st) {
+    or_stats st_local;
+    if (!st && (filt || dump)) {
+        memset(&st_local, 0, sizeof st_local);
+        st = &st_local;
+    }
+    if (n_dump) *n_dump = 0;
+    if (n_tdump) *n_tdump = 0;
     or_axes ax;
     int rc = or_get_axes(gc, &ax);
     if (rc) return rc;
@@ -658,6 +775,16 @@ int or_seeding(const or_finder_config* fc, const or_grid_config* gc,
                 if (mt.n > st->max_mt_per_middle) st->max_mt_per_middle = mt.n;
             }
             if (mt.n == 0) continue;
+            if (filt || dump) {
+                /* bottoms first; a middle left without bottoms has no seeds
+                 * and its tops are not scored */
+                score_role(filt, 0, spM, m, sps, &mb, dump, dump_cap, n_dump,
+                           &st->n_scored_mb, &st->n_pruned_mb);
+                if (mb.n == 0) continue;
+                score_role(filt, 1, spM, m, sps, &mt, dump, dump_cap, n_dump,
+                           &st->n_scored_mt, &st->n_pruned_mt);
+                if (mt.n == 0) continue;
+            }
             if (st) {
                 st->n_middles_both++;
                 st->n_triplet_tests += (uint64_t)mb.n * mt.n;
@@ -686,6 +813,16 @@ int or_seeding(const or_finder_config* fc, const or_grid_config* gc,
                     tp.weight = -impact * flt->impactWeightFactor;
                     tp.z_vertex = lb[0];
                     if (vec_push(&tr, &tp)) { rc = -2; break; }
+                    if (tdump && n_tdump) {
+                        if (*n_tdump < tdump_cap) {
+                            or_triplet_rec* r = &tdump[*n_tdump];
+                            r->middle = spM;
+                            r->bottom = MB[k].sp;
+                            r->top = MT[t].sp;
+                            r->event = 0;
+                        }
+                        ++*n_tdump;
+                    }
                 }
                 /* compatible-seed weights, triplet_finding.hpp:107-179 */
                 trip_t* T = (trip_t*)tr.p;

@@ -138,6 +138,9 @@ typedef struct {
     /* decisions whose deciding quantity lies within 1e-6 relative of its cut */
     uint64_t near_doublet_cuts, near_triplet_cuts, near_bin_edges;
     uint64_t phi_cr_undecided;        /* CR atan2 too close to a float midpoint */
+    /* learned doublet filter (or_seeding_ex with a filter) */
+    uint64_t n_scored_mb, n_scored_mt;  /* doublets of middles with both roles */
+    uint64_t n_pruned_mb, n_pruned_mt;  /* of those, dropped by the filter     */
 } or_stats;
 
 /* Config construction: defaults and setup() (seeding_config.hpp:19,120-138). */
@@ -183,6 +186,76 @@ int or_seeding(const or_finder_config* fc, const or_grid_config* gc,
                const or_filter_config* flt, const or_spacepoints* sps,
                int phi_mode, or_seed* out, uint32_t cap, uint32_t* n_out,
                or_stats* stats);
+
+/* ------------------------------------------------------------------------ */
+/* Learned doublet filter (no counterpart in the reference).                 */
+/*                                                                          */
+/* A doublet (middle m, other o) of a middle spacepoint that has both       */
+/* middle-bottom and middle-top doublets is described by 8 features, in     */
+/* float arithmetic without contraction:                                    */
+/*   0 r_m   1 z_m   2 dr = r_o - r_m   3 dz = z_o - z_m                    */
+/*   4 cot(theta) of the doublet's lin_circle (bottom-to-top direction)     */
+/*   5 s = y * iDeltaR of the lin_circle's frame: the sine of the angle     */
+/*     between the doublet and the middle spacepoint's radial direction    */
+/*     (the azimuthal bending feature)                                       */
+/*   6 z-intercept at r = 0 of the lin_circle (Zo)                           */
+/*   7 layer-pair id = band(r_m) * (n_edges + 1) + band(r_o), band(r) =     */
+/*     number of radial band edges <= r                                     */
+/* The network is an MLP 8 -> 32 -> 32 -> 1: inputs standardised          */
+/* ((f - mu) * isd) and rounded to bf16, bf16 weights, float biases and     */
+/* accumulation (bias first, then inputs in index order), ReLU, hidden      */
+/* activations rounded to bf16; the output is a logit.  A doublet is kept   */
+/* when logit >= threshold[role] (role 0 middle-bottom, 1 middle-top).       */
+/* ------------------------------------------------------------------------ */
+#define OR_MLP_IN 8
+#define OR_MLP_H 32
+#define OR_MAX_BAND_EDGES 15
+typedef struct {
+    float mu[OR_MLP_IN], isd[OR_MLP_IN];
+    float w1[OR_MLP_IN * OR_MLP_H];   /* [in][out], rounded to bf16 when used */
+    float b1[OR_MLP_H];
+    float w2[OR_MLP_H * OR_MLP_H];    /* [in][out] */
+    float b2[OR_MLP_H];
+    float w3[OR_MLP_H];
+    float b3;
+    float threshold[2];               /* keep when logit >= threshold[top] */
+    uint32_t n_edges;
+    float edges[OR_MAX_BAND_EDGES];   /* ascending radial band edges */
+    uint32_t prune_bottom, prune_top; /* which roles the filter may drop */
+} or_doublet_filter;
+
+/* One scored doublet (dump of or_seeding_ex). */
+typedef struct {
+    uint32_t middle, other;
+    uint32_t top;                     /* 0 middle-bottom, 1 middle-top */
+    float feat[OR_MLP_IN];
+    float logit;                      /* 0 when no filter was given */
+} or_doublet_rec;
+
+/* One triplet of a scored middle (dump of or_seeding_ex). */
+typedef struct {
+    uint32_t middle, bottom, top, event;
+} or_triplet_rec;
+
+float or_bf16_round(float x);
+void or_doublet_features(int top, const float m[6], const float o[6],
+                         const float lc[6], const or_doublet_filter* f,
+                         float feat[OR_MLP_IN]);
+float or_mlp_logit(const or_doublet_filter* f, const float feat[OR_MLP_IN]);
+
+/* or_seeding with the learned filter: the doublets of every middle that has
+ * both roles are scored, those below the threshold (of the roles the filter
+ * may prune) dropped, and the unchanged triplet finding and seed filtering
+ * run on the survivors.  filt == NULL: plain seeding.  dump != NULL: every
+ * scored doublet is written (up to dump_cap; n_dump = the count).
+ * tdump != NULL: every triplet (before seed filtering) of the middles that
+ * have both roles is written (up to tdump_cap; n_tdump = the count). */
+int or_seeding_ex(const or_finder_config* fc, const or_grid_config* gc,
+                  const or_filter_config* flt, const or_spacepoints* sps,
+                  int phi_mode, const or_doublet_filter* filt,
+                  or_doublet_rec* dump, uint64_t dump_cap, uint64_t* n_dump,
+                  or_triplet_rec* tdump, uint64_t tdump_cap, uint64_t* n_tdump,
+                  or_seed* out, uint32_t cap, uint32_t* n_out, or_stats* stats);
 
 /* Host track-parameter estimation (core/src/seeding/
  * track_params_estimation.cpp:23-91). */

@@ -1,0 +1,245 @@
+"""The learned doublet filter on the GPU against the CPU oracle.
+
+* Network: the tensor-core forward kernel's logits and the backward kernel's
+  gradient and loss agree with the numpy reference (oracle/mlp_reference.py)
+  to fp32 accumulation rounding; one Adam step matches numpy.
+* Doublet dump: the seeding kernel scores exactly the doublets the oracle
+  scores (same middles, partners, roles), with bit-identical features and
+  logits equal to fp32 accumulation rounding.
+* Learned seeding: the GPU seeds equal the oracle's learned seeds with the
+  same network and thresholds, except where a doublet's logit lies within
+  the tolerance of its threshold (counted, expected zero or a few).
+* Fallback: an event whose pruned fraction leaves the band is re-seeded
+  without the filter in the same launch sequence (seeds = plain seeds).
+* Training: the kernels lower the loss, and the trained network prunes far
+  more doublets than an untrained one at the same seed recall (the gain of
+  the network over the method without it).
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+from oracle import mlp_reference as R
+from traccc_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+
+def _rand_model(seed):
+    rng = np.random.default_rng(seed)
+    p = rng.normal(0, 0.25, R.N_PARAMS).astype(np.float32)
+    mu = np.array([100, 0, 0, 0, 0, 0, 0, 10], np.float32)
+    isd = np.array([1 / 50, 1 / 400, 1 / 60, 1 / 100, 1, 20, 1 / 80, 1 / 8], np.float32)
+    return p, np.concatenate([mu, isd])
+
+
+def _features(n, seed):
+    rng = np.random.default_rng(seed)
+    return np.stack([rng.uniform(30, 200, n), rng.uniform(-1000, 1000, n),
+                     rng.uniform(-150, 150, n), rng.uniform(-300, 300, n),
+                     rng.normal(0, 2, n), rng.normal(0, 0.05, n), rng.normal(0, 100, n),
+                     rng.integers(0, 25, n)], 1).astype(np.float32)
+
+
+def _oracle_filter(model, threshold, prune=(True, True)):
+    p = np.asarray(model.params, np.float32)
+    w1, b1, w2, b2, w3, b3 = R.unpack(p)
+    d = dict(mu=model.norm[:8], isd=model.norm[8:], w1=w1, b1=b1, w2=w2, b2=b2, w3=w3, b3=b3,
+             edges=model.edges)
+    return O.doublet_filter(d, threshold, prune_bottom=prune[0], prune_top=prune[1])
+
+
+def test_forward_matches_reference():
+    import torch
+
+    from traccc_gb300 import seeding
+    p, norm = _rand_model(1)
+    x = _features(10007, 2)
+    ref, _ = R.forward(p, norm, x)
+    got = seeding.mlp_forward(torch.from_numpy(p).cuda(), torch.from_numpy(norm).cuda(),
+                              torch.from_numpy(x).cuda()).cpu().numpy()
+    d = np.abs(got - ref)
+    scale = 1 + np.abs(ref)
+    assert np.median(d / scale) < 1e-5
+    assert np.mean(d / scale < 1e-4) > 0.99
+    assert np.max(d / scale) < 0.05
+
+
+def test_gradient_matches_reference():
+    import torch
+
+    from traccc_gb300 import seeding
+    p, norm = _rand_model(3)
+    x = _features(4099, 4)
+    y = (np.random.default_rng(5).random(len(x)) < 0.2).astype(np.float32)
+    loss_ref, g_ref = R.loss_and_grad(p, norm, x, y, 4.0)
+    P = torch.from_numpy(p).cuda()
+    G = torch.empty_like(P)
+    L = torch.empty(1, dtype=torch.float32, device="cuda")
+    seeding.mlp_grad(P, torch.from_numpy(norm).cuda(), torch.from_numpy(x).cuda(),
+                     torch.from_numpy(y).cuda(), 4.0, G, L)
+    g = G.cpu().numpy().astype(np.float64)
+    assert abs(float(L.item()) - loss_ref) < 1e-4 * abs(loss_ref)
+    assert np.linalg.norm(g - g_ref) < 2e-3 * np.linalg.norm(g_ref)
+    # every block, not just the total
+    for a, b in ((R.OFF_W1, R.OFF_B1), (R.OFF_B1, R.OFF_W2), (R.OFF_W2, R.OFF_B2),
+                 (R.OFF_B2, R.OFF_W3), (R.OFF_W3, R.OFF_B3), (R.OFF_B3, R.N_PARAMS)):
+        assert np.linalg.norm(g[a:b] - g_ref[a:b]) <= 5e-3 * np.linalg.norm(g_ref[a:b]) + 1e-9
+    # the same gradient is the exact one up to the bf16 operands
+    _, g_exact = R.loss_and_grad(p, norm, x, y, 4.0, exact=True)
+    assert np.linalg.norm(g - g_exact) < 0.05 * np.linalg.norm(g_exact)
+
+
+def test_adam_step():
+    import torch
+
+    from traccc_gb300 import seeding
+    rng = np.random.default_rng(6)
+    p = rng.normal(0, 1, 1377).astype(np.float32)
+    g = rng.normal(0, 1, 1377).astype(np.float32)
+    m = rng.normal(0, 0.1, 1377).astype(np.float32)
+    v = rng.uniform(0, 0.1, 1377).astype(np.float32)
+    P, G, M, V = (torch.from_numpy(a.copy()).cuda() for a in (p, g, m, v))
+    seeding.mlp_adam(P, G, M, V, 3, 1e-2)
+    m2 = 0.9 * m + 0.1 * g
+    v2 = 0.999 * v + 0.001 * g * g
+    p2 = p - 1e-2 * (m2 / (1 - 0.9 ** 3)) / (np.sqrt(v2 / (1 - 0.999 ** 3)) + 1e-8)
+    assert np.allclose(P.cpu().numpy(), p2, rtol=1e-5, atol=1e-6)
+    assert np.allclose(M.cpu().numpy(), m2, rtol=1e-6, atol=1e-7)
+
+
+@pytest.fixture(scope="module")
+def model_and_event():
+    from traccc_gb300 import learned
+    p, norm = _rand_model(7)
+    model = learned.FilterModel(p, norm, learned.band_edges())
+    return model, synth.workload_event("cfg1", 11)
+
+
+def test_dump_matches_oracle(model_and_event):
+    from traccc_gb300 import learned, seeding
+    model, ev = model_and_event
+    alg = seeding.TripletSeedingAlgorithm()
+    sps = [seeding.SpacepointCollection.from_numpy(ev)]
+    outs, rec = learned.run_dump(alg, sps, model)
+    got = rec.cpu().numpy().view(seeding.DOUBLET_DTYPE).reshape(-1)
+    _, _, ref = O.seeding_ex(ev, filt=_oracle_filter(model, -np.inf), dump=True)
+    assert len(got) == len(ref) > 0
+    order_g = np.lexsort((got["role"], got["other"], got["middle"]))
+    order_r = np.lexsort((ref["top"], ref["other"], ref["middle"]))
+    g, r = got[order_g], ref[order_r]
+    assert np.array_equal(g["middle"], r["middle"])
+    assert np.array_equal(g["other"], r["other"])
+    assert np.array_equal(g["role"], r["top"])  # event 0
+    assert np.array_equal(g["feat"].view(np.uint32), r["feat"].view(np.uint32))
+    d = np.abs(g["logit"] - r["logit"]) / (1 + np.abs(r["logit"]))
+    assert np.median(d) < 1e-5 and np.mean(d < 1e-4) > 0.99
+    # the dump run is plain seeding
+    plain, _ = O.seeding(ev)
+    assert np.array_equal(outs[0].to_numpy(), plain)
+
+
+def test_triplet_dump_matches_oracle(model_and_event):
+    from traccc_gb300 import learned, seeding
+    model, ev = model_and_event
+    alg = seeding.TripletSeedingAlgorithm()
+    outs, rec, trec = learned.run_dump(alg, [seeding.SpacepointCollection.from_numpy(ev)], model,
+                                       triplets=True)
+    got = trec.cpu().numpy().astype(np.uint32)
+    _, _, _, ref = O.seeding_ex(ev, filt=_oracle_filter(model, -np.inf), dump=True,
+                                triplets=True)
+    assert len(got) == len(ref) > 0
+    g = np.unique(got[:, :3], axis=0)
+    r = np.unique(np.stack([ref["middle"], ref["bottom"], ref["top"]], 1), axis=0)
+    assert np.array_equal(g, r)
+    assert np.all(got[:, 3] == 0)
+
+
+@pytest.mark.parametrize("prune", [(True, True), (False, True)], ids=["both", "tops"])
+def test_learned_seeds_match_oracle(model_and_event, prune):
+    from traccc_gb300 import seeding
+    model, ev = model_and_event
+    _, _, d = O.seeding_ex(ev, filt=_oracle_filter(model, -np.inf), dump=True)
+    th = (float(np.quantile(d["logit"][d["top"] == 0], 0.4)),
+          float(np.quantile(d["logit"][d["top"] == 1], 0.4)))
+    ref, st = O.seeding_ex(ev, filt=_oracle_filter(model, th, prune))[:2]
+    alg = seeding.TripletSeedingAlgorithm()
+    alg.set_filter(model.struct(threshold=th, band=(0.0, 1.0), prune=prune))
+    sps = seeding.SpacepointCollection.from_numpy(ev)
+    out = alg(sps)
+    assert alg.last_status() == seeding.OK
+    per, fb, _ = alg.filter_stats(1)
+    assert not fb[0]
+    # middle-bottom doublets are scored only when the filter prunes them
+    assert per[0, 0] == (st["n_scored_mb"] if prune[0] else 0)
+    assert per[0, 2] == st["n_scored_mt"]
+    got = out.to_numpy()
+    if not np.array_equal(got, ref):
+        # only middles with a doublet whose logit is within the accumulation
+        # tolerance of its threshold may differ
+        thr = np.where(d["top"] == 1, th[1], th[0] if prune[0] else -np.inf)
+        near = np.abs(d["logit"] - thr) < 1e-3 * (1 + np.abs(thr))
+        amb = set(d["middle"][near].tolist())
+        diff = set(got["middle"].tolist()) ^ set(ref["middle"].tolist())
+        gk = set(map(tuple, np.stack([got["bottom"], got["middle"], got["top"]], 1).tolist()))
+        rk = set(map(tuple, np.stack([ref["bottom"], ref["middle"], ref["top"]], 1).tolist()))
+        diff |= {k[1] for k in gk ^ rk}
+        assert diff <= amb, sorted(diff - amb)[:10]
+    assert abs(int(per[0, 1]) - st["n_pruned_mb"]) <= 2
+    assert abs(int(per[0, 3]) - st["n_pruned_mt"]) <= 2
+
+
+def test_fallback_reseeds_plain(model_and_event):
+    from traccc_gb300 import seeding
+    model, ev = model_and_event
+    plain, _ = O.seeding(ev)
+    evs = [ev, synth.workload_event("cfg1", 12)]
+    plain2, _ = O.seeding(evs[1])
+    alg = seeding.TripletSeedingAlgorithm()
+    sps = [seeding.SpacepointCollection.from_numpy(e) for e in evs]
+    # a band nothing reaches: every event falls back
+    alg.set_filter(model.struct(threshold=(0.0, 0.0), band=(2.0, 3.0)))
+    outs = alg.run_batch(sps)
+    assert alg.last_status() == seeding.OK
+    _, fb, _ = alg.filter_stats(2)
+    assert fb.all()
+    assert np.array_equal(outs[0].to_numpy(), plain)
+    assert np.array_equal(outs[1].to_numpy(), plain2)
+    # the whole band: no event falls back, seeds are pruned
+    alg.set_filter(model.struct(threshold=(0.0, 0.0), band=(0.0, 1.0)))
+    outs = alg.run_batch(sps)
+    _, fb, _ = alg.filter_stats(2)
+    assert not fb.any()
+    assert len(outs[0].to_numpy()) < len(plain)
+    # and through a captured graph
+    alg.graph_create(2, sum(len(s) for s in sps))
+    alg.set_filter(model.struct(threshold=(0.0, 0.0), band=(2.0, 3.0)))
+    outs = alg.graph_launch(sps)
+    assert alg.last_status() == seeding.OK
+    assert np.array_equal(outs[0].to_numpy(), plain)
+
+
+def test_training_gains_over_untrained():
+    import torch
+
+    from traccc_gb300 import learned, seeding
+    alg = seeding.TripletSeedingAlgorithm()
+    train_ev = [synth.workload_event("cfg2", 500 + s, n_tracks=3000) for s in range(6)]
+    calib_ev = [synth.workload_event("cfg2", 600 + s, n_tracks=3000) for s in range(3)]
+    data = learned.collect(alg, train_ev, neg_keep=0.1)
+    assert data.n_positive > 0 and len(data.labels) > data.n_positive
+    params, norm, hist = learned.train(data, epochs=3)
+    assert hist[-1] < hist[0]
+    trained = learned.FilterModel(params, norm, learned.band_edges())
+    untrained = learned.FilterModel(learned.init_params(1), norm, learned.band_edges())
+    m1, r1 = learned.calibrate(alg, trained, calib_ev, target=0.99, criterion="event")
+    m0, r0 = learned.calibrate(alg, untrained, calib_ev, target=0.99, criterion="event",
+                               quantiles=(0.2, 0.1, 0.05, 0.02, 0.01, 0.005, 0.002, 0.001,
+                                          0.0005, 0.0001, 0.0))
+    f1 = np.mean(r1["chosen"]["pruned_fraction"])
+    f0 = np.mean(r0["chosen"]["pruned_fraction"])
+    assert r1["chosen"]["min_recall"] >= 0.99
+    # small training set: the trained network prunes several times more
+    # doublets than an untrained one at the same recall (~0.11 vs ~0.015)
+    assert f1 > 0.06 and f1 > 3 * f0 + 0.02, (f1, f0)
+    torch.cuda.synchronize()

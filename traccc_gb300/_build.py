@@ -19,7 +19,7 @@ LIBDIR = os.path.join(HERE, "_lib")
 REPO = os.path.dirname(HERE)
 INCLUDE = os.path.join(REPO, "include")
 
-CUDA_SOURCES = ["seedgb_kernels.cu", "seedgb_api.cu", "seedgb_noalloc.cu"]
+CUDA_SOURCES = ["seedgb_kernels.cu", "seedgb_api.cu", "seedgb_noalloc.cu", "seedgb_learned.cu"]
 HOST_SOURCES = ["seedgb_config.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

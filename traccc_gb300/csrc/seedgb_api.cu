@@ -57,6 +57,12 @@ struct seedgb_seeding {
     int g_next = 0;
     cudaStream_t cap_stream = nullptr;
     unsigned long long h_counters[kNumCounters] = {};
+    // learned doublet filter (device copy of the packed network) and dump
+    void* d_mlp = nullptr;
+    void* dump = nullptr;
+    uint64_t dump_cap = 0;
+    void* tdump = nullptr;
+    uint64_t tdump_cap = 0;
     bool timing = false;
     bool timed_run = false;
     cudaEvent_t tev[kNumKernels + 1] = {};
@@ -121,6 +127,9 @@ DevConfig make_dev_config(const seedgb_seedfinder_config& f,
     d.z_min = ax.z_min;
     d.z_max = ax.z_max;
     d.brute_force_triplets = 0;
+    d.mlp = nullptr;
+    d.band_lo = 0.f;
+    d.band_hi = 1.f;
     return d;
 }
 
@@ -218,8 +227,10 @@ seedgb_status ensure_arena(seedgb_seeding* h, uint32_t n_events, uint64_t total_
     const size_t o_items = take(sizeof(uint2) * ci);
     const size_t o_cnt = take(sizeof(uint8_t) * cs);
     const size_t o_slot = take(sizeof(SeedSlot) * cs * kMaxSeedsPerMiddle);
-    const size_t o_ovf = take(sizeof(uint32_t) * cs);
+    const size_t o_ovf = take(sizeof(uint32_t) * cs * 2);
     const size_t o_ctr = take(sizeof(unsigned long long) * kNumCounters);
+    const size_t o_evf = take(sizeof(uint32_t) * 4 * static_cast<size_t>(ce));
+    const size_t o_evm = take(sizeof(uint8_t) * static_cast<size_t>(ce));
     static_assert(kHdrBytes >= sizeof(BatchHeader) && kHdrBytes % 256 == 0,
                   "the descriptors follow the header directly");
     drop_graphs(h);
@@ -260,6 +271,12 @@ seedgb_status ensure_arena(seedgb_seeding* h, uint32_t n_events, uint64_t total_
     a.seed_slot = reinterpret_cast<SeedSlot*>(base + o_slot);
     a.ovf = reinterpret_cast<uint32_t*>(base + o_ovf);
     a.counters = reinterpret_cast<unsigned long long*>(base + o_ctr);
+    a.ev_filter = reinterpret_cast<uint32_t*>(base + o_evf);
+    a.ev_mode = reinterpret_cast<uint8_t*>(base + o_evm);
+    a.dump = h->dump;
+    a.dump_cap = h->dump_cap;
+    a.tdump = static_cast<uint4*>(h->tdump);
+    a.tdump_cap = h->tdump_cap;
     a.cap_events = ce;
     a.cap_chunks = cc;
     a.cap_sp = static_cast<uint32_t>(cs);
@@ -337,6 +354,8 @@ cudaError_t enqueue_batch(seedgb_seeding* h, Staging& st, uint32_t staged_events
     if (err == cudaSuccess && copied) err = cudaEventRecord(copied, s);
     if (err == cudaSuccess)
         err = cudaMemsetAsync(h->a.counters, 0, sizeof(unsigned long long) * kNumCounters, s);
+    if (err == cudaSuccess && h->dc.mlp)
+        err = cudaMemsetAsync(h->a.ev_filter, 0, sizeof(uint32_t) * 4 * grid.n_events, s);
     if (err == cudaSuccess)
         err = launch_seeding(h->dc, h->a, grid, h->tune, h->num_sms, s, timing);
     return err;
@@ -453,6 +472,7 @@ seedgb_status seedgb_seeding_destroy(seedgb_seeding* h) {
         if (st.host) cudaFreeHost(st.host);
     }
     if (h->cap_stream) cudaStreamDestroy(h->cap_stream);
+    if (h->d_mlp) cudaFree(h->d_mlp);
     for (auto& e : h->tev)
         if (e) cudaEventDestroy(e);
     delete h;
@@ -539,6 +559,93 @@ seedgb_status seedgb_seeding_set_tune(seedgb_seeding* h, const seedgb_tune* t) {
     if (h->arena && cudaDeviceSynchronize() != cudaSuccess) return SEEDGB_CUDA_ERROR;
     h->tune = tp;
     h->g_valid = false;
+    return SEEDGB_OK;
+}
+
+seedgb_status seedgb_seeding_set_filter(seedgb_seeding* h, const seedgb_doublet_filter* f) {
+    if (!h) return SEEDGB_INVALID_ARGUMENT;
+    // kernels in flight may read the current network
+    if (cudaDeviceSynchronize() != cudaSuccess) return SEEDGB_CUDA_ERROR;
+    h->g_valid = false;
+    if (!f) {
+        h->dc.mlp = nullptr;
+        return SEEDGB_OK;
+    }
+    if (f->n_edges > 15 || !(f->band[0] <= f->band[1])) return SEEDGB_INVALID_ARGUMENT;
+    for (int i = 0; i < 8; ++i)
+        if (!std::isfinite(f->mu[i]) || !std::isfinite(f->isd[i])) return SEEDGB_INVALID_ARGUMENT;
+    for (uint32_t i = 1; i < f->n_edges; ++i)
+        if (!(f->edges[i - 1] <= f->edges[i])) return SEEDGB_INVALID_ARGUMENT;
+    std::vector<uint8_t> frag(mlp_frag_bytes());
+    pack_mlp_frag(*f, *reinterpret_cast<MlpFrag*>(frag.data()));
+    if (!h->d_mlp && cudaMalloc(&h->d_mlp, frag.size()) != cudaSuccess) {
+        h->d_mlp = nullptr;
+        return SEEDGB_CUDA_ERROR;
+    }
+    if (cudaMemcpy(h->d_mlp, frag.data(), frag.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+        return SEEDGB_CUDA_ERROR;
+    h->dc.mlp = static_cast<const MlpFrag*>(h->d_mlp);
+    h->dc.band_lo = f->band[0];
+    h->dc.band_hi = f->band[1];
+    for (int i = 0; i < 8; ++i) {
+        h->dc.mlp_mu[i] = f->mu[i];
+        h->dc.mlp_isd[i] = f->isd[i];
+    }
+    h->dc.mlp_thr[0] = f->threshold[0];
+    h->dc.mlp_thr[1] = f->threshold[1];
+    h->dc.mlp_n_edges = f->n_edges;
+    for (uint32_t i = 0; i < 15; ++i) h->dc.mlp_edges[i] = i < f->n_edges ? f->edges[i] : 0.f;
+    h->dc.mlp_prune_bottom = f->prune_bottom;
+    h->dc.mlp_prune_top = f->prune_top;
+    return SEEDGB_OK;
+}
+
+seedgb_status seedgb_seeding_set_doublet_dump(seedgb_seeding* h, void* records,
+                                              uint64_t capacity) {
+    if (!h || (records && (reinterpret_cast<uintptr_t>(records) % 16))) return SEEDGB_INVALID_ARGUMENT;
+    if (cudaDeviceSynchronize() != cudaSuccess) return SEEDGB_CUDA_ERROR;
+    h->dump = records;
+    h->dump_cap = records ? capacity : 0;
+    h->a.dump = h->dump;
+    h->a.dump_cap = h->dump_cap;
+    h->g_valid = false;  // the arena view is baked into the graphs
+    return SEEDGB_OK;
+}
+
+seedgb_status seedgb_seeding_set_triplet_dump(seedgb_seeding* h, void* records,
+                                               uint64_t capacity) {
+    if (!h || (records && (reinterpret_cast<uintptr_t>(records) % 16))) return SEEDGB_INVALID_ARGUMENT;
+    if (cudaDeviceSynchronize() != cudaSuccess) return SEEDGB_CUDA_ERROR;
+    h->tdump = records;
+    h->tdump_cap = records ? capacity : 0;
+    h->a.tdump = static_cast<uint4*>(h->tdump);
+    h->a.tdump_cap = h->tdump_cap;
+    h->g_valid = false;
+    return SEEDGB_OK;
+}
+
+seedgb_status seedgb_seeding_filter_stats(seedgb_seeding* h, uint32_t n_events,
+                                          uint32_t* per_event, uint8_t* fell_back,
+                                          uint64_t* n_records, uint64_t* n_triplet_records,
+                                          void* stream) {
+    if (!h) return SEEDGB_INVALID_ARGUMENT;
+    if (!h->arena) return SEEDGB_INVALID_ARGUMENT;
+    if ((per_event || fell_back) && n_events > h->cap_events) return SEEDGB_INVALID_ARGUMENT;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    cudaError_t err = cudaSuccess;
+    if (per_event && n_events)
+        err = cudaMemcpyAsync(per_event, h->a.ev_filter, sizeof(uint32_t) * 4 * n_events,
+                              cudaMemcpyDeviceToHost, s);
+    if (err == cudaSuccess && fell_back && n_events)
+        err = cudaMemcpyAsync(fell_back, h->a.ev_mode, n_events, cudaMemcpyDeviceToHost, s);
+    if (err == cudaSuccess)
+        err = cudaMemcpyAsync(h->h_counters, h->a.counters,
+                              sizeof(unsigned long long) * kNumCounters, cudaMemcpyDeviceToHost, s);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(s);
+    if (err != cudaSuccess) return SEEDGB_CUDA_ERROR;
+    if (fell_back && !h->dc.mlp) std::memset(fell_back, 0, n_events);
+    if (n_records) *n_records = h->h_counters[kDumpCount];
+    if (n_triplet_records) *n_triplet_records = h->h_counters[kTripDumpCount];
     return SEEDGB_OK;
 }
 

@@ -50,8 +50,15 @@ enum Counter : int {
     kNumValid = 9,
     kAnyVariance = 10,  // nonzero if any spacepoint has a nonzero variance
     kPhiUndecided = 11, // correctly rounded phi not decidable from double
-    kNumCounters = 16
+    kItemFetch2 = 12,   // work-item counter of the fallback (plain) pass
+    kDumpCount = 13,    // doublet records written (may exceed the capacity)
+    kFallbackEvents = 14,  // events re-seeded without the learned filter
+    kOvfFetch2 = 15,    // large-capacity queue counter of the fallback pass
+    kTripDumpCount = 16,  // triplet records written (may exceed the capacity)
+    kNumCounters = 24
 };
+
+struct MlpFrag;  // seedgb_mlp.cuh
 
 // Kernel-side copy of the configuration (host-derived, passed by value).
 struct DevConfig {
@@ -77,6 +84,14 @@ struct DevConfig {
     float phi_min, phi_max, z_min, z_max;
     // behaviour switches (tests)
     uint32_t brute_force_triplets;  // 1: test every MB x MT pair (no cot window)
+    // learned doublet filter: nullptr = plain seeding
+    const MlpFrag* mlp;         // weight fragments and biases (device)
+    float band_lo, band_hi;     // pruned-fraction band; outside it: plain re-run
+    float mlp_mu[8], mlp_isd[8];
+    float mlp_thr[2];           // keep when logit >= mlp_thr[role], role 1 = top
+    float mlp_edges[15];        // radial band edges of the layer-pair feature
+    uint32_t mlp_n_edges;
+    uint32_t mlp_prune_bottom, mlp_prune_top;
 };
 
 // One event of a batch, as the kernels see it.
@@ -131,8 +146,14 @@ struct Arena {
     uint2* items;
     uint8_t* seed_cnt;
     SeedSlot* seed_slot;
-    uint32_t* ovf;
+    uint32_t* ovf;          // [2 * cap_sp] middles for the large-capacity path
     unsigned long long* counters;
+    uint32_t* ev_filter;    // [E][4] scored / pruned middle-bottom, scored / pruned middle-top
+    uint8_t* ev_mode;       // [E] 1: re-seed without the filter (fallback pass)
+    void* dump;             // doublet records (48 B each) or nullptr
+    unsigned long long dump_cap;
+    uint4* tdump;           // triplet records {middle, bottom, top, event} or nullptr
+    unsigned long long tdump_cap;
     uint32_t cap_events;    // capacities of the arena (launch grids of a graph)
     uint32_t cap_chunks;
     uint32_t cap_sp;
@@ -178,6 +199,9 @@ cudaError_t launch_params(const ParamsConfig& cfg, const float bfield[3],
                           cudaStream_t stream);
 
 size_t fast_kernel_smem(const TuneParams& tp);
+// Packs the host-side network into the fragment layout the kernels read.
+void pack_mlp_frag(const seedgb_doublet_filter& m, MlpFrag& f);
+size_t mlp_frag_bytes();
 // Most warps per CTA whose scratch fits next to an nb_cap staging buffer with
 // ctas_per_sm CTAs resident on one SM.
 int fast_kernel_max_warps(int nb_cap, int ctas_per_sm = 1);

@@ -26,6 +26,7 @@
 
 #include "seedgb_device.cuh"
 #include "seedgb_internal.h"
+#include "seedgb_mlp.cuh"
 
 namespace seedgb {
 namespace {
@@ -299,6 +300,7 @@ __global__ void __launch_bounds__(kBinWarps * 32) k_bin_scatter(DevConfig c, Are
 
 struct LinCircle {
     float Zo, cot, idr, er, u, v;
+    float s;  // y * iDeltaR: sine of the doublet's angle to the radial direction
 };
 
 // First part of doublet_finding_helper::isCompatible<bottom>
@@ -420,6 +422,7 @@ __device__ __forceinline__ LinCircle lin_circle_cs(bool top, const float4 m,
     l.u = x * iDeltaR2;
     l.v = y * iDeltaR2;
     l.er = ((vm.x + vo.x) + (cot_theta * cot_theta) * (vm.y + vo.y)) * iDeltaR2;
+    l.s = y * iDeltaR;
     return l;
 }
 
@@ -722,17 +725,117 @@ __device__ __forceinline__ uint32_t cot_bucket(float x, float cmin, float scale)
     return static_cast<uint32_t>(b < 0 ? 0 : (b >= kBuckets ? kBuckets - 1 : b));
 }
 
+// One scored doublet as the dump records it (48 bytes).
+struct DoubletRec {
+    uint32_t middle, other, role;  // role: 1 = middle-top, | event << 1
+    float feat[kMlpIn];
+    float logit;
+};
+static_assert(sizeof(DoubletRec) == 48, "doublet record layout");
+
+// Scores one chunk of up to 32 doublets (lane i: doublet i, valid when
+// `valid`): the features x go to the warp scratch xs as packed bf16 inputs,
+// the network runs on the tensor cores (two 16-doublet tiles), and each
+// lane gets its doublet's logit back through lg.  Records the doublets when
+// a dump buffer is set.  xs: 128 words of warp scratch, lg: 32 floats.
+template <bool TOP>
+__device__ __forceinline__ float score_chunk(const DevConfig& c, const Arena& a,
+                                             const MlpRegs& R, const float (&x)[kMlpIn],
+                                             bool valid, uint32_t* xs, float* lg,
+                                             uint32_t ev, uint32_t mid_idx, uint32_t oth_idx,
+                                             uint32_t lane, uint32_t lt) {
+    uint32_t pk[4] = {0u, 0u, 0u, 0u};
+    if (valid) mlp_pack_inputs(c.mlp_mu, c.mlp_isd, x, pk);
+    *reinterpret_cast<uint4*>(xs + 4 * lane) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+    __syncwarp();
+    float lo0, hi0, lo1, hi1;
+    mlp_tile16_regs(R, xs, lane, lo0, hi0);
+    mlp_tile16_regs(R, xs + 64, lane, lo1, hi1);
+    if ((lane & 3) == 0) {
+        const uint32_t g = lane >> 2;
+        lg[g] = lo0;
+        lg[g + 8] = hi0;
+        lg[16 + g] = lo1;
+        lg[24 + g] = hi1;
+    }
+    __syncwarp();
+    const float logit = lg[lane];
+    if (a.dump) {
+        const uint32_t vm = __ballot_sync(0xffffffffu, valid);
+        unsigned long long b = 0;
+        if (lane == 0)
+            b = atomicAdd(&a.counters[kDumpCount], static_cast<unsigned long long>(__popc(vm)));
+        b = __shfl_sync(0xffffffffu, b, 0) + __popc(vm & lt);
+        if (valid && b < a.dump_cap) {
+            uint4* r = reinterpret_cast<uint4*>(reinterpret_cast<DoubletRec*>(a.dump) + b);
+            r[0] = make_uint4(mid_idx, oth_idx, (TOP ? 1u : 0u) | (ev << 1), __float_as_uint(x[0]));
+            r[1] = make_uint4(__float_as_uint(x[1]), __float_as_uint(x[2]),
+                              __float_as_uint(x[3]), __float_as_uint(x[4]));
+            r[2] = make_uint4(__float_as_uint(x[5]), __float_as_uint(x[6]),
+                              __float_as_uint(x[7]), __float_as_uint(logit));
+        }
+    }
+    __syncwarp();
+    return logit;
+}
+
+// Learned doublet filter on the middle-bottom doublets q[0..n) of middle M:
+// in-order compaction of those with logit >= threshold when the filter
+// prunes bottoms (otherwise scoring only, for the dump).  Adds the scored /
+// pruned counts to the event's filter counters.
+__device__ __noinline__ uint32_t filter_bottoms(const DevConfig& c, const Arena& a,
+                                                const NbView& nb, const float4 M, uint16_t* q,
+                                                uint32_t n, uint32_t* xs, float* lg,
+                                                uint32_t ev, uint32_t gm, uint32_t lane,
+                                                uint32_t lt) {
+    MlpRegs R;
+    mlp_load_regs(*c.mlp, lane, R);
+    const bool prune = c.mlp_prune_bottom != 0;
+    const float cosPhiM = M.x / M.w, sinPhiM = M.y / M.w;
+    const float thr = c.mlp_thr[0];
+    const float2 zero2 = make_float2(0.f, 0.f);
+    const uint32_t mid_idx = a.dump ? a.g_idx[gm] : 0u;
+    uint32_t w = 0;
+    for (uint32_t base = 0; base < n; base += 32) {
+        const uint32_t i = base + lane;
+        const bool valid = i < n;
+        uint16_t p = 0;
+        float x[kMlpIn] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        uint32_t oth = 0;
+        if (valid) {
+            p = q[i];
+            const float4 o = nb.get(p);
+            const LinCircle l = lin_circle_cs(false, M, cosPhiM, sinPhiM, zero2, o, zero2);
+            mlp_features(c.mlp_edges, c.mlp_n_edges, M, o, l.cot, l.s, l.Zo, x);
+            if (a.dump) oth = a.g_idx[nb.gpos(nb.hpos(p))];
+        }
+        const float logit =
+            score_chunk<false>(c, a, R, x, valid, xs, lg, ev, mid_idx, oth, lane, lt);
+        const bool keep = valid && (!prune || logit >= thr);
+        const uint32_t mask = __ballot_sync(0xffffffffu, keep);
+        if (keep) q[w + __popc(mask & lt)] = p;
+        w += __popc(mask);
+        __syncwarp();
+    }
+    if (lane == 0) {
+        atomicAdd(&a.ev_filter[4 * ev + 0], n);
+        atomicAdd(&a.ev_filter[4 * ev + 1], n - w);
+    }
+    return w;
+}
+
 // Seeds of one middle spacepoint, following host seed_finding::operator()
 // (core/src/seeding/seed_finding.cpp:69-118) with triplet_finding
 // (triplet_finding.hpp:60-183) and seed_filtering (seed_filtering.cpp:28-123).
 // Executed by one full warp.  The order-dependent steps (compatible-seed
 // weights, ties of the final sort) use host positions, so the result does not
 // depend on the order in which doublets are found.
-template <bool RSORTED, int CAPB, int CAPT, int CAPLC, int CAPCT>
+template <bool RSORTED, bool SCORE, int CAPB, int CAPT, int CAPLC, int CAPCT>
 __device__ MiddleResult process_middle(const DevConfig& c, const Arena& a,
                                        const NbView& nb, const uint32_t gm,
                                        const bool any_var, const bool check_r,
                                        const float nb_minr, const float nb_maxr,
+                                       const uint32_t ev,
                                        WarpScratch<CAPB, CAPT, CAPLC, CAPCT>& ws) {
     MiddleResult res{0, 0, 0, 0};
     const uint32_t lane = threadIdx.x & 31;
@@ -824,13 +927,27 @@ __device__ MiddleResult process_middle(const DevConfig& c, const Arena& a,
     }
     if (nqb > CAPB || nqt > CAPT) { res.status = 1; return res; }
     __syncwarp();
-    const uint32_t n_mb = nqb ? helix_compact(c, nb, M, ws.qb, nqb, lane, lt) : 0u;
-    const uint32_t n_mt = (n_mb && nqt) ? helix_compact(c, nb, M, ws.qt, nqt, lane, lt) : 0u;
+    uint32_t n_mb = nqb ? helix_compact(c, nb, M, ws.qb, nqb, lane, lt) : 0u;
+    uint32_t n_mt = (n_mb && nqt) ? helix_compact(c, nb, M, ws.qt, nqt, lane, lt) : 0u;
     res.n_mb = n_mb;
     res.n_mt = n_mt;
     if (n_mb == 0 || n_mt == 0) {
         if (lane == 0) a.seed_cnt[gm] = 0;
         return res;
+    }
+    if constexpr (SCORE) {
+        // learned doublet filter on the middle-bottom doublets (when it prunes
+        // them, or to record them); the cot-bucket tables are free until the
+        // middle-top doublets are sorted below
+        if (c.mlp_prune_bottom || a.dump) {
+            uint32_t* xs = ws.bstart;
+            float* lg = reinterpret_cast<float*>(ws.bstart + 128);
+            n_mb = filter_bottoms(c, a, nb, M, ws.qb, n_mb, xs, lg, ev, gm, lane, lt);
+            if (n_mb == 0) {
+                if (lane == 0) a.seed_cnt[gm] = 0;
+                return res;
+            }
+        }
     }
     if (n_mt > CAPLC) { res.status = 1; return res; }
 
@@ -838,22 +955,82 @@ __device__ MiddleResult process_middle(const DevConfig& c, const Arena& a,
     const float cosPhiM = M.x / M.w, sinPhiM = M.y / M.w;
     float maxEr = 0.f, minEr = 0.f, maxCot = 0.f, maxIdr = 0.f;
     float cmin = __int_as_float(0x7f800000), cmax = -__int_as_float(0x7f800000);
-    for (uint32_t i = lane; i < n_mt; i += 32) {
-        const uint32_t p = ws.qt[i];
-        const uint32_t hp = nb.hpos(p);
-        const float2 vo = any_var ? a.g_var[nb.gpos(hp)] : make_float2(0.f, 0.f);
-        const LinCircle l = lin_circle_cs(true, M, cosPhiM, sinPhiM, vM, nb.get(p), vo);
-        ws.mtd[i] = make_float4(l.cot, l.idr, l.u, l.v);
-        ws.er[i] = l.er;
-        ws.hpt[i] = static_cast<uint16_t>(hp);
-        ws.ppt[i] = static_cast<uint16_t>(p);
-        maxEr = fmaxf(maxEr, l.er);
-        minEr = fminf(minEr, l.er);
-        maxCot = fmaxf(maxCot, fabsf(l.cot));
-        maxIdr = fmaxf(maxIdr, l.idr);
-        cmin = fminf(cmin, l.cot);
-        cmax = fmaxf(cmax, l.cot);
-        if (!(l.er == l.er)) minEr = -1.f;  // NaN error term: no window
+    if constexpr (SCORE) {
+        // learned doublet filter on the middle-top doublets, fused into their
+        // lin_circle set-up: the survivors are written in order
+        MlpRegs R;
+        mlp_load_regs(*c.mlp, lane, R);
+        uint32_t* xs = ws.bstart;
+        float* lg = reinterpret_cast<float*>(ws.bstart + 128);
+        const bool prune = c.mlp_prune_top != 0;
+        const float thr = c.mlp_thr[1];
+        const uint32_t mid_idx = a.dump ? a.g_idx[gm] : 0u;
+        uint32_t w = 0;
+        for (uint32_t base = 0; base < n_mt; base += 32) {
+            const uint32_t i = base + lane;
+            const bool valid = i < n_mt;
+            uint32_t p = 0, hp = 0, oth = 0;
+            LinCircle l{};
+            float x[kMlpIn] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            if (valid) {
+                p = ws.qt[i];
+                hp = nb.hpos(p);
+                const float2 vo = any_var ? a.g_var[nb.gpos(hp)] : make_float2(0.f, 0.f);
+                const float4 o = nb.get(p);
+                l = lin_circle_cs(true, M, cosPhiM, sinPhiM, vM, o, vo);
+                mlp_features(c.mlp_edges, c.mlp_n_edges, M, o, l.cot, l.s, l.Zo, x);
+                if (a.dump) oth = a.g_idx[nb.gpos(hp)];
+            }
+            const float logit =
+                score_chunk<true>(c, a, R, x, valid, xs, lg, ev, mid_idx, oth, lane, lt);
+            const bool keep = valid && (!prune || logit >= thr);
+            const uint32_t mask = __ballot_sync(0xffffffffu, keep);
+            if (keep) {
+                const uint32_t k = w + __popc(mask & lt);
+                ws.mtd[k] = make_float4(l.cot, l.idr, l.u, l.v);
+                ws.er[k] = l.er;
+                ws.hpt[k] = static_cast<uint16_t>(hp);
+                ws.ppt[k] = static_cast<uint16_t>(p);
+                maxEr = fmaxf(maxEr, l.er);
+                minEr = fminf(minEr, l.er);
+                maxCot = fmaxf(maxCot, fabsf(l.cot));
+                maxIdr = fmaxf(maxIdr, l.idr);
+                cmin = fminf(cmin, l.cot);
+                cmax = fmaxf(cmax, l.cot);
+                if (!(l.er == l.er)) minEr = -1.f;
+            }
+            w += __popc(mask);
+            __syncwarp();
+        }
+        if (lane == 0) {
+            atomicAdd(&a.ev_filter[4 * ev + 2], n_mt);
+            atomicAdd(&a.ev_filter[4 * ev + 3], n_mt - w);
+        }
+        __syncwarp();
+        n_mt = w;
+        res.n_mt = w;
+        if (n_mt == 0) {
+            if (lane == 0) a.seed_cnt[gm] = 0;
+            return res;
+        }
+    } else {
+        for (uint32_t i = lane; i < n_mt; i += 32) {
+            const uint32_t p = ws.qt[i];
+            const uint32_t hp = nb.hpos(p);
+            const float2 vo = any_var ? a.g_var[nb.gpos(hp)] : make_float2(0.f, 0.f);
+            const LinCircle l = lin_circle_cs(true, M, cosPhiM, sinPhiM, vM, nb.get(p), vo);
+            ws.mtd[i] = make_float4(l.cot, l.idr, l.u, l.v);
+            ws.er[i] = l.er;
+            ws.hpt[i] = static_cast<uint16_t>(hp);
+            ws.ppt[i] = static_cast<uint16_t>(p);
+            maxEr = fmaxf(maxEr, l.er);
+            minEr = fminf(minEr, l.er);
+            maxCot = fmaxf(maxCot, fabsf(l.cot));
+            maxIdr = fmaxf(maxIdr, l.idr);
+            cmin = fminf(cmin, l.cot);
+            cmax = fmaxf(cmax, l.cot);
+            if (!(l.er == l.er)) minEr = -1.f;  // NaN error term: no window
+        }
     }
     for (uint32_t b = lane; b <= kBuckets; b += 32) ws.bstart[b] = 0;
     for (int o = 16; o > 0; o >>= 1) {
@@ -913,6 +1090,7 @@ __device__ MiddleResult process_middle(const DevConfig& c, const Arena& a,
     float klo = 0.f, khi = 0.f;
     uint32_t lo = 0, cnt = 0;
     for (;;) {
+        __syncwarp();
         if (!have_chunk && c0 < n_mb) {
             const uint32_t ib = c0 + lane;
             cnt = 0;
@@ -1083,6 +1261,24 @@ __device__ MiddleResult process_middle(const DevConfig& c, const Arena& a,
     }
     if (n_ct > CAPCT) { res.status = 1; return res; }
     res.n_trip = n_ct;
+    if constexpr (SCORE) {
+        if (a.tdump && n_ct) {
+            // record the middle's triplets (labels of the filter's training data)
+            unsigned long long b = 0;
+            if (lane == 0) b = atomicAdd(&a.counters[kTripDumpCount], static_cast<unsigned long long>(n_ct));
+            __syncwarp();
+            b = __shfl_sync(0xffffffffu, b, 0);
+            const uint32_t mid_idx = a.g_idx[gm];
+            for (uint32_t i = lane; i < n_ct; i += 32) {
+                if (b + i < a.tdump_cap) {
+                    const TripCand T = ws.ct[i];
+                    a.tdump[b + i] = make_uint4(mid_idx, a.g_idx[nb.gpos(nb.hpos(ws.qb[T.ib]))],
+                                                a.g_idx[nb.gpos(ws.hpt[T.tp])], ev);
+                }
+            }
+            __syncwarp();
+        }
+    }
 
     // -- the middle's triplets in host order: (bottom host position, top
     //    host position) ascending, so the triplets of one middle-bottom
@@ -1228,7 +1424,8 @@ __device__ MiddleResult process_middle(const DevConfig& c, const Arena& a,
 
 __device__ __forceinline__ void push_overflow(const Arena& a, uint32_t gm) {
     const unsigned long long k = atomicAdd(&a.counters[kOvfCount], 1ull);
-    if (k < a.cap_sp) a.ovf[k] = gm;
+    if (k < 2ull * a.cap_sp) a.ovf[k] = gm;
+    else raise_status(a.counters, SEEDGB_CAPACITY_OVERFLOW);
     a.seed_cnt[gm] = 0;
 }
 
@@ -1255,8 +1452,15 @@ __host__ __device__ constexpr size_t fast_scratch_offset(uint32_t nb_cap) {
 // Persistent kernel over work items (event, bin, chunk of middles).  The CTA
 // stages the bin's neighbourhood (radius-sorted runs) once per item; its warps
 // then take middles of the item one at a time.
-__global__ void __launch_bounds__(512) k_seed_fast(DevConfig c, Arena a, uint32_t mpi,
-                                                    uint32_t nb_cap) {
+// pass 0: every event (with the learned filter when one is installed);
+// pass 1: only the events marked for the fallback, without the filter.
+// SCORE: run the learned doublet filter (pass 0 with a filter installed).
+// The scoring variant holds the network in registers: at most
+// kScoreWarps warps per CTA, so that more registers are available.
+constexpr int kScoreWarps = 10;
+template <bool SCORE>
+__global__ void __launch_bounds__(SCORE ? kScoreWarps * 32 : 512)
+    k_seed_fast(DevConfig c, Arena a, uint32_t mpi, uint32_t nb_cap, uint32_t pass) {
     extern __shared__ __align__(128) uint8_t smem[];
     float4* nb_xyzr = reinterpret_cast<float4*>(smem);
     uint16_t* nb_hp = reinterpret_cast<uint16_t*>(nb_xyzr + nb_cap);      // [nb_cap]
@@ -1270,10 +1474,11 @@ __global__ void __launch_bounds__(512) k_seed_fast(DevConfig c, Arena a, uint32_
     const bool any_var = a.counters[kAnyVariance] != 0;
     const uint32_t total_items = static_cast<uint32_t>(
         min(a.counters[kItemTotal], static_cast<unsigned long long>(a.max_items)));
+    unsigned long long* fetch = &a.counters[pass ? kItemFetch2 : kItemFetch];
 
     for (;;) {
         if (threadIdx.x == 0) {
-            misc[0] = static_cast<uint32_t>(atomicAdd(&a.counters[kItemFetch], 1ull));
+            misc[0] = static_cast<uint32_t>(atomicAdd(fetch, 1ull));
             misc[3] = 0x7f800000u;  // min r (as bits, r >= 0)
             misc[4] = 0u;           // max r
             misc[5] = 0u;           // next middle of the item
@@ -1284,6 +1489,10 @@ __global__ void __launch_bounds__(512) k_seed_fast(DevConfig c, Arena a, uint32_
         if (item >= total_items) break;
         const uint2 it = a.items[item];
         const uint32_t e = it.x, bin = it.y & 0xffffu, ch = it.y >> 16;
+        if (pass && !a.ev_mode[e]) {
+            __syncthreads();  // misc[0] is rewritten by the next fetch
+            continue;
+        }
         const uint32_t* bs = a.bin_start + static_cast<size_t>(e) * (c.nbins + 1);
         const uint32_t pbin = bin % c.phi_bins, zbin = bin / c.phi_bins;
         uint32_t zlo, zhi;
@@ -1347,8 +1556,8 @@ __global__ void __launch_bounds__(512) k_seed_fast(DevConfig c, Arena a, uint32_
                 if (lane == 0) push_overflow(a, gm);
                 continue;
             }
-            const MiddleResult r = process_middle<true, 1024, 1024, 256, 128>(
-                c, a, nb, gm, any_var, true, nb_minr, nb_maxr, ws);
+            const MiddleResult r = process_middle<true, SCORE, 1024, 1024, 256, 128>(
+                c, a, nb, gm, any_var, true, nb_minr, nb_maxr, e, ws);
             if (lane == 0) {
                 if (r.status) push_overflow(a, gm);
                 else count_middle(a, r);
@@ -1360,7 +1569,8 @@ __global__ void __launch_bounds__(512) k_seed_fast(DevConfig c, Arena a, uint32_
 
 // Large-capacity path: one warp per CTA, neighbourhood read from global
 // memory in host order, per-middle z neighbourhood.
-__global__ void __launch_bounds__(32) k_seed_slow(DevConfig c, Arena a) {
+template <bool SCORE>
+__global__ void __launch_bounds__(32) k_seed_slow(DevConfig c, Arena a, uint32_t pass) {
     extern __shared__ __align__(128) uint8_t smem[];
     uint32_t* seg_pos = reinterpret_cast<uint32_t*>(smem);     // [kMaxSegments+1]
     uint32_t* seg_g = seg_pos + kMaxSegments + 1;              // [kMaxSegments]
@@ -1370,11 +1580,12 @@ __global__ void __launch_bounds__(32) k_seed_slow(DevConfig c, Arena a) {
     const uint32_t lane = threadIdx.x & 31;
     const bool any_var = a.counters[kAnyVariance] != 0;
     const uint32_t n = static_cast<uint32_t>(
-        min(a.counters[kOvfCount], static_cast<unsigned long long>(a.cap_sp)));
+        min(a.counters[kOvfCount], 2ull * a.cap_sp));
     const uint32_t n_events = a.hdr->n_events;
+    unsigned long long* fetch = &a.counters[pass ? kOvfFetch2 : kOvfFetch];
     for (;;) {
         uint32_t idx = 0;
-        if (lane == 0) idx = static_cast<uint32_t>(atomicAdd(&a.counters[kOvfFetch], 1ull));
+        if (lane == 0) idx = static_cast<uint32_t>(atomicAdd(fetch, 1ull));
         idx = __shfl_sync(0xffffffffu, idx, 0);
         if (idx >= n) break;
         const uint32_t gm = a.ovf[idx];
@@ -1385,6 +1596,7 @@ __global__ void __launch_bounds__(32) k_seed_slow(DevConfig c, Arena a) {
             if (a.events[mid].sp_base <= gm) lo = mid; else hi = mid;
         }
         const uint32_t e = lo;
+        if (pass && !a.ev_mode[e]) continue;
         const uint32_t* bs = a.bin_start + static_cast<size_t>(e) * (c.nbins + 1);
         uint32_t b0 = 0, b1 = c.nbins;  // last bin with bs[b] <= gm
         while (b1 - b0 > 1) {
@@ -1404,8 +1616,8 @@ __global__ void __launch_bounds__(32) k_seed_slow(DevConfig c, Arena a) {
         MiddleResult r{0, 0, 0, 1};
         if (size <= 65535u) {
             NbView nb{nullptr, nullptr, a.g_xyzr, seg_pos, seg_g, nseg, size};
-            r = process_middle<false, 8192, 8192, 4096, 2048>(c, a, nb, gm, any_var,
-                                                                   false, 0.f, 0.f, ws);
+            r = process_middle<false, SCORE, 8192, 8192, 4096, 2048>(c, a, nb, gm, any_var,
+                                                                          false, 0.f, 0.f, e, ws);
         }
         if (lane == 0) {
             if (r.status) {
@@ -1417,6 +1629,22 @@ __global__ void __launch_bounds__(32) k_seed_slow(DevConfig c, Arena a) {
         }
         __syncwarp();
     }
+}
+
+// Events whose pruned fraction (of all scored doublets) leaves the filter's
+// band are marked for the fallback pass.
+__global__ void k_filter_mark(DevConfig c, Arena a) {
+    const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= a.hdr->n_events) return;
+    const uint32_t* f = a.ev_filter + 4 * e;
+    const uint32_t scored = f[0] + f[2], pruned = f[1] + f[3];
+    uint8_t mode = 0;
+    if (scored > 0) {
+        const float frac = static_cast<float>(pruned) / static_cast<float>(scored);
+        mode = (frac < c.band_lo || frac > c.band_hi) ? 1 : 0;
+    }
+    a.ev_mode[e] = mode;
+    if (mode) atomicAdd(&a.counters[kFallbackEvents], 1ull);
 }
 
 // Seeds of one event in host order (bin, middle, rank) into its buffer.
@@ -1591,11 +1819,15 @@ cudaError_t prepare_kernels() {
     int dev = -1;
     cudaError_t err = cudaGetDevice(&dev);
     if (err != cudaSuccess || dev == done_for) return err;
-    err = cudaFuncSetAttribute(k_seed_fast, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               227 * 1024);
-    if (err == cudaSuccess)
-        err = cudaFuncSetAttribute(k_seed_slow, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   static_cast<int>(slow_kernel_smem()));
+    for (auto k : {k_seed_fast<false>, k_seed_fast<true>}) {
+        if (err == cudaSuccess)
+            err = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    }
+    for (auto k : {k_seed_slow<false>, k_seed_slow<true>}) {
+        if (err == cudaSuccess)
+            err = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       static_cast<int>(slow_kernel_smem()));
+    }
     if (err == cudaSuccess) done_for = dev;
     return err;
 }
@@ -1630,10 +1862,25 @@ cudaError_t launch_seeding(const DevConfig& cfg, const Arena& a, const BatchHead
     mark(3);
     k_bin_rsort<<<grid.n_events * cfg.nbins, 256, 0, stream>>>(cfg, a);
     mark(4);
-    k_seed_fast<<<num_sms * tp.ctas_per_sm, tp.fast_warps * 32, fsm, stream>>>(
-        cfg, a, static_cast<uint32_t>(tp.middles_per_item), static_cast<uint32_t>(tp.nb_cap));
-    mark(5);
-    k_seed_slow<<<num_sms, 32, ssm, stream>>>(cfg, a);
+    const uint32_t mpi = static_cast<uint32_t>(tp.middles_per_item);
+    const uint32_t nbc = static_cast<uint32_t>(tp.nb_cap);
+    const dim3 fgrid(num_sms * tp.ctas_per_sm), fblock(tp.fast_warps * 32);
+    if (cfg.mlp) {
+        TuneParams ts = tp;
+        ts.fast_warps = std::min(tp.fast_warps, kScoreWarps);
+        k_seed_fast<true><<<fgrid, ts.fast_warps * 32, fast_kernel_smem(ts), stream>>>(
+            cfg, a, mpi, nbc, 0u);
+        mark(5);
+        k_seed_slow<true><<<num_sms, 32, ssm, stream>>>(cfg, a, 0u);
+        // fallback: events whose pruned fraction left the band, without the filter
+        k_filter_mark<<<(grid.n_events + 255) / 256, 256, 0, stream>>>(cfg, a);
+        k_seed_fast<false><<<fgrid, fblock, fsm, stream>>>(cfg, a, mpi, nbc, 1u);
+        k_seed_slow<false><<<num_sms, 32, ssm, stream>>>(cfg, a, 1u);
+    } else {
+        k_seed_fast<false><<<fgrid, fblock, fsm, stream>>>(cfg, a, mpi, nbc, 0u);
+        mark(5);
+        k_seed_slow<false><<<num_sms, 32, ssm, stream>>>(cfg, a, 0u);
+    }
     mark(6);
     k_seed_compact<<<grid.n_events, 1024, 0, stream>>>(a);
     mark(7);

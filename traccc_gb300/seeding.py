@@ -111,6 +111,19 @@ class Tune(C.Structure):
                 self.ctas_per_sm)
 
 
+class DoubletFilter(C.Structure):
+    """seedgb_doublet_filter: the learned doublet filter's network, input
+    standardisation, per-role thresholds, radial band edges and the
+    pruned-fraction band outside which an event is re-seeded plain."""
+    _fields_ = [("mu", C.c_float * 8), ("isd", C.c_float * 8),
+                ("w1", C.c_float * 256), ("b1", C.c_float * 32),
+                ("w2", C.c_float * 1024), ("b2", C.c_float * 32),
+                ("w3", C.c_float * 32), ("b3", C.c_float),
+                ("threshold", C.c_float * 2), ("n_edges", C.c_uint32),
+                ("edges", C.c_float * 15), ("prune_bottom", C.c_uint32),
+                ("prune_top", C.c_uint32), ("band", C.c_float * 2)]
+
+
 class _ParamsBuffer(C.Structure):
     _fields_ = [("data", C.c_void_p), ("capacity", C.c_uint32),
                 ("size", C.c_void_p)]
@@ -201,6 +214,23 @@ def lib():
         L.seedgb_seeding_set_tune.restype = C.c_int
         L.seedgb_seeding_get_tune.argtypes = [vp, P(Tune)]
         L.seedgb_seeding_get_tune.restype = C.c_int
+        L.seedgb_seeding_set_filter.argtypes = [vp, P(DoubletFilter)]
+        L.seedgb_seeding_set_filter.restype = C.c_int
+        L.seedgb_seeding_set_doublet_dump.argtypes = [vp, vp, C.c_uint64]
+        L.seedgb_seeding_set_doublet_dump.restype = C.c_int
+        L.seedgb_seeding_set_triplet_dump.argtypes = [vp, vp, C.c_uint64]
+        L.seedgb_seeding_set_triplet_dump.restype = C.c_int
+        L.seedgb_seeding_filter_stats.argtypes = [vp, C.c_uint32, P(C.c_uint32),
+                                                  P(C.c_uint8), P(C.c_uint64), P(C.c_uint64), vp]
+        L.seedgb_seeding_filter_stats.restype = C.c_int
+        L.seedgb_mlp_num_params.restype = C.c_uint32
+        L.seedgb_mlp_forward.argtypes = [vp, vp, vp, C.c_uint32, vp, vp]
+        L.seedgb_mlp_forward.restype = C.c_int
+        L.seedgb_mlp_grad.argtypes = [vp, vp, vp, vp, C.c_uint32, C.c_float, vp, vp, vp]
+        L.seedgb_mlp_grad.restype = C.c_int
+        L.seedgb_mlp_adam.argtypes = [vp, vp, vp, vp, C.c_uint32, C.c_uint32, C.c_float,
+                                      C.c_float, C.c_float, C.c_float, vp]
+        L.seedgb_mlp_adam.restype = C.c_int
         L.seedgb_params_create.argtypes = [P(TrackParamsEstimationConfig), P(vp)]
         L.seedgb_params_create.restype = C.c_int
         L.seedgb_params_destroy.argtypes = [vp]
@@ -492,6 +522,44 @@ class TripletSeedingAlgorithm:
         _check(lib().seedgb_seeding_get_tune(self._h, C.byref(t)), "seedgb_seeding_get_tune")
         return t.astuple()
 
+    def set_filter(self, filt: "DoubletFilter | None"):
+        """Install the learned doublet filter (None: plain seeding)."""
+        _check(lib().seedgb_seeding_set_filter(self._h, C.byref(filt) if filt is not None
+                                               else None), "seedgb_seeding_set_filter")
+
+    def set_doublet_dump(self, records, capacity: int = 0):
+        """Record scored doublets into `records` (a device uint8 tensor of
+        48-byte records, or None to stop)."""
+        ptr = records.data_ptr() if records is not None else None
+        cap = capacity or (records.numel() * records.element_size() // 48 if records is not None
+                           else 0)
+        _check(lib().seedgb_seeding_set_doublet_dump(self._h, ptr, cap),
+               "seedgb_seeding_set_doublet_dump")
+
+    def set_triplet_dump(self, records, capacity: int = 0):
+        """Record the triplets of scored middles into `records` (a device
+        uint8 tensor of 16-byte records, or None to stop)."""
+        ptr = records.data_ptr() if records is not None else None
+        cap = capacity or (records.numel() * records.element_size() // 16 if records is not None
+                           else 0)
+        _check(lib().seedgb_seeding_set_triplet_dump(self._h, ptr, cap),
+               "seedgb_seeding_set_triplet_dump")
+
+    def filter_stats(self, n_events: int, stream=None, triplets=False):
+        """(per-event [n, 4] scored/pruned MB, scored/pruned MT counts,
+        fell_back [n] bools, number of doublet records[, number of triplet
+        records]) of the last run."""
+        per = np.zeros((max(1, n_events), 4), np.uint32)
+        fb = np.zeros(max(1, n_events), np.uint8)
+        nrec = C.c_uint64(0)
+        ntrip = C.c_uint64(0)
+        _check(lib().seedgb_seeding_filter_stats(
+            self._h, n_events, per.ctypes.data_as(C.POINTER(C.c_uint32)),
+            fb.ctypes.data_as(C.POINTER(C.c_uint8)), C.byref(nrec), C.byref(ntrip),
+            _stream_ptr(stream)), "seedgb_seeding_filter_stats")
+        res = (per[:n_events], fb[:n_events].astype(bool), int(nrec.value))
+        return res + (int(ntrip.value),) if triplets else res
+
     def last_status(self, stream=None) -> int:
         return int(lib().seedgb_seeding_last_status(self._h, _stream_ptr(stream)))
 
@@ -520,6 +588,41 @@ class TripletSeedingAlgorithm:
             sps.ctypes.data_as(C.POINTER(C.c_uint32)), len(sps), C.byref(nv),
             _stream_ptr(stream)), "seedgb_seeding_copy_grid")
         return off, sps[: nv.value].copy()
+
+
+DOUBLET_DTYPE = np.dtype([("middle", "<u4"), ("other", "<u4"), ("role", "<u4"),
+                          ("feat", "<f4", (8,)), ("logit", "<f4")])
+
+
+def mlp_num_params() -> int:
+    return int(lib().seedgb_mlp_num_params())
+
+
+def mlp_forward(params, norm, features, logits=None, stream=None):
+    """Logits of n doublets (device tensors: params fp32 [num_params], norm
+    fp32 [16], features fp32 [n, 8]) on the tensor cores."""
+    torch = _torch()
+    n = int(features.shape[0])
+    if logits is None:
+        logits = torch.empty(n, dtype=torch.float32, device=features.device)
+    _check(lib().seedgb_mlp_forward(params.data_ptr(), norm.data_ptr(), features.data_ptr(), n,
+                                    logits.data_ptr(), _stream_ptr(stream)), "seedgb_mlp_forward")
+    return logits
+
+
+def mlp_grad(params, norm, features, labels, pos_weight, grad, loss, stream=None):
+    """Gradient and value of the mean weighted logistic loss (overwrites grad, loss)."""
+    _check(lib().seedgb_mlp_grad(params.data_ptr(), norm.data_ptr(), features.data_ptr(),
+                                 labels.data_ptr(), int(features.shape[0]), float(pos_weight),
+                                 grad.data_ptr(), loss.data_ptr(), _stream_ptr(stream)),
+           "seedgb_mlp_grad")
+
+
+def mlp_adam(params, grad, m, v, step, lr, beta1=0.9, beta2=0.999, eps=1e-8, stream=None):
+    _check(lib().seedgb_mlp_adam(params.data_ptr(), grad.data_ptr(), m.data_ptr(), v.data_ptr(),
+                                 int(params.numel()), int(step), float(lr), float(beta1),
+                                 float(beta2), float(eps), _stream_ptr(stream)),
+           "seedgb_mlp_adam")
 
 
 class SeedParameterEstimationAlgorithm:
