@@ -738,6 +738,28 @@ static_assert(sizeof(DoubletRec) == 48, "doublet record layout");
 // the network runs on the tensor cores (two 16-doublet tiles), and each
 // lane gets its doublet's logit back through lg.  Records the doublets when
 // a dump buffer is set.  xs: 128 words of warp scratch, lg: 32 floats.
+// Records one chunk of scored doublets (cold path, kept out of line).
+__device__ __noinline__ void dump_chunk(unsigned long long* count, DoubletRec* dump,
+                                        unsigned long long cap, bool valid, uint32_t mid_idx,
+                                        uint32_t oth_idx, uint32_t role, const float (&x)[kMlpIn],
+                                        float logit) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t vm = __ballot_sync(0xffffffffu, valid);
+    unsigned long long b = 0;
+    if (lane == 0) b = atomicAdd(count, static_cast<unsigned long long>(__popc(vm)));
+    __syncwarp();
+    b = __shfl_sync(0xffffffffu, b, 0) + __popc(vm & lanemask_lt());
+    if (valid && b < cap) {
+        uint4* r = reinterpret_cast<uint4*>(dump + b);
+        r[0] = make_uint4(mid_idx, oth_idx, role, __float_as_uint(x[0]));
+        r[1] = make_uint4(__float_as_uint(x[1]), __float_as_uint(x[2]), __float_as_uint(x[3]),
+                          __float_as_uint(x[4]));
+        r[2] = make_uint4(__float_as_uint(x[5]), __float_as_uint(x[6]), __float_as_uint(x[7]),
+                          __float_as_uint(logit));
+    }
+    __syncwarp();
+}
+
 template <bool TOP>
 __device__ __forceinline__ float score_chunk(const DevConfig& c, const Arena& a,
                                              const MlpRegs& R, const float (&x)[kMlpIn],
@@ -748,33 +770,21 @@ __device__ __forceinline__ float score_chunk(const DevConfig& c, const Arena& a,
     if (valid) mlp_pack_inputs(c.mlp_mu, c.mlp_isd, x, pk);
     *reinterpret_cast<uint4*>(xs + 4 * lane) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
     __syncwarp();
-    float lo0, hi0, lo1, hi1;
-    mlp_tile16_regs(R, xs, lane, lo0, hi0);
-    mlp_tile16_regs(R, xs + 64, lane, lo1, hi1);
-    if ((lane & 3) == 0) {
-        const uint32_t g = lane >> 2;
-        lg[g] = lo0;
-        lg[g + 8] = hi0;
-        lg[16 + g] = lo1;
-        lg[24 + g] = hi1;
+    // one copy of the tile code for both 16-doublet tiles (instruction cache)
+#pragma unroll 1
+    for (uint32_t tt = 0; tt < 2; ++tt) {
+        float lo, hi;
+        mlp_tile16_regs(R, xs + 64 * tt, lane, lo, hi);
+        if ((lane & 3) == 0) {
+            const uint32_t g = lane >> 2;
+            lg[16 * tt + g] = lo;
+            lg[16 * tt + g + 8] = hi;
+        }
     }
     __syncwarp();
     const float logit = lg[lane];
-    if (a.dump) {
-        const uint32_t vm = __ballot_sync(0xffffffffu, valid);
-        unsigned long long b = 0;
-        if (lane == 0)
-            b = atomicAdd(&a.counters[kDumpCount], static_cast<unsigned long long>(__popc(vm)));
-        b = __shfl_sync(0xffffffffu, b, 0) + __popc(vm & lt);
-        if (valid && b < a.dump_cap) {
-            uint4* r = reinterpret_cast<uint4*>(reinterpret_cast<DoubletRec*>(a.dump) + b);
-            r[0] = make_uint4(mid_idx, oth_idx, (TOP ? 1u : 0u) | (ev << 1), __float_as_uint(x[0]));
-            r[1] = make_uint4(__float_as_uint(x[1]), __float_as_uint(x[2]),
-                              __float_as_uint(x[3]), __float_as_uint(x[4]));
-            r[2] = make_uint4(__float_as_uint(x[5]), __float_as_uint(x[6]),
-                              __float_as_uint(x[7]), __float_as_uint(logit));
-        }
-    }
+    if (a.dump) dump_chunk(a.counters + kDumpCount, static_cast<DoubletRec*>(a.dump), a.dump_cap,
+                           valid, mid_idx, oth_idx, (TOP ? 1u : 0u) | (ev << 1), x, logit);
     __syncwarp();
     return logit;
 }
