@@ -648,7 +648,9 @@ using SlowScratch = WarpScratch<8192, 8192, 4096, 2048>;
 
 // Keep the positions whose doublet passes the minimum-helix-radius test, in
 // order, in q[0..n).  Two doublets per lane per iteration.
-__device__ __forceinline__ uint32_t helix_compact(const DevConfig& c, const NbView& nb,
+// Out of line: one copy serves both roles (instruction-cache pressure of the
+// fused kernel; measured faster than two inlined copies).
+__device__ __noinline__ uint32_t helix_compact(const DevConfig& c, const NbView& nb,
                                                   const float4 m, uint16_t* q,
                                                   uint32_t n, uint32_t lane,
                                                   uint32_t lt) {

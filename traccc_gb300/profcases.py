@@ -40,9 +40,10 @@ def case_plain4():
     from traccc_gb300 import seeding
     sps = [seeding.SpacepointCollection.from_numpy(e) for e in _events(4)]
     alg = seeding.TripletSeedingAlgorithm()
+    outs = [seeding.SeedBuffer(alg.max_seeds(len(s))) for s in sps]
     for _ in range(2):
-        alg.run_batch(sps)
-    _range(torch, lambda: alg.run_batch(sps))
+        alg.run_batch(sps, outs)
+    _range(torch, lambda: alg.run_batch(sps, outs))
     assert alg.last_status() == seeding.OK
 
 
@@ -60,10 +61,11 @@ def case_learned4():
     alg = seeding.TripletSeedingAlgorithm()
     model, rep = _trained_model(alg)
     sps = [seeding.SpacepointCollection.from_numpy(e) for e in _events(4)]
+    outs = [seeding.SeedBuffer(alg.max_seeds(len(s))) for s in sps]
     alg.set_filter(model.struct())
     for _ in range(2):
-        alg.run_batch(sps)
-    _range(torch, lambda: alg.run_batch(sps))
+        alg.run_batch(sps, outs)
+    _range(torch, lambda: alg.run_batch(sps, outs))
     assert alg.last_status() == seeding.OK
     per, fb, _ = alg.filter_stats(4)
     print("pruned fraction per event:", ((per[:, 1] + per[:, 3]) / per[:, 2].clip(1)).round(3),
@@ -94,10 +96,11 @@ def case_batch64():
     from traccc_gb300 import seeding, synth
     sps = [seeding.SpacepointCollection.from_numpy(e) for e in synth.batch_events(64, 3)]
     alg = seeding.TripletSeedingAlgorithm()
+    outs = [seeding.SeedBuffer(alg.max_seeds(len(s))) for s in sps]
     alg.graph_create(64, sum(len(s) for s in sps))
     for _ in range(2):
-        alg.graph_launch(sps)
-    _range(torch, lambda: alg.graph_launch(sps))
+        alg.graph_launch(sps, outs)
+    _range(torch, lambda: alg.graph_launch(sps, outs))
     assert alg.last_status() == seeding.OK
 
 
