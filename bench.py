@@ -19,6 +19,18 @@ estimation (one launch per event).
   cpu_baseline : the oracle (restated reference host seeding, libm phi) on a
           bounded sample of the same events, one event per host thread
 
+Also in the JSON line (one GPU):
+  learned : the same 20-event step with the learned doublet filter, trained
+            on the GPU by the library's kernels (200 events, cfg2 per-track
+            statistics, U(500, 12000) tracks) and calibrated for 99.5 % seed
+            recall on 20 held-out events; events/s, speed-up against the
+            plain step, per-event recall, seeds outside the plain set,
+            pruned fraction, fallback events, training report
+  batched : the 64-event uneven batch (5k-114k spacepoints per event) through
+            the captured graph with the autotuned launch shape, plain and
+            with the filter: events/s, p50/p99 batch latency (device and end
+            to end), autotuner report
+
 ``--impl reference`` times the reference's CPU seeding path (the oracle port;
 the reference itself cannot be built here) with all host
 threads on the same workload and metric.
