@@ -262,6 +262,78 @@ seedgb_status seedgb_seeding_set_option(seedgb_seeding* h, seedgb_option opt,
 seedgb_status seedgb_seeding_kernel_times(seedgb_seeding* h, float ms[7]);
 
 /* ------------------------------------------------------------------------ */
+/* Spacepoint formation (the step in front of the seeding path)              */
+/* ------------------------------------------------------------------------ */
+
+/* A measurement surface: local -> global placement and shape, the part of
+ * detray's tracking_surface::local_to_global that spacepoint formation uses
+ * (core/include/traccc/seeding/impl/spacepoint_formation.ipp:30-38).
+ *  type 0, plane:    (l0, l1)      -> R (l0, l1, 0) + t
+ *  type 1, cylinder: (r phi, z)    -> R (r cos phi, r sin phi, z) + t,
+ *                    phi = l0 / radius
+ * R is row-major; each global coordinate is (R[i][0] a + R[i][1] b) +
+ * R[i][2] c + t[i] in float arithmetic without contraction; cos and sin of
+ * the cylinder angle are evaluated in double and rounded to float. */
+typedef struct {
+    uint32_t type;
+    float radius;
+    float rotation[9];
+    float translation[3];
+} seedgb_surface;
+
+/* Replaces silicon_pixel_spacepoint_formation (core/src/seeding/
+ * silicon_pixel_spacepoint_formation.hpp:31-60; device form_spacepoints,
+ * device/common/include/traccc/seeding/device/impl/form_spacepoints.ipp):
+ * one spacepoint per 2-dimensional measurement (dimensions == NULL: all
+ * are), global position from its surface, measurement_index_1 = the
+ * measurement's index, measurement_index_2 = SEEDGB_INVALID_MEASUREMENT_INDEX,
+ * variances 0.  The surface of a measurement is surfaces[surface_link];
+ * measurements whose surface_link is >= n_surfaces form no spacepoint.
+ * Spacepoints are written in measurement order (the host algorithm's order;
+ * the reference's device version appends in no fixed order).  All pointers
+ * are device memory except `surfaces_host`, copied on the stream; outputs
+ * have room for meas->size spacepoints; *n_out (device) receives the count. */
+seedgb_status seedgb_form_spacepoints(const seedgb_surface* surfaces_host, uint32_t n_surfaces,
+                                      const seedgb_measurement_view* meas,
+                                      const uint8_t* dimensions,
+                                      uint32_t* measurement_index_1,
+                                      uint32_t* measurement_index_2, float* global,
+                                      float* z_variance, float* radius_variance,
+                                      uint32_t* n_out, void* stream);
+
+/* ------------------------------------------------------------------------ */
+/* CSV input (traccc's on-disk event format)                                 */
+/* ------------------------------------------------------------------------ */
+
+/* Number of data rows of a CSV file (its header line excluded), or -1. */
+int64_t seedgb_csv_rows(const char* path);
+
+/* Replaces traccc::io::csv::read_spacepoints (io/src/csv/read_spacepoints.cpp:
+ * 25-77): one spacepoint per row of the hit file (columns tx, ty, tz, found
+ * by name), measurement_index_1 = the measurement whose measurement-hit-id
+ * row names this hit's row index (else SEEDGB_INVALID_MEASUREMENT_INDEX),
+ * measurement_index_2 = invalid, variances 0.  Host memory, capacity rows;
+ * *n gets the row count.  meas_hit_map_path may be NULL (all invalid).
+ * Measurements keep file order (the reader's sort_measurements = false). */
+seedgb_status seedgb_csv_read_spacepoints(const char* hits_path, const char* meas_hit_map_path,
+                                          uint64_t capacity, uint32_t* measurement_index_1,
+                                          uint32_t* measurement_index_2, float* global,
+                                          float* z_variance, float* radius_variance,
+                                          uint64_t* n);
+
+/* The measurement columns parameter estimation reads, from a measurement
+ * file (io/include/traccc/io/csv/measurement.hpp: measurement_id,
+ * geometry_id, local_key, local0, local1, ...): local_position = (local0,
+ * local1), surface_link = geometry_id as written (the reference maps the
+ * ACTS geometry id to a detray barcode through the detector description,
+ * which is not part of this library), dimensions from local_key as
+ * make_measurement_edm.cpp:36-52 decodes it (bit 1: loc0 active, bit 2:
+ * loc1 active; inactive local coordinates are 0).  Host memory. */
+seedgb_status seedgb_csv_read_measurements(const char* meas_path, uint64_t capacity,
+                                           float* local_position, uint64_t* surface_link,
+                                           uint8_t* dimensions, uint64_t* n);
+
+/* ------------------------------------------------------------------------ */
 /* Batched, graph-captured launches.  No counterpart in the reference, which */
 /* overlaps events with one CUDA stream per host thread (throughput_mt.ipp:  */
 /* 171-179); here a whole batch of uneven events runs as one captured launch */

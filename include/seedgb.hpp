@@ -1,0 +1,239 @@
+/*
+ * seedgb.hpp -- C++ surface of the GB300 seeding library: the reference's
+ * algorithm classes and operator() calls over the C ABI of seedgb.h.
+ *
+ *  seedgb::triplet_seeding_algorithm          <- traccc::cuda::triplet_seeding_algorithm
+ *      constructor: device/cuda/include/traccc/cuda/seeding/
+ *                   triplet_seeding_algorithm.hpp:35-40 (configs + stream)
+ *      operator():  device/common/include/traccc/seeding/device/
+ *                   triplet_seeding_algorithm.hpp:68-69 (spacepoint view ->
+ *                   seed buffer, asynchronous on the stream)
+ *  seedgb::seed_parameter_estimation_algorithm <- traccc::cuda::seed_parameter_estimation_algorithm
+ *      operator():  device/common/include/traccc/seeding/device/
+ *                   seed_parameter_estimation_algorithm.hpp:48-67
+ *
+ * Header-only, C++17, needs cuda_runtime.h for the device buffers.  Errors
+ * are exceptions as in the reference: std::domain_error for a rejected
+ * configuration (spacepoint_binning_helper.hpp:33-38), std::runtime_error
+ * for CUDA and capacity failures.  Buffers own device memory (cudaMalloc /
+ * cudaFree); views are borrowed.  One algorithm object per stream.
+ */
+#ifndef SEEDGB_HPP
+#define SEEDGB_HPP
+
+#include <cuda_runtime.h>
+
+#include <array>
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "seedgb.h"
+
+namespace seedgb {
+
+inline void check(seedgb_status st, const char* what) {
+    if (st == SEEDGB_OK) return;
+    const std::string msg = std::string(what) + ": " + seedgb_status_string(st);
+    if (st == SEEDGB_BAD_CONFIG) throw std::domain_error(msg);
+    throw std::runtime_error(msg);
+}
+
+/* Device array owned by the object. */
+template <typename T>
+class device_buffer {
+public:
+    device_buffer() = default;
+    explicit device_buffer(std::size_t n) : n_(n) {
+        if (n && cudaMalloc(&p_, n * sizeof(T)) != cudaSuccess)
+            throw std::runtime_error("cudaMalloc failed");
+    }
+    device_buffer(const device_buffer&) = delete;
+    device_buffer& operator=(const device_buffer&) = delete;
+    device_buffer(device_buffer&& o) noexcept { swap(o); }
+    device_buffer& operator=(device_buffer&& o) noexcept {
+        swap(o);
+        return *this;
+    }
+    ~device_buffer() {
+        if (p_) cudaFree(p_);
+    }
+    T* data() const { return p_; }
+    std::size_t size() const { return n_; }
+    void swap(device_buffer& o) noexcept {
+        std::swap(p_, o.p_);
+        std::swap(n_, o.n_);
+    }
+
+private:
+    T* p_ = nullptr;
+    std::size_t n_ = 0;
+};
+
+/* One seed on the host (edm::seed: bottom, middle, top, quality). */
+struct seed {
+    uint32_t bottom, middle, top;
+    float quality;
+};
+
+/* edm::seed_collection::buffer: four device columns and a device size,
+ * resizable like the reference's buffer (triplet_seeding_algorithm.cpp:249-252). */
+class seed_collection_buffer {
+public:
+    explicit seed_collection_buffer(uint32_t capacity)
+        : bottom(capacity), middle(capacity), top(capacity), quality(capacity), size(1),
+          capacity_(capacity) {}
+    seedgb_seed_buffer view() const {
+        return seedgb_seed_buffer{bottom.data(), middle.data(), top.data(), quality.data(),
+                                  capacity_, size.data()};
+    }
+    uint32_t capacity() const { return capacity_; }
+    /* Copy to the host (synchronises `stream`). */
+    std::vector<seed> to_host(cudaStream_t stream) const {
+        uint32_t n = 0;
+        if (cudaMemcpyAsync(&n, size.data(), sizeof n, cudaMemcpyDeviceToHost, stream) !=
+                cudaSuccess ||
+            cudaStreamSynchronize(stream) != cudaSuccess)
+            throw std::runtime_error("seed size copy failed");
+        n = n < capacity_ ? n : capacity_;
+        std::vector<uint32_t> b(n), m(n), t(n);
+        std::vector<float> q(n);
+        if (n) {
+            cudaMemcpyAsync(b.data(), bottom.data(), 4 * n, cudaMemcpyDeviceToHost, stream);
+            cudaMemcpyAsync(m.data(), middle.data(), 4 * n, cudaMemcpyDeviceToHost, stream);
+            cudaMemcpyAsync(t.data(), top.data(), 4 * n, cudaMemcpyDeviceToHost, stream);
+            cudaMemcpyAsync(q.data(), quality.data(), 4 * n, cudaMemcpyDeviceToHost, stream);
+            if (cudaStreamSynchronize(stream) != cudaSuccess)
+                throw std::runtime_error("seed copy failed");
+        }
+        std::vector<seed> out(n);
+        for (uint32_t i = 0; i < n; ++i) out[i] = seed{b[i], m[i], t[i], q[i]};
+        return out;
+    }
+
+    device_buffer<uint32_t> bottom, middle, top;
+    device_buffer<float> quality;
+    device_buffer<uint32_t> size;
+
+private:
+    uint32_t capacity_;
+};
+
+/* bound_track_parameters_collection_types::buffer. */
+class track_params_buffer {
+public:
+    explicit track_params_buffer(uint32_t capacity) : data(capacity), size(1), capacity_(capacity) {}
+    seedgb_params_buffer view() const {
+        return seedgb_params_buffer{data.data(), capacity_, size.data()};
+    }
+    std::vector<seedgb_bound_track_parameters> to_host(cudaStream_t stream) const {
+        uint32_t n = 0;
+        if (cudaMemcpyAsync(&n, size.data(), sizeof n, cudaMemcpyDeviceToHost, stream) !=
+                cudaSuccess ||
+            cudaStreamSynchronize(stream) != cudaSuccess)
+            throw std::runtime_error("parameter size copy failed");
+        n = n < capacity_ ? n : capacity_;
+        std::vector<seedgb_bound_track_parameters> out(n);
+        if (n && (cudaMemcpyAsync(out.data(), data.data(), sizeof(out[0]) * n,
+                                  cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
+                  cudaStreamSynchronize(stream) != cudaSuccess))
+            throw std::runtime_error("parameter copy failed");
+        return out;
+    }
+
+    device_buffer<seedgb_bound_track_parameters> data;
+    device_buffer<uint32_t> size;
+
+private:
+    uint32_t capacity_;
+};
+
+/* traccc::cuda::triplet_seeding_algorithm. */
+class triplet_seeding_algorithm {
+public:
+    triplet_seeding_algorithm(const seedgb_seedfinder_config& finder,
+                              const seedgb_spacepoint_grid_config& grid,
+                              const seedgb_seedfilter_config& filter, cudaStream_t stream)
+        : finder_(finder), stream_(stream) {
+        check(seedgb_seeding_create(&finder, &grid, &filter, &h_), "triplet_seeding_algorithm");
+    }
+    triplet_seeding_algorithm(const triplet_seeding_algorithm&) = delete;
+    triplet_seeding_algorithm& operator=(const triplet_seeding_algorithm&) = delete;
+    ~triplet_seeding_algorithm() { seedgb_seeding_destroy(h_); }
+
+    /* Seeds of one event, in the host seeding's order; asynchronous. */
+    seed_collection_buffer operator()(const seedgb_spacepoint_view& spacepoints) const {
+        seed_collection_buffer out(capacity(spacepoints.size));
+        seedgb_seed_buffer b = out.view();
+        check(seedgb_seeding_run(h_, &spacepoints, &b, stream_), "triplet_seeding_algorithm()");
+        return out;
+    }
+
+    /* Many events in one launch sequence. */
+    std::vector<seed_collection_buffer> operator()(
+        const std::vector<seedgb_spacepoint_view>& events) const {
+        std::vector<seed_collection_buffer> out;
+        std::vector<seedgb_seed_buffer> views;
+        out.reserve(events.size());
+        for (const auto& e : events) {
+            out.emplace_back(capacity(e.size));
+            views.push_back(out.back().view());
+        }
+        if (!events.empty())
+            check(seedgb_seeding_run_batch(h_, events.data(), static_cast<uint32_t>(events.size()),
+                                           views.data(), stream_),
+                  "triplet_seeding_algorithm(batch)");
+        return out;
+    }
+
+    /* Device status of the last call (synchronises the stream). */
+    void check_status() const {
+        check(seedgb_seeding_last_status(h_, stream_), "triplet_seeding_algorithm status");
+    }
+    seedgb_seeding* handle() const { return h_; }
+
+private:
+    uint32_t capacity(uint32_t n_sp) const {
+        const uint64_t c = static_cast<uint64_t>(finder_.maxSeedsPerSpM) * n_sp;
+        return static_cast<uint32_t>(c > 0 ? (c < 0xFFFFFFFFull ? c : 0xFFFFFFFFull) : 1);
+    }
+    seedgb_seedfinder_config finder_;
+    cudaStream_t stream_;
+    seedgb_seeding* h_ = nullptr;
+};
+
+/* traccc::cuda::seed_parameter_estimation_algorithm (constant field). */
+class seed_parameter_estimation_algorithm {
+public:
+    seed_parameter_estimation_algorithm(const seedgb_track_params_estimation_config& cfg,
+                                        cudaStream_t stream)
+        : stream_(stream) {
+        check(seedgb_params_create(&cfg, &h_), "seed_parameter_estimation_algorithm");
+    }
+    seed_parameter_estimation_algorithm(const seed_parameter_estimation_algorithm&) = delete;
+    seed_parameter_estimation_algorithm& operator=(const seed_parameter_estimation_algorithm&) =
+        delete;
+    ~seed_parameter_estimation_algorithm() { seedgb_params_destroy(h_); }
+
+    track_params_buffer operator()(const std::array<float, 3>& bfield,
+                                   const seedgb_measurement_view& measurements,
+                                   const seedgb_spacepoint_view& spacepoints,
+                                   const seed_collection_buffer& seeds) const {
+        track_params_buffer out(seeds.capacity());
+        seedgb_seed_buffer s = seeds.view();
+        seedgb_params_buffer p = out.view();
+        check(seedgb_params_run(h_, bfield.data(), &measurements, &spacepoints, &s, &p, stream_),
+              "seed_parameter_estimation_algorithm()");
+        return out;
+    }
+
+private:
+    cudaStream_t stream_;
+    seedgb_params* h_ = nullptr;
+};
+
+}  // namespace seedgb
+
+#endif

@@ -164,6 +164,10 @@ def lib():
                                     P(C.c_uint64), C.c_void_p, C.c_uint32,
                                     P(C.c_uint32), P(Stats)]
         L.or_seeding_ex.restype = C.c_int
+        L.or_form_spacepoints.argtypes = [C.c_void_p, C.c_uint32, P(Measurements), C.c_void_p,
+                                          C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                          C.c_void_p]
+        L.or_form_spacepoints.restype = C.c_uint32
         L.or_mlp_logit.argtypes = [P(DoubletFilter), P(C.c_float)]
         L.or_mlp_logit.restype = C.c_float
         L.or_bf16_round.argtypes = [C.c_float]
@@ -360,6 +364,34 @@ def seeding_ex(ev, f=None, g=None, fl=None, phi_mode=PHI_CR, filt=None, dump=Fal
         tcap = nt.value
     res = (out[: n.value].copy(), st.as_dict(), (drec[: nd.value].copy() if dump else None))
     return res + (trec[: nt.value].copy(),) if triplets else res
+
+
+SURFACE_DTYPE = np.dtype([("type", "<u4"), ("radius", "<f4"), ("rotation", "<f4", (9,)),
+                          ("translation", "<f4", (3,))])
+
+
+def form_spacepoints(surfaces, local_position, surface_link, dimensions=None):
+    """Spacepoint formation: returns the spacepoint columns (dict) of the
+    2-dimensional measurements, in measurement order."""
+    surfaces = np.ascontiguousarray(surfaces, SURFACE_DTYPE)
+    lp = np.ascontiguousarray(local_position, np.float32).reshape(-1)
+    sl = np.ascontiguousarray(surface_link, np.uint64)
+    n = len(sl)
+    m = Measurements(lp.ctypes.data_as(C.POINTER(C.c_float)),
+                     sl.ctypes.data_as(C.POINTER(C.c_uint64)), n)
+    dims = None if dimensions is None else np.ascontiguousarray(dimensions, np.uint8)
+    out = {"measurement_index_1": np.zeros(n, np.uint32),
+           "measurement_index_2": np.zeros(n, np.uint32),
+           "global": np.zeros((n, 3), np.float32),
+           "z_variance": np.zeros(n, np.float32),
+           "radius_variance": np.zeros(n, np.float32)}
+    k = lib().or_form_spacepoints(
+        surfaces.ctypes.data if len(surfaces) else None, len(surfaces), C.byref(m),
+        dims.ctypes.data if dims is not None else None,
+        out["measurement_index_1"].ctypes.data, out["measurement_index_2"].ctypes.data,
+        out["global"].ctypes.data, out["z_variance"].ctypes.data,
+        out["radius_variance"].ctypes.data)
+    return {key: v[:k].copy() for key, v in out.items()}
 
 
 def track_params(ev, seeds, bfield, tp=None):

@@ -1028,3 +1028,45 @@ int or_track_params(const or_tp_config* c, const or_measurements* meas,
     }
     return 0;
 }
+
+/* ------------------------------------------------------------------------ */
+/* Spacepoint formation                                                      */
+/* ------------------------------------------------------------------------ */
+
+/* silicon_pixel_spacepoint_formation.hpp:31-60 with fill_pixel_spacepoint
+ * (spacepoint_formation.ipp:27-47): valid = 2-dimensional measurement. */
+uint32_t or_form_spacepoints(const or_surface* surfaces, uint32_t n_surfaces,
+                             const or_measurements* meas, const uint8_t* dims,
+                             uint32_t* mi1, uint32_t* mi2, float* global,
+                             float* zvar, float* rvar) {
+    uint32_t k = 0;
+    for (uint32_t i = 0; i < meas->size; ++i) {
+        if (dims && dims[i] != 2u) continue;
+        if (meas->surface_link[i] >= n_surfaces) continue;
+        const or_surface* S = &surfaces[meas->surface_link[i]];
+        const float l0 = meas->local_position[2 * i];
+        const float l1 = meas->local_position[2 * i + 1];
+        float a, b, c;
+        if (S->type == 1u) {
+            const double phi = (double)l0 / (double)S->radius;
+            a = S->radius * (float)cos(phi);
+            b = S->radius * (float)sin(phi);
+            c = l1;
+        } else {
+            a = l0;
+            b = l1;
+            c = 0.f;
+        }
+        for (int r = 0; r < 3; ++r) {
+            float v = S->rotation[3 * r] * a + S->rotation[3 * r + 1] * b;
+            v = v + S->rotation[3 * r + 2] * c;
+            global[3 * k + r] = v + S->translation[r];
+        }
+        mi1[k] = i;
+        mi2[k] = 0xFFFFFFFFu;
+        zvar[k] = 0.f;
+        rvar[k] = 0.f;
+        ++k;
+    }
+    return k;
+}

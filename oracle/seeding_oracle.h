@@ -257,6 +257,28 @@ int or_seeding_ex(const or_finder_config* fc, const or_grid_config* gc,
                   or_triplet_rec* tdump, uint64_t tdump_cap, uint64_t* n_tdump,
                   or_seed* out, uint32_t cap, uint32_t* n_out, or_stats* stats);
 
+/* Spacepoint formation (core/src/seeding/silicon_pixel_spacepoint_formation.hpp:
+ * 31-60, core/include/traccc/seeding/impl/spacepoint_formation.ipp:20-47):
+ * one spacepoint per 2-dimensional measurement, in measurement order, global
+ * position = the surface's local_to_global.  Surfaces: type 0 plane,
+ * (l0, l1) -> R (l0, l1, 0) + t; type 1 cylinder, (r phi, z) ->
+ * R (r cos phi, r sin phi, z) + t with phi = l0 / radius (cos, sin in
+ * double, rounded to float); each coordinate (R[i][0] a + R[i][1] b) +
+ * R[i][2] c + t[i] in float.  (detray's algebra is not vendored: the
+ * placement arithmetic is this definition; parity unpinned against detray.)
+ * dims == NULL: all measurements are 2-dimensional.  Measurements whose
+ * surface_link >= n_surfaces form no spacepoint.  Returns the count. */
+typedef struct {
+    uint32_t type;
+    float radius;
+    float rotation[9];
+    float translation[3];
+} or_surface;
+uint32_t or_form_spacepoints(const or_surface* surfaces, uint32_t n_surfaces,
+                             const or_measurements* meas, const uint8_t* dims,
+                             uint32_t* mi1, uint32_t* mi2, float* global,
+                             float* zvar, float* rvar);
+
 /* Host track-parameter estimation (core/src/seeding/
  * track_params_estimation.cpp:23-91). */
 int or_track_params(const or_tp_config* c, const or_measurements* meas,

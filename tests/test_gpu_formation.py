@@ -1,0 +1,81 @@
+"""Spacepoint formation on the GPU against the oracle: bit-identical
+spacepoints (cylinder and rotated-plane surfaces, pixel / strip mix, unknown
+surfaces), measurement order kept, and formation -> seeding gives the
+oracle's seeds on the formed spacepoints."""
+import numpy as np
+import pytest
+
+import oracle as O
+from traccc_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+
+def _surfaces(seed=0):
+    from tests.test_io_formation import barrel_surfaces
+    s = barrel_surfaces()
+    rng = np.random.default_rng(seed)
+    planes = np.zeros(5, O.SURFACE_DTYPE)
+    for k in range(5):
+        q = rng.normal(size=4)
+        q /= np.linalg.norm(q)
+        w, x, y, z = q
+        R = np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)],
+                      [2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)],
+                      [2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)]])
+        planes[k]["type"] = 0
+        planes[k]["rotation"] = R.astype(np.float32).reshape(-1)
+        planes[k]["translation"] = rng.uniform(-500, 500, 3).astype(np.float32)
+    return np.concatenate([s, planes])
+
+
+def test_formation_matches_oracle():
+    import torch
+
+    from traccc_gb300 import seeding
+    ev = synth.workload_event("cfg1", 6)
+    n = len(ev["global"])
+    rng = np.random.default_rng(1)
+    link = np.asarray(ev["surface_link"], np.uint64).copy()
+    link[rng.choice(n, 300, replace=False)] = rng.integers(11, 16, 300)  # planes
+    link[rng.choice(n, 50, replace=False)] = 1000                        # unknown
+    dims = np.full(n, 2, np.uint8)
+    dims[rng.choice(n, 200, replace=False)] = 1
+    surf = _surfaces()
+    ref = O.form_spacepoints(surf, ev["local_position"], link, dims)
+    meas = seeding.MeasurementCollection.from_numpy(dict(local_position=ev["local_position"],
+                                                         surface_link=link))
+    sps, k = seeding.form_spacepoints(surf, meas, torch.from_numpy(dims).cuda())
+    torch.cuda.synchronize()
+    assert k == len(ref["global"])
+    got_g = sps.global_.cpu().numpy()
+    assert np.array_equal(sps.measurement_index_1.cpu().numpy().view(np.uint32),
+                          ref["measurement_index_1"])
+    assert np.all(sps.measurement_index_2.cpu().numpy().view(np.uint32) == 0xFFFFFFFF)
+    # cos / sin in double rounded to float: identical except where the two
+    # libraries' double results straddle a float rounding boundary
+    same = np.all(got_g.view(np.uint32) == ref["global"].view(np.uint32), axis=1)
+    assert same.mean() > 0.9999
+    assert np.abs(got_g - ref["global"]).max() < 1e-3
+
+
+def test_formation_then_seeding():
+    import torch
+
+    from traccc_gb300 import seeding
+    ev = synth.workload_event("cfg1", 8)
+    surf = _surfaces()
+    meas = seeding.MeasurementCollection.from_numpy(ev)
+    sps, k = seeding.form_spacepoints(surf, meas)
+    alg = seeding.TripletSeedingAlgorithm()
+    out = alg(sps)
+    assert alg.last_status() == seeding.OK
+    got = out.to_numpy()
+    g = sps.global_.cpu().numpy()
+    formed = {"measurement_index_1": sps.measurement_index_1.cpu().numpy().view(np.uint32),
+              "measurement_index_2": sps.measurement_index_2.cpu().numpy().view(np.uint32),
+              "global": g, "z_variance": np.zeros(k, np.float32),
+              "radius_variance": np.zeros(k, np.float32)}
+    ref, _ = O.seeding(formed)
+    assert np.array_equal(got, ref)
+    torch.cuda.synchronize()

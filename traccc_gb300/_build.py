@@ -19,8 +19,9 @@ LIBDIR = os.path.join(HERE, "_lib")
 REPO = os.path.dirname(HERE)
 INCLUDE = os.path.join(REPO, "include")
 
-CUDA_SOURCES = ["seedgb_kernels.cu", "seedgb_api.cu", "seedgb_noalloc.cu", "seedgb_learned.cu"]
-HOST_SOURCES = ["seedgb_config.cpp"]
+CUDA_SOURCES = ["seedgb_kernels.cu", "seedgb_api.cu", "seedgb_noalloc.cu", "seedgb_learned.cu",
+                "seedgb_formation.cu"]
+HOST_SOURCES = ["seedgb_config.cpp", "seedgb_io.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 # The cut arithmetic must match the reference's host float semantics: no FMA

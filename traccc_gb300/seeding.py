@@ -223,6 +223,17 @@ def lib():
         L.seedgb_seeding_filter_stats.argtypes = [vp, C.c_uint32, P(C.c_uint32),
                                                   P(C.c_uint8), P(C.c_uint64), P(C.c_uint64), vp]
         L.seedgb_seeding_filter_stats.restype = C.c_int
+        L.seedgb_form_spacepoints.argtypes = [vp, C.c_uint32, P(_MeasurementView), vp, vp, vp,
+                                              vp, vp, vp, vp, vp]
+        L.seedgb_form_spacepoints.restype = C.c_int
+        L.seedgb_csv_rows.argtypes = [C.c_char_p]
+        L.seedgb_csv_rows.restype = C.c_int64
+        L.seedgb_csv_read_spacepoints.argtypes = [C.c_char_p, C.c_char_p, C.c_uint64, vp, vp,
+                                                  vp, vp, vp, P(C.c_uint64)]
+        L.seedgb_csv_read_spacepoints.restype = C.c_int
+        L.seedgb_csv_read_measurements.argtypes = [C.c_char_p, C.c_uint64, vp, vp, vp,
+                                                   P(C.c_uint64)]
+        L.seedgb_csv_read_measurements.restype = C.c_int
         L.seedgb_mlp_num_params.restype = C.c_uint32
         L.seedgb_mlp_forward.argtypes = [vp, vp, vp, C.c_uint32, vp, vp]
         L.seedgb_mlp_forward.restype = C.c_int
@@ -588,6 +599,75 @@ class TripletSeedingAlgorithm:
             sps.ctypes.data_as(C.POINTER(C.c_uint32)), len(sps), C.byref(nv),
             _stream_ptr(stream)), "seedgb_seeding_copy_grid")
         return off, sps[: nv.value].copy()
+
+
+SURFACE_DTYPE = np.dtype([("type", "<u4"), ("radius", "<f4"), ("rotation", "<f4", (9,)),
+                          ("translation", "<f4", (3,))])
+SURFACE_PLANE, SURFACE_CYLINDER = 0, 1
+
+
+def form_spacepoints(surfaces, measurements: MeasurementCollection, dimensions=None,
+                     stream=None):
+    """silicon_pixel_spacepoint_formation on the GPU: a SpacepointCollection
+    (device, capacity = number of measurements) and the number of
+    spacepoints formed.  surfaces: numpy array of SURFACE_DTYPE indexed by
+    surface_link; dimensions: optional device uint8 tensor (2 = pixel)."""
+    torch = _torch()
+    surfaces = np.ascontiguousarray(surfaces, SURFACE_DTYPE)
+    dev = measurements.local_position.device
+    n = len(measurements.surface_link)
+    cols = SpacepointCollection(torch.empty(n, dtype=torch.int32, device=dev),
+                                torch.empty(n, dtype=torch.int32, device=dev),
+                                torch.empty((n, 3), dtype=torch.float32, device=dev),
+                                torch.empty(n, dtype=torch.float32, device=dev),
+                                torch.empty(n, dtype=torch.float32, device=dev))
+    count = torch.zeros(1, dtype=torch.int32, device=dev)
+    mv = measurements.view()
+    _check(lib().seedgb_form_spacepoints(
+        surfaces.ctypes.data if len(surfaces) else None, len(surfaces), C.byref(mv),
+        dimensions.data_ptr() if dimensions is not None else None,
+        cols.measurement_index_1.data_ptr(), cols.measurement_index_2.data_ptr(),
+        cols.global_.data_ptr(), cols.z_variance.data_ptr(), cols.radius_variance.data_ptr(),
+        count.data_ptr(), _stream_ptr(stream)), "seedgb_form_spacepoints")
+    k = int(count.item())
+    return SpacepointCollection(cols.measurement_index_1[:k], cols.measurement_index_2[:k],
+                                cols.global_[:k], cols.z_variance[:k],
+                                cols.radius_variance[:k]), k
+
+
+def read_spacepoints_csv(hits_path, meas_hit_map_path=None) -> dict:
+    """traccc's CSV spacepoints (hits + measurement-hit-id map) as numpy columns."""
+    n = int(lib().seedgb_csv_rows(str(hits_path).encode()))
+    if n < 0:
+        raise SeedingError(INVALID_ARGUMENT, f"cannot read {hits_path}")
+    out = {"measurement_index_1": np.zeros(n, np.uint32),
+           "measurement_index_2": np.zeros(n, np.uint32),
+           "global": np.zeros((n, 3), np.float32),
+           "z_variance": np.zeros(n, np.float32),
+           "radius_variance": np.zeros(n, np.float32)}
+    got = C.c_uint64(0)
+    _check(lib().seedgb_csv_read_spacepoints(
+        str(hits_path).encode(),
+        str(meas_hit_map_path).encode() if meas_hit_map_path is not None else None, n,
+        out["measurement_index_1"].ctypes.data, out["measurement_index_2"].ctypes.data,
+        out["global"].ctypes.data, out["z_variance"].ctypes.data,
+        out["radius_variance"].ctypes.data, C.byref(got)), "seedgb_csv_read_spacepoints")
+    return {k: v[: got.value] for k, v in out.items()}
+
+
+def read_measurements_csv(meas_path) -> dict:
+    """local_position, surface_link (the file's geometry_id) and dimensions."""
+    n = int(lib().seedgb_csv_rows(str(meas_path).encode()))
+    if n < 0:
+        raise SeedingError(INVALID_ARGUMENT, f"cannot read {meas_path}")
+    out = {"local_position": np.zeros((n, 2), np.float32),
+           "surface_link": np.zeros(n, np.uint64), "dimensions": np.zeros(n, np.uint8)}
+    got = C.c_uint64(0)
+    _check(lib().seedgb_csv_read_measurements(
+        str(meas_path).encode(), n, out["local_position"].ctypes.data,
+        out["surface_link"].ctypes.data, out["dimensions"].ctypes.data, C.byref(got)),
+        "seedgb_csv_read_measurements")
+    return {k: v[: got.value] for k, v in out.items()}
 
 
 DOUBLET_DTYPE = np.dtype([("middle", "<u4"), ("other", "<u4"), ("role", "<u4"),
