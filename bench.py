@@ -15,7 +15,8 @@ estimation (one launch per event).
           the launching stream, L2 flushed between steps by a 256 MiB write)
   e2e   : events/s through the public API from pinned host buffers: the
           spacepoint columns are copied in, seeds and parameters copied out
-          every step
+          every step (two steps in flight: step k-1's results are copied out
+          on a second stream while step k computes)
   cpu_baseline : the oracle (restated reference host seeding, libm phi) on a
           bounded sample of the same events, one event per host thread
 
@@ -507,51 +508,94 @@ def run_gpu(args):
     alg.reserve(n_ev, total)
     alg.set_option(seeding.OPTION_KERNEL_TIMING, 1)
 
-    sps, meas, souts, pouts = [], [], [], []
-    size_all = torch.zeros(2 * n_ev, dtype=torch.int32, device=dev)
+    sps, meas = [], []
     for e in range(n_ev):
         a, b = int(offs[e]), int(offs[e + 1])
         sps.append(seeding.SpacepointCollection(dcols["mi1"][a:b], dcols["mi2"][a:b],
                                                 dcols["glob"][a:b], dcols["zvar"][a:b],
                                                 dcols["rvar"][a:b]))
         meas.append(seeding.MeasurementCollection(dcols["lp"][a:b], dcols["sl"][a:b]))
-        so = seeding.SeedBuffer(alg.max_seeds(b - a), device=dev)
-        so.size = size_all[e:e + 1]
-        po = seeding.ParamsBuffer(so.capacity, device=dev)
-        po.size = size_all[n_ev + e:n_ev + e + 1]
-        souts.append(so)
-        pouts.append(po)
+
+    def make_outputs():
+        """Seed and parameter buffers of the 20 events, sizes in one array
+        (seeds first, then parameters)."""
+        size_all = torch.zeros(2 * n_ev, dtype=torch.int32, device=dev)
+        souts, pouts = [], []
+        for e in range(n_ev):
+            so = seeding.SeedBuffer(alg.max_seeds(int(offs[e + 1] - offs[e])), device=dev)
+            so.size = size_all[e:e + 1]
+            po = seeding.ParamsBuffer(so.capacity, device=dev)
+            po.size = size_all[n_ev + e:n_ev + e + 1]
+            souts.append(so)
+            pouts.append(po)
+        return souts, pouts, size_all
+
+    souts, pouts, size_all = make_outputs()
     stream = torch.cuda.current_stream()
     flush_buf = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device=dev)
 
-    def step_device():
-        alg.run_batch(sps, souts, stream=stream)
+    def step_device(outs=None):
+        so, po = (souts, pouts) if outs is None else outs
+        alg.run_batch(sps, so, stream=stream)
         for e in range(n_ev):
-            est(bfield, meas[e], sps[e], souts[e], pouts[e], stream=stream)
+            est(bfield, meas[e], sps[e], so[e], po[e], stream=stream)
 
-    # host-side result buffers for the end-to-end path
-    h_sizes = torch.zeros(2 * n_ev, dtype=torch.int32).pin_memory()
-    h_seeds = [torch.empty((4, max(1, s.capacity)), dtype=torch.int32).pin_memory()
-               for s in souts]
-    h_params = [torch.empty(p.data.numel(), dtype=torch.uint8).pin_memory() for p in pouts]
+    # End to end, pipelined two deep: step k's inputs are copied in and its
+    # seeds and parameters computed on the compute stream while step k-1's
+    # results are copied out on a second stream (two output sets, two host
+    # result sets).  Every step copies its whole input in from pinned memory
+    # and its seeds and parameters out.
+    out_sets = [(souts, pouts, size_all), make_outputs()]
+    copy_stream = torch.cuda.Stream(device=dev)
+    h_sizes = [torch.zeros(2 * n_ev, dtype=torch.int32).pin_memory() for _ in range(2)]
+    h_seeds = [[torch.empty((4, max(1, so.capacity)), dtype=torch.int32).pin_memory()
+                for so in out_sets[0][0]] for _ in range(2)]
+    h_params = [[torch.empty(po.data.numel(), dtype=torch.uint8).pin_memory()
+                 for po in out_sets[0][1]] for _ in range(2)]
+    computed = [torch.cuda.Event() for _ in range(2)]
+    copied = [torch.cuda.Event() for _ in range(2)]
     h2d_bytes = sum(v.numel() * v.element_size() for v in pinned.values())
 
-    def step_e2e():
-        for k in dcols:
-            dcols[k].copy_(pinned[k], non_blocking=True)
-        step_device()
-        h_sizes.copy_(size_all, non_blocking=True)
-        stream.synchronize()
-        d2h = h_sizes.numel() * 4
-        for e in range(n_ev):
-            ns, npar = int(h_sizes[e]), int(h_sizes[n_ev + e])
-            so = souts[e]
-            for j, col in enumerate((so.bottom_index, so.middle_index, so.top_index)):
-                h_seeds[e][j, :ns].copy_(col[:ns], non_blocking=True)
-            h_seeds[e][3, :ns].copy_(so.quality[:ns].view(torch.int32), non_blocking=True)
-            nb = npar * seeding.PARAMS_DTYPE.itemsize
-            h_params[e][:nb].copy_(pouts[e].data[:nb], non_blocking=True)
-            d2h += 16 * ns + nb
+    def e2e_issue(k):
+        b = k % 2
+        so, po, sz = out_sets[b]
+        # the copies of step k-2 read this output set
+        stream.wait_event(copied[b])
+        flush_buf.fill_(1)
+        for key in dcols:
+            dcols[key].copy_(pinned[key], non_blocking=True)
+        step_device((so, po))
+        h_sizes[b].copy_(sz, non_blocking=True)
+        computed[b].record(stream)
+
+    def e2e_collect(k):
+        b = k % 2
+        so, po, _ = out_sets[b]
+        computed[b].synchronize()
+        d2h = h_sizes[b].numel() * 4
+        with torch.cuda.stream(copy_stream):
+            copy_stream.wait_event(computed[b])
+            for e in range(n_ev):
+                ns, npar = int(h_sizes[b][e]), int(h_sizes[b][n_ev + e])
+                for j, col in enumerate((so[e].bottom_index, so[e].middle_index,
+                                         so[e].top_index)):
+                    h_seeds[b][e][j, :ns].copy_(col[:ns], non_blocking=True)
+                h_seeds[b][e][3, :ns].copy_(so[e].quality[:ns].view(torch.int32),
+                                            non_blocking=True)
+                nb = npar * seeding.PARAMS_DTYPE.itemsize
+                h_params[b][e][:nb].copy_(po[e].data[:nb], non_blocking=True)
+                d2h += 16 * ns + nb
+            copied[b].record(copy_stream)
+        return d2h
+
+    def run_e2e(n_steps):
+        d2h = 0
+        for k in range(n_steps):
+            e2e_issue(k)
+            if k >= 1:
+                d2h = e2e_collect(k - 1)
+        d2h = e2e_collect(n_steps - 1)
+        copy_stream.synchronize()
         return d2h
 
     # -- warm-up (also checks the device status once)
@@ -586,23 +630,15 @@ def run_gpu(args):
     barrier()
     dev_s = sum(step_ms) / 1e3
 
-    # -- timed: end to end through the API from host buffers
-    e2e_ms, d2h_bytes = [], 0
-    for _ in range(max(1, args.warmup)):
-        step_e2e()
+    # -- timed: end to end through the API from host buffers (pipelined)
+    run_e2e(max(2, args.warmup))
     torch.cuda.synchronize()
     barrier()
-    for _ in range(args.steps):
-        flush_buf.fill_(1)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        e0.record(stream)
-        d2h_bytes = step_e2e()
-        e1.record(stream)
-        e1.synchronize()
-        e2e_ms.append(1e3 * (time.perf_counter() - t0))
+    t0 = time.perf_counter()
+    d2h_bytes = run_e2e(args.steps)
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
     barrier()
-    e2e_s = sum(e2e_ms) / 1e3
 
     learned_line = None
     batched = None
@@ -718,7 +754,10 @@ def run_gpu(args):
                    "path": "plain (no learned filter)"},
         "e2e": {"value": e2e_value, "unit": "events/s", "h2d_bytes_per_step": int(h2d_bytes),
                 "d2h_bytes_per_step": int(d2h_bytes),
-                "ms_per_step": e2e_s * 1e3 / args.steps},
+                "ms_per_step": e2e_s * 1e3 / args.steps,
+                "timing": "wall clock over all steps, host->device input copy, seeding, "
+                          "parameters and device->host result copy of every step; two steps "
+                          "in flight (copies of step k-1 overlap step k)"},
         "gpu_launches": len(seeding.KERNEL_NAMES) + n_ev,
         "kernel_ms_per_step": kernels,
         "wall_s_timed": wall,
