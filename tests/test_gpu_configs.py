@@ -1,0 +1,111 @@
+"""GPU seeding vs the oracle across configurations other than the default:
+several z bins, a wider neighbourhood (which sends every middle through the
+large-capacity kernel), one and eight seeds per middle, an offset beam spot,
+a higher pT threshold (fewer phi bins) and tighter impact / pT cuts.  Grids
+and seed sets bit-exact, parameters to 1e-5."""
+import numpy as np
+import pytest
+
+import oracle as O
+from traccc_gb300 import seeding, synth
+
+pytestmark = pytest.mark.gpu
+
+
+def _zbins(f):
+    f.cotThetaMax = 7.4
+
+
+def _scope2(f):
+    f.neighbor_scope[0] = 2
+    f.neighbor_scope[1] = 2
+
+
+def _zbins_scope2(f):
+    _zbins(f)
+    _scope2(f)
+
+
+def _seeds(n):
+    def mod(f):
+        f.maxSeedsPerSpM = n
+    return mod
+
+
+def _beam(f):
+    f.beamPos[0] = 0.5
+    f.beamPos[1] = -0.3
+
+
+def _minpt(f):
+    f.minPt = 0.9
+
+
+def _tight(f):
+    f.impactMax = 5.0
+    f.maxPtScattering = 5.0
+
+
+VARIANTS = {"zbins": _zbins, "scope2": _scope2, "zbins_scope2": _zbins_scope2,
+            "seeds1": _seeds(1), "seeds8": _seeds(8), "beam": _beam, "minpt": _minpt,
+            "tight": _tight}
+
+
+def _configs(mod, module):
+    f, g, fl, tp = module.default_configs()
+    mod(f)
+    if module is O:
+        O.lib().or_finder_config_setup(__import__("ctypes").byref(f))
+        g = O.GridConfig()
+        O.lib().or_grid_config_from_finder(__import__("ctypes").byref(g),
+                                           __import__("ctypes").byref(f))
+    else:
+        f.setup()
+        g = seeding.grid_config_from_finder(f)
+    return f, g, fl, tp
+
+
+@pytest.mark.parametrize("variant", list(VARIANTS))
+def test_config_variant_matches_oracle(variant):
+    import torch
+    ev = synth.workload_event("cfg1", 9)
+    mod = VARIANTS[variant]
+    f, g, fl, tp = _configs(mod, seeding)
+    of, og, ofl, otp = _configs(mod, O)
+    ax = seeding.get_axes(g)
+    if variant.startswith("zbins"):
+        assert ax.z_bins > 1
+    alg = seeding.TripletSeedingAlgorithm(f, g, fl)
+    sps = seeding.SpacepointCollection.from_numpy(ev)
+    out = alg(sps)
+    torch.cuda.synchronize()
+    assert alg.last_status() == seeding.OK
+    off, bsp = alg.grid(0, len(ev["global"]))
+    roff, rsp, _, _ = O.binning(ev, of, og, phi_mode=O.PHI_CR)
+    assert np.array_equal(off, roff)
+    assert np.array_equal(bsp, rsp)
+    got = out.to_numpy()
+    ref, _ = O.seeding(ev, of, og, ofl, phi_mode=O.PHI_CR)
+    assert len(ref) > 0
+    assert np.array_equal(got, ref)
+    if variant == "beam":
+        est = seeding.SeedParameterEstimationAlgorithm(tp)
+        params = est((0.0, 0.0, float(f.bFieldInZ)), seeding.MeasurementCollection.from_numpy(ev),
+                     sps, out).to_numpy()
+        refp = O.track_params(ev, ref, (0.0, 0.0, float(of.bFieldInZ)), otp)
+        assert np.array_equal(params["surface_link"], refp["surface_link"])
+        assert np.allclose(params["params"], refp["params"], rtol=1e-5, atol=1e-6)
+
+
+def test_zbins_dense_event():
+    """Several z bins on a 100k-spacepoint event (fast path with z segments)."""
+    import torch
+    ev = synth.workload_event("cfg2", 5)
+    f, g, fl, _ = _configs(_zbins, seeding)
+    of, og, ofl, _ = _configs(_zbins, O)
+    alg = seeding.TripletSeedingAlgorithm(f, g, fl)
+    out = alg(seeding.SpacepointCollection.from_numpy(ev))
+    torch.cuda.synchronize()
+    assert alg.last_status() == seeding.OK
+    ref, _ = O.seeding(ev, of, og, ofl, phi_mode=O.PHI_CR)
+    assert np.array_equal(out.to_numpy(), ref)
