@@ -22,7 +22,7 @@ estimation (one launch per event).
 
 Also in the JSON line (one GPU):
   learned : the same 20-event step with the learned doublet filter, trained
-            on the GPU by the library's kernels (200 events, cfg2 per-track
+            on the GPU by the library's kernels (200 events, pileup9k per-track
             statistics, U(500, 12000) tracks) and calibrated for 99.5 % seed
             recall on 20 held-out events; events/s, speed-up against the
             plain step, per-event recall, seeds outside the plain set,
@@ -33,7 +33,8 @@ Also in the JSON line (one GPU):
             to end), autotuner report
 
 ``--impl reference`` times the reference's CPU seeding path (the oracle port;
-the reference itself cannot be built here) with all host
+the reference itself cannot be built: its seeding path needs vecmem, detray,
+covfie and the ACTS logger, none of them vendored) with all host
 threads on the same workload and metric.
 
 Multi-GPU (``torchrun --nproc-per-node N``): replicas only -- every rank seeds
@@ -59,7 +60,7 @@ if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
 METRIC = "events/s seeding @100k SP/event, plain vs learned-pruned at >=99.5% seed recall"
-WORKLOAD = ("cfg2: 20 synthetic events (seeds 0-19), 9000 helices + 12% noise, "
+WORKLOAD = ("pileup9k: 20 synthetic events (seeds 0-19), 9000 helices + 12% noise, "
             "~88k spacepoints/event, reference default seeding config")
 N_EVENTS = 20
 L2_FLUSH_BYTES = 256 << 20
@@ -108,13 +109,13 @@ def job_throughput(events_per_rank_step, steps, world, seconds):
 
 def make_events(n):
     from traccc_gb300 import synth
-    return [synth.workload_event("cfg2", s) for s in range(n)]
+    return [synth.workload_event("pileup9k", s) for s in range(n)]
 
 
 BATCH_EVENTS = 64
 BATCH_SEED = 3
-BATCH_WORKLOAD = ("cfg3: 64 synthetic events (batch seed 3) with U(500, 12000) helices each "
-                  "+ 12% noise, cfg2 pT/eta/z0 statistics, one graph launch per batch")
+BATCH_WORKLOAD = ("uneven64: 64 synthetic events (batch seed 3) with U(500, 12000) helices each "
+                  "+ 12% noise, pileup9k pT/eta/z0 statistics, one graph launch per batch")
 
 
 def quantile(xs, q):
@@ -283,7 +284,7 @@ FILTER_CALIB_EVENTS = 20
 
 
 def train_filter(args):
-    """Learned doublet filter: 200 training events with cfg2's per-track
+    """Learned doublet filter: 200 training events with pileup9k's per-track
     statistics and U(500, 12000) tracks each (batch seed 10, so that the
     filter sees the densities of the uneven batch), labels from the plain
     seeder, trained with the library's kernels; thresholds and band
@@ -357,7 +358,7 @@ def cpu_baseline(events):
     dt, _ = cpu_run(sample, threads)
     return {"value": len(sample) / dt, "unit": "events/s", "cores": threads,
             "kind": "port",
-            "sample": f"{len(sample)} cfg2 events (seeds 0-{min(len(events), len(sample)) - 1}), "
+            "sample": f"{len(sample)} pileup9k events (seeds 0-{min(len(events), len(sample)) - 1}), "
                       f"one per thread on {threads} threads ({cpu_model()}), oracle with libm "
                       f"phi, seeding + params, {dt:.1f} s"}
 
@@ -368,7 +369,7 @@ def run_reference(args):
         return 0
     threads = cpu_threads()
     from traccc_gb300 import synth
-    warm = [synth.workload_event("cfg0", s) for s in range(threads)]
+    warm = [synth.workload_event("trk100", s) for s in range(threads)]
     events = make_events(min(threads, args.events))
     sample = [events[i % len(events)] for i in range(threads)]
     for _ in range(args.warmup):
@@ -389,8 +390,8 @@ def run_reference(args):
                    "l2": "n/a (CPU)"},
         "cpu_baseline": {"value": value, "unit": "events/s", "cores": threads,
                          "kind": "port",
-                         "sample": f"{len(sample)} cfg2 events per step on {threads} threads "
-                                   f"({cpu_model()}); warm-up steps on cfg0 events"},
+                         "sample": f"{len(sample)} pileup9k events per step on {threads} threads "
+                                   f"({cpu_model()}); warm-up steps on trk100 events"},
         "e2e": {"value": value, "unit": "events/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -690,7 +691,7 @@ def run_gpu(args):
             b_learn, outs_learn = run_batched(args, dev, stream, flush_buf, inputs, model)
             b_learn["recall"] = recall_report(pk, learned.seed_keys(outs_learn))
             b_learn["speedup_vs_plain_batched"] = b_learn["value"] / b_plain["value"]
-            b_learn["speedup_vs_plain_cfg2"] = (
+            b_learn["speedup_vs_plain_pileup9k"] = (
                 b_learn["value"] / job_throughput(n_ev, args.steps, 1, dev_s))
             batched["learned"] = b_learn
     clocks = sampler.stop()

@@ -1,6 +1,6 @@
 """CPU reference of the learned doublet filter's network (numpy).
 
-TEST INFRASTRUCTURE ONLY: the checker for the GPU forward and backward
+TEST INFRASTRUCTURE ONLY: the oracle of the GPU forward and backward
 kernels of the network (traccc_gb300/csrc/seedgb_learned.cu,
 seedgb_mlp.cuh).  The product never imports it.
 

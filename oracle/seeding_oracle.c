@@ -2,7 +2,7 @@
  * seeding_oracle.c -- CPU restatement of traccc's host triplet seeding and
  * track-parameter estimation.
  *
- * TEST INFRASTRUCTURE ONLY: the correctness checker for the GB300 path (and
+ * TEST INFRASTRUCTURE ONLY: the correctness oracle for the GB300 path (and
  * the timed CPU baseline of bench.py).  The product library never links or
  * calls this file.
  *

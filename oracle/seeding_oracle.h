@@ -2,7 +2,7 @@
  * seeding_oracle.h -- CPU restatement of traccc's host triplet seeding and
  * track-parameter estimation.
  *
- * TEST INFRASTRUCTURE ONLY.  This library is the correctness checker for the
+ * TEST INFRASTRUCTURE ONLY.  This library is the correctness oracle for the
  * GB300 seeding path.  Only the test-suite, the smoke check and the timed CPU
  * baseline of bench.py may load it; the product library never links or calls
  * it, and nothing in the product falls back to it.

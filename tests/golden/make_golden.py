@@ -31,7 +31,7 @@ COLUMNS = ("measurement_index_1", "measurement_index_2", "global", "z_variance",
 
 
 def edge_event():
-    ev = synth.workload_event("cfg1", 5)
+    ev = synth.workload_event("trk1000", 5)
     rng = np.random.default_rng(12345)
     n = len(ev["layer"])
     ev["z_variance"] = rng.uniform(0.0, 0.05, n).astype(np.float32)
@@ -59,10 +59,10 @@ def edge_event():
 
 
 def fixtures():
-    yield "cfg0_s0", synth.workload_event("cfg0", 0)
-    yield "cfg0_s1", synth.workload_event("cfg0", 1)
-    yield "cfg0_s2", synth.workload_event("cfg0", 2)
-    yield "cfg1_s0", synth.workload_event("cfg1", 0)
+    yield "trk100_s0", synth.workload_event("trk100", 0)
+    yield "trk100_s1", synth.workload_event("trk100", 1)
+    yield "trk100_s2", synth.workload_event("trk100", 2)
+    yield "trk1000_s0", synth.workload_event("trk1000", 0)
     yield "edge", edge_event()
 
 

@@ -39,7 +39,7 @@ def same_params(a, b, tol=1e-5):
 
 
 def test_fixtures_present():
-    assert {"cfg0_s0", "cfg1_s0", "edge"} <= set(NAMES)
+    assert {"trk100_s0", "trk1000_s0", "edge"} <= set(NAMES)
 
 
 @pytest.mark.parametrize("name", NAMES)

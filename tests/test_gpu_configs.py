@@ -68,7 +68,7 @@ def _configs(mod, module):
 @pytest.mark.parametrize("variant", list(VARIANTS))
 def test_config_variant_matches_oracle(variant):
     import torch
-    ev = synth.workload_event("cfg1", 9)
+    ev = synth.workload_event("trk1000", 9)
     mod = VARIANTS[variant]
     f, g, fl, tp = _configs(mod, seeding)
     of, og, ofl, otp = _configs(mod, O)
@@ -100,7 +100,7 @@ def test_config_variant_matches_oracle(variant):
 def test_zbins_dense_event():
     """Several z bins on a 100k-spacepoint event (fast path with z segments)."""
     import torch
-    ev = synth.workload_event("cfg2", 5)
+    ev = synth.workload_event("pileup9k", 5)
     f, g, fl, _ = _configs(_zbins, seeding)
     of, og, ofl, _ = _configs(_zbins, O)
     alg = seeding.TripletSeedingAlgorithm(f, g, fl)

@@ -29,7 +29,7 @@ def test_cpp_adapter(tmp_path):
                     os.path.join(ROOT, "tests", "cpp", "adapter_check.cpp"),
                     "-L", os.path.dirname(lib), "-lseedgb",
                     "-Xlinker", "-rpath=" + os.path.dirname(lib), "-o", exe], check=True)
-    ev = synth.workload_event("cfg1", 4)
+    ev = synth.workload_event("trk1000", 4)
     n = len(ev["global"])
     inp = tmp_path / "event.bin"
     with open(inp, "wb") as f:

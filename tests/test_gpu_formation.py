@@ -33,7 +33,7 @@ def test_formation_matches_oracle():
     import torch
 
     from traccc_gb300 import seeding
-    ev = synth.workload_event("cfg1", 6)
+    ev = synth.workload_event("trk1000", 6)
     n = len(ev["global"])
     rng = np.random.default_rng(1)
     link = np.asarray(ev["surface_link"], np.uint64).copy()
@@ -63,7 +63,7 @@ def test_formation_then_seeding():
     import torch
 
     from traccc_gb300 import seeding
-    ev = synth.workload_event("cfg1", 8)
+    ev = synth.workload_event("trk1000", 8)
     surf = _surfaces()
     meas = seeding.MeasurementCollection.from_numpy(ev)
     sps, k = seeding.form_spacepoints(surf, meas)

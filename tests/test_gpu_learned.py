@@ -113,7 +113,7 @@ def model_and_event():
     from traccc_gb300 import learned
     p, norm = _rand_model(7)
     model = learned.FilterModel(p, norm, learned.band_edges())
-    return model, synth.workload_event("cfg1", 11)
+    return model, synth.workload_event("trk1000", 11)
 
 
 def test_dump_matches_oracle(model_and_event):
@@ -193,7 +193,7 @@ def test_fallback_reseeds_plain(model_and_event):
     from traccc_gb300 import seeding
     model, ev = model_and_event
     plain, _ = O.seeding(ev)
-    evs = [ev, synth.workload_event("cfg1", 12)]
+    evs = [ev, synth.workload_event("trk1000", 12)]
     plain2, _ = O.seeding(evs[1])
     alg = seeding.TripletSeedingAlgorithm()
     sps = [seeding.SpacepointCollection.from_numpy(e) for e in evs]
@@ -224,8 +224,8 @@ def test_training_gains_over_untrained():
 
     from traccc_gb300 import learned, seeding
     alg = seeding.TripletSeedingAlgorithm()
-    train_ev = [synth.workload_event("cfg2", 500 + s, n_tracks=3000) for s in range(6)]
-    calib_ev = [synth.workload_event("cfg2", 600 + s, n_tracks=3000) for s in range(3)]
+    train_ev = [synth.workload_event("pileup9k", 500 + s, n_tracks=3000) for s in range(6)]
+    calib_ev = [synth.workload_event("pileup9k", 600 + s, n_tracks=3000) for s in range(3)]
     data = learned.collect(alg, train_ev, neg_keep=0.1)
     assert data.n_positive > 0 and len(data.labels) > data.n_positive
     params, norm, hist = learned.train(data, epochs=3)

@@ -41,7 +41,7 @@ def same_params(a, b, tol=PARAM_TOL):
     return ok
 
 
-@pytest.mark.parametrize("name,seed", [("cfg0", 0), ("cfg0", 1), ("cfg1", 0), ("cfg1", 3)])
+@pytest.mark.parametrize("name,seed", [("trk100", 0), ("trk100", 1), ("trk1000", 0), ("trk1000", 3)])
 def test_seeds_and_grid_match_oracle(name, seed):
     ev = synth.workload_event(name, seed)
     alg, sps, out, st = run_gpu(ev)
@@ -58,7 +58,7 @@ def test_seeds_and_grid_match_oracle(name, seed):
 
 def test_params_match_oracle():
     import torch
-    ev = synth.workload_event("cfg1", 5)
+    ev = synth.workload_event("trk1000", 5)
     f, g, fl, tp = seeding.default_configs()
     alg, sps, out, st = run_gpu(ev)
     est = seeding.SeedParameterEstimationAlgorithm(tp)
@@ -73,8 +73,8 @@ def test_params_match_oracle():
     assert ok.all(), np.nonzero(~ok)[0][:10]
 
 
-def test_cfg2_event_matches_oracle():
-    ev = synth.workload_event("cfg2", 0)
+def test_pileup9k_event_matches_oracle():
+    ev = synth.workload_event("pileup9k", 0)
     alg, sps, out, st = run_gpu(ev)
     assert st == seeding.OK
     got = out.to_numpy()
@@ -88,11 +88,11 @@ def test_cfg2_event_matches_oracle():
     assert c["n_valid"] == stats["n_valid"]
 
 
-@pytest.mark.parametrize("name,seed", [("cfg1", 7), ("cfg2", 3), ("cfg2", 11)])
+@pytest.mark.parametrize("name,seed", [("trk1000", 7), ("pileup9k", 3), ("pileup9k", 11)])
 def test_fast_paths_equal_exhaustive(name, seed):
     """The cot(theta) window and the fast helix pre-check give exactly the
     results of evaluating every pair with the reference arithmetic."""
-    ev = synth.workload_event(name, seed, n_tracks=12000 if name == "cfg2" else None)
+    ev = synth.workload_event(name, seed, n_tracks=12000 if name == "pileup9k" else None)
     _, _, a, sa = run_gpu(ev)
     _, _, b, sb = run_gpu(ev, exhaustive=True)
     assert sa == sb == seeding.OK

@@ -13,16 +13,16 @@ LAYERS = np.array([32., 72., 116., 172., 260., 360., 500., 600., 700., 820.])
 
 
 def test_generator_is_deterministic():
-    a = synth.workload_event("cfg1", 3)
-    b = synth.workload_event("cfg1", 3)
-    c = synth.workload_event("cfg1", 4)
+    a = synth.workload_event("trk1000", 3)
+    b = synth.workload_event("trk1000", 3)
+    c = synth.workload_event("trk1000", 4)
     for k in a:
         assert np.array_equal(a[k], b[k])
     assert not np.array_equal(a["global"][:100], c["global"][:100])
 
 
 def test_generator_geometry_and_sizes():
-    ev = synth.workload_event("cfg2", 0)
+    ev = synth.workload_event("pileup9k", 0)
     n = len(ev["layer"])
     assert 80_000 < n < 100_000  # ~100k spacepoints per event
     r = np.hypot(ev["global"][:, 0].astype(np.float64), ev["global"][:, 1])

@@ -35,7 +35,7 @@ def write_csv(path, header, rows):
 
 
 def test_csv_spacepoints_round_trip(tmp_path):
-    ev = synth.workload_event("cfg0", 3)
+    ev = synth.workload_event("trk100", 3)
     g = np.asarray(ev["global"], np.float32)
     n = len(g)
     hits = tmp_path / "event000000000-hits.csv"
@@ -93,7 +93,7 @@ def test_csv_errors(tmp_path):
 
 
 def test_oracle_formation_on_the_barrel():
-    ev = synth.workload_event("cfg1", 2)
+    ev = synth.workload_event("trk1000", 2)
     sp = O.form_spacepoints(barrel_surfaces(), ev["local_position"], ev["surface_link"])
     assert len(sp["global"]) == len(ev["global"])
     assert np.array_equal(sp["measurement_index_1"], np.arange(len(ev["global"]), dtype=np.uint32))

@@ -90,15 +90,15 @@ def test_c_network_matches_numpy_reference():
 
 
 @pytest.fixture(scope="module")
-def cfg1_event():
-    return synth.workload_event("cfg1", 3)
+def trk1000_event():
+    return synth.workload_event("trk1000", 3)
 
 
-def test_keep_all_is_plain_seeding(cfg1_event):
+def test_keep_all_is_plain_seeding(trk1000_event):
     p, norm = _model(5)
     f = O.doublet_filter(_model_dict(p, norm), (-np.inf, -np.inf))
-    seeds, st, d = O.seeding_ex(cfg1_event, filt=f, dump=True)
-    plain, st0 = O.seeding(cfg1_event)
+    seeds, st, d = O.seeding_ex(trk1000_event, filt=f, dump=True)
+    plain, st0 = O.seeding(trk1000_event)
     assert np.array_equal(seeds, plain)
     assert st["n_pruned_mb"] == 0 and st["n_pruned_mt"] == 0
     assert len(d) == st["n_scored_mb"] + st["n_scored_mt"] > 0
@@ -106,16 +106,16 @@ def test_keep_all_is_plain_seeding(cfg1_event):
     assert 0 < st["n_scored_mb"] <= st0["n_mb"] and 0 < st["n_scored_mt"] <= st0["n_mt"]
     # nothing kept: no seeds
     f2 = O.doublet_filter(_model_dict(p, norm), (np.inf, np.inf))
-    none, st2, _ = O.seeding_ex(cfg1_event, filt=f2)
+    none, st2, _ = O.seeding_ex(trk1000_event, filt=f2)
     assert len(none) == 0 and st2["n_pruned_mb"] == st2["n_scored_mb"]
 
 
-def test_dump_features(cfg1_event):
+def test_dump_features(trk1000_event):
     p, norm = _model(6)
     edges = (52.0, 94.0, 144.0, 216.0)
     f = O.doublet_filter(_model_dict(p, norm, edges), (-np.inf, -np.inf))
-    _, _, d = O.seeding_ex(cfg1_event, filt=f, dump=True)
-    g = cfg1_event["global"].astype(np.float32)
+    _, _, d = O.seeding_ex(trk1000_event, filt=f, dump=True)
+    g = trk1000_event["global"].astype(np.float32)
     r = np.sqrt(g[:, 0] * g[:, 0] + g[:, 1] * g[:, 1]).astype(np.float32)
     m, o = d["middle"], d["other"]
     F = d["feat"]
@@ -141,16 +141,16 @@ def test_dump_features(cfg1_event):
     assert np.median(np.abs(ref - d["logit"])) <= 1e-5 * (1 + np.median(np.abs(ref)))
 
 
-def test_pruning_is_monotone(cfg1_event):
+def test_pruning_is_monotone(trk1000_event):
     p, norm = _model(7)
-    _, _, d = O.seeding_ex(cfg1_event, filt=O.doublet_filter(_model_dict(p, norm), -np.inf),
+    _, _, d = O.seeding_ex(trk1000_event, filt=O.doublet_filter(_model_dict(p, norm), -np.inf),
                            dump=True)
-    plain, _ = O.seeding(cfg1_event)
+    plain, _ = O.seeding(trk1000_event)
     pk = set(zip(plain["bottom"], plain["middle"], plain["top"]))
     fracs, recalls = [], []
     for q in (0.1, 0.3, 0.5):
         th = np.quantile(d["logit"], q)
-        s, st, _ = O.seeding_ex(cfg1_event, filt=O.doublet_filter(_model_dict(p, norm), th))
+        s, st, _ = O.seeding_ex(trk1000_event, filt=O.doublet_filter(_model_dict(p, norm), th))
         fracs.append((st["n_pruned_mb"] + st["n_pruned_mt"]) /
                      (st["n_scored_mb"] + st["n_scored_mt"]))
         recalls.append(len(pk & set(zip(s["bottom"], s["middle"], s["top"]))) / len(pk))

@@ -43,7 +43,7 @@ def _handle_grid(f, g, fl, ev):
 
 def test_noalloc_binning_equals_seeding_grid_two_calls():
     f, g, fl, _ = seeding.default_configs()
-    events = [synth.workload_event("cfg1", 21), synth.workload_event("cfg2", 22, 5000)]
+    events = [synth.workload_event("trk1000", 21), synth.workload_event("pileup9k", 22, 5000)]
     # two calls in a row on the shared scratch, then the reference grids
     got = [_noalloc_grid(f, g, ev) for ev in events]
     for ev, (off, bsp) in zip(events, got):

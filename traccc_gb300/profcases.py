@@ -23,7 +23,7 @@ import sys
 
 def _events(n, seed0=0):
     from traccc_gb300 import synth
-    return [synth.workload_event("cfg2", seed0 + s) for s in range(n)]
+    return [synth.workload_event("pileup9k", seed0 + s) for s in range(n)]
 
 
 def _range(torch, fn):

@@ -3,10 +3,10 @@
 The generator itself is C (``csrc/synth_events.c``); this module wraps it and
 names the benchmark workloads:
 
-* ``cfg0``: 100 tracks, pT U(1, 10) GeV, 5 % noise           (~1k spacepoints)
-* ``cfg1``: 1000 tracks, pT log-U(0.5, 20) GeV, 10 % noise   (~11k)
-* ``cfg2``: 9000 tracks, pT exp(mean 0.6 GeV) >= 0.1 GeV, 12 % noise (~100k)
-* ``cfg3``: batch events as cfg2 with U(500, 12000) tracks per event
+* ``trk100``: 100 tracks, pT U(1, 10) GeV, 5 % noise           (~1k spacepoints)
+* ``trk1000``: 1000 tracks, pT log-U(0.5, 20) GeV, 10 % noise   (~11k)
+* ``pileup9k``: 9000 tracks, pT exp(mean 0.6 GeV) >= 0.1 GeV, 12 % noise (~100k)
+* ``uneven64``: batch events as pileup9k with U(500, 12000) tracks per event
 
 All share the detector (10 barrel layers, |z| <= 1000 mm), a 2 T field along
 z, |eta| < 1.5, z0 ~ N(0, 50 mm), d0 ~ N(0, 0.02 mm), smearing 15 um (r*phi)
@@ -39,9 +39,9 @@ class SynthOutput(C.Structure):
 
 
 WORKLOADS = {
-    "cfg0": dict(n_tracks=100, pt_dist=0, pt_a=1.0, pt_b=10.0, noise_frac=0.05),
-    "cfg1": dict(n_tracks=1000, pt_dist=1, pt_a=0.5, pt_b=20.0, noise_frac=0.10),
-    "cfg2": dict(n_tracks=9000, pt_dist=2, pt_a=0.6, pt_b=0.1, noise_frac=0.12),
+    "trk100": dict(n_tracks=100, pt_dist=0, pt_a=1.0, pt_b=10.0, noise_frac=0.05),
+    "trk1000": dict(n_tracks=1000, pt_dist=1, pt_a=0.5, pt_b=20.0, noise_frac=0.10),
+    "pileup9k": dict(n_tracks=9000, pt_dist=2, pt_a=0.6, pt_b=0.1, noise_frac=0.12),
 }
 
 _lib = None
@@ -89,7 +89,7 @@ def make_event(n_tracks, pt_dist, pt_a, pt_b, noise_frac, seed, eta_max=1.5,
 
 
 def workload_event(name: str, seed: int, n_tracks: int | None = None):
-    """An event of a named workload (cfg0, cfg1, cfg2) with the given seed."""
+    """An event of a named workload (trk100, trk1000, pileup9k) with the given seed."""
     kw = dict(WORKLOADS[name])
     if n_tracks is not None:
         kw["n_tracks"] = n_tracks
@@ -97,8 +97,8 @@ def workload_event(name: str, seed: int, n_tracks: int | None = None):
 
 
 def batch_events(n_events: int, seed: int, lo: int = 500, hi: int = 12000):
-    """The uneven batch: cfg2 statistics with U(lo, hi) tracks per event."""
+    """The uneven batch: pileup9k statistics with U(lo, hi) tracks per event."""
     rng = np.random.default_rng(seed)
     counts = rng.integers(lo, hi + 1, size=n_events)
-    return [workload_event("cfg2", seed * 100003 + i, int(c))
+    return [workload_event("pileup9k", seed * 100003 + i, int(c))
             for i, c in enumerate(counts)]
