@@ -406,6 +406,14 @@ typedef struct {
     float edges[15];    /* ascending radial band edges (mm) */
     uint32_t prune_bottom, prune_top;
     float band[2];
+    /* Optional per-event-size classes (n_size_classes <= 8; 0: threshold and
+     * band above apply to every event).  An event with n spacepoints belongs
+     * to the first class k with n <= size_class_max[k] (ascending), else to
+     * the last; its thresholds and band are that class's. */
+    uint32_t n_size_classes;
+    uint32_t size_class_max[8];
+    float size_class_threshold[8][2];
+    float size_class_band[8][2];
 } seedgb_doublet_filter;
 
 /* Install (copy) a filter on the handle, or remove it with f == NULL. */

@@ -243,3 +243,37 @@ def test_training_gains_over_untrained():
     # doublets than an untrained one at the same recall (~0.11 vs ~0.015)
     assert f1 > 0.06 and f1 > 3 * f0 + 0.02, (f1, f0)
     torch.cuda.synchronize()
+
+
+def test_size_classes_apply_per_event(model_and_event):
+    """Thresholds and band follow each event's size class: a small event in a
+    class that prunes every top has no seeds, a large one in a keep-all class
+    gets the plain seeds, and a class band nothing reaches re-seeds plain."""
+    import dataclasses
+
+    from traccc_gb300 import seeding
+    model, _ = model_and_event
+    small = synth.workload_event("trk1000", 21)
+    large = synth.workload_event("trk1000", 22, n_tracks=3000)
+    assert len(small["global"]) < 20000 < len(large["global"])
+    plain_l, _ = O.seeding(large)
+    plain_s, _ = O.seeding(small)
+    sps = [seeding.SpacepointCollection.from_numpy(e) for e in (small, large)]
+    alg = seeding.TripletSeedingAlgorithm()
+    m = dataclasses.replace(model, classes=[(20000, (-np.inf, np.inf), (0.0, 1.0)),
+                                            (1 << 31, (-np.inf, -np.inf), (0.0, 1.0))])
+    alg.set_filter(m.struct())
+    outs = alg.run_batch(sps)
+    assert alg.last_status() == seeding.OK
+    per, fb, _ = alg.filter_stats(2)
+    assert len(outs[0].to_numpy()) == 0 and per[0, 3] == per[0, 2] > 0
+    assert np.array_equal(outs[1].to_numpy(), plain_l) and per[1, 3] == 0
+    # the small class's band excludes "everything pruned": it falls back
+    m2 = dataclasses.replace(model, classes=[(20000, (-np.inf, np.inf), (0.0, 0.5)),
+                                             (1 << 31, (-np.inf, -np.inf), (0.0, 1.0))])
+    alg.set_filter(m2.struct())
+    outs = alg.run_batch(sps)
+    _, fb, _ = alg.filter_stats(2)
+    assert list(fb) == [True, False]
+    assert np.array_equal(outs[0].to_numpy(), plain_s)
+    assert np.array_equal(outs[1].to_numpy(), plain_l)

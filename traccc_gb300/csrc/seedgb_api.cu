@@ -130,6 +130,7 @@ DevConfig make_dev_config(const seedgb_seedfinder_config& f,
     d.mlp = nullptr;
     d.band_lo = 0.f;
     d.band_hi = 1.f;
+    d.mlp_n_classes = 0;
     return d;
 }
 
@@ -597,6 +598,18 @@ seedgb_status seedgb_seeding_set_filter(seedgb_seeding* h, const seedgb_doublet_
     for (uint32_t i = 0; i < 15; ++i) h->dc.mlp_edges[i] = i < f->n_edges ? f->edges[i] : 0.f;
     h->dc.mlp_prune_bottom = f->prune_bottom;
     h->dc.mlp_prune_top = f->prune_top;
+    if (f->n_size_classes > 8) return SEEDGB_INVALID_ARGUMENT;
+    h->dc.mlp_n_classes = f->n_size_classes;
+    for (uint32_t k = 0; k < 8; ++k) {
+        const bool on = k < f->n_size_classes;
+        if (on && k > 0 && !(f->size_class_max[k - 1] <= f->size_class_max[k]))
+            return SEEDGB_INVALID_ARGUMENT;
+        h->dc.mlp_class_max[k] = on ? f->size_class_max[k] : 0u;
+        for (int r = 0; r < 2; ++r) {
+            h->dc.mlp_class_thr[k][r] = on ? f->size_class_threshold[k][r] : 0.f;
+            h->dc.mlp_class_band[k][r] = on ? f->size_class_band[k][r] : 0.f;
+        }
+    }
     return SEEDGB_OK;
 }
 

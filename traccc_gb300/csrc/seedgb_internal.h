@@ -92,6 +92,11 @@ struct DevConfig {
     float mlp_edges[15];        // radial band edges of the layer-pair feature
     uint32_t mlp_n_edges;
     uint32_t mlp_prune_bottom, mlp_prune_top;
+    // per-event-size classes of thresholds and band (0 classes: the above)
+    uint32_t mlp_n_classes;
+    uint32_t mlp_class_max[8];
+    float mlp_class_thr[8][2];
+    float mlp_class_band[8][2];
 };
 
 // One event of a batch, as the kernels see it.

@@ -740,6 +740,19 @@ static_assert(sizeof(DoubletRec) == 48, "doublet record layout");
 // the network runs on the tensor cores (two 16-doublet tiles), and each
 // lane gets its doublet's logit back through lg.  Records the doublets when
 // a dump buffer is set.  xs: 128 words of warp scratch, lg: 32 floats.
+// The learned filter's threshold of a role and band for event `ev`: its
+// size class when classes are set, else the filter-wide values.
+__device__ __forceinline__ uint32_t filter_class(const DevConfig& c, const Arena& a, uint32_t ev) {
+    const uint32_t n_sp = a.events[ev].n_sp;
+    uint32_t k = 0;
+    while (k + 1 < c.mlp_n_classes && n_sp > c.mlp_class_max[k]) ++k;
+    return k;
+}
+__device__ __forceinline__ float filter_threshold(const DevConfig& c, const Arena& a, uint32_t ev,
+                                                  int role) {
+    return c.mlp_n_classes ? c.mlp_class_thr[filter_class(c, a, ev)][role] : c.mlp_thr[role];
+}
+
 // Records one chunk of scored doublets (cold path, kept out of line).
 __device__ __noinline__ void dump_chunk(unsigned long long* count, DoubletRec* dump,
                                         unsigned long long cap, bool valid, uint32_t mid_idx,
@@ -804,7 +817,7 @@ __device__ __noinline__ uint32_t filter_bottoms(const DevConfig& c, const Arena&
     mlp_load_regs(*c.mlp, lane, R);
     const bool prune = c.mlp_prune_bottom != 0;
     const float cosPhiM = M.x / M.w, sinPhiM = M.y / M.w;
-    const float thr = c.mlp_thr[0];
+    const float thr = filter_threshold(c, a, ev, 0);
     const float2 zero2 = make_float2(0.f, 0.f);
     const uint32_t mid_idx = a.dump ? a.g_idx[gm] : 0u;
     uint32_t w = 0;
@@ -975,7 +988,7 @@ __device__ MiddleResult process_middle(const DevConfig& c, const Arena& a,
         uint32_t* xs = ws.bstart;
         float* lg = reinterpret_cast<float*>(ws.bstart + 128);
         const bool prune = c.mlp_prune_top != 0;
-        const float thr = c.mlp_thr[1];
+        const float thr = filter_threshold(c, a, ev, 1);
         const uint32_t mid_idx = a.dump ? a.g_idx[gm] : 0u;
         uint32_t w = 0;
         for (uint32_t base = 0; base < n_mt; base += 32) {
@@ -1653,7 +1666,13 @@ __global__ void k_filter_mark(DevConfig c, Arena a) {
     uint8_t mode = 0;
     if (scored > 0) {
         const float frac = static_cast<float>(pruned) / static_cast<float>(scored);
-        mode = (frac < c.band_lo || frac > c.band_hi) ? 1 : 0;
+        float lo = c.band_lo, hi = c.band_hi;
+        if (c.mlp_n_classes) {
+            const uint32_t k = filter_class(c, a, e);
+            lo = c.mlp_class_band[k][0];
+            hi = c.mlp_class_band[k][1];
+        }
+        mode = (frac < lo || frac > hi) ? 1 : 0;
     }
     a.ev_mode[e] = mode;
     if (mode) atomicAdd(&a.counters[kFallbackEvents], 1ull);

@@ -56,9 +56,13 @@ class FilterModel:
     # triplet search of every middle-bottom doublet
     prune_bottom: bool = False
     prune_top: bool = True
+    # per-event-size classes: [(max spacepoints, (thr bottom, thr top),
+    # (band lo, band hi)), ...] ascending, or None
+    classes: list = None
 
     def struct(self, threshold=None, band=None, prune=None) -> seeding.DoubletFilter:
-        """The C struct, optionally with other thresholds / band / pruning."""
+        """The C struct, optionally with other thresholds / band / pruning
+        (an explicit threshold or band replaces the size classes)."""
         p = np.asarray(self.params, np.float32)
         f = seeding.DoubletFilter()
         f.mu[:] = self.norm[:8].tolist()
@@ -81,21 +85,33 @@ class FilterModel:
         b = self.band if band is None else band
         f.band[0] = float(b[0])
         f.band[1] = float(b[1])
+        if self.classes and threshold is None and band is None:
+            f.n_size_classes = len(self.classes)
+            for k, (mx, th_k, band_k) in enumerate(self.classes):
+                f.size_class_max[k] = int(min(mx, 0xFFFFFFFF))
+                f.size_class_threshold[k][0] = float(np.float32(th_k[0]))
+                f.size_class_threshold[k][1] = float(np.float32(th_k[1]))
+                f.size_class_band[k][0] = float(band_k[0])
+                f.size_class_band[k][1] = float(band_k[1])
         return f
 
     def save(self, path):
+        cl = np.asarray([[mx, t[0], t[1], b[0], b[1]] for mx, t, b in (self.classes or [])],
+                        np.float64).reshape(-1, 5)
         np.savez(path, params=self.params, norm=self.norm, edges=self.edges,
                  threshold=np.asarray(self.threshold, np.float32),
                  band=np.asarray(self.band, np.float32),
-                 prune=np.asarray([self.prune_bottom, self.prune_top], np.uint8))
+                 prune=np.asarray([self.prune_bottom, self.prune_top], np.uint8), classes=cl)
 
     @classmethod
     def load(cls, path):
         with np.load(path) as z:
+            cl = [(int(r[0]), (float(r[1]), float(r[2])), (float(r[3]), float(r[4])))
+                  for r in z["classes"]] if "classes" in z.files else []
             return cls(z["params"].astype(np.float32), z["norm"].astype(np.float32),
                        z["edges"].astype(np.float32), tuple(float(v) for v in z["threshold"]),
                        tuple(float(v) for v in z["band"]), bool(z["prune"][0]),
-                       bool(z["prune"][1]))
+                       bool(z["prune"][1]), cl or None)
 
 
 def init_params(seed=0) -> np.ndarray:
@@ -371,9 +387,36 @@ def calibrate(alg, model: FilterModel, events, target=0.995, margin=0.05,
     return model, report
 
 
+def calibrate_classes(alg, model: FilterModel, events, class_max, target=0.995, margin=0.05,
+                      log=None, **kw):
+    """calibrate() separately for the held-out events of each size class
+    (class k: events with <= class_max[k] spacepoints, the last class takes
+    the rest).  Returns (model with size classes, report)."""
+    sizes = np.asarray([len(e["global"]) for e in events])
+    bounds = list(class_max)
+    classes, reports = [], []
+    lo = -1
+    for k, mx in enumerate(bounds):
+        last = k == len(bounds) - 1
+        sel = [e for e, n in zip(events, sizes) if n > lo and (last or n <= mx)]
+        if not sel:
+            raise RuntimeError(f"no calibration event in size class {k}")
+        m, rep = calibrate(alg, model, sel, target=target, margin=margin, log=log, **kw)
+        classes.append((int(mx), tuple(m.threshold), tuple(m.band)))
+        rep["events"] = len(sel)
+        rep.pop("candidates", None)
+        reports.append(rep)
+        lo = mx
+    out = dataclasses.replace(model, classes=classes, threshold=classes[-1][1],
+                              band=classes[-1][2])
+    return out, {"classes": reports}
+
+
 def build_filter(alg, train_events, calib_events, epochs=3, neg_keep=0.05, target=0.995,
-                 seed=0, log=None, quantiles=None, label="seed", criterion="total"):
-    """collect -> train -> calibrate.  Returns (model, report)."""
+                 seed=0, log=None, quantiles=None, label="seed", criterion="total",
+                 class_max=None):
+    """collect -> train -> calibrate (per size class when class_max is
+    given).  Returns (model, report)."""
     import torch
     t0 = time.perf_counter()
     data = collect(alg, train_events, neg_keep=neg_keep, seed=seed, label=label)
@@ -384,8 +427,12 @@ def build_filter(alg, train_events, calib_events, epochs=3, neg_keep=0.05, targe
     t2 = time.perf_counter()
     model = FilterModel(params, norm, band_edges())
     kw = {} if quantiles is None else {"quantiles": quantiles}
-    model, rep = calibrate(alg, model, calib_events, target=target, log=log,
-                           criterion=criterion, **kw)
+    if class_max:
+        model, rep = calibrate_classes(alg, model, calib_events, class_max, target=target,
+                                       log=log, criterion=criterion, **kw)
+    else:
+        model, rep = calibrate(alg, model, calib_events, target=target, log=log,
+                               criterion=criterion, **kw)
     t3 = time.perf_counter()
     rep.update({"label": label, "criterion": criterion,
                 "train_events": len(train_events), "calib_events": len(calib_events),

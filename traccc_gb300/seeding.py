@@ -121,7 +121,10 @@ class DoubletFilter(C.Structure):
                 ("w3", C.c_float * 32), ("b3", C.c_float),
                 ("threshold", C.c_float * 2), ("n_edges", C.c_uint32),
                 ("edges", C.c_float * 15), ("prune_bottom", C.c_uint32),
-                ("prune_top", C.c_uint32), ("band", C.c_float * 2)]
+                ("prune_top", C.c_uint32), ("band", C.c_float * 2),
+                ("n_size_classes", C.c_uint32), ("size_class_max", C.c_uint32 * 8),
+                ("size_class_threshold", (C.c_float * 2) * 8),
+                ("size_class_band", (C.c_float * 2) * 8)]
 
 
 class _ParamsBuffer(C.Structure):
