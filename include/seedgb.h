@@ -24,9 +24,15 @@
  *
  * Semantics: all work is enqueued on the caller's stream and the calls return
  * before it finishes (as the reference's device algorithms do); no call of the
- * run functions blocks on the device.  Errors are status codes, never
- * exceptions.  A handle is not thread-safe: use one handle per host thread /
- * stream, as the reference uses one algorithm object per thread.
+ * run functions blocks on the device, except that growing a handle's work
+ * space (a batch larger than anything reserved before) waits for the device.
+ * set_tune, set_filter and the dump setters wait for the device before they
+ * change what kernels in flight read (set_option applies to the next run);
+ * status, counter and grid queries synchronise the given stream;
+ * seedgb_form_spacepoints returns after its stream has finished the call.
+ * Errors are status codes, never exceptions.  A handle is not thread-safe:
+ * use one handle per host thread / stream, as the reference uses one
+ * algorithm object per thread.
  */
 #ifndef SEEDGB_H
 #define SEEDGB_H
@@ -292,7 +298,9 @@ typedef struct {
  * Spacepoints are written in measurement order (the host algorithm's order;
  * the reference's device version appends in no fixed order).  All pointers
  * are device memory except `surfaces_host`, copied on the stream; outputs
- * have room for meas->size spacepoints; *n_out (device) receives the count. */
+ * have room for meas->size spacepoints; *n_out (device) receives the count.
+ * Returns after the stream has finished the call (the surface table is then
+ * free to change); calls from one host thread share a scratch area. */
 seedgb_status seedgb_form_spacepoints(const seedgb_surface* surfaces_host, uint32_t n_surfaces,
                                       const seedgb_measurement_view* meas,
                                       const uint8_t* dimensions,

@@ -15,7 +15,7 @@ import pytest
 import oracle as O
 from traccc_gb300 import seeding, synth
 
-RADII = (32.0, 72.0, 116.0, 172.0, 260.0, 360.0, 500.0, 600.0, 700.0, 820.0)
+RADII = synth.LAYER_RADII
 
 
 def barrel_surfaces():

@@ -31,11 +31,10 @@ import time
 
 import numpy as np
 
-from . import seeding
+from . import seeding, synth
 
 N_IN, N_H = 8, 32
-# synthetic barrel detector (traccc_gb300.synth): layer radii in mm
-LAYER_RADII = (32.0, 72.0, 116.0, 172.0, 260.0, 360.0, 500.0, 600.0, 700.0, 820.0)
+LAYER_RADII = synth.LAYER_RADII
 
 
 def band_edges(layer_radii=LAYER_RADII):

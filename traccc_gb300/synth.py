@@ -38,6 +38,10 @@ class SynthOutput(C.Structure):
                 ("surface_link", C.c_void_p), ("capacity", C.c_uint32)]
 
 
+# layer radii (mm) of the synthetic barrel, as generated by synth_events.c;
+# measurement surface_link = layer index + 1
+LAYER_RADII = (32.0, 72.0, 116.0, 172.0, 260.0, 360.0, 500.0, 600.0, 700.0, 820.0)
+
 WORKLOADS = {
     "trk100": dict(n_tracks=100, pt_dist=0, pt_a=1.0, pt_b=10.0, noise_frac=0.05),
     "trk1000": dict(n_tracks=1000, pt_dist=1, pt_a=0.5, pt_b=20.0, noise_frac=0.10),
