@@ -505,7 +505,7 @@ seedgb_status seedgb_mlp_grad(const float* params, const float* norm, const floa
     if (err == cudaSuccess) err = cudaMemsetAsync(loss, 0, sizeof(float), s);
     if (err != cudaSuccess) return SEEDGB_CUDA_ERROR;
     if (n == 0) return SEEDGB_OK;
-    static int attr_dev = -1;
+    static thread_local int attr_dev = -1;  // the attribute is per context
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return SEEDGB_CUDA_ERROR;
     if (attr_dev != dev) {
