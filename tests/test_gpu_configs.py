@@ -1,8 +1,10 @@
 """GPU seeding vs the oracle across configurations other than the default:
-several z bins, a wider neighbourhood (which sends every middle through the
-large-capacity kernel), one and eight seeds per middle, an offset beam spot,
-a higher pT threshold (fewer phi bins) and tighter impact / pT cuts.  Grids
-and seed sets bit-exact, parameters to 1e-5."""
+several z bins, a wider neighbourhood (with several z bins: up to 25 grid
+bins around a middle, more than the fast kernel stages, so most middles go
+through the large-capacity kernel), one and eight seeds per middle, an offset beam spot,
+a higher pT threshold (fewer phi bins) and tighter impact / pT cuts, and
+nonzero spacepoint variances on both seeding kernels.  Grids and seed sets
+bit-exact, parameters to 1e-5."""
 import numpy as np
 import pytest
 
@@ -95,6 +97,30 @@ def test_config_variant_matches_oracle(variant):
         refp = O.track_params(ev, ref, (0.0, 0.0, float(of.bFieldInZ)), otp)
         assert np.array_equal(params["surface_link"], refp["surface_link"])
         assert np.allclose(params["params"], refp["params"], rtol=1e-5, atol=1e-6)
+
+
+@pytest.mark.parametrize("variant", ["default", "zbins_scope2"])
+def test_variance_event_matches_oracle(variant):
+    """Nonzero spacepoint variances (the kernels' variance bodies): the
+    default config through the fast kernel, several z bins with scope 2
+    mostly through the large-capacity kernel."""
+    import torch
+    ev = synth.workload_event("trk1000", 9)
+    rng = np.random.default_rng(9)
+    ev["z_variance"] = rng.uniform(0.0, 0.05, len(ev["layer"])).astype(np.float32)
+    ev["radius_variance"] = rng.uniform(0.0, 0.01, len(ev["layer"])).astype(np.float32)
+    mod = VARIANTS.get(variant, lambda f: None)
+    f, g, fl, _ = _configs(mod, seeding)
+    of, og, ofl, _ = _configs(mod, O)
+    alg = seeding.TripletSeedingAlgorithm(f, g, fl)
+    out = alg(seeding.SpacepointCollection.from_numpy(ev))
+    torch.cuda.synchronize()
+    assert alg.last_status() == seeding.OK
+    assert (alg.counters()["n_overflow_middles"] > 0) == (variant == "zbins_scope2")
+    got = out.to_numpy()
+    ref, _ = O.seeding(ev, of, og, ofl, phi_mode=O.PHI_CR)
+    assert len(ref) > 0
+    assert np.array_equal(got, ref)
 
 
 def test_zbins_dense_event():
