@@ -287,7 +287,7 @@ FILTER_CALIB_EVENTS = 48
 FILTER_SIZE_CLASSES = (25000, 50000, 80000, 1 << 31)
 # calibrated with a margin above the 99.5 % recall target, for events the
 # calibration did not see
-FILTER_CALIB_TARGET = 0.996
+FILTER_CALIB_TARGET = 0.997
 
 
 def train_filter(args):
@@ -296,7 +296,7 @@ def train_filter(args):
     filter sees the densities of the uneven batch), labels from the plain
     seeder, trained with the library's kernels; thresholds and band
     calibrated per event-size class on 48 held-out events of the same kind
-    (batch seed 20) for >= 99.6 % seed recall over each class's events (a
+    (batch seed 20) for >= 99.7 % seed recall over each class's events (a
     margin above the 99.5 % target for unseen events)."""
     from traccc_gb300 import learned, seeding, synth
     t0 = time.perf_counter()

@@ -466,7 +466,10 @@ seedgb_status seedgb_mlp_forward(const float* params, const float* norm,
                                  void* stream);
 /* grad (device, num_params floats) and loss (device, 1 float) are
  * overwritten with the gradient and value of the mean weighted logistic loss
- * -(p y log s(z) + (1 - y) log(1 - s(z))), p = pos_weight. */
+ * -(p y log s(z) + (1 - y) log(1 - s(z))), p = pos_weight.  The sums run in a
+ * fixed order (no atomics): the same inputs give bit-identical results on
+ * the same device.  Keeps a per-thread device scratch of one gradient row per
+ * SM, allocated on the first call. */
 seedgb_status seedgb_mlp_grad(const float* params, const float* norm,
                               const float* features, const float* labels, uint32_t n,
                               float pos_weight, float* grad, float* loss, void* stream);

@@ -11,6 +11,8 @@
   the tolerance of its threshold (counted, expected zero or a few).
 * Fallback: an event whose pruned fraction leaves the band is re-seeded
   without the filter in the same launch sequence (seeds = plain seeds).
+* Determinism: gradients are bit-identical across calls, and a whole
+  collect + train run is reproducible bit for bit.
 * Training: the kernels lower the loss, and the trained network prunes far
   more doublets than an untrained one at the same seed recall (the gain of
   the network over the method without it).
@@ -88,6 +90,45 @@ def test_gradient_matches_reference():
     # the same gradient is the exact one up to the bf16 operands
     _, g_exact = R.loss_and_grad(p, norm, x, y, 4.0, exact=True)
     assert np.linalg.norm(g - g_exact) < 0.05 * np.linalg.norm(g_exact)
+
+
+def test_gradient_is_deterministic():
+    """The gradient sums run in a fixed order: repeated calls over many CTAs
+    give bit-identical gradients and losses."""
+    import torch
+
+    from traccc_gb300 import seeding
+    p, norm = _rand_model(8)
+    x = torch.from_numpy(_features(300_001, 9)).cuda()
+    y = torch.from_numpy((np.random.default_rng(10).random(len(x)) < 0.1)
+                         .astype(np.float32)).cuda()
+    P, N = torch.from_numpy(p).cuda(), torch.from_numpy(norm).cuda()
+    res = []
+    for _ in range(3):
+        G = torch.full_like(P, float("nan"))
+        L = torch.full((1,), float("nan"), dtype=torch.float32, device="cuda")
+        seeding.mlp_grad(P, N, x, y, 3.0, G, L)
+        res.append((G.clone(), L.clone()))
+    for G, L in res[1:]:
+        assert torch.equal(G, res[0][0]) and torch.equal(L, res[0][1])
+    assert torch.isfinite(res[0][0]).all()
+
+
+def test_training_is_reproducible():
+    """collect + train twice on the same events give the same network bit
+    for bit (dump records put in a fixed order, gradients summed in a fixed
+    order)."""
+    from traccc_gb300 import learned, seeding
+    alg = seeding.TripletSeedingAlgorithm()
+    events = [synth.workload_event("trk1000", 40 + s, n_tracks=2000) for s in range(3)]
+    runs = []
+    for _ in range(2):
+        data = learned.collect(alg, events, neg_keep=0.2, batch=2)
+        params, norm, hist = learned.train(data, epochs=2, batch=4096)
+        runs.append((params, norm, hist))
+    assert np.array_equal(runs[0][0], runs[1][0])
+    assert np.array_equal(runs[0][1], runs[1][1])
+    assert runs[0][2] == runs[1][2]
 
 
 def test_adam_step():

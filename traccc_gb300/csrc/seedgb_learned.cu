@@ -28,6 +28,7 @@ namespace seedgb {
 namespace {
 
 constexpr int kTrainWarps = 8;
+constexpr int kGradRow = kMlpParams + 3;  // gradient, loss, padding to 16 bytes
 
 // Packs the bf16 B fragments of the forward pass from the fp32 parameters.
 __device__ void build_frag(MlpFrag& f, const float* __restrict__ P, const float* __restrict__ norm) {
@@ -118,8 +119,9 @@ struct TrainSmem {
     MlpFrag f;
     uint2 w2t[2][4][32];  // B fragments of W2^T (bf16)
     float w3r[kMlpH];     // bf16-rounded w3
-    float grad[kMlpParams + 3];
-    float loss;
+    // per-warp gradient and loss (index kMlpParams); every entry has exactly
+    // one owning lane, so the CTA sum runs in a fixed order
+    float wg[kTrainWarps][kGradRow];
     struct Warp {
         uint32_t xs[16 * 4];         // packed inputs, row-major (16 x 8 bf16)
         __nv_bfloat16 h1[16][kMlpH];  // [sample][feature]
@@ -142,7 +144,7 @@ __device__ __forceinline__ float softplus(float x) {
 __global__ void __launch_bounds__(kTrainWarps * 32)
 k_mlp_grad(const float* __restrict__ P, const float* __restrict__ norm,
            const float* __restrict__ feat, const float* __restrict__ label, uint32_t n,
-           float pos_weight, float* __restrict__ grad, float* __restrict__ loss) {
+           float pos_weight, float* __restrict__ part) {
     extern __shared__ __align__(16) uint8_t smem_raw[];
     TrainSmem& S = *reinterpret_cast<TrainSmem*>(smem_raw);
     build_frag(S.f, P, norm);
@@ -155,8 +157,6 @@ k_mlp_grad(const float* __restrict__ P, const float* __restrict__ norm,
             pack_bf16(P[kOffW2 + j * kMlpH + k0 + 8], P[kOffW2 + j * kMlpH + k0 + 9]));
     }
     for (uint32_t i = threadIdx.x; i < kMlpH; i += blockDim.x) S.w3r[i] = bf16_round(P[kOffW3 + i]);
-    for (uint32_t i = threadIdx.x; i < kMlpParams; i += blockDim.x) S.grad[i] = 0.f;
-    if (threadIdx.x == 0) S.loss = 0.f;
     __syncthreads();
 
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -344,20 +344,23 @@ k_mlp_grad(const float* __restrict__ P, const float* __restrict__ norm,
         __syncwarp();
     }
 
-    // ---- reduce: lanes -> shared (CTA) -> global
+    // ---- reduce in a fixed order: lanes -> the warp's slice (one owner per
+    //      entry) -> the CTA's row of `part` (warps in order); k_grad_sum adds
+    //      the rows in CTA order, so a training run is reproducible
+    float* wg = S.wg[warp];
 #pragma unroll
     for (int nt = 0; nt < 4; ++nt) {
         const int j = nt * 8 + 2 * t;
         // dW1 rows g (< 8); rows g + 8 are padding
-        atomicAdd(&S.grad[kOffW1 + g * kMlpH + j], aW1[nt][0]);
-        atomicAdd(&S.grad[kOffW1 + g * kMlpH + j + 1], aW1[nt][1]);
+        wg[kOffW1 + g * kMlpH + j] = aW1[nt][0];
+        wg[kOffW1 + g * kMlpH + j + 1] = aW1[nt][1];
 #pragma unroll
         for (int mt = 0; mt < 2; ++mt) {
             const int i = mt * 16 + g;
-            atomicAdd(&S.grad[kOffW2 + i * kMlpH + j], aW2[mt][nt][0]);
-            atomicAdd(&S.grad[kOffW2 + i * kMlpH + j + 1], aW2[mt][nt][1]);
-            atomicAdd(&S.grad[kOffW2 + (i + 8) * kMlpH + j], aW2[mt][nt][2]);
-            atomicAdd(&S.grad[kOffW2 + (i + 8) * kMlpH + j + 1], aW2[mt][nt][3]);
+            wg[kOffW2 + i * kMlpH + j] = aW2[mt][nt][0];
+            wg[kOffW2 + i * kMlpH + j + 1] = aW2[mt][nt][1];
+            wg[kOffW2 + (i + 8) * kMlpH + j] = aW2[mt][nt][2];
+            wg[kOffW2 + (i + 8) * kMlpH + j + 1] = aW2[mt][nt][3];
         }
         float b1x = aB1[nt][0], b1y = aB1[nt][1], b2x = aB2[nt][0], b2y = aB2[nt][1];
         for (int o = 4; o < 32; o <<= 1) {
@@ -367,17 +370,17 @@ k_mlp_grad(const float* __restrict__ P, const float* __restrict__ norm,
             b2y += __shfl_xor_sync(0xffffffffu, b2y, o);
         }
         if (g == 0) {
-            atomicAdd(&S.grad[kOffB1 + j], b1x);
-            atomicAdd(&S.grad[kOffB1 + j + 1], b1y);
-            atomicAdd(&S.grad[kOffB2 + j], b2x);
-            atomicAdd(&S.grad[kOffB2 + j + 1], b2y);
+            wg[kOffB1 + j] = b1x;
+            wg[kOffB1 + j + 1] = b1y;
+            wg[kOffB2 + j] = b2x;
+            wg[kOffB2 + j + 1] = b2y;
         }
     }
     if (t == 0) {
 #pragma unroll
         for (int mt = 0; mt < 2; ++mt) {
-            atomicAdd(&S.grad[kOffW3 + mt * 16 + g], aW3[mt][0]);
-            atomicAdd(&S.grad[kOffW3 + mt * 16 + g + 8], aW3[mt][2]);
+            wg[kOffW3 + mt * 16 + g] = aW3[mt][0];
+            wg[kOffW3 + mt * 16 + g + 8] = aW3[mt][2];
         }
     }
     for (int o = 16; o > 0; o >>= 1) {
@@ -385,13 +388,39 @@ k_mlp_grad(const float* __restrict__ P, const float* __restrict__ norm,
         aL += __shfl_xor_sync(0xffffffffu, aL, o);
     }
     if (lane == 0) {
-        atomicAdd(&S.grad[kOffB3], aB3);
-        atomicAdd(&S.loss, aL);
+        wg[kOffB3] = aB3;
+        wg[kMlpParams] = aL;
     }
     __syncthreads();
-    for (uint32_t i = threadIdx.x; i < kMlpParams; i += blockDim.x) atomicAdd(&grad[i], S.grad[i]);
-    if (threadIdx.x == 0) atomicAdd(loss, S.loss);
+    for (uint32_t i = threadIdx.x; i <= kMlpParams; i += blockDim.x) {
+        float sum = 0.f;
+#pragma unroll
+        for (int w = 0; w < kTrainWarps; ++w) sum += S.wg[w][i];
+        part[static_cast<size_t>(blockIdx.x) * kGradRow + i] = sum;
+    }
 }
+
+// grad / loss = the CTA rows of `part` added in CTA order.
+__global__ void k_grad_sum(const float* __restrict__ part, uint32_t rows,
+                           float* __restrict__ grad, float* __restrict__ loss) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i > static_cast<uint32_t>(kMlpParams)) return;
+    float sum = 0.f;
+    for (uint32_t r = 0; r < rows; ++r) sum += part[static_cast<size_t>(r) * kGradRow + i];
+    if (i < static_cast<uint32_t>(kMlpParams)) grad[i] = sum;
+    else *loss = sum;
+}
+
+// Per-thread scratch for the CTA rows of the gradient (one stream per host
+// thread, as for the seeding handles).
+struct GradScratch {
+    float* p = nullptr;
+    uint32_t rows = 0;
+    int device = -1;
+    ~GradScratch() {
+        if (p) cudaFree(p);
+    }
+};
 
 __global__ void k_adam(float* __restrict__ P, const float* __restrict__ G, float* __restrict__ M,
                        float* __restrict__ V, uint32_t n, float lr, float b1, float b2, float eps,
@@ -501,11 +530,13 @@ seedgb_status seedgb_mlp_grad(const float* params, const float* norm, const floa
         return SEEDGB_INVALID_ARGUMENT;
     if (reinterpret_cast<uintptr_t>(features) % 16) return SEEDGB_INVALID_ARGUMENT;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    cudaError_t err = cudaMemsetAsync(grad, 0, sizeof(float) * kMlpParams, s);
-    if (err == cudaSuccess) err = cudaMemsetAsync(loss, 0, sizeof(float), s);
-    if (err != cudaSuccess) return SEEDGB_CUDA_ERROR;
-    if (n == 0) return SEEDGB_OK;
+    if (n == 0) {
+        cudaError_t err = cudaMemsetAsync(grad, 0, sizeof(float) * kMlpParams, s);
+        if (err == cudaSuccess) err = cudaMemsetAsync(loss, 0, sizeof(float), s);
+        return err == cudaSuccess ? SEEDGB_OK : SEEDGB_CUDA_ERROR;
+    }
     static thread_local int attr_dev = -1;  // the attribute is per context
+    static thread_local GradScratch scratch;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return SEEDGB_CUDA_ERROR;
     if (attr_dev != dev) {
@@ -519,8 +550,21 @@ seedgb_status seedgb_mlp_grad(const float* params, const float* norm, const floa
     const uint32_t tiles = (n + 15) / 16;
     const uint32_t grid = std::min<uint32_t>((tiles + kTrainWarps - 1) / kTrainWarps,
                                              static_cast<uint32_t>(sms));
+    if (scratch.rows < grid || scratch.device != dev) {
+        // the previous scratch may still be in use by work on any stream
+        if (scratch.p && cudaDeviceSynchronize() != cudaSuccess) return SEEDGB_CUDA_ERROR;
+        if (scratch.p) cudaFree(scratch.p);
+        scratch.p = nullptr;
+        scratch.rows = 0;
+        const uint32_t rows = std::max<uint32_t>(grid, static_cast<uint32_t>(sms));
+        if (cudaMalloc(&scratch.p, sizeof(float) * kGradRow * rows) != cudaSuccess)
+            return SEEDGB_CUDA_ERROR;
+        scratch.rows = rows;
+        scratch.device = dev;
+    }
     k_mlp_grad<<<grid, kTrainWarps * 32, sizeof(TrainSmem), s>>>(params, norm, features, labels,
-                                                                n, pos_weight, grad, loss);
+                                                                n, pos_weight, scratch.p);
+    k_grad_sum<<<(kMlpParams + 1 + 255) / 256, 256, 0, s>>>(scratch.p, grid, grad, loss);
     return cudaGetLastError() == cudaSuccess ? SEEDGB_OK : SEEDGB_CUDA_ERROR;
 }
 

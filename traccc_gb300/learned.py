@@ -174,6 +174,18 @@ def run_dump(alg, sps, model: FilterModel, stream=None, records=None, triplets=F
     return outs, records[:nrec]
 
 
+def _ordered(torch, rec):
+    """Doublet records in a fixed order (event, role, middle, other): the dump
+    appends them in the order the GPU finds them, which varies between runs."""
+    if len(rec) < 2:
+        return rec
+    words = rec.view(torch.int32).to(torch.int64) & 0xffffffff
+    minor = (words[:, 0] << 32) | words[:, 1]
+    order = torch.sort(minor, stable=True).indices
+    order = order[torch.sort(words[order, 2], stable=True).indices]
+    return rec[order]
+
+
 def _labels(torch, rec, outs, trec=None):
     """Per-record label: the doublet belongs to an accepted seed, or, with
     triplet records `trec`, to any triplet (a doublet in no triplet can
@@ -239,6 +251,7 @@ def collect(alg, events, neg_keep=0.05, batch=8, seed=0, model=None, roles=(1,),
         else:
             outs, rec = run_dump(alg, sps, model, records=records)
             trec = None
+        rec = _ordered(torch, rec)
         lab, top = _labels(torch, rec, outs, trec)
         want = torch.zeros_like(top)
         for r in roles:
