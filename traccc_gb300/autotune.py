@@ -29,8 +29,9 @@ import statistics
 
 from . import seeding
 
-WARPS = (4, 6, 8, 10)
-MIDDLES = (32, 64, 128, 256)
+# 16 warps: as many as fit in shared memory with the neighbourhood capacity
+WARPS = (8, 12, 16)
+MIDDLES = (64, 256, 1024)
 NEIGHBOURHOOD = (1536, 2048, 2560, 3072)
 CTAS = (1, 2)
 

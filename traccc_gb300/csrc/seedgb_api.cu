@@ -438,7 +438,7 @@ seedgb_status seedgb_seeding_create(const seedgb_seedfinder_config* finder,
         return SEEDGB_CUDA_ERROR;
     }
     h->tune.fast_warps = 16;  // clamped below to what fits in shared memory
-    h->tune.middles_per_item = 128;
+    h->tune.middles_per_item = 256;
     h->tune.nb_cap = 2560;
     h->tune.ctas_per_sm = 1;
     if (const char* s = std::getenv("SEEDGB_TUNE")) {

@@ -622,31 +622,36 @@ struct Stage1Cand {
 
 template <int CAPB, int CAPT, int CAPLC, int CAPCT>
 struct WarpScratch {
-    // middle-top doublets in list order: {cot(theta), iDeltaR, U, V}, Er
-    float4 mtd[CAPLC];
+    union {
+        // middle-top doublets in list order: {cot(theta), iDeltaR, U, V}
+        float4 mtd[CAPLC];
+        struct {  // the doublet scans' radius windows and candidate prefixes (before mtd)
+            uint32_t bnd[4 * kFastSegs];        // radius windows per bin
+            uint32_t pre[2 * (kFastSegs + 1)];  // candidate prefix per bin
+        };
+    };
     float er[CAPLC];
     uint16_t hpt[CAPLC];  // host position of the top
     uint16_t ppt[CAPLC];  // neighbourhood position of the top
     uint16_t perm[CAPLC]; // bucket-sorted slot -> list index
     uint32_t bstart[kBuckets + 1];
-    uint32_t bcur[kBuckets];
     uint16_t qb[CAPB];  // middle-bottom doublets (neighbourhood positions)
     union {
-        uint16_t qt[CAPT];  // middle-top doublets, until their lin_circles exist
+        uint16_t qt[CAPT];        // middle-top doublets, until their lin_circles exist
+        uint32_t bcur[kBuckets];  // counting-sort cursors, after the lin_circles
         struct {
             Stage0Cand q0[96];  // in-window candidates awaiting stage 1 (< 32 + 64)
             Stage1Cand q1[64];  // stage-1 survivors awaiting stage 2 (< 32 + 32)
-        } q;
+        } q;                    // during the triplet search
+        struct {                // after the triplet search
+            uint32_t skey[CAPCT]; // host-order sort key of the triplets
+            uint16_t sidx[CAPCT]; // sorted -> ct index
+            float wf[CAPCT];      // final weight in sorted order, -inf when cut
+            float ts[CAPCT];      // tie sum of the sort, sorted order
+        };
     };
     TripCand ct[CAPCT];   // triplets of the middle
-    uint32_t skey[CAPCT]; // host-order sort key of the triplets
-    uint16_t sidx[CAPCT]; // sorted -> ct index
-    float wf[CAPCT];      // final weight in sorted order, -inf when cut
-    float ts[CAPCT];      // tie sum of the sort, sorted order
-    uint32_t bnd[4 * kFastSegs];        // radius windows per bin
-    uint32_t pre[2 * (kFastSegs + 1)];  // candidate prefix per bin
 };
-
 // shared memory per warp: fast ~15 KB, slow ~190 KB
 using FastScratch = WarpScratch<1024, 1024, 256, 128>;
 using SlowScratch = WarpScratch<8192, 8192, 4096, 2048>;
