@@ -267,7 +267,7 @@ def run_batched(args, dev, stream, flush_buf, inputs, model=None):
                 "latency_ms": {"p50": quantile(e2e_lat, 0.5), "p99": quantile(e2e_lat, 0.99)},
                 "h2d_bytes_per_batch": int(h2d), "d2h_bytes_per_batch": int(d2h)},
         "autotune": tuned,
-        "gpu_launches_per_batch": len(seeding.KERNEL_NAMES) + (3 if model is not None else 0),
+        "gpu_launches_per_batch": len(seeding.KERNEL_NAMES) + (4 if model is not None else 0),
         "l2": "flushed before each batch (256 MiB write)",
     }
     if model is not None:

@@ -231,10 +231,13 @@ seedgb_status seedgb_seeding_run_batch(seedgb_seeding* h,
 seedgb_status seedgb_seeding_last_status(seedgb_seeding* h, void* stream);
 
 /* Work counters of the last run (after seedgb_seeding_last_status):
- * out[0] valid spacepoints, out[1] middles sent to the large-capacity path,
- * out[2] middle-bottom doublets, out[3] middle-top doublets,
- * out[4] triplets, out[5] seeds. */
-seedgb_status seedgb_seeding_counters(seedgb_seeding* h, uint64_t out[8]);
+ * out[0] valid spacepoints, out[1] middles the fast kernel handed to the
+ * general path, out[2] middle-bottom doublets, out[3] middle-top doublets,
+ * out[4] triplets, out[5] seeds, out[6] spacepoints whose correctly rounded
+ * phi the double-precision atan2 could not decide (expected 0), out[7] work
+ * items, out[8] middles that reached the general path's last
+ * (large-capacity) tier. */
+seedgb_status seedgb_seeding_counters(seedgb_seeding* h, uint64_t out[9]);
 
 /* Copy the phi-z grid of event `event` of the last run to host memory
  * (synchronises `stream`): bin_offsets[nbins+1] (CSR) and bin_sps[n_valid] =
@@ -263,9 +266,11 @@ seedgb_status seedgb_seeding_set_option(seedgb_seeding* h, seedgb_option opt,
 
 /* Device durations (ms) of the kernels of the last run with
  * SEEDGB_OPTION_KERNEL_TIMING on, in launch order: bin_count, bin_scan,
- * bin_scatter, bin_rsort, seed_fast, seed_slow, seed_compact.  Waits for the
- * last recorded event.  Returns SEEDGB_INVALID_ARGUMENT if timing was off. */
-seedgb_status seedgb_seeding_kernel_times(seedgb_seeding* h, float ms[7]);
+ * bin_scatter, bin_rsort, seed_fast, seed_mid, seed_slow, seed_compact (with
+ * the learned filter, seed_slow also covers the fallback pass).  Waits for
+ * the last recorded event.  Returns SEEDGB_INVALID_ARGUMENT if timing was
+ * off. */
+seedgb_status seedgb_seeding_kernel_times(seedgb_seeding* h, float ms[8]);
 
 /* ------------------------------------------------------------------------ */
 /* Spacepoint formation (the step in front of the seeding path)              */

@@ -229,6 +229,7 @@ seedgb_status ensure_arena(seedgb_seeding* h, uint32_t n_events, uint64_t total_
     const size_t o_cnt = take(sizeof(uint8_t) * cs);
     const size_t o_slot = take(sizeof(SeedSlot) * cs * kMaxSeedsPerMiddle);
     const size_t o_ovf = take(sizeof(uint32_t) * cs * 2);
+    const size_t o_ovf2 = take(sizeof(uint32_t) * cs * 2);
     const size_t o_ctr = take(sizeof(unsigned long long) * kNumCounters);
     const size_t o_evf = take(sizeof(uint32_t) * 4 * static_cast<size_t>(ce));
     const size_t o_evm = take(sizeof(uint8_t) * static_cast<size_t>(ce));
@@ -271,6 +272,7 @@ seedgb_status ensure_arena(seedgb_seeding* h, uint32_t n_events, uint64_t total_
     a.seed_cnt = reinterpret_cast<uint8_t*>(base + o_cnt);
     a.seed_slot = reinterpret_cast<SeedSlot*>(base + o_slot);
     a.ovf = reinterpret_cast<uint32_t*>(base + o_ovf);
+    a.ovf2 = reinterpret_cast<uint32_t*>(base + o_ovf2);
     a.counters = reinterpret_cast<unsigned long long*>(base + o_ctr);
     a.ev_filter = reinterpret_cast<uint32_t*>(base + o_evf);
     a.ev_mode = reinterpret_cast<uint8_t*>(base + o_evm);
@@ -439,7 +441,7 @@ seedgb_status seedgb_seeding_create(const seedgb_seedfinder_config* finder,
     }
     h->tune.fast_warps = 16;  // clamped below to what fits in shared memory
     h->tune.middles_per_item = 256;
-    h->tune.nb_cap = 2560;
+    h->tune.nb_cap = 2048;
     h->tune.ctas_per_sm = 1;
     if (const char* s = std::getenv("SEEDGB_TUNE")) {
         int w, m, nb, c;
@@ -692,7 +694,7 @@ seedgb_status seedgb_seeding_last_status(seedgb_seeding* h, void* stream) {
     return SEEDGB_OK;
 }
 
-seedgb_status seedgb_seeding_counters(seedgb_seeding* h, uint64_t out[8]) {
+seedgb_status seedgb_seeding_counters(seedgb_seeding* h, uint64_t out[9]) {
     if (!h || !out) return SEEDGB_INVALID_ARGUMENT;
     out[0] = h->h_counters[kNumValid];
     out[1] = h->h_counters[kOvfCount];
@@ -702,6 +704,7 @@ seedgb_status seedgb_seeding_counters(seedgb_seeding* h, uint64_t out[8]) {
     out[5] = h->h_counters[kNumSeeds];
     out[6] = h->h_counters[kPhiUndecided];
     out[7] = h->h_counters[kItemTotal];
+    out[8] = h->h_counters[kOvf2Count];
     return SEEDGB_OK;
 }
 
@@ -751,7 +754,7 @@ seedgb_status seedgb_seeding_set_option(seedgb_seeding* h, seedgb_option opt, in
     return SEEDGB_INVALID_ARGUMENT;
 }
 
-seedgb_status seedgb_seeding_kernel_times(seedgb_seeding* h, float ms[7]) {
+seedgb_status seedgb_seeding_kernel_times(seedgb_seeding* h, float ms[8]) {
     if (!h || !ms || !h->timed_run) return SEEDGB_INVALID_ARGUMENT;
     if (cudaEventSynchronize(h->tev[kNumKernels]) != cudaSuccess) return SEEDGB_CUDA_ERROR;
     for (int i = 0; i < kNumKernels; ++i) {

@@ -16,7 +16,8 @@
 //   items       uint2 [max_items]           (event, bin | chunk<<16) work items
 //   seed_cnt    uint8 [total_sp]            seeds per middle spacepoint
 //   seed_slot   SeedSlot[total_sp][KMAX]    seeds per middle, in final order
-//   ovf         uint32[total_sp]            middles for the large-capacity path
+//   ovf         uint32[2 total_sp]          middles the fast kernel hands to the general path
+//   ovf2        uint32[2 total_sp]          middles beyond the general path's middle tier
 //   counters    uint64[kNumCounters]
 #pragma once
 
@@ -55,6 +56,9 @@ enum Counter : int {
     kFallbackEvents = 14,  // events re-seeded without the learned filter
     kOvfFetch2 = 15,    // large-capacity queue counter of the fallback pass
     kTripDumpCount = 16,  // triplet records written (may exceed the capacity)
+    kOvf2Count = 17,    // middles queued for the last (large-capacity) tier
+    kOvf2Fetch = 18,
+    kOvf2Fetch2 = 19,   // last-tier queue counter of the fallback pass
     kNumCounters = 24
 };
 
@@ -151,7 +155,8 @@ struct Arena {
     uint2* items;
     uint8_t* seed_cnt;
     SeedSlot* seed_slot;
-    uint32_t* ovf;          // [2 * cap_sp] middles for the large-capacity path
+    uint32_t* ovf;          // [2 * cap_sp] middles for the general path (middle tier)
+    uint32_t* ovf2;         // [2 * cap_sp] middles for its last, large-capacity tier
     unsigned long long* counters;
     uint32_t* ev_filter;    // [E][4] scored / pruned middle-bottom, scored / pruned middle-top
     uint8_t* ev_mode;       // [E] 1: re-seed without the filter (fallback pass)
@@ -183,7 +188,7 @@ DevConfig make_dev_config(const seedgb_seedfinder_config& f,
 // grid: the batch sizes that size the launch grids (the actual batch, or the
 // arena capacities when capturing a graph); the kernels read the actual
 // sizes from a.hdr.
-constexpr int kNumKernels = 7;
+constexpr int kNumKernels = 8;
 // Sets the kernels' shared-memory attributes on the current device (once).
 cudaError_t prepare_kernels();
 cudaError_t launch_seeding(const DevConfig& cfg, const Arena& a, const BatchHeader& grid,

@@ -9,9 +9,12 @@
 //                  runs doublet finding (ballot compaction), triplet finding
 //                  (cot-sorted middle-top doublets, exact reference cuts),
 //                  compatible-seed weights and seed selection
-//   k_seed_slow    the same per-middle routine with large capacities, reading
-//                  the neighbourhood from global memory, for the few middles
-//                  that overflow the fast kernel's shared-memory buffers
+//   k_seed_mid     the same per-middle routine on the middles the fast kernel
+//                  hands over (neighbourhood too large to stage, per-middle z
+//                  neighbourhood, lists beyond its buffers), reading the
+//                  neighbourhood from global memory, many warps per SM
+//   k_seed_slow    the same with large capacities, one warp per SM, for the
+//                  few middles whose lists overflow k_seed_mid's buffers
 //   k_seed_compact per event: seeds in host order into the output buffer
 //
 // Floating-point semantics follow the reference host code: the file is built
@@ -640,7 +643,7 @@ struct WarpScratch {
         uint16_t qt[CAPT];        // middle-top doublets, until their lin_circles exist
         uint32_t bcur[kBuckets];  // counting-sort cursors, after the lin_circles
         struct {
-            Stage0Cand q0[96];  // in-window candidates awaiting stage 1 (< 32 + 64)
+            Stage0Cand q0[64];  // in-window candidates awaiting stage 1 (< 32 + 32)
             Stage1Cand q1[64];  // stage-1 survivors awaiting stage 2 (< 32 + 32)
         } q;                    // during the triplet search
         struct {                // after the triplet search
@@ -652,8 +655,14 @@ struct WarpScratch {
     };
     TripCand ct[CAPCT];   // triplets of the middle
 };
-// shared memory per warp: fast ~15 KB, slow ~190 KB
-using FastScratch = WarpScratch<1024, 1024, 256, 128>;
+// shared memory per warp: fast 13.5 KiB, slow 173 KiB.  Fast capacities: 640
+// middle-bottom and 1024 middle-top candidates (the largest lists on a batch
+// of 5k-114k-spacepoint events: 497 and 383), 256 middle-top doublets and 128
+// triplets (exceeded by fewer than 0.3 % and 0.2 % of that batch's middles);
+// a middle beyond one of them is seeded by the large-capacity kernel.
+// Smaller scratch means more warps per SM, which is what hides this kernel's
+// latency.
+using FastScratch = WarpScratch<640, 1024, 256, 128>;
 using SlowScratch = WarpScratch<8192, 8192, 4096, 2048>;
 
 // Keep the positions whose doublet passes the minimum-helix-radius test, in
@@ -1119,9 +1128,9 @@ __device__ MiddleResult process_middle(const DevConfig& c, const Arena& a,
     // -- triplets.  The middle-bottom doublets are set up 32 at a time (one
     //    per lane); each lane walks the middle-top doublets of its cot
     //    buckets and queues those inside its exact cot window (q0, with the
-    //    doublet's lin_circle); stage 1 runs on 64 queued candidates at a
-    //    time, stage 2 on 32 stage-1 survivors at a time, so both run with
-    //    full lanes across doublets and chunks.
+    //    doublet's lin_circle), one entry per lane per step; stage 1 runs on
+    //    32 queued candidates at a time, stage 2 on 32 stage-1 survivors at a
+    //    time, so both run with full lanes across doublets and chunks.
     const float sig2 = c.sigmaScattering * c.sigmaScattering;
     uint32_t n_ct = 0, n0 = 0, n1 = 0;
     uint32_t c0 = 0, it = 0, maxc = 0;
@@ -1182,9 +1191,8 @@ __device__ MiddleResult process_middle(const DevConfig& c, const Arena& a,
         }
         if (have_chunk) {
             while (it < maxc && n0 < 32) {
-#pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    const uint32_t j = it + h;
+                {
+                    const uint32_t j = it;
                     bool ok = false;
                     uint32_t tp = 0;
                     if (j < cnt) {
@@ -1206,7 +1214,7 @@ __device__ MiddleResult process_middle(const DevConfig& c, const Arena& a,
                     }
                     n0 += __popc(mask);
                 }
-                it += 2;
+                ++it;
             }
             if (it >= maxc) {
                 have_chunk = false;
@@ -1598,7 +1606,7 @@ __device__ __forceinline__ void seed_fast_items(const DevConfig& c, const Arena&
                 if (lane == 0) push_overflow(a, gm);
                 continue;
             }
-            const MiddleResult r = process_middle<true, SCORE, VAR, 1024, 1024, 256, 128>(
+            const MiddleResult r = process_middle<true, SCORE, VAR, 640, 1024, 256, 128>(
                 c, a, nb, gm, true, nb_minr, nb_maxr, e, ws);
             if (lane == 0) {
                 if (r.status) push_overflow(a, gm);
@@ -1619,28 +1627,46 @@ __global__ void __launch_bounds__(SCORE ? kScoreWarps * 32 : 512)
     else seed_fast_items<SCORE, false>(c, a, mpi, nb_cap, pass);
 }
 
-// Large-capacity path: one warp per CTA, neighbourhood read from global
-// memory in host order, per-middle z neighbourhood; always with the variance
-// terms (exact for zero variances too; few middles take this path).
-template <bool SCORE>
-__global__ void __launch_bounds__(32) k_seed_slow(DevConfig c, Arena a, uint32_t pass) {
+// General path, for the middles the fast kernel hands over (neighbourhood not
+// staged: too many spacepoints or bins, an unsorted bin, or a per-middle z
+// neighbourhood other than the bin's; or a list beyond the fast capacities).
+// Every warp takes one middle at a time from its tier's queue, builds the
+// middle's own neighbourhood and reads it from global memory in host order.
+// Two tiers: the middle tier (many warps per SM, the fast kernel's list
+// capacities) takes every handed-over middle and passes the ones whose lists
+// do not fit to the last tier (one warp per SM with large capacities).
+constexpr size_t kGeneralSegBytes = 1024;  // per warp: segments of the middle's neighbourhood
+
+template <typename Scratch>
+__host__ __device__ constexpr size_t general_warp_bytes() {
+    return (kGeneralSegBytes + sizeof(Scratch) + 127) & ~static_cast<size_t>(127);
+}
+
+template <bool SCORE, bool VAR, bool LAST, int CAPB, int CAPT, int CAPLC, int CAPCT>
+__device__ __forceinline__ void general_middles(const DevConfig& c, const Arena& a,
+                                                uint32_t pass) {
+    using Scratch = WarpScratch<CAPB, CAPT, CAPLC, CAPCT>;
     extern __shared__ __align__(128) uint8_t smem[];
-    uint32_t* seg_pos = reinterpret_cast<uint32_t*>(smem);     // [kMaxSegments+1]
-    uint32_t* seg_g = seg_pos + kMaxSegments + 1;              // [kMaxSegments]
-    uint32_t* misc = seg_g + kMaxSegments;                     // [2]
-    static_assert(sizeof(uint32_t) * (2 * kMaxSegments + 3) <= 1024, "slow layout");
-    SlowScratch& ws = *reinterpret_cast<SlowScratch*>(smem + 1024);
-    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    uint8_t* wbase = smem + static_cast<size_t>(warp) * general_warp_bytes<Scratch>();
+    uint32_t* seg_pos = reinterpret_cast<uint32_t*>(wbase);   // [kMaxSegments+1]
+    uint32_t* seg_g = seg_pos + kMaxSegments + 1;             // [kMaxSegments]
+    uint32_t* misc = seg_g + kMaxSegments;                    // [1]
+    static_assert(sizeof(uint32_t) * (2 * kMaxSegments + 2) <= kGeneralSegBytes,
+                  "general segment layout");
+    Scratch& ws = *reinterpret_cast<Scratch*>(wbase + kGeneralSegBytes);
+    const uint32_t* queue = LAST ? a.ovf2 : a.ovf;
     const uint32_t n = static_cast<uint32_t>(
-        min(a.counters[kOvfCount], 2ull * a.cap_sp));
+        min(a.counters[LAST ? kOvf2Count : kOvfCount], 2ull * a.cap_sp));
     const uint32_t n_events = a.hdr->n_events;
-    unsigned long long* fetch = &a.counters[pass ? kOvfFetch2 : kOvfFetch];
+    unsigned long long* fetch =
+        &a.counters[LAST ? (pass ? kOvf2Fetch2 : kOvf2Fetch) : (pass ? kOvfFetch2 : kOvfFetch)];
     for (;;) {
         uint32_t idx = 0;
         if (lane == 0) idx = static_cast<uint32_t>(atomicAdd(fetch, 1ull));
         idx = __shfl_sync(0xffffffffu, idx, 0);
         if (idx >= n) break;
-        const uint32_t gm = a.ovf[idx];
+        const uint32_t gm = queue[idx];
         // event: last with sp_base <= gm
         uint32_t lo = 0, hi = n_events;
         while (hi - lo > 1) {
@@ -1668,19 +1694,41 @@ __global__ void __launch_bounds__(32) k_seed_slow(DevConfig c, Arena a, uint32_t
         MiddleResult r{0, 0, 0, 1};
         if (size <= 65535u) {
             NbViewT<false> nb{nullptr, nullptr, a.g_xyzr, seg_pos, seg_g, nseg, size};
-            r = process_middle<false, SCORE, true, 8192, 8192, 4096, 2048>(c, a, nb, gm, false,
-                                                                                0.f, 0.f, e, ws);
+            r = process_middle<false, SCORE, VAR, CAPB, CAPT, CAPLC, CAPCT>(c, a, nb, gm, false,
+                                                                            0.f, 0.f, e, ws);
         }
         if (lane == 0) {
-            if (r.status) {
+            if (!r.status) {
+                count_middle(a, r);
+            } else if (LAST) {
                 raise_status(a.counters, SEEDGB_CAPACITY_OVERFLOW);
                 a.seed_cnt[gm] = 0;
             } else {
-                count_middle(a, r);
+                const unsigned long long k = atomicAdd(&a.counters[kOvf2Count], 1ull);
+                if (k < 2ull * a.cap_sp) a.ovf2[k] = gm;
+                else raise_status(a.counters, SEEDGB_CAPACITY_OVERFLOW);
+                a.seed_cnt[gm] = 0;
             }
         }
         __syncwarp();
     }
+}
+
+// Middle tier: the fast kernel's capacities, as many warps as fit.
+template <bool SCORE>
+__global__ void __launch_bounds__(SCORE ? kScoreWarps * 32 : 512)
+    k_seed_mid(DevConfig c, Arena a, uint32_t pass) {
+    if (a.counters[kAnyVariance] != 0)
+        general_middles<SCORE, true, false, 640, 1024, 256, 128>(c, a, pass);
+    else
+        general_middles<SCORE, false, false, 640, 1024, 256, 128>(c, a, pass);
+}
+
+// Last tier: one warp per CTA with large capacities; always with the
+// variance terms (exact for zero variances too; very few middles get here).
+template <bool SCORE>
+__global__ void __launch_bounds__(32) k_seed_slow(DevConfig c, Arena a, uint32_t pass) {
+    general_middles<SCORE, true, true, 8192, 8192, 4096, 2048>(c, a, pass);
 }
 
 // Events whose pruned fraction (of all scored doublets) leaves the filter's
@@ -1869,7 +1917,16 @@ int fast_kernel_max_warps(int nb_cap, int ctas_per_sm) {
     return static_cast<int>(std::min<size_t>(16, (limit - fixed) / sizeof(FastScratch)));
 }
 
-static size_t slow_kernel_smem() { return 1024 + sizeof(SlowScratch); }
+static size_t slow_kernel_smem() { return general_warp_bytes<SlowScratch>(); }
+
+// Warps per CTA of the general path's middle tier (all that fit in 227 KiB).
+static int mid_kernel_warps(bool score) {
+    const int fit = static_cast<int>((227 * 1024) / general_warp_bytes<FastScratch>());
+    return std::min(score ? kScoreWarps : 16, fit);
+}
+static size_t mid_kernel_smem(bool score) {
+    return static_cast<size_t>(mid_kernel_warps(score)) * general_warp_bytes<FastScratch>();
+}
 
 cudaError_t prepare_kernels() {
     // per device: the attribute belongs to the current context
@@ -1886,6 +1943,12 @@ cudaError_t prepare_kernels() {
             err = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        static_cast<int>(slow_kernel_smem()));
     }
+    if (err == cudaSuccess)
+        err = cudaFuncSetAttribute(k_seed_mid<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   static_cast<int>(mid_kernel_smem(false)));
+    if (err == cudaSuccess)
+        err = cudaFuncSetAttribute(k_seed_mid<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   static_cast<int>(mid_kernel_smem(true)));
     if (err == cudaSuccess) done_for = dev;
     return err;
 }
@@ -1929,19 +1992,27 @@ cudaError_t launch_seeding(const DevConfig& cfg, const Arena& a, const BatchHead
         k_seed_fast<true><<<fgrid, ts.fast_warps * 32, fast_kernel_smem(ts), stream>>>(
             cfg, a, mpi, nbc, 0u);
         mark(5);
+        k_seed_mid<true><<<num_sms, mid_kernel_warps(true) * 32, mid_kernel_smem(true), stream>>>(
+            cfg, a, 0u);
+        mark(6);
         k_seed_slow<true><<<num_sms, 32, ssm, stream>>>(cfg, a, 0u);
         // fallback: events whose pruned fraction left the band, without the filter
         k_filter_mark<<<(grid.n_events + 255) / 256, 256, 0, stream>>>(cfg, a);
         k_seed_fast<false><<<fgrid, fblock, fsm, stream>>>(cfg, a, mpi, nbc, 1u);
+        k_seed_mid<false><<<num_sms, mid_kernel_warps(false) * 32, mid_kernel_smem(false),
+                             stream>>>(cfg, a, 1u);
         k_seed_slow<false><<<num_sms, 32, ssm, stream>>>(cfg, a, 1u);
     } else {
         k_seed_fast<false><<<fgrid, fblock, fsm, stream>>>(cfg, a, mpi, nbc, 0u);
         mark(5);
+        k_seed_mid<false><<<num_sms, mid_kernel_warps(false) * 32, mid_kernel_smem(false),
+                             stream>>>(cfg, a, 0u);
+        mark(6);
         k_seed_slow<false><<<num_sms, 32, ssm, stream>>>(cfg, a, 0u);
     }
-    mark(6);
-    k_seed_compact<<<grid.n_events, 1024, 0, stream>>>(a);
     mark(7);
+    k_seed_compact<<<grid.n_events, 1024, 0, stream>>>(a);
+    mark(8);
     return cudaGetLastError();
 }
 

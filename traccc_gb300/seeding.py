@@ -142,7 +142,7 @@ NOALLOC_MAX_SPACEPOINTS = 65536
 OPTION_EXHAUSTIVE_TRIPLETS = 1
 OPTION_KERNEL_TIMING = 2
 KERNEL_NAMES = ("bin_count", "bin_scan", "bin_scatter", "bin_rsort", "seed_fast",
-                "seed_slow", "seed_compact")
+                "seed_mid", "seed_slow", "seed_compact")
 
 PARAMS_DTYPE = np.dtype([("surface_link", "<u8"), ("params", "<f4", (6,)),
                          ("cov", "<f4", (36,))])
@@ -578,15 +578,15 @@ class TripletSeedingAlgorithm:
         return int(lib().seedgb_seeding_last_status(self._h, _stream_ptr(stream)))
 
     def counters(self) -> dict:
-        arr = (C.c_uint64 * 8)()
+        arr = (C.c_uint64 * 9)()
         _check(lib().seedgb_seeding_counters(self._h, arr), "seedgb_seeding_counters")
         keys = ("n_valid", "n_overflow_middles", "n_mb", "n_mt", "n_triplets",
-                "n_seeds", "phi_undecided", "n_items")
+                "n_seeds", "phi_undecided", "n_items", "n_last_tier_middles")
         return {k: int(v) for k, v in zip(keys, arr)}
 
     def kernel_times(self) -> dict:
         """Per-kernel device ms of the last run (OPTION_KERNEL_TIMING on)."""
-        arr = (C.c_float * 7)()
+        arr = (C.c_float * len(KERNEL_NAMES))()
         _check(lib().seedgb_seeding_kernel_times(self._h, arr), "seedgb_seeding_kernel_times")
         return {k: float(v) for k, v in zip(KERNEL_NAMES, arr)}
 
