@@ -471,6 +471,20 @@ def load_profile_traffic(kernel):
         return None
 
 
+def load_op_model(n_events):
+    """Reference FP32 work of the bench events (profiles/op_model.json,
+    counted by the oracle offline), or None when it does not cover them."""
+    p = os.path.join(ROOT, "profiles", "op_model.json")
+    try:
+        with open(p) as fh:
+            m = json.load(fh)
+    except Exception:
+        return None
+    if m.get("events") != n_events or [e["seed"] for e in m["per_event"]] != list(range(n_events)):
+        return None
+    return m
+
+
 def run_gpu(args):
     import torch
     import torch.distributed as dist
@@ -751,6 +765,22 @@ def run_gpu(args):
             "source": "warp instructions issued per launch from the ncu capture in "
                       "profiles/, launch duration measured live, peak = SMs x 4 "
                       "schedulers x median SM clock"}
+    om = load_op_model(n_ev) if dom == "seed_fast" else None
+    if om is not None:
+        sm_mhz = clocks.get("sm_mhz") or 1900.0
+        n_sm = torch.cuda.get_device_properties(dev).multi_processor_count
+        peak_fma = n_sm * 128 * 2 * sm_mhz * 1e6
+        ach = om["flop_seeding_total"] / (dom_ms * 1e-3)
+        roofline["fp32_op_model"] = {
+            "flop_per_launch": om["flop_seeding_total"],
+            "achieved_tflops": ach / 1e12, "peak_tflops": peak_fma / 1e12,
+            "frac": ach / peak_fma, "frac_of_fma_free_peak": 2 * ach / peak_fma,
+            "source": "profiles/op_model.json: FP32 operations of the reference's doublet "
+                      "and triplet tests and lin_circles for these 20 events, counted by "
+                      "the oracle; peak = SMs x 128 lanes x 2 (FMA) x median SM clock. The "
+                      "build is FMA-free (bit-exact cuts), so half that peak is attainable; "
+                      "the GPU skips most triplet tests (exact cot(theta) window), so this "
+                      "is a reference-work-equivalent rate"}
 
     kernels = {k: v / args.steps for k, v in kt_sum.items()}
     line = {

@@ -106,7 +106,8 @@ _STATS_FIELDS = (
     "max_triplets_per_mb", "max_triplets_per_middle", "max_bin_size",
     "max_neighbourhood", "near_doublet_cuts", "near_triplet_cuts",
     "near_bin_edges", "phi_cr_undecided", "n_scored_mb", "n_scored_mt",
-    "n_pruned_mb", "n_pruned_mt")
+    "n_pruned_mb", "n_pruned_mt", "n_window_pairs", "ops_doublet_tests",
+    "ops_triplet_tests")
 
 
 class Stats(C.Structure):

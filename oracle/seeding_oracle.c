@@ -345,7 +345,13 @@ int or_binning(const or_finder_config* c, const or_axes* a,
 /* Doublet / triplet helpers                                                 */
 /* ------------------------------------------------------------------------ */
 
-static uint64_t g_near_doublet, g_near_triplet; /* per-call scratch counters */
+/* per-call scratch counters (per host thread) */
+static _Thread_local uint64_t g_near_doublet, g_near_triplet;
+/* FP32 operations (+ - * / sqrt, one each) of the doublet and triplet tests
+ * as written, every operation of a stage counted once the stage is reached
+ * (short-circuited comparisons included), and the pairs that pass the
+ * doublet window (first stage) */
+static _Thread_local uint64_t g_ops_doublet, g_ops_triplet, g_window_pass;
 
 /* doublet_finding_helper::isCompatible, core/include/traccc/seeding/
  * doublet_finding_helper.hpp:51-216.  m = middle, o = bottom or top.
@@ -367,6 +373,7 @@ int or_doublet_compatible(int top, const float m[6], const float o[6],
         (zOrigin <= c->collisionRegionMin * deltaR) ||
         (zOrigin >= c->collisionRegionMax * deltaR) ||
         fabsf(cotTheta) >= c->deltaZMax) {
+        g_ops_doublet += 8;
         if (near_rel(deltaR, c->deltaRMax) || near_rel(deltaR, c->deltaRMin) ||
             near_rel(fabsf(cotTheta), c->cotThetaMax * deltaR) ||
             near_rel(zOrigin, c->collisionRegionMin * deltaR) ||
@@ -375,6 +382,10 @@ int or_doublet_compatible(int top, const float m[6], const float o[6],
             g_near_doublet++;
         return 0;
     }
+    /* window: 5 for deltaR, cotTheta, zOrigin + 3 products in the cuts;
+     * helix stage: 39 */
+    g_ops_doublet += 8 + 39;
+    g_window_pass++;
     float midX = 0.5f * (m[0] + o[0]);
     float midY = 0.5f * (m[1] + o[1]);
     float slope = (o[1] - m[1]) / (o[0] - m[0]);
@@ -446,7 +457,9 @@ int or_triplet_compatible(const float m[6], const float lb[6],
     float deltaCotTheta2 = deltaCotTheta * deltaCotTheta;
     float error = 0.f;
     float dCotThetaMinusError2 = 0.f;
+    g_ops_triplet += 11; /* error2 8, deltaCotTheta 1, its square 1, the gate 1 */
     if (deltaCotTheta2 - error2 > 0) {
+        g_ops_triplet += 5; /* sqrt, 2 products, 2 sums */
         deltaCotTheta = fabsf(deltaCotTheta);
         error = sqrtf(error2);
         dCotThetaMinusError2 =
@@ -456,13 +469,16 @@ int or_triplet_compatible(const float m[6], const float lb[6],
         if (dCotThetaMinusError2 > scatteringInRegion2) return 0;
     }
     float dU = ltU - lbU;
+    g_ops_triplet += 1;
     if (dU == 0.f) return 0;
+    g_ops_triplet += 8; /* A 2, S2 2, B 2, B2 1, the cut's product 1 */
     float A = (ltV - lbV) / dU;
     float S2 = 1.f + A * A;
     float B = lbV - A * lbU;
     float B2 = B * B;
     if (near_rel(S2, B2 * c->minHelixDiameter2)) g_near_triplet++;
     if (S2 < B2 * c->minHelixDiameter2) return 0;
+    g_ops_triplet += 15; /* pT-dependent scattering 10, curvature 2, impact 3 */
     float iHelixDiameter2 = B2 / S2;
     float pT2scatter = 4.f * iHelixDiameter2 * c->pT2perRadius;
     float pT = c->pTPerHelixRadius * sqrtf(S2 / B2) / 2.f;
@@ -746,6 +762,7 @@ int or_seeding_ex(const or_finder_config* fc, const or_grid_config* gc,
     if (!bin_off || !bin_sps) { free(bin_off); free(bin_sps); return -2; }
     uint32_t n_valid = 0;
     g_near_doublet = g_near_triplet = 0;
+    g_ops_doublet = g_ops_triplet = g_window_pass = 0;
     rc = or_binning(fc, &ax, sps, phi_mode, bin_off, bin_sps, &n_valid, st);
     if (rc) { free(bin_off); free(bin_sps); return rc; }
 
@@ -925,6 +942,9 @@ int or_seeding_ex(const or_finder_config* fc, const or_grid_config* gc,
         st->n_seeds += n_seeds;
         st->near_doublet_cuts += g_near_doublet;
         st->near_triplet_cuts += g_near_triplet;
+        st->n_window_pairs += g_window_pass;
+        st->ops_doublet_tests += g_ops_doublet;
+        st->ops_triplet_tests += g_ops_triplet;
     }
     free(mb.p); free(mt.p); free(tr.p); free(sel.p); free(tmp.p); free(cr.p);
     free(bin_off); free(bin_sps);

@@ -141,6 +141,10 @@ typedef struct {
     /* learned doublet filter (or_seeding_ex with a filter) */
     uint64_t n_scored_mb, n_scored_mt;  /* doublets of middles with both roles */
     uint64_t n_pruned_mb, n_pruned_mt;  /* of those, dropped by the filter     */
+    /* algorithmic work: pairs passing the doublet window (first stage), and
+     * the FP32 operations (+ - * / sqrt, one each) executed by the doublet
+     * and triplet tests */
+    uint64_t n_window_pairs, ops_doublet_tests, ops_triplet_tests;
 } or_stats;
 
 /* Config construction: defaults and setup() (seeding_config.hpp:19,120-138). */
