@@ -226,11 +226,14 @@ seedgb_status ensure_arena(seedgb_seeding* h, uint32_t n_events, uint64_t total_
     const size_t o_rsgp = take(sizeof(uint32_t) * cs);
     const size_t o_uns = take(sizeof(uint8_t) * static_cast<size_t>(ce) * nb);
     const size_t o_items = take(sizeof(uint2) * ci);
+    const size_t o_ikey = take(sizeof(uint8_t) * ci);
+    const size_t o_iord = take(sizeof(uint2) * ci);
     const size_t o_cnt = take(sizeof(uint8_t) * cs);
     const size_t o_slot = take(sizeof(SeedSlot) * cs * kMaxSeedsPerMiddle);
     const size_t o_ovf = take(sizeof(uint32_t) * cs * 2);
     const size_t o_ovf2 = take(sizeof(uint32_t) * cs * 2);
-    const size_t o_ctr = take(sizeof(unsigned long long) * kNumCounters);
+    // the counters and the work-item order histogram are zeroed together
+    const size_t o_ctr = take(kCounterBytes);
     const size_t o_evf = take(sizeof(uint32_t) * 4 * static_cast<size_t>(ce));
     const size_t o_evm = take(sizeof(uint8_t) * static_cast<size_t>(ce));
     static_assert(kHdrBytes >= sizeof(BatchHeader) && kHdrBytes % 256 == 0,
@@ -269,11 +272,15 @@ seedgb_status ensure_arena(seedgb_seeding* h, uint32_t n_events, uint64_t total_
     a.g_rs_gp = reinterpret_cast<uint32_t*>(base + o_rsgp);
     a.bin_unsorted = reinterpret_cast<uint8_t*>(base + o_uns);
     a.items = reinterpret_cast<uint2*>(base + o_items);
+    a.item_key = reinterpret_cast<uint8_t*>(base + o_ikey);
+    a.items_ord = reinterpret_cast<uint2*>(base + o_iord);
     a.seed_cnt = reinterpret_cast<uint8_t*>(base + o_cnt);
     a.seed_slot = reinterpret_cast<SeedSlot*>(base + o_slot);
     a.ovf = reinterpret_cast<uint32_t*>(base + o_ovf);
     a.ovf2 = reinterpret_cast<uint32_t*>(base + o_ovf2);
     a.counters = reinterpret_cast<unsigned long long*>(base + o_ctr);
+    a.order_hist = reinterpret_cast<uint32_t*>(base + o_ctr +
+                                               sizeof(unsigned long long) * kNumCounters);
     a.ev_filter = reinterpret_cast<uint32_t*>(base + o_evf);
     a.ev_mode = reinterpret_cast<uint8_t*>(base + o_evm);
     a.dump = h->dump;
@@ -356,7 +363,7 @@ cudaError_t enqueue_batch(seedgb_seeding* h, Staging& st, uint32_t staged_events
                                       cudaMemcpyHostToDevice, s);
     if (err == cudaSuccess && copied) err = cudaEventRecord(copied, s);
     if (err == cudaSuccess)
-        err = cudaMemsetAsync(h->a.counters, 0, sizeof(unsigned long long) * kNumCounters, s);
+        err = cudaMemsetAsync(h->a.counters, 0, kCounterBytes, s);
     if (err == cudaSuccess && h->dc.mlp)
         err = cudaMemsetAsync(h->a.ev_filter, 0, sizeof(uint32_t) * 4 * grid.n_events, s);
     if (err == cudaSuccess)
@@ -754,7 +761,7 @@ seedgb_status seedgb_seeding_set_option(seedgb_seeding* h, seedgb_option opt, in
     return SEEDGB_INVALID_ARGUMENT;
 }
 
-seedgb_status seedgb_seeding_kernel_times(seedgb_seeding* h, float ms[8]) {
+seedgb_status seedgb_seeding_kernel_times(seedgb_seeding* h, float ms[9]) {
     if (!h || !ms || !h->timed_run) return SEEDGB_INVALID_ARGUMENT;
     if (cudaEventSynchronize(h->tev[kNumKernels]) != cudaSuccess) return SEEDGB_CUDA_ERROR;
     for (int i = 0; i < kNumKernels; ++i) {

@@ -14,6 +14,8 @@
 //   g_rs_gp     uint32[total_sp]            grid position of each g_rs entry
 //   bin_unsorted uint8[E][nbins]            bin too large to sort in shared memory
 //   items       uint2 [max_items]           (event, bin | chunk<<16) work items
+//   item_key    uint8 [max_items]           cost bucket of each work item
+//   items_ord   uint2 [max_items]           work items, most costly first
 //   seed_cnt    uint8 [total_sp]            seeds per middle spacepoint
 //   seed_slot   SeedSlot[total_sp][KMAX]    seeds per middle, in final order
 //   ovf         uint32[2 total_sp]          middles the fast kernel hands to the general path
@@ -21,6 +23,7 @@
 //   counters    uint64[kNumCounters]
 #pragma once
 
+#include <cstddef>
 #include <cstdint>
 
 #include "seedgb.h"
@@ -31,6 +34,7 @@ constexpr int kMaxSeedsPerMiddle = SEEDGB_MAX_SEEDS_PER_MIDDLE;
 constexpr int kMaxSegments = 64;      // neighbourhood bins per middle
 constexpr int kMaxBins = 4096;        // phi x z bins
 constexpr uint32_t kMaxEventsPerBatch = 65535;
+constexpr uint32_t kOrderBuckets = 256;  // log-scale cost buckets of the work items
 
 // Binning chunk geometry: NWB warps x RB rounds x 32 spacepoints, each warp a
 // contiguous run of spacepoints (stable order inside a bin).
@@ -61,6 +65,10 @@ enum Counter : int {
     kOvf2Fetch2 = 19,   // last-tier queue counter of the fallback pass
     kNumCounters = 24
 };
+// bytes of the per-batch counters and the work-item order histogram
+// (zeroed with one memset at the start of every batch)
+constexpr size_t kCounterBytes =
+    sizeof(unsigned long long) * kNumCounters + sizeof(uint32_t) * 2 * kOrderBuckets;
 
 struct MlpFrag;  // seedgb_mlp.cuh
 
@@ -153,6 +161,9 @@ struct Arena {
     uint32_t* g_rs_gp;      // [total_sp] grid position of each g_rs entry
     uint8_t* bin_unsorted;  // [E][nbins] bin too large to sort
     uint2* items;
+    uint8_t* item_key;      // [max_items] cost bucket of each item
+    uint2* items_ord;       // [max_items] items, most costly first
+    uint32_t* order_hist;   // [2 * kOrderBuckets] items per bucket, scatter cursors
     uint8_t* seed_cnt;
     SeedSlot* seed_slot;
     uint32_t* ovf;          // [2 * cap_sp] middles for the general path (middle tier)
@@ -188,7 +199,7 @@ DevConfig make_dev_config(const seedgb_seedfinder_config& f,
 // grid: the batch sizes that size the launch grids (the actual batch, or the
 // arena capacities when capturing a graph); the kernels read the actual
 // sizes from a.hdr.
-constexpr int kNumKernels = 8;
+constexpr int kNumKernels = 9;
 // Sets the kernels' shared-memory attributes on the current device (once).
 cudaError_t prepare_kernels();
 cudaError_t launch_seeding(const DevConfig& cfg, const Arena& a, const BatchHeader& grid,

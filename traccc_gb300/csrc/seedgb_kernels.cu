@@ -3,6 +3,7 @@
 // Pipeline for a batch of events (one launch each, all asynchronous):
 //   k_bin_count    validity + (phi, z) bin per spacepoint, per-warp histograms
 //   k_bin_scan     per event: stable offsets, bin ranges, work items
+//   k_item_order   work items in longest-processing-time order
 //   k_bin_scatter  stable counting-sort scatter into the binned SoA grid
 //   k_seed_fast    per work item (event, bin, chunk of middles): stage the
 //                  bin's neighbourhood in shared memory; one warp per middle
@@ -194,6 +195,15 @@ __device__ uint32_t block_exclusive_scan(uint32_t* data, uint32_t n, uint32_t* t
 // One CTA per event: turns the per-(chunk, warp) histograms into absolute
 // grid positions (bin-major, then spacepoint order), the bin ranges, the
 // number of valid spacepoints and the event's work items.
+// Log-scale bucket of a work item's estimated cost (8 buckets per power of
+// two, largest last).
+__device__ __forceinline__ uint32_t cost_bucket(unsigned long long cost) {
+    if (cost == 0) return 0;
+    const uint32_t e = 63u - static_cast<uint32_t>(__clzll(cost));  // floor(log2)
+    const uint32_t f = static_cast<uint32_t>(e >= 3 ? (cost >> (e - 3)) : (cost << (3 - e))) & 7u;
+    return min(8u * e + f, kOrderBuckets - 1u);
+}
+
 __global__ void __launch_bounds__(1024) k_bin_scan(DevConfig c, Arena a, uint32_t mpi) {
     extern __shared__ uint32_t sh[];
     const uint32_t e = blockIdx.x;
@@ -252,15 +262,76 @@ __global__ void __launch_bounds__(1024) k_bin_scan(DevConfig c, Arena a, uint32_
             run += v;
         }
     }
-    // work items: (event, bin | chunk << 16)
+    // work items: (event, bin | chunk << 16), with the bucket of their cost
+    // (middles x spacepoints of the bin's neighbourhood) for k_item_order
     for (uint32_t b = threadIdx.x; b < nb; b += blockDim.x) {
         const uint32_t i0 = items[b];
         const uint32_t i1 = (b + 1 < nb) ? items[b + 1] : n_items;
-        for (uint32_t k = i0; k < i1 && item_base + k < a.max_items; ++k)
+        const uint32_t size = ((b + 1 < nb) ? tot[b + 1] : n_valid) - tot[b];
+        uint32_t nbsize = 0;
+        {
+            uint32_t phis[kMaxSegments];
+            const uint32_t np = phi_zone(c, b % c.phi_bins, phis, kMaxSegments);
+            const uint32_t zb = b / c.phi_bins;
+            const uint32_t zlo = zb >= c.scope0 ? zb - c.scope0 : 0u;
+            const uint32_t zhi = min(zb + c.scope1, c.z_bins - 1u);
+            for (uint32_t ip = 0; ip < np; ++ip)
+                for (uint32_t z = zlo; z <= zhi; ++z) {
+                    const uint32_t nbin = phis[ip] + z * c.phi_bins;
+                    nbsize += ((nbin + 1 < nb) ? tot[nbin + 1] : n_valid) - tot[nbin];
+                }
+        }
+        for (uint32_t k = i0; k < i1 && item_base + k < a.max_items; ++k) {
             a.items[item_base + k] = make_uint2(e, b | ((k - i0) << 16));
+            const uint32_t m = min(mpi, size - (k - i0) * mpi);
+            const uint32_t q = cost_bucket(static_cast<unsigned long long>(m) * nbsize);
+            a.item_key[item_base + k] = static_cast<uint8_t>(q);
+            atomicAdd(&a.order_hist[q], 1u);
+        }
     }
     if (threadIdx.x == 0 && item_base + n_items > a.max_items)
         raise_status(a.counters, SEEDGB_CAPACITY_OVERFLOW);
+}
+
+// Work items in longest-processing-time order: the persistent seeding
+// kernel then ends on its cheapest items instead of whichever items the last
+// event appended, which leaves fewer SMs idle at its end.  A counting sort
+// over the cost buckets k_bin_scan recorded; the order inside a bucket is
+// arbitrary.  Results do not depend on the order of the items.
+__global__ void __launch_bounds__(1024) k_item_order(Arena a) {
+    __shared__ uint32_t start[kOrderBuckets];
+    const uint32_t n = static_cast<uint32_t>(
+        min(a.counters[kItemTotal], static_cast<unsigned long long>(a.max_items)));
+    if (blockIdx.x * blockDim.x >= n) return;
+    if (threadIdx.x < 32) {
+        // exclusive prefix over the buckets, most costly first
+        constexpr uint32_t kPer = kOrderBuckets / 32;
+        const uint32_t lane = threadIdx.x;
+        uint32_t v[kPer], sum = 0;
+#pragma unroll
+        for (uint32_t j = 0; j < kPer; ++j) {
+            v[j] = a.order_hist[kOrderBuckets - 1 - (kPer * lane + j)];
+            sum += v[j];
+        }
+        uint32_t incl = sum;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= static_cast<uint32_t>(o)) incl += t;
+        }
+        uint32_t run = incl - sum;
+#pragma unroll
+        for (uint32_t j = 0; j < kPer; ++j) {
+            start[kOrderBuckets - 1 - (kPer * lane + j)] = run;
+            run += v[j];
+        }
+    }
+    __syncthreads();
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        const uint32_t q = a.item_key[i];
+        const uint32_t k = start[q] + atomicAdd(&a.order_hist[kOrderBuckets + q], 1u);
+        if (k < n) a.items_ord[k] = a.items[i];
+    }
 }
 
 __global__ void __launch_bounds__(kBinWarps * 32) k_bin_scatter(DevConfig c, Arena a) {
@@ -1535,7 +1606,7 @@ __device__ __forceinline__ void seed_fast_items(const DevConfig& c, const Arena&
         __syncthreads();
         const uint32_t item = misc[0];
         if (item >= total_items) break;
-        const uint2 it = a.items[item];
+        const uint2 it = a.items_ord[item];
         const uint32_t e = it.x, bin = it.y & 0xffffu, ch = it.y >> 16;
         if (pass && !a.ev_mode[e]) {
             __syncthreads();  // misc[0] is rewritten by the next fetch
@@ -1977,12 +2048,14 @@ cudaError_t launch_seeding(const DevConfig& cfg, const Arena& a, const BatchHead
                                                       static_cast<uint32_t>(tp.middles_per_item));
     }
     mark(2);
+    k_item_order<<<(a.max_items + 1023) / 1024, 1024, 0, stream>>>(a);
+    mark(3);
     if (grid.total_chunks > 0) {
         k_bin_scatter<<<grid.total_chunks, kBinWarps * 32, hsm, stream>>>(cfg, a);
     }
-    mark(3);
-    k_bin_rsort<<<grid.n_events * cfg.nbins, 256, 0, stream>>>(cfg, a);
     mark(4);
+    k_bin_rsort<<<grid.n_events * cfg.nbins, 256, 0, stream>>>(cfg, a);
+    mark(5);
     const uint32_t mpi = static_cast<uint32_t>(tp.middles_per_item);
     const uint32_t nbc = static_cast<uint32_t>(tp.nb_cap);
     const dim3 fgrid(num_sms * tp.ctas_per_sm), fblock(tp.fast_warps * 32);
@@ -1991,10 +2064,10 @@ cudaError_t launch_seeding(const DevConfig& cfg, const Arena& a, const BatchHead
         ts.fast_warps = std::min(tp.fast_warps, kScoreWarps);
         k_seed_fast<true><<<fgrid, ts.fast_warps * 32, fast_kernel_smem(ts), stream>>>(
             cfg, a, mpi, nbc, 0u);
-        mark(5);
+        mark(6);
         k_seed_mid<true><<<num_sms, mid_kernel_warps(true) * 32, mid_kernel_smem(true), stream>>>(
             cfg, a, 0u);
-        mark(6);
+        mark(7);
         k_seed_slow<true><<<num_sms, 32, ssm, stream>>>(cfg, a, 0u);
         // fallback: events whose pruned fraction left the band, without the filter
         k_filter_mark<<<(grid.n_events + 255) / 256, 256, 0, stream>>>(cfg, a);
@@ -2004,15 +2077,15 @@ cudaError_t launch_seeding(const DevConfig& cfg, const Arena& a, const BatchHead
         k_seed_slow<false><<<num_sms, 32, ssm, stream>>>(cfg, a, 1u);
     } else {
         k_seed_fast<false><<<fgrid, fblock, fsm, stream>>>(cfg, a, mpi, nbc, 0u);
-        mark(5);
+        mark(6);
         k_seed_mid<false><<<num_sms, mid_kernel_warps(false) * 32, mid_kernel_smem(false),
                              stream>>>(cfg, a, 0u);
-        mark(6);
+        mark(7);
         k_seed_slow<false><<<num_sms, 32, ssm, stream>>>(cfg, a, 0u);
     }
-    mark(7);
-    k_seed_compact<<<grid.n_events, 1024, 0, stream>>>(a);
     mark(8);
+    k_seed_compact<<<grid.n_events, 1024, 0, stream>>>(a);
+    mark(9);
     return cudaGetLastError();
 }
 
