@@ -15,8 +15,9 @@ estimation (one launch per event).
           the launching stream, L2 flushed between steps by a 256 MiB write)
   e2e   : events/s through the public API from pinned host buffers: the
           spacepoint columns are copied in, seeds and parameters copied out
-          every step (two steps in flight: step k-1's results are copied out
-          on a second stream while step k computes)
+          every step (two steps in flight: step k+1's inputs are copied in
+          and step k-1's results copied out on two copy streams while step k
+          computes)
   cpu_baseline : the oracle (restated reference host seeding, libm phi) on a
           bounded sample of the same events, one event per host thread
 
@@ -202,7 +203,7 @@ def run_batched(args, dev, stream, flush_buf, inputs, model=None):
         tuned = {"shape": list(shape), "source": "searched", "measured": len(report),
                  "search_s": time.perf_counter() - t0,
                  "top3": report[:3], "default_ms": next(
-                     (r["ms"] for r in report if r["shape"][1:] == [128, 2560, 1]), None)}
+                     (r["ms"] for r in report if r["shape"][1:] == [256, 2048, 1]), None)}
     else:
         alg.set_tune(*shape)
         alg.graph_create(BATCH_EVENTS, total)
@@ -531,13 +532,17 @@ def run_gpu(args):
     alg.reserve(n_ev, total)
     alg.set_option(seeding.OPTION_KERNEL_TIMING, 1)
 
-    sps, meas = [], []
-    for e in range(n_ev):
-        a, b = int(offs[e]), int(offs[e + 1])
-        sps.append(seeding.SpacepointCollection(dcols["mi1"][a:b], dcols["mi2"][a:b],
-                                                dcols["glob"][a:b], dcols["zvar"][a:b],
-                                                dcols["rvar"][a:b]))
-        meas.append(seeding.MeasurementCollection(dcols["lp"][a:b], dcols["sl"][a:b]))
+    def make_views(cols):
+        sps, meas = [], []
+        for e in range(n_ev):
+            a, b = int(offs[e]), int(offs[e + 1])
+            sps.append(seeding.SpacepointCollection(cols["mi1"][a:b], cols["mi2"][a:b],
+                                                    cols["glob"][a:b], cols["zvar"][a:b],
+                                                    cols["rvar"][a:b]))
+            meas.append(seeding.MeasurementCollection(cols["lp"][a:b], cols["sl"][a:b]))
+        return sps, meas
+
+    sps, meas = make_views(dcols)
 
     def make_outputs():
         """Seed and parameter buffers of the 20 events, sizes in one array
@@ -557,18 +562,25 @@ def run_gpu(args):
     stream = torch.cuda.current_stream()
     flush_buf = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device=dev)
 
-    def step_device(outs=None):
+    def step_device(outs=None, ins=None):
         so, po = (souts, pouts) if outs is None else outs
-        alg.run_batch(sps, so, stream=stream)
+        sp, me = (sps, meas) if ins is None else ins
+        alg.run_batch(sp, so, stream=stream)
         for e in range(n_ev):
-            est(bfield, meas[e], sps[e], so[e], po[e], stream=stream)
+            est(bfield, me[e], sp[e], so[e], po[e], stream=stream)
 
-    # End to end, pipelined two deep: step k's inputs are copied in and its
-    # seeds and parameters computed on the compute stream while step k-1's
-    # results are copied out on a second stream (two output sets, two host
-    # result sets).  Every step copies its whole input in from pinned memory
-    # and its seeds and parameters out.
+    # End to end, pipelined two deep: step k's inputs are copied in on an
+    # input stream while step k-1 computes, step k's seeds and parameters are
+    # computed on the compute stream while step k-1's results are copied out
+    # on an output stream (two input sets, two output sets, two host result
+    # sets).  Every step copies its whole input in from pinned memory and its
+    # seeds and parameters out.
     out_sets = [(souts, pouts, size_all), make_outputs()]
+    dcols2 = {k: torch.empty_like(v) for k, v in dcols.items()}
+    in_sets = [(sps, meas), make_views(dcols2)]
+    in_cols = [dcols, dcols2]
+    h2d_stream = torch.cuda.Stream(device=dev)
+    h2d_done = [torch.cuda.Event() for _ in range(2)]
     copy_stream = torch.cuda.Stream(device=dev)
     h_sizes = [torch.zeros(2 * n_ev, dtype=torch.int32).pin_memory() for _ in range(2)]
     h_seeds = [[torch.empty((4, max(1, so.capacity)), dtype=torch.int32).pin_memory()
@@ -582,12 +594,17 @@ def run_gpu(args):
     def e2e_issue(k):
         b = k % 2
         so, po, sz = out_sets[b]
+        with torch.cuda.stream(h2d_stream):
+            # step k-2 computed from this input set
+            h2d_stream.wait_event(computed[b])
+            for key, col in in_cols[b].items():
+                col.copy_(pinned[key], non_blocking=True)
+            h2d_done[b].record(h2d_stream)
         # the copies of step k-2 read this output set
         stream.wait_event(copied[b])
         flush_buf.fill_(1)
-        for key in dcols:
-            dcols[key].copy_(pinned[key], non_blocking=True)
-        step_device((so, po))
+        stream.wait_event(h2d_done[b])
+        step_device((so, po), in_sets[b])
         h_sizes[b].copy_(sz, non_blocking=True)
         computed[b].record(stream)
 
@@ -798,7 +815,8 @@ def run_gpu(args):
                 "ms_per_step": e2e_s * 1e3 / args.steps,
                 "timing": "wall clock over all steps, host->device input copy, seeding, "
                           "parameters and device->host result copy of every step; two steps "
-                          "in flight (copies of step k-1 overlap step k)"},
+                          "in flight (the input copy of step k+1 and the result copy of "
+                          "step k-1 overlap step k, on two copy streams)"},
         "gpu_launches": len(seeding.KERNEL_NAMES) + n_ev,
         "kernel_ms_per_step": kernels,
         "wall_s_timed": wall,
