@@ -9,7 +9,7 @@ config is the reference default.
 
 One step = the whole stage for all 20 events: spacepoint binning, doublets,
 triplets, seed filtering (one batched launch sequence) and track-parameter
-estimation (one launch per event).
+estimation (one batched launch for all events).
 
   value : events/s with inputs resident in HBM (device time, CUDA events on
           the launching stream, L2 flushed between steps by a 256 MiB write)
@@ -566,8 +566,7 @@ def run_gpu(args):
         so, po = (souts, pouts) if outs is None else outs
         sp, me = (sps, meas) if ins is None else ins
         alg.run_batch(sp, so, stream=stream)
-        for e in range(n_ev):
-            est(bfield, me[e], sp[e], so[e], po[e], stream=stream)
+        est.run_batch(bfield, me, sp, so, po, stream=stream)
 
     # End to end, pipelined two deep: step k's inputs are copied in on an
     # input stream while step k-1 computes, step k's seeds and parameters are
@@ -817,7 +816,7 @@ def run_gpu(args):
                           "parameters and device->host result copy of every step; two steps "
                           "in flight (the input copy of step k+1 and the result copy of "
                           "step k-1 overlap step k, on two copy streams)"},
-        "gpu_launches": len(seeding.KERNEL_NAMES) + n_ev,
+        "gpu_launches": len(seeding.KERNEL_NAMES) + 1,
         "kernel_ms_per_step": kernels,
         "wall_s_timed": wall,
         "roofline": roofline,

@@ -505,6 +505,20 @@ seedgb_status seedgb_params_run(seedgb_params* h, const float bfield[3],
                                 const seedgb_seed_buffer* seeds,
                                 seedgb_params_buffer* out, void* stream);
 
+/* n_events calls of seedgb_params_run in one launch (no counterpart in the
+ * reference, whose operator() takes one event): element e of each host
+ * array describes event e.  Same results as the per-event calls.  The
+ * descriptors travel in one copy from a pinned buffer of the handle (two
+ * used in turn: the call waits only for the copy of the call before the
+ * previous one).  One stream per handle.  SEEDGB_SIZE_LIMIT above 65535
+ * events. */
+seedgb_status seedgb_params_run_batch(seedgb_params* h, const float bfield[3],
+                                      const seedgb_measurement_view* meas,
+                                      const seedgb_spacepoint_view* sps,
+                                      const seedgb_seed_buffer* seeds,
+                                      seedgb_params_buffer* outs, uint32_t n_events,
+                                      void* stream);
+
 /* ------------------------------------------------------------------------ */
 
 /* ------------------------------------------------------------------------ */

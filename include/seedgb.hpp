@@ -229,6 +229,31 @@ public:
         return out;
     }
 
+    /* Many events in one launch (element e of each vector is event e). */
+    std::vector<track_params_buffer> operator()(
+        const std::array<float, 3>& bfield,
+        const std::vector<seedgb_measurement_view>& measurements,
+        const std::vector<seedgb_spacepoint_view>& spacepoints,
+        const std::vector<seed_collection_buffer>& seeds) const {
+        if (measurements.size() != seeds.size() || spacepoints.size() != seeds.size())
+            throw std::invalid_argument("seed_parameter_estimation_algorithm(batch): sizes");
+        std::vector<track_params_buffer> out;
+        std::vector<seedgb_seed_buffer> sv;
+        std::vector<seedgb_params_buffer> pv;
+        out.reserve(seeds.size());
+        for (const auto& sb : seeds) {
+            out.emplace_back(sb.capacity());
+            sv.push_back(sb.view());
+            pv.push_back(out.back().view());
+        }
+        if (!seeds.empty())
+            check(seedgb_params_run_batch(h_, bfield.data(), measurements.data(),
+                                          spacepoints.data(), sv.data(), pv.data(),
+                                          static_cast<uint32_t>(seeds.size()), stream_),
+                  "seed_parameter_estimation_algorithm(batch)");
+        return out;
+    }
+
 private:
     cudaStream_t stream_;
     seedgb_params* h_ = nullptr;

@@ -11,11 +11,13 @@
 //   local_position f32[2 n_meas], surface_link u64[n_meas]
 // out.bin: uint32 n_seeds, seeds {u32 b, m, t; f32 q}[n_seeds],
 //   parameters seedgb_bound_track_parameters[n_seeds],
-//   uint32 batch seed counts [2] (the same event twice through the batch call)
+//   uint32 batch seed counts [2] (the same event twice through the batch call;
+//   the batch's parameters, one launch, must equal the single call's: exit 4)
 #include <cuda_runtime.h>
 
 #include <cstdio>
 #include <cstdlib>
+#include <cstring>
 #include <vector>
 
 #include "seedgb.hpp"
@@ -82,6 +84,17 @@ int main(int argc, char** argv) {
         seeding.check_status();
         uint32_t nb[2] = {static_cast<uint32_t>(batch[0].to_host(stream).size()),
                           static_cast<uint32_t>(batch[1].to_host(stream).size())};
+        // parameters of the batch in one launch: the same bytes as the
+        // single-event call
+        const auto bpars =
+            params({0.f, 0.f, finder.bFieldInZ}, std::vector<seedgb_measurement_view>{meas, meas},
+                   std::vector<seedgb_spacepoint_view>{sps, sps}, batch);
+        for (const auto& bp : bpars) {
+            const auto h = bp.to_host(stream);
+            if (h.size() != hp.size() ||
+                (!h.empty() && std::memcmp(h.data(), hp.data(), sizeof(h[0]) * h.size()) != 0))
+                return 4;
+        }
         // a rejected configuration is a std::domain_error, as in the reference
         bool threw = false;
         try {

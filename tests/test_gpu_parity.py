@@ -73,6 +73,29 @@ def test_params_match_oracle():
     assert ok.all(), np.nonzero(~ok)[0][:10]
 
 
+def test_params_batch_equals_per_event():
+    """seedgb_params_run_batch (one launch for several events) gives the same
+    bytes as one seedgb_params_run per event, and the oracle's parameters."""
+    import torch
+    evs = [synth.workload_event("trk1000", s) for s in (5, 6, 7)]
+    f, g, fl, tp = seeding.default_configs()
+    alg = seeding.TripletSeedingAlgorithm(f, g, fl)
+    sps = [seeding.SpacepointCollection.from_numpy(e) for e in evs]
+    meas = [seeding.MeasurementCollection.from_numpy(e) for e in evs]
+    outs = alg.run_batch(sps)
+    est = seeding.SeedParameterEstimationAlgorithm(tp)
+    bf = (0.0, 0.0, float(f.bFieldInZ))
+    batch = est.run_batch(bf, meas, sps, outs)
+    single = [est(bf, m, s, o) for m, s, o in zip(meas, sps, outs)]
+    torch.cuda.synchronize()
+    for e, ev in enumerate(evs):
+        a, b = batch[e].to_numpy(), single[e].to_numpy()
+        assert len(a) == len(b) > 0
+        assert a.tobytes() == b.tobytes()
+        ok = same_params(a, oracle.track_params(ev, outs[e].to_numpy(), bf))
+        assert ok.all()
+
+
 def test_pileup9k_event_matches_oracle():
     ev = synth.workload_event("pileup9k", 0)
     alg, sps, out, st = run_gpu(ev)

@@ -68,9 +68,28 @@ struct seedgb_seeding {
     cudaEvent_t tev[kNumKernels + 1] = {};
 };
 
+// Descriptors of a batched parameter estimation: pinned host copy and
+// device copy, two slots used in turn so that the host fills one while the
+// previous call's copy of the other may still be in flight.
+struct ParamsSlot {
+    seedgb::ParamsEvent* host = nullptr;
+    seedgb::ParamsEvent* dev = nullptr;
+    uint32_t cap = 0;
+    cudaEvent_t copied = nullptr;
+};
+
 struct seedgb_params {
     ParamsConfig pc;
     int num_sms = 0;
+    ParamsSlot slot[2];
+    int next = 0;
+    ~seedgb_params() {
+        for (auto& s : slot) {
+            if (s.copied) cudaEventDestroy(s.copied);
+            if (s.host) cudaFreeHost(s.host);
+            if (s.dev) cudaFree(s.dev);
+        }
+    }
 };
 
 namespace seedgb {
@@ -808,6 +827,50 @@ seedgb_status seedgb_params_run(seedgb_params* h, const float bfield[3],
         return SEEDGB_INVALID_ARGUMENT;
     return cuda_status(launch_params(h->pc, bfield, *meas, *sps, *seeds, *out, h->num_sms,
                                      static_cast<cudaStream_t>(stream)));
+}
+
+seedgb_status seedgb_params_run_batch(seedgb_params* h, const float bfield[3],
+                                      const seedgb_measurement_view* meas,
+                                      const seedgb_spacepoint_view* sps,
+                                      const seedgb_seed_buffer* seeds,
+                                      seedgb_params_buffer* outs, uint32_t n_events,
+                                      void* stream) {
+    if (!h || !bfield || (n_events && (!meas || !sps || !seeds || !outs)))
+        return SEEDGB_INVALID_ARGUMENT;
+    if (n_events == 0) return SEEDGB_OK;
+    if (n_events > 65535u) return SEEDGB_SIZE_LIMIT;
+    for (uint32_t e = 0; e < n_events; ++e)
+        if (!seeds[e].size || !outs[e].size) return SEEDGB_INVALID_ARGUMENT;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    ParamsSlot& sl = h->slot[h->next];
+    // the previous copy out of this slot's pinned descriptors must be done
+    if (sl.copied && cudaEventSynchronize(sl.copied) != cudaSuccess) return SEEDGB_CUDA_ERROR;
+    if (sl.cap < n_events) {
+        // in-flight launches may still read the old device descriptors
+        if (sl.dev && cudaDeviceSynchronize() != cudaSuccess) return SEEDGB_CUDA_ERROR;
+        if (sl.host) cudaFreeHost(sl.host);
+        if (sl.dev) cudaFree(sl.dev);
+        sl.host = nullptr;
+        sl.dev = nullptr;
+        sl.cap = 0;
+        const uint32_t cap = std::max(n_events, 64u);
+        if (cudaMallocHost(reinterpret_cast<void**>(&sl.host), sizeof(seedgb::ParamsEvent) * cap) !=
+                cudaSuccess ||
+            cudaMalloc(reinterpret_cast<void**>(&sl.dev), sizeof(seedgb::ParamsEvent) * cap) !=
+                cudaSuccess)
+            return SEEDGB_CUDA_ERROR;
+        sl.cap = cap;
+    }
+    if (!sl.copied && cudaEventCreateWithFlags(&sl.copied, cudaEventDisableTiming) != cudaSuccess)
+        return SEEDGB_CUDA_ERROR;
+    for (uint32_t e = 0; e < n_events; ++e)
+        sl.host[e] = seedgb::ParamsEvent{meas[e], sps[e], seeds[e], outs[e]};
+    if (cudaMemcpyAsync(sl.dev, sl.host, sizeof(seedgb::ParamsEvent) * n_events,
+                        cudaMemcpyHostToDevice, s) != cudaSuccess ||
+        cudaEventRecord(sl.copied, s) != cudaSuccess)
+        return SEEDGB_CUDA_ERROR;
+    h->next ^= 1;
+    return cuda_status(launch_params_batch(h->pc, bfield, sl.dev, n_events, h->num_sms, s));
 }
 
 }  // extern "C"

@@ -219,6 +219,17 @@ cudaError_t launch_params(const ParamsConfig& cfg, const float bfield[3],
                           const seedgb_params_buffer& out, int num_sms,
                           cudaStream_t stream);
 
+// One event of a batched parameter estimation (device-side descriptor).
+struct ParamsEvent {
+    seedgb_measurement_view meas;
+    seedgb_spacepoint_view sps;
+    seedgb_seed_buffer seeds;
+    seedgb_params_buffer out;
+};
+cudaError_t launch_params_batch(const ParamsConfig& cfg, const float bfield[3],
+                                const ParamsEvent* events, uint32_t n_events, int num_sms,
+                                cudaStream_t stream);
+
 size_t fast_kernel_smem(const TuneParams& tp);
 // Packs the host-side network into the fragment layout the kernels read.
 void pack_mlp_frag(const seedgb_doublet_filter& m, MlpFrag& f);

@@ -1888,16 +1888,16 @@ __device__ __forceinline__ float perp2(float a, float b) { return sqrtf(a * a + 
 // track_params_estimation_helper.hpp:48-129) and the covariance of
 // core/src/seeding/track_params_estimation.cpp:59-86.  Frame algebra with
 // point_to_local(p) = R^T (p - t), rotate(v) = R v, R = [x y z] columns.
-__global__ void __launch_bounds__(128)
-k_params(ParamsConfig c, float bx, float by, float bz, seedgb_measurement_view meas,
-         seedgb_spacepoint_view sps, seedgb_seed_buffer seeds, seedgb_params_buffer out) {
-    const uint32_t n = min(*seeds.size, seeds.capacity);
-    const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        if (i >= out.capacity) break;
+// Parameters of seed i of one event into out.data[i].
+__device__ __forceinline__ void params_of_seed(const ParamsConfig& c, float bx, float by,
+                                               float bz, const seedgb_measurement_view& meas,
+                                               const seedgb_spacepoint_view& sps,
+                                               const seedgb_seed_buffer& seeds,
+                                               const seedgb_params_buffer& out, uint32_t i) {
+    {
         const uint32_t ib = seeds.bottom_index[i], im = seeds.middle_index[i],
                        it = seeds.top_index[i];
-        if (ib >= sps.size || im >= sps.size || it >= sps.size) continue;
+        if (ib >= sps.size || im >= sps.size || it >= sps.size) return;
         const float gB[3] = {sps.global[3 * ib], sps.global[3 * ib + 1], sps.global[3 * ib + 2]};
         const float gM[3] = {sps.global[3 * im], sps.global[3 * im + 1], sps.global[3 * im + 2]};
         const float gT[3] = {sps.global[3 * it], sps.global[3 * it + 1], sps.global[3 * it + 2]};
@@ -1965,7 +1965,30 @@ k_params(ParamsConfig c, float bx, float by, float bz, seedgb_measurement_view m
         }
         out.data[i] = p;
     }
+}
+
+__global__ void __launch_bounds__(128)
+k_params(ParamsConfig c, float bx, float by, float bz, seedgb_measurement_view meas,
+         seedgb_spacepoint_view sps, seedgb_seed_buffer seeds, seedgb_params_buffer out) {
+    const uint32_t n = min(*seeds.size, seeds.capacity);
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < min(n, out.capacity);
+         i += stride)
+        params_of_seed(c, bx, by, bz, meas, sps, seeds, out, i);
     if (blockIdx.x == 0 && threadIdx.x == 0) *out.size = min(n, out.capacity);
+}
+
+// Many events in one launch: blockIdx.y is the event, the x blocks stride
+// over its seeds.
+__global__ void __launch_bounds__(128)
+k_params_batch(ParamsConfig c, float bx, float by, float bz, const ParamsEvent* events) {
+    const ParamsEvent& ev = events[blockIdx.y];
+    const uint32_t n = min(*ev.seeds.size, ev.seeds.capacity);
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < min(n, ev.out.capacity);
+         i += stride)
+        params_of_seed(c, bx, by, bz, ev.meas, ev.sps, ev.seeds, ev.out, i);
+    if (blockIdx.x == 0 && threadIdx.x == 0) *ev.out.size = min(n, ev.out.capacity);
 }
 
 }  // namespace
@@ -2097,6 +2120,16 @@ cudaError_t launch_params(const ParamsConfig& cfg, const float bfield[3],
                           int num_sms, cudaStream_t stream) {
     k_params<<<num_sms * 4, 128, 0, stream>>>(cfg, bfield[0], bfield[1], bfield[2], meas, sps,
                                                seeds, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_params_batch(const ParamsConfig& cfg, const float bfield[3],
+                                const ParamsEvent* events, uint32_t n_events, int num_sms,
+                                cudaStream_t stream) {
+    if (n_events == 0) return cudaSuccess;
+    const uint32_t gx = std::max(1u, (static_cast<uint32_t>(num_sms) * 4 + n_events - 1) / n_events);
+    k_params_batch<<<dim3(gx, n_events), 128, 0, stream>>>(cfg, bfield[0], bfield[1], bfield[2],
+                                                           events);
     return cudaGetLastError();
 }
 

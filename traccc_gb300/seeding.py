@@ -253,6 +253,10 @@ def lib():
                                         P(_SpacepointView), P(_SeedBuffer),
                                         P(_ParamsBuffer), vp]
         L.seedgb_params_run.restype = C.c_int
+        L.seedgb_params_run_batch.argtypes = [vp, P(C.c_float), P(_MeasurementView),
+                                              P(_SpacepointView), P(_SeedBuffer),
+                                              P(_ParamsBuffer), C.c_uint32, vp]
+        L.seedgb_params_run_batch.restype = C.c_int
         L.seedgb_spacepoint_binning_noalloc.argtypes = [
             P(SeedfinderConfig), P(SpacepointGridConfig), P(_SpacepointView), vp, vp, vp]
         L.seedgb_spacepoint_binning_noalloc.restype = C.c_int
@@ -736,3 +740,22 @@ class SeedParameterEstimationAlgorithm:
                                        C.byref(sb), C.byref(pb), _stream_ptr(stream)),
                "seedgb_params_run")
         return out
+
+    def run_batch(self, bfield, measurements, spacepoints, seeds, outs=None, stream=None):
+        """Parameters of many events in one launch (seedgb_params_run_batch):
+        element e of each list belongs to event e."""
+        n = len(seeds)
+        if not (len(measurements) == len(spacepoints) == n):
+            raise ValueError("one measurement and spacepoint collection per seed buffer")
+        if outs is None:
+            outs = [ParamsBuffer(s.capacity, device=sp.global_.device)
+                    for s, sp in zip(seeds, spacepoints)]
+        bf = (C.c_float * 3)(*[float(x) for x in bfield])
+        mv = (_MeasurementView * n)(*[m.view() for m in measurements])
+        sv = (_SpacepointView * n)(*[sp.view() for sp in spacepoints])
+        sb = (_SeedBuffer * n)(*[s.buf() for s in seeds])
+        pb = (_ParamsBuffer * n)(*[o.buf() for o in outs])
+        _check(lib().seedgb_params_run_batch(self._h, bf, mv, sv, sb, pb, n,
+                                             _stream_ptr(stream)),
+               "seedgb_params_run_batch")
+        return outs
