@@ -267,10 +267,10 @@ seedgb_status seedgb_seeding_set_option(seedgb_seeding* h, seedgb_option opt,
 /* Device durations (ms) of the kernels of the last run with
  * SEEDGB_OPTION_KERNEL_TIMING on, in launch order: bin_count, bin_scan,
  * item_order, bin_scatter, bin_rsort, seed_fast, seed_mid, seed_slow,
- * seed_compact (with the learned filter, seed_slow also covers the fallback
- * pass).  Waits for the last recorded event.  Returns
+ * seed_count, seed_compact (with the learned filter, seed_slow also covers
+ * the fallback pass).  Waits for the last recorded event.  Returns
  * SEEDGB_INVALID_ARGUMENT if timing was off. */
-seedgb_status seedgb_seeding_kernel_times(seedgb_seeding* h, float ms[9]);
+seedgb_status seedgb_seeding_kernel_times(seedgb_seeding* h, float ms[10]);
 
 /* ------------------------------------------------------------------------ */
 /* Spacepoint formation (the step in front of the seeding path)              */

@@ -249,6 +249,7 @@ seedgb_status ensure_arena(seedgb_seeding* h, uint32_t n_events, uint64_t total_
     const size_t o_iord = take(sizeof(uint2) * ci);
     const size_t o_cnt = take(sizeof(uint8_t) * cs);
     const size_t o_slot = take(sizeof(SeedSlot) * cs * kMaxSeedsPerMiddle);
+    const size_t o_cseeds = take(sizeof(uint32_t) * static_cast<size_t>(cc));
     const size_t o_ovf = take(sizeof(uint32_t) * cs * 2);
     const size_t o_ovf2 = take(sizeof(uint32_t) * cs * 2);
     // the counters and the work-item order histogram are zeroed together
@@ -295,6 +296,7 @@ seedgb_status ensure_arena(seedgb_seeding* h, uint32_t n_events, uint64_t total_
     a.items_ord = reinterpret_cast<uint2*>(base + o_iord);
     a.seed_cnt = reinterpret_cast<uint8_t*>(base + o_cnt);
     a.seed_slot = reinterpret_cast<SeedSlot*>(base + o_slot);
+    a.chunk_seeds = reinterpret_cast<uint32_t*>(base + o_cseeds);
     a.ovf = reinterpret_cast<uint32_t*>(base + o_ovf);
     a.ovf2 = reinterpret_cast<uint32_t*>(base + o_ovf2);
     a.counters = reinterpret_cast<unsigned long long*>(base + o_ctr);
@@ -780,7 +782,7 @@ seedgb_status seedgb_seeding_set_option(seedgb_seeding* h, seedgb_option opt, in
     return SEEDGB_INVALID_ARGUMENT;
 }
 
-seedgb_status seedgb_seeding_kernel_times(seedgb_seeding* h, float ms[9]) {
+seedgb_status seedgb_seeding_kernel_times(seedgb_seeding* h, float ms[10]) {
     if (!h || !ms || !h->timed_run) return SEEDGB_INVALID_ARGUMENT;
     if (cudaEventSynchronize(h->tev[kNumKernels]) != cudaSuccess) return SEEDGB_CUDA_ERROR;
     for (int i = 0; i < kNumKernels; ++i) {

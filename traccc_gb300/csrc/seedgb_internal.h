@@ -18,6 +18,7 @@
 //   items_ord   uint2 [max_items]           work items, most costly first
 //   seed_cnt    uint8 [total_sp]            seeds per middle spacepoint
 //   seed_slot   SeedSlot[total_sp][KMAX]    seeds per middle, in final order
+//   chunk_seeds uint32[chunks]              seeds of each 2048-middle chunk
 //   ovf         uint32[2 total_sp]          middles the fast kernel hands to the general path
 //   ovf2        uint32[2 total_sp]          middles beyond the general path's middle tier
 //   counters    uint64[kNumCounters]
@@ -166,6 +167,7 @@ struct Arena {
     uint32_t* order_hist;   // [2 * kOrderBuckets] items per bucket, scatter cursors
     uint8_t* seed_cnt;
     SeedSlot* seed_slot;
+    uint32_t* chunk_seeds;  // [cap_chunks] seeds of each binning chunk of middles
     uint32_t* ovf;          // [2 * cap_sp] middles for the general path (middle tier)
     uint32_t* ovf2;         // [2 * cap_sp] middles for its last, large-capacity tier
     unsigned long long* counters;
@@ -199,7 +201,7 @@ DevConfig make_dev_config(const seedgb_seedfinder_config& f,
 // grid: the batch sizes that size the launch grids (the actual batch, or the
 // arena capacities when capturing a graph); the kernels read the actual
 // sizes from a.hdr.
-constexpr int kNumKernels = 9;
+constexpr int kNumKernels = 10;
 // Sets the kernels' shared-memory attributes on the current device (once).
 cudaError_t prepare_kernels();
 cudaError_t launch_seeding(const DevConfig& cfg, const Arena& a, const BatchHeader& grid,

@@ -16,7 +16,9 @@
 //                  neighbourhood from global memory, many warps per SM
 //   k_seed_slow    the same with large capacities, one warp per SM, for the
 //                  few middles whose lists overflow k_seed_mid's buffers
-//   k_seed_compact per event: seeds in host order into the output buffer
+//   k_seed_count   seeds per chunk of middles
+//   k_seed_compact per chunk of middles: seeds in host order into the output
+//                  buffers
 //
 // Floating-point semantics follow the reference host code: the file is built
 // with -fmad=false --prec-div=true --prec-sqrt=true --ftz=false, and every
@@ -1825,42 +1827,94 @@ __global__ void k_filter_mark(DevConfig c, Arena a) {
     if (mode) atomicAdd(&a.counters[kFallbackEvents], 1ull);
 }
 
-// Seeds of one event in host order (bin, middle, rank) into its buffer.
-__global__ void __launch_bounds__(1024) k_seed_compact(Arena a) {
-    __shared__ uint32_t tmp[33];
-    const uint32_t e = blockIdx.x;
-    if (e >= a.hdr->n_events) return;
-    const EventDesc ev = a.events[e];
-    const uint32_t nv = a.n_valid[e];
-    const uint32_t t = threadIdx.x, nt = blockDim.x;
-    const uint32_t per = (nv + nt - 1) / nt;
-    const uint32_t i0 = ev.sp_base + min(nv, t * per), i1 = ev.sp_base + min(nv, (t + 1) * per);
-    uint32_t s = 0;
-    for (uint32_t i = i0; i < i1; ++i) s += a.seed_cnt[i];
-    const uint32_t lane = t & 31, warp = t >> 5;
-    uint32_t incl = s;
+// Sum of v over the block (512 threads); every thread gets the total.
+__device__ __forceinline__ uint32_t block_sum_512(uint32_t v, uint32_t* sh) {
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    __syncthreads();
+    if (lane == 0) sh[warp] = v;
+    __syncthreads();
+    uint32_t t = lane < (blockDim.x >> 5) ? sh[lane] : 0u;
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    return t;
+}
+
+// Exclusive prefix of v over the block (in thread order); total in *total.
+__device__ __forceinline__ uint32_t block_exclusive_512(uint32_t v, uint32_t* sh,
+                                                        uint32_t* total) {
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    uint32_t incl = v;
     for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= static_cast<uint32_t>(o)) incl += v;
+        const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= static_cast<uint32_t>(o)) incl += t;
     }
-    if (lane == 31) tmp[warp] = incl;
+    __syncthreads();
+    if (lane == 31) sh[warp] = incl;
     __syncthreads();
     if (warp == 0) {
-        const uint32_t nw = nt / 32;
-        const uint32_t w = lane < nw ? tmp[lane] : 0u;
+        const uint32_t w = lane < nw ? sh[lane] : 0u;
         uint32_t wi = w;
         for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t v = __shfl_up_sync(0xffffffffu, wi, o);
-            if (lane >= static_cast<uint32_t>(o)) wi += v;
+            const uint32_t t = __shfl_up_sync(0xffffffffu, wi, o);
+            if (lane >= static_cast<uint32_t>(o)) wi += t;
         }
-        if (lane < nw) tmp[lane] = wi - w;
-        if (lane == 31) tmp[32] = wi;
+        if (lane < nw) sh[lane] = wi - w;
+        if (lane == 31) sh[32] = wi;
     }
     __syncthreads();
-    uint32_t o = tmp[warp] + incl - s;
-    const uint32_t total = tmp[32];
-    for (uint32_t i = i0; i < i1; ++i) {
-        const uint32_t cnt = a.seed_cnt[i];
+    *total = sh[32];
+    return sh[warp] + incl - v;
+}
+
+// Seeds of every chunk of kBinChunk middles (the binning chunks; chunk c of
+// an event covers its grid positions sp_base + c kBinChunk onwards).  Also
+// sets the seed count of events without spacepoints, which have no chunk.
+__global__ void __launch_bounds__(512) k_seed_count(Arena a) {
+    __shared__ uint32_t sh[33];
+    const BatchHeader hb = *a.hdr;
+    if (blockIdx.x < hb.n_events && threadIdx.x == 0) {
+        const EventDesc& ev = a.events[blockIdx.x];
+        if (ev.n_chunks == 0) *ev.out_size = 0;
+    }
+    const uint32_t chunk = blockIdx.x;
+    if (chunk >= hb.total_chunks) return;
+    const uint32_t e = event_of_chunk(a, hb.n_events, chunk);
+    const EventDesc ev = a.events[e];
+    const uint32_t end = ev.sp_base + a.n_valid[e];
+    const uint32_t m0 = ev.sp_base + (chunk - ev.chunk_base) * kBinChunk;
+    const uint32_t m1 = min(m0 + kBinChunk, end);
+    uint32_t s = 0;
+    for (uint32_t i = m0 + threadIdx.x; i < m1; i += blockDim.x) s += a.seed_cnt[i];
+    s = block_sum_512(s, sh);
+    if (threadIdx.x == 0) a.chunk_seeds[chunk] = s;
+}
+
+// The seeds of every event in host order (middles in grid order, each
+// middle's seeds in final order) into the caller's buffer: each chunk starts
+// after its event's earlier chunks and writes its middles' seeds in rounds
+// of one middle per thread.  The event's last chunk with middles (chunk 0
+// when it has none) sets the seed count.
+__global__ void __launch_bounds__(512) k_seed_compact(Arena a) {
+    __shared__ uint32_t sh[33];
+    const BatchHeader hb = *a.hdr;
+    const uint32_t chunk = blockIdx.x;
+    if (chunk >= hb.total_chunks) return;
+    const uint32_t e = event_of_chunk(a, hb.n_events, chunk);
+    const EventDesc ev = a.events[e];
+    const uint32_t nv = a.n_valid[e];
+    const uint32_t c = chunk - ev.chunk_base;
+    const uint32_t last = nv ? (nv - 1) / kBinChunk : 0u;
+    if (c > last) return;
+    uint32_t before = 0;
+    for (uint32_t k = threadIdx.x; k < c; k += blockDim.x) before += a.chunk_seeds[ev.chunk_base + k];
+    uint32_t run = block_sum_512(before, sh);
+    const uint32_t m0 = ev.sp_base + c * kBinChunk;
+    const uint32_t m1 = min(m0 + kBinChunk, ev.sp_base + nv);
+    for (uint32_t r0 = m0; r0 < m1; r0 += blockDim.x) {
+        const uint32_t i = r0 + threadIdx.x;
+        const uint32_t cnt = i < m1 ? a.seed_cnt[i] : 0u;
+        uint32_t round_total;
+        uint32_t o = run + block_exclusive_512(cnt, sh, &round_total);
         for (uint32_t k = 0; k < cnt; ++k, ++o) {
             if (o < ev.out_cap) {
                 const SeedSlot sl = a.seed_slot[static_cast<size_t>(i) * kMaxSeedsPerMiddle + k];
@@ -1870,11 +1924,12 @@ __global__ void __launch_bounds__(1024) k_seed_compact(Arena a) {
                 ev.out_q[o] = sl.q;
             }
         }
+        run += round_total;
     }
-    if (t == 0) {
-        *ev.out_size = min(total, ev.out_cap);
-        atomicAdd(&a.counters[kNumSeeds], static_cast<unsigned long long>(total));
-        if (total > ev.out_cap) raise_status(a.counters, SEEDGB_CAPACITY_OVERFLOW);
+    if (c == last && threadIdx.x == 0) {
+        *ev.out_size = min(run, ev.out_cap);
+        atomicAdd(&a.counters[kNumSeeds], static_cast<unsigned long long>(run));
+        if (run > ev.out_cap) raise_status(a.counters, SEEDGB_CAPACITY_OVERFLOW);
     }
 }
 
@@ -2108,8 +2163,10 @@ cudaError_t launch_seeding(const DevConfig& cfg, const Arena& a, const BatchHead
         k_seed_slow<false><<<num_sms, 32, ssm, stream>>>(cfg, a, 0u);
     }
     mark(8);
-    k_seed_compact<<<grid.n_events, 1024, 0, stream>>>(a);
+    k_seed_count<<<std::max(std::max(grid.total_chunks, grid.n_events), 1u), 512, 0, stream>>>(a);
     mark(9);
+    k_seed_compact<<<std::max(grid.total_chunks, 1u), 512, 0, stream>>>(a);
+    mark(10);
     return cudaGetLastError();
 }
 

@@ -142,7 +142,7 @@ NOALLOC_MAX_SPACEPOINTS = 65536
 OPTION_EXHAUSTIVE_TRIPLETS = 1
 OPTION_KERNEL_TIMING = 2
 KERNEL_NAMES = ("bin_count", "bin_scan", "item_order", "bin_scatter", "bin_rsort",
-                "seed_fast", "seed_mid", "seed_slow", "seed_compact")
+                "seed_fast", "seed_mid", "seed_slow", "seed_count", "seed_compact")
 
 PARAMS_DTYPE = np.dtype([("surface_link", "<u8"), ("params", "<f4", (6,)),
                          ("cov", "<f4", (36,))])
