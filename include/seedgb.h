@@ -259,7 +259,11 @@ typedef enum {
     SEEDGB_OPTION_EXHAUSTIVE_TRIPLETS = 1,
     /* 1: record CUDA events around every kernel of a run on the run's stream
      * (read back with seedgb_seeding_kernel_times) */
-    SEEDGB_OPTION_KERNEL_TIMING = 2
+    SEEDGB_OPTION_KERNEL_TIMING = 2,
+    /* 1: the general path's middle tier (k_seed_mid) hands every middle it
+     * receives on to the last, large-capacity tier (verification of that
+     * tier; the results are identical, only slower) */
+    SEEDGB_OPTION_LAST_TIER_ONLY = 3
 } seedgb_option;
 seedgb_status seedgb_seeding_set_option(seedgb_seeding* h, seedgb_option opt,
                                         int64_t value);

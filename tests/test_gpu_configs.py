@@ -125,24 +125,29 @@ def test_variance_event_matches_oracle(variant):
 
 def test_general_path_tiers_match_oracle():
     """A staging capacity too small for any neighbourhood sends every middle
-    to the general path.  On a 100k-spacepoint event every list fits the
-    middle tier; the densest event of an uneven batch (114k spacepoints) has
-    middles with more triplets or middle-top doublets than the middle tier
-    holds, which go on to the last tier.  Seeds equal the oracle's."""
+    to the general path; its middle tier seeds them (lists above the fast
+    capacities included), and with SEEDGB_OPTION_LAST_TIER_ONLY the last,
+    large-capacity tier seeds all of them.  Seeds equal the oracle's on a
+    100k-spacepoint event and on the densest event of an uneven batch."""
     import torch
     dense = max(synth.batch_events(64, 3), key=lambda e: len(e["global"]))
     assert len(dense["global"]) > 110000
-    for ev, want_last in ((synth.workload_event("pileup9k", 6), False), (dense, True)):
-        alg = seeding.TripletSeedingAlgorithm()
-        alg.set_tune(16, 256, 256, 1)
-        out = alg(seeding.SpacepointCollection.from_numpy(ev))
-        torch.cuda.synchronize()
-        assert alg.last_status() == seeding.OK
-        c = alg.counters()
-        assert c["n_overflow_middles"] >= 0.9 * c["n_valid"] > 0
-        assert (c["n_last_tier_middles"] > 0) == want_last, c
+    for ev in (synth.workload_event("pileup9k", 6), dense):
         ref, _ = O.seeding(ev, phi_mode=O.PHI_CR)
-        assert np.array_equal(out.to_numpy(), ref)
+        for last_only in (False, True):
+            alg = seeding.TripletSeedingAlgorithm()
+            alg.set_tune(16, 256, 256, 1)
+            alg.set_option(seeding.OPTION_LAST_TIER_ONLY, int(last_only))
+            out = alg(seeding.SpacepointCollection.from_numpy(ev))
+            torch.cuda.synchronize()
+            assert alg.last_status() == seeding.OK
+            c = alg.counters()
+            assert c["n_overflow_middles"] >= 0.9 * c["n_valid"] > 0
+            if last_only:
+                assert c["n_last_tier_middles"] == c["n_overflow_middles"], c
+            else:
+                assert c["n_last_tier_middles"] == 0, c
+            assert np.array_equal(out.to_numpy(), ref)
 
 
 def test_zbins_dense_event():

@@ -146,6 +146,7 @@ DevConfig make_dev_config(const seedgb_seedfinder_config& f,
     d.z_min = ax.z_min;
     d.z_max = ax.z_max;
     d.brute_force_triplets = 0;
+    d.last_tier_only = 0;
     d.mlp = nullptr;
     d.band_lo = 0.f;
     d.band_hi = 1.f;
@@ -770,6 +771,10 @@ seedgb_status seedgb_seeding_set_option(seedgb_seeding* h, seedgb_option opt, in
         case SEEDGB_OPTION_EXHAUSTIVE_TRIPLETS:
             h->dc.brute_force_triplets = value ? 1u : 0u;
             h->g_valid = false;  // the configuration is baked into the graphs
+            return SEEDGB_OK;
+        case SEEDGB_OPTION_LAST_TIER_ONLY:
+            h->dc.last_tier_only = value ? 1u : 0u;
+            h->g_valid = false;
             return SEEDGB_OK;
         case SEEDGB_OPTION_KERNEL_TIMING:
             if (value && !h->tev[0]) {

@@ -97,6 +97,7 @@ struct DevConfig {
     float phi_min, phi_max, z_min, z_max;
     // behaviour switches (tests)
     uint32_t brute_force_triplets;  // 1: test every MB x MT pair (no cot window)
+    uint32_t last_tier_only;        // 1: the general path's middle tier passes every middle on
     // learned doublet filter: nullptr = plain seeding
     const MlpFrag* mlp;         // weight fragments and biases (device)
     float band_lo, band_hi;     // pruned-fraction band; outside it: plain re-run

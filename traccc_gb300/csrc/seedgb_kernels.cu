@@ -672,7 +672,7 @@ struct NbViewT {
     }
 };
 
-constexpr int kBuckets = 256;  // cot(theta) buckets of the middle-top doublets
+constexpr int kBuckets = 160;  // cot(theta) buckets of the middle-top doublets
 
 // A triplet of the middle spacepoint (before the compatible-seed weights).
 struct TripCand {
@@ -698,6 +698,12 @@ struct Stage1Cand {
 
 template <int CAPB, int CAPT, int CAPLC, int CAPCT>
 struct WarpScratch {
+    // the host-order sort pads the triplets to the next power of two
+    static_assert((CAPCT & (CAPCT - 1)) == 0, "triplet capacity must be a power of two");
+    // the bucket prefix gives kBuckets / 32 buckets to each lane, and the
+    // learned filter uses bstart as 160 words of scratch
+    static_assert(kBuckets % 32 == 0 && kBuckets + 1 >= 160, "cot buckets");
+    static_assert(CAPB <= 65536 && CAPT <= 65536 && CAPLC <= 65536, "16-bit positions");
     union {
         // middle-top doublets in list order: {cot(theta), iDeltaR, U, V}
         float4 mtd[CAPLC];
@@ -728,14 +734,18 @@ struct WarpScratch {
     };
     TripCand ct[CAPCT];   // triplets of the middle
 };
-// shared memory per warp: fast 13.5 KiB, slow 173 KiB.  Fast capacities: 640
-// middle-bottom and 1024 middle-top candidates (the largest lists on a batch
-// of 5k-114k-spacepoint events: 497 and 383), 256 middle-top doublets and 128
-// triplets (exceeded by fewer than 0.3 % and 0.2 % of that batch's middles);
-// a middle beyond one of them is seeded by the large-capacity kernel.
-// Smaller scratch means more warps per SM, which is what hides this kernel's
-// latency.
-using FastScratch = WarpScratch<640, 1024, 256, 128>;
+// Shared memory per warp: fast 11.9 KiB, middle tier 22.1 KiB, last tier
+// 173 KiB.  The fast capacities sit at the measured list sizes so that 16
+// warps fit beside a 2048-spacepoint neighbourhood (smaller scratch means more
+// warps per SM, which is what hides this kernel's latency): 512 middle-bottom
+// and 1024 middle-top candidates (largest lists on a batch of
+// 5k-114k-spacepoint events: 497 and 383), 216 middle-top doublets and 128
+// triplets (at most 208 and 101 on 100k-spacepoint events; a few per cent of
+// the batch's middles exceed them).  A middle beyond a fast capacity goes to
+// the general path's middle tier, whose capacities are above every list
+// measured; the last tier takes what exceeds those.
+using FastScratch = WarpScratch<512, 1024, 216, 128>;
+using MidScratch = WarpScratch<1024, 1024, 512, 256>;
 using SlowScratch = WarpScratch<8192, 8192, 4096, 2048>;
 
 // Keep the positions whose doublet passes the minimum-helix-radius test, in
@@ -1680,7 +1690,7 @@ __device__ __forceinline__ void seed_fast_items(const DevConfig& c, const Arena&
                 if (lane == 0) push_overflow(a, gm);
                 continue;
             }
-            const MiddleResult r = process_middle<true, SCORE, VAR, 640, 1024, 256, 128>(
+            const MiddleResult r = process_middle<true, SCORE, VAR, 512, 1024, 216, 128>(
                 c, a, nb, gm, true, nb_minr, nb_maxr, e, ws);
             if (lane == 0) {
                 if (r.status) push_overflow(a, gm);
@@ -1706,9 +1716,10 @@ __global__ void __launch_bounds__(SCORE ? kScoreWarps * 32 : 512)
 // neighbourhood other than the bin's; or a list beyond the fast capacities).
 // Every warp takes one middle at a time from its tier's queue, builds the
 // middle's own neighbourhood and reads it from global memory in host order.
-// Two tiers: the middle tier (many warps per SM, the fast kernel's list
-// capacities) takes every handed-over middle and passes the ones whose lists
-// do not fit to the last tier (one warp per SM with large capacities).
+// Two tiers: the middle tier (many warps per SM, about twice the fast
+// kernel's list capacities) takes every handed-over middle and passes the
+// ones whose lists do not fit to the last tier (one warp per SM with large
+// capacities).
 constexpr size_t kGeneralSegBytes = 1024;  // per warp: segments of the middle's neighbourhood
 
 template <typename Scratch>
@@ -1741,6 +1752,16 @@ __device__ __forceinline__ void general_middles(const DevConfig& c, const Arena&
         idx = __shfl_sync(0xffffffffu, idx, 0);
         if (idx >= n) break;
         const uint32_t gm = queue[idx];
+        if (!LAST && c.last_tier_only) {
+            if (lane == 0) {
+                const unsigned long long k = atomicAdd(&a.counters[kOvf2Count], 1ull);
+                if (k < 2ull * a.cap_sp) a.ovf2[k] = gm;
+                else raise_status(a.counters, SEEDGB_CAPACITY_OVERFLOW);
+                a.seed_cnt[gm] = 0;
+            }
+            __syncwarp();
+            continue;
+        }
         // event: last with sp_base <= gm
         uint32_t lo = 0, hi = n_events;
         while (hi - lo > 1) {
@@ -1788,14 +1809,14 @@ __device__ __forceinline__ void general_middles(const DevConfig& c, const Arena&
     }
 }
 
-// Middle tier: the fast kernel's capacities, as many warps as fit.
+// Middle tier: larger capacities than the fast kernel's, as many warps as fit.
 template <bool SCORE>
 __global__ void __launch_bounds__(SCORE ? kScoreWarps * 32 : 512)
     k_seed_mid(DevConfig c, Arena a, uint32_t pass) {
     if (a.counters[kAnyVariance] != 0)
-        general_middles<SCORE, true, false, 640, 1024, 256, 128>(c, a, pass);
+        general_middles<SCORE, true, false, 1024, 1024, 512, 256>(c, a, pass);
     else
-        general_middles<SCORE, false, false, 640, 1024, 256, 128>(c, a, pass);
+        general_middles<SCORE, false, false, 1024, 1024, 512, 256>(c, a, pass);
 }
 
 // Last tier: one warp per CTA with large capacities; always with the
@@ -2071,11 +2092,11 @@ static size_t slow_kernel_smem() { return general_warp_bytes<SlowScratch>(); }
 
 // Warps per CTA of the general path's middle tier (all that fit in 227 KiB).
 static int mid_kernel_warps(bool score) {
-    const int fit = static_cast<int>((227 * 1024) / general_warp_bytes<FastScratch>());
+    const int fit = static_cast<int>((227 * 1024) / general_warp_bytes<MidScratch>());
     return std::min(score ? kScoreWarps : 16, fit);
 }
 static size_t mid_kernel_smem(bool score) {
-    return static_cast<size_t>(mid_kernel_warps(score)) * general_warp_bytes<FastScratch>();
+    return static_cast<size_t>(mid_kernel_warps(score)) * general_warp_bytes<MidScratch>();
 }
 
 cudaError_t prepare_kernels() {

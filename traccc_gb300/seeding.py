@@ -141,6 +141,7 @@ INVALID_ARGUMENT, UNSUPPORTED, SIZE_LIMIT = 6, 7, 8
 NOALLOC_MAX_SPACEPOINTS = 65536
 OPTION_EXHAUSTIVE_TRIPLETS = 1
 OPTION_KERNEL_TIMING = 2
+OPTION_LAST_TIER_ONLY = 3
 KERNEL_NAMES = ("bin_count", "bin_scan", "item_order", "bin_scatter", "bin_rsort",
                 "seed_fast", "seed_mid", "seed_slow", "seed_count", "seed_compact")
 
