@@ -73,6 +73,30 @@ def test_params_match_oracle():
     assert ok.all(), np.nonzero(~ok)[0][:10]
 
 
+def test_small_seed_buffer_reports_overflow():
+    """A seed buffer smaller than the event's seeds: the call reports
+    SEEDGB_CAPACITY_OVERFLOW through the device status, the buffer holds the
+    first seeds in host order and its size is its capacity; the next run
+    with room is complete again."""
+    import torch
+    ev = synth.workload_event("trk1000", 2)
+    ref, _ = oracle.seeding(ev, phi_mode=oracle.PHI_CR)
+    assert len(ref) > 40
+    alg = seeding.TripletSeedingAlgorithm()
+    sps = seeding.SpacepointCollection.from_numpy(ev)
+    small = seeding.SeedBuffer(37, device=sps.global_.device)
+    out = alg(sps, small)
+    torch.cuda.synchronize()
+    assert alg.last_status() == seeding.CAPACITY_OVERFLOW
+    got = out.to_numpy()
+    assert len(got) == 37
+    assert np.array_equal(got, ref[:37])
+    full = alg(sps)
+    torch.cuda.synchronize()
+    assert alg.last_status() == seeding.OK
+    assert np.array_equal(full.to_numpy(), ref)
+
+
 def test_params_batch_equals_per_event():
     """seedgb_params_run_batch (one launch for several events) gives the same
     bytes as one seedgb_params_run per event, and the oracle's parameters."""
