@@ -1,6 +1,7 @@
 /*
  * seeding_algorithm.hpp -- C++ face of the CPU oracle (test infrastructure
- * only: the checker the GPU path is compared with, never a product path).
+ * only: the reference the GPU path is compared with in the tests, never a
+ * product path).
  *
  * The reference's host algorithm classes over the C restatement in
  * seeding_oracle.c, with the same constructor arguments and operator():
