@@ -344,11 +344,12 @@ def compare(plain, learned):
 
 def calibrate(alg, model: FilterModel, events, target=0.995, margin=0.05,
               quantiles=(0.02, 0.015, 0.01, 0.007, 0.005, 0.003, 0.002, 0.001, 0.0005),
-              log=None, criterion="total"):
+              log=None, criterion="total", min_event=0.0):
     """Thresholds and pruned-fraction band on held-out events (numpy dicts):
     the most aggressive quantile whose seed recall against plain seeding
     reaches `target` over all held-out seeds (criterion "total") or on every
-    event ("event").  Returns (model with threshold/band set, report)."""
+    event ("event"), and `min_event` on every event.  Returns (model with
+    threshold/band set, report)."""
     import torch
     dev = torch.device("cuda", torch.cuda.current_device())
     sps = _device_events(torch, events, dev)
@@ -386,7 +387,7 @@ def calibrate(alg, model: FilterModel, events, target=0.995, margin=0.05,
         if log:
             log(f"q={q}: thresholds ({tb:.3f}, {tt:.3f}) recall {agg:.4f} (event min "
                 f"{r.min():.4f}) outside {o.sum()} pruned {frac.mean():.3f}")
-        if (agg if criterion == "total" else r.min()) >= target:
+        if (agg if criterion == "total" else r.min()) >= target and r.min() >= min_event:
             chosen = c
             break
     if chosen is None:
@@ -426,7 +427,7 @@ def calibrate_classes(alg, model: FilterModel, events, class_max, target=0.995, 
 
 def build_filter(alg, train_events, calib_events, epochs=3, neg_keep=0.05, target=0.995,
                  seed=0, log=None, quantiles=None, label="seed", criterion="total",
-                 class_max=None):
+                 class_max=None, min_event=0.0):
     """collect -> train -> calibrate (per size class when class_max is
     given).  Returns (model, report)."""
     import torch
@@ -438,7 +439,9 @@ def build_filter(alg, train_events, calib_events, epochs=3, neg_keep=0.05, targe
     torch.cuda.synchronize()
     t2 = time.perf_counter()
     model = FilterModel(params, norm, band_edges())
-    kw = {} if quantiles is None else {"quantiles": quantiles}
+    kw = {"min_event": min_event}
+    if quantiles is not None:
+        kw["quantiles"] = quantiles
     if class_max:
         model, rep = calibrate_classes(alg, model, calib_events, class_max, target=target,
                                        log=log, criterion=criterion, **kw)
