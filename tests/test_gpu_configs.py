@@ -150,6 +150,24 @@ def test_general_path_tiers_match_oracle():
             assert np.array_equal(out.to_numpy(), ref)
 
 
+@pytest.mark.parametrize("variant", ["seeds8", "beam", "tight"])
+def test_config_variant_dense_event(variant):
+    """Config variants on a 100k-spacepoint event: eight seeds per middle
+    (the most the seed slots hold), an offset beam spot, tighter cuts."""
+    import torch
+    ev = synth.workload_event("pileup9k", 8)
+    mod = VARIANTS[variant]
+    f, g, fl, _ = _configs(mod, seeding)
+    of, og, ofl, _ = _configs(mod, O)
+    alg = seeding.TripletSeedingAlgorithm(f, g, fl)
+    out = alg(seeding.SpacepointCollection.from_numpy(ev))
+    torch.cuda.synchronize()
+    assert alg.last_status() == seeding.OK
+    ref, _ = O.seeding(ev, of, og, ofl, phi_mode=O.PHI_CR)
+    assert len(ref) > 0
+    assert np.array_equal(out.to_numpy(), ref)
+
+
 def test_zbins_dense_event():
     """Several z bins on a 100k-spacepoint event (fast path with z segments)."""
     import torch
