@@ -641,15 +641,27 @@ constexpr uint32_t kFastSegs = 16;  // neighbourhood bins on the fast path
 
 // Neighbourhood of a middle spacepoint: the concatenation of its grid bins in
 // host order (phi zone outer, z zone inner).  "Host position" = position in
-// that concatenation.  The fast path (STAGED) stages every bin as a
-// radius-sorted run in shared memory (staged / staged_hp give the spacepoint
-// and its host position); the large-capacity path reads the grid in host
-// order.  The choice is a template parameter so that the fused kernel carries
-// no per-access branch on it (measured 9% faster than a runtime test).
-template <bool STAGED>
+// that concatenation.  Three ways to read it (a template parameter, so that
+// the fused kernel carries no per-access branch on it: measured 9 % faster
+// than a runtime test):
+//   kNbShared    every bin staged as a radius-sorted run in shared memory
+//                (staged / staged_hp give the spacepoint and its host
+//                position): the fast kernel;
+//   kNbGlobalRs  the bins are consecutive in the grid, so their radius-sorted
+//                copies (g_rs) form one array in host order of the bins:
+//                staged = g_rs from the first bin on, the host position is
+//                the grid position (staged_gp) minus the first one (base);
+//   kNbHost      the grid itself in host order (any neighbourhood).
+// The first two give radius-sorted runs (the exact radial windows).
+enum NbMode : int { kNbHost = 0, kNbShared = 1, kNbGlobalRs = 2 };
+
+template <int MODE>
 struct NbViewT {
-    const float4* staged;       // STAGED only
-    const uint16_t* staged_hp;  // host position of each staged spacepoint
+    static constexpr bool kRSorted = MODE != kNbHost;
+    const float4* staged;       // radius-sorted runs (kNbShared, kNbGlobalRs)
+    const uint16_t* staged_hp;  // kNbShared: host position of each staged spacepoint
+    const uint32_t* staged_gp;  // kNbGlobalRs: grid position of each run element
+    uint32_t base;              // kNbGlobalRs: grid position of host position 0
     const float4* g_xyzr;
     const uint32_t* seg_pos;    // [nseg + 1] host-position prefix
     const uint32_t* seg_g;      // [nseg] first grid position of each bin
@@ -658,16 +670,21 @@ struct NbViewT {
 
     // host position -> grid position
     __device__ __forceinline__ uint32_t gpos(uint32_t hp) const {
-        uint32_t s = 0;
-        while (s + 1 < nseg && seg_pos[s + 1] <= hp) ++s;
-        return seg_g[s] + (hp - seg_pos[s]);
+        if constexpr (MODE == kNbGlobalRs) {
+            return base + hp;
+        } else {
+            uint32_t s = 0;
+            while (s + 1 < nseg && seg_pos[s + 1] <= hp) ++s;
+            return seg_g[s] + (hp - seg_pos[s]);
+        }
     }
     __device__ __forceinline__ float4 get(uint32_t p) const {
-        if constexpr (STAGED) return staged[p];
+        if constexpr (MODE != kNbHost) return staged[p];
         else return g_xyzr[gpos(p)];
     }
     __device__ __forceinline__ uint32_t hpos(uint32_t p) const {
-        if constexpr (STAGED) return staged_hp[p];
+        if constexpr (MODE == kNbShared) return staged_hp[p];
+        else if constexpr (MODE == kNbGlobalRs) return staged_gp[p] - base;
         else return p;
     }
 };
@@ -752,8 +769,8 @@ using SlowScratch = WarpScratch<8192, 8192, 4096, 2048>;
 // order, in q[0..n).  Two doublets per lane per iteration.
 // Out of line: one copy serves both roles (instruction-cache pressure of the
 // fused kernel; measured faster than two inlined copies).
-template <bool STAGED>
-__device__ __noinline__ uint32_t helix_compact(const DevConfig& c, const NbViewT<STAGED>& nb,
+template <int MODE>
+__device__ __noinline__ uint32_t helix_compact(const DevConfig& c, const NbViewT<MODE>& nb,
                                                   const float4 m, uint16_t* q,
                                                   uint32_t n, uint32_t lane,
                                                   uint32_t lt) {
@@ -790,8 +807,8 @@ struct MiddleResult {
 
 // Append the positions passing the window cuts of one role to q (in order of
 // the flattened per-bin ranges).  Two candidates per lane per iteration.
-template <bool TOP>
-__device__ __forceinline__ uint32_t scan_runs(const DevConfig& c, const NbViewT<true>& nb,
+template <bool TOP, int MODE>
+__device__ __forceinline__ uint32_t scan_runs(const DevConfig& c, const NbViewT<MODE>& nb,
                                               const float4 M, const uint32_t* bnd,
                                               const uint32_t* pre, uint32_t ns,
                                               uint16_t* q, uint32_t cap, uint32_t lane,
@@ -911,9 +928,9 @@ __device__ __forceinline__ float score_chunk(const DevConfig& c, const Arena& a,
 // in-order compaction of those with logit >= threshold when the filter
 // prunes bottoms (otherwise scoring only, for the dump).  Adds the scored /
 // pruned counts to the event's filter counters.
-template <bool STAGED>
+template <int MODE>
 __device__ __noinline__ uint32_t filter_bottoms(const DevConfig& c, const Arena& a,
-                                                const NbViewT<STAGED>& nb, const float4 M, uint16_t* q,
+                                                const NbViewT<MODE>& nb, const float4 M, uint16_t* q,
                                                 uint32_t n, uint32_t* xs, float* lg,
                                                 uint32_t ev, uint32_t gm, uint32_t lane,
                                                 uint32_t lt) {
@@ -962,14 +979,15 @@ __device__ __noinline__ uint32_t filter_bottoms(const DevConfig& c, const Arena&
 // VAR: read the spacepoint variances.  With VAR false every variance term is
 // zero (valid when no spacepoint of the batch has a variance); the results
 // are the same as with VAR true on such a batch, without the variance loads.
-template <bool RSORTED, bool SCORE, bool VAR, int CAPB, int CAPT, int CAPLC, int CAPCT>
+template <int MODE, bool SCORE, bool VAR, int CAPB, int CAPT, int CAPLC, int CAPCT>
 __device__ MiddleResult process_middle(const DevConfig& c, const Arena& a,
-                                       const NbViewT<RSORTED>& nb, const uint32_t gm,
+                                       const NbViewT<MODE>& nb, const uint32_t gm,
                                        const bool check_r,
                                        const float nb_minr, const float nb_maxr,
                                        const uint32_t ev,
                                        WarpScratch<CAPB, CAPT, CAPLC, CAPCT>& ws) {
     MiddleResult res{0, 0, 0, 0};
+    constexpr bool RSORTED = NbViewT<MODE>::kRSorted;
     constexpr bool any_var = VAR;
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t lt = lanemask_lt();
@@ -1032,9 +1050,9 @@ __device__ MiddleResult process_middle(const DevConfig& c, const Arena& a,
             if (lane == 0) a.seed_cnt[gm] = 0;
             return res;
         }
-        nqb = scan_runs<false>(c, nb, M, ws.bnd, ws.pre, ns, ws.qb, CAPB, lane, lt);
-        nqt = scan_runs<true>(c, nb, M, ws.bnd, ws.pre + kFastSegs + 1, ns, ws.qt, CAPT,
-                              lane, lt);
+        nqb = scan_runs<false, MODE>(c, nb, M, ws.bnd, ws.pre, ns, ws.qb, CAPB, lane, lt);
+        nqt = scan_runs<true, MODE>(c, nb, M, ws.bnd, ws.pre + kFastSegs + 1, ns, ws.qt, CAPT,
+                                    lane, lt);
     } else {
         for (uint32_t base = 0; base < nb.size; base += 32) {
             const uint32_t p = base + lane;
@@ -1671,7 +1689,7 @@ __device__ __forceinline__ void seed_fast_items(const DevConfig& c, const Arena&
         const float nb_minr = __uint_as_float(misc[3]), nb_maxr = __uint_as_float(misc[4]);
         // only staged neighbourhoods reach process_middle here (the others go
         // to the large-capacity kernel)
-        NbViewT<true> nb{nb_xyzr, nb_hp, a.g_xyzr, seg_pos, seg_g, nseg, size};
+        NbViewT<kNbShared> nb{nb_xyzr, nb_hp, nullptr, 0u, a.g_xyzr, seg_pos, seg_g, nseg, size};
         const uint32_t m0 = bs[bin] + ch * mpi;
         const uint32_t m1 = min(m0 + mpi, bs[bin + 1]);
         for (;;) {
@@ -1690,7 +1708,7 @@ __device__ __forceinline__ void seed_fast_items(const DevConfig& c, const Arena&
                 if (lane == 0) push_overflow(a, gm);
                 continue;
             }
-            const MiddleResult r = process_middle<true, SCORE, VAR, 512, 1024, 216, 128>(
+            const MiddleResult r = process_middle<kNbShared, SCORE, VAR, 512, 1024, 216, 128>(
                 c, a, nb, gm, true, nb_minr, nb_maxr, e, ws);
             if (lane == 0) {
                 if (r.status) push_overflow(a, gm);
@@ -1714,8 +1732,10 @@ __global__ void __launch_bounds__(SCORE ? kScoreWarps * 32 : 512)
 // General path, for the middles the fast kernel hands over (neighbourhood not
 // staged: too many spacepoints or bins, an unsorted bin, or a per-middle z
 // neighbourhood other than the bin's; or a list beyond the fast capacities).
-// Every warp takes one middle at a time from its tier's queue, builds the
-// middle's own neighbourhood and reads it from global memory in host order.
+// Every warp takes one middle at a time from its tier's queue and builds the
+// middle's own neighbourhood in global memory: the bins' radius-sorted copies
+// (exact radial windows) when the bins are consecutive in the grid, else the
+// grid in host order.
 // Two tiers: the middle tier (many warps per SM, about twice the fast
 // kernel's list capacities) takes every handed-over middle and passes the
 // ones whose lists do not fit to the last tier (one warp per SM with large
@@ -1736,8 +1756,9 @@ __device__ __forceinline__ void general_middles(const DevConfig& c, const Arena&
     uint8_t* wbase = smem + static_cast<size_t>(warp) * general_warp_bytes<Scratch>();
     uint32_t* seg_pos = reinterpret_cast<uint32_t*>(wbase);   // [kMaxSegments+1]
     uint32_t* seg_g = seg_pos + kMaxSegments + 1;             // [kMaxSegments]
-    uint32_t* misc = seg_g + kMaxSegments;                    // [1]
-    static_assert(sizeof(uint32_t) * (2 * kMaxSegments + 2) <= kGeneralSegBytes,
+    uint32_t* seg_bin = seg_g + kMaxSegments;                 // [kMaxSegments]
+    uint32_t* misc = seg_bin + kMaxSegments;                  // [2]
+    static_assert(sizeof(uint32_t) * (3 * kMaxSegments + 3) <= kGeneralSegBytes,
                   "general segment layout");
     Scratch& ws = *reinterpret_cast<Scratch*>(wbase + kGeneralSegBytes);
     const uint32_t* queue = LAST ? a.ovf2 : a.ovf;
@@ -1780,17 +1801,35 @@ __device__ __forceinline__ void general_middles(const DevConfig& c, const Arena&
         z_range(c, a.g_xyzr[gm].z, zlo, zhi);
         if (lane == 0) {
             uint32_t ns;
-            build_segments(c, bs, b0 % c.phi_bins, zlo, zhi, seg_pos, seg_g, &ns, nullptr);
+            build_segments(c, bs, b0 % c.phi_bins, zlo, zhi, seg_pos, seg_g, &ns, seg_bin);
+            // the bins' radius-sorted copies serve as one array (exact radial
+            // windows) when the bins are consecutive in the grid, all sorted,
+            // and few enough for the windows' scratch
+            uint32_t rs = (ns >= 1 && ns <= kFastSegs) ? 1u : 0u;
+            for (uint32_t s = 0; rs && s < ns; ++s) {
+                if (a.bin_unsorted[static_cast<size_t>(e) * c.nbins + seg_bin[s]]) rs = 0;
+                if (s + 1 < ns && seg_g[s + 1] != seg_g[s] + (seg_pos[s + 1] - seg_pos[s])) rs = 0;
+            }
             misc[0] = ns;
+            misc[1] = rs;
         }
         __syncwarp();
         const uint32_t nseg = misc[0];
         const uint32_t size = seg_pos[nseg];
         MiddleResult r{0, 0, 0, 1};
         if (size <= 65535u) {
-            NbViewT<false> nb{nullptr, nullptr, a.g_xyzr, seg_pos, seg_g, nseg, size};
-            r = process_middle<false, SCORE, VAR, CAPB, CAPT, CAPLC, CAPCT>(c, a, nb, gm, false,
-                                                                            0.f, 0.f, e, ws);
+            if (misc[1]) {
+                const uint32_t base = seg_g[0];
+                NbViewT<kNbGlobalRs> nb{a.g_rs + base, nullptr, a.g_rs_gp + base, base,
+                                        a.g_xyzr, seg_pos, seg_g, nseg, size};
+                r = process_middle<kNbGlobalRs, SCORE, VAR, CAPB, CAPT, CAPLC, CAPCT>(
+                    c, a, nb, gm, false, 0.f, 0.f, e, ws);
+            } else {
+                NbViewT<kNbHost> nb{nullptr, nullptr, nullptr, 0u, a.g_xyzr, seg_pos, seg_g,
+                                    nseg, size};
+                r = process_middle<kNbHost, SCORE, VAR, CAPB, CAPT, CAPLC, CAPCT>(
+                    c, a, nb, gm, false, 0.f, 0.f, e, ws);
+            }
         }
         if (lane == 0) {
             if (!r.status) {
@@ -1809,10 +1848,11 @@ __device__ __forceinline__ void general_middles(const DevConfig& c, const Arena&
     }
 }
 
-// Middle tier: larger capacities than the fast kernel's, as many warps as fit.
+// Middle tier: larger capacities than the fast kernel's, as many warps as fit
+// (9 with its 23.4 KiB per warp; the launch bound leaves it the registers).
+constexpr int kMidMaxWarps = 10;
 template <bool SCORE>
-__global__ void __launch_bounds__(SCORE ? kScoreWarps * 32 : 512)
-    k_seed_mid(DevConfig c, Arena a, uint32_t pass) {
+__global__ void __launch_bounds__(kMidMaxWarps * 32) k_seed_mid(DevConfig c, Arena a, uint32_t pass) {
     if (a.counters[kAnyVariance] != 0)
         general_middles<SCORE, true, false, 1024, 1024, 512, 256>(c, a, pass);
     else
@@ -2093,7 +2133,7 @@ static size_t slow_kernel_smem() { return general_warp_bytes<SlowScratch>(); }
 // Warps per CTA of the general path's middle tier (all that fit in 227 KiB).
 static int mid_kernel_warps(bool score) {
     const int fit = static_cast<int>((227 * 1024) / general_warp_bytes<MidScratch>());
-    return std::min(score ? kScoreWarps : 16, fit);
+    return std::min(std::min(score ? kScoreWarps : 16, kMidMaxWarps), fit);
 }
 static size_t mid_kernel_smem(bool score) {
     return static_cast<size_t>(mid_kernel_warps(score)) * general_warp_bytes<MidScratch>();
