@@ -2079,7 +2079,20 @@ __device__ __forceinline__ void params_of_seed(const ParamsConfig& c, float bx, 
             var *= c.initial_inflation[j];
             p.cov[j * 6 + j] = var;
         }
-        out.data[i] = p;
+        // A record is 11 16-byte words: on a 16-byte aligned buffer, 11
+        // vector stores instead of the 22 of the member-wise copy (the
+        // kernel waits on its load/store queue).
+        static_assert(sizeof(seedgb_bound_track_parameters) == 11 * sizeof(uint4),
+                      "parameter record size");
+        if ((reinterpret_cast<uintptr_t>(out.data) & 15u) == 0u) {
+            uint4 w[11];
+            memcpy(w, &p, sizeof(p));
+            uint4* dst = reinterpret_cast<uint4*>(out.data + i);
+#pragma unroll
+            for (int k = 0; k < 11; ++k) dst[k] = w[k];
+        } else {
+            out.data[i] = p;
+        }
     }
 }
 
