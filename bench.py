@@ -549,15 +549,17 @@ class ClockSampler:
                 "samples": len(s)}
 
 
-def load_profile_traffic(kernel):
-    """DRAM bytes per launch of `kernel` on this workload from the committed
-    ncu summary (profiles/traffic.json), or None."""
+def load_profile_traffic(kernel, n_events):
+    """DRAM bytes and warp instructions per launch of `kernel` from the
+    committed ncu summary (profiles/traffic.json), or None when the summary
+    is for another number of events than this run's launch."""
     p = os.path.join(ROOT, "profiles", "traffic.json")
     try:
         with open(p) as fh:
-            return json.load(fh).get(kernel)
+            prof = json.load(fh).get(kernel)
     except Exception:
         return None
+    return prof if prof and prof.get("events") == n_events else None
 
 
 def load_op_model(n_events):
@@ -847,7 +849,7 @@ def run_gpu(args):
         pass
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
     achieved = ab / (dom_ms * 1e-3) / 1e9
-    prof = load_profile_traffic(dom) or {}
+    prof = load_profile_traffic(dom, n_ev) or {}
     roofline = {
         "bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak,
         "unit": "GB/s", "frac": achieved / hbm_peak,
