@@ -135,17 +135,28 @@ k_bin_count(DevConfig c, Arena a) {
     __syncthreads();
     uint32_t* h = hist + warp * c.nbins;
     const uint32_t base = (chunk - ev.chunk_base) * kBinChunk + warp * (kBinRounds * 32);
+    // all rounds' loads first: one memory latency per warp instead of one
+    // per round (the kernel waits on its loads)
+    float px[kBinRounds], py[kBinRounds], pz[kBinRounds];
     bool anyvar = false;
-#pragma unroll 2
+#pragma unroll
+    for (int r = 0; r < kBinRounds; ++r) {
+        const uint32_t i = base + r * 32 + lane;
+        px[r] = py[r] = pz[r] = 0.f;
+        if (i < ev.n_sp) {
+            px[r] = ev.global[3 * i];
+            py[r] = ev.global[3 * i + 1];
+            pz[r] = ev.global[3 * i + 2];
+            anyvar |= (ev.zvar && ev.zvar[i] != 0.f) || (ev.rvar && ev.rvar[i] != 0.f);
+        }
+    }
+#pragma unroll
     for (int r = 0; r < kBinRounds; ++r) {
         const uint32_t i = base + r * 32 + lane;
         if (i < ev.n_sp) {
-            const float x = ev.global[3 * i], y = ev.global[3 * i + 1],
-                        z = ev.global[3 * i + 2];
-            const int32_t bin = classify(c, x, y, z, a.counters);
+            const int32_t bin = classify(c, px[r], py[r], pz[r], a.counters);
             a.sp_bin[ev.sp_base + i] = bin;
             if (bin >= 0) atomicAdd(&h[bin], 1u);
-            anyvar |= (ev.zvar && ev.zvar[i] != 0.f) || (ev.rvar && ev.rvar[i] != 0.f);
         }
     }
     if (__any_sync(0xffffffffu, anyvar) && lane == 0)
@@ -350,15 +361,31 @@ __global__ void __launch_bounds__(kBinWarps * 32) k_bin_scatter(DevConfig c, Are
     uint32_t* wb = base + warp * c.nbins;
     const uint32_t b0 = (chunk - ev.chunk_base) * kBinChunk + warp * (kBinRounds * 32);
     const uint32_t lt = lanemask_lt();
+    // all rounds' bins and coordinates first: one memory latency per warp
+    // instead of two per round (the kernel waits on its loads)
+    int32_t pbin[kBinRounds];
+    float px[kBinRounds], py[kBinRounds], pz[kBinRounds];
+#pragma unroll
     for (int r = 0; r < kBinRounds; ++r) {
         const uint32_t i = b0 + r * 32 + lane;
-        const int32_t bin = (i < ev.n_sp) ? a.sp_bin[ev.sp_base + i] : -1;
+        pbin[r] = -1;
+        px[r] = py[r] = pz[r] = 0.f;
+        if (i < ev.n_sp) {
+            pbin[r] = a.sp_bin[ev.sp_base + i];
+            px[r] = ev.global[3 * i];
+            py[r] = ev.global[3 * i + 1];
+            pz[r] = ev.global[3 * i + 2];
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < kBinRounds; ++r) {
+        const uint32_t i = b0 + r * 32 + lane;
+        const int32_t bin = pbin[r];
         const uint32_t peers = __match_any_sync(0xffffffffu, bin);
         const uint32_t rank = __popc(peers & lt);
         if (bin >= 0) {
             const uint32_t pos = wb[bin] + rank;
-            const float x = ev.global[3 * i], y = ev.global[3 * i + 1],
-                        z = ev.global[3 * i + 2];
+            const float x = px[r], y = py[r], z = pz[r];
             // spacepoint::radius, spacepoint_collection.ipp:52-57
             a.g_xyzr[pos] = make_float4(x, y, z, sqrtf(x * x + y * y));
             a.g_var[pos] = make_float2(ev.zvar ? ev.zvar[i] : 0.f, ev.rvar ? ev.rvar[i] : 0.f);
@@ -589,13 +616,14 @@ __device__ __forceinline__ bool better(float wa, float sa, uint32_t ka, float wb
 
 constexpr int kSortCap = 4096;  // largest bin sorted in shared memory
 
-// One CTA per (event, bin): the bin's spacepoints sorted by radius (ties in
-// any order), with the grid position of each.  A bin larger than kSortCap is
+// One CTA per (event, bin): the bin's spacepoints sorted by radius (ties by
+// grid position), with the grid position of each.  One 64-bit key per
+// spacepoint, radius bits above the grid position: a bitonic network over
+// single keys (radii are non-negative, so their bits order as the values).  A bin larger than kSortCap is
 // flagged; middles whose neighbourhood holds such a bin take the
 // large-capacity path, which scans in host order.
 __global__ void __launch_bounds__(256) k_bin_rsort(DevConfig c, Arena a) {
-    __shared__ uint32_t key[kSortCap];
-    __shared__ uint32_t val[kSortCap];
+    __shared__ unsigned long long key[kSortCap];
     const uint32_t e = blockIdx.x / c.nbins, b = blockIdx.x % c.nbins;
     if (e >= a.hdr->n_events) return;
     const uint32_t* bs = a.bin_start + static_cast<size_t>(e) * (c.nbins + 1);
@@ -604,10 +632,10 @@ __global__ void __launch_bounds__(256) k_bin_rsort(DevConfig c, Arena a) {
     if (n == 0 || n > kSortCap) return;
     uint32_t P = 1;
     while (P < n) P <<= 1;
-    for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) {
-        key[i] = i < n ? __float_as_uint(a.g_xyzr[g0 + i].w) : 0xffffffffu;
-        val[i] = g0 + i;
-    }
+    for (uint32_t i = threadIdx.x; i < P; i += blockDim.x)
+        key[i] = i < n ? (static_cast<unsigned long long>(__float_as_uint(a.g_xyzr[g0 + i].w))
+                          << 32) | (g0 + i)
+                       : ~0ull;
     __syncthreads();
     for (uint32_t k = 2; k <= P; k <<= 1) {
         for (uint32_t j = k >> 1; j > 0; j >>= 1) {
@@ -615,21 +643,19 @@ __global__ void __launch_bounds__(256) k_bin_rsort(DevConfig c, Arena a) {
                 const uint32_t i = 2 * t - (t & (j - 1));
                 const uint32_t l = i + j;
                 const bool up = (i & k) == 0;
-                const uint32_t ki = key[i], kl = key[l];
+                const unsigned long long ki = key[i], kl = key[l];
                 if (up ? (ki > kl) : (ki < kl)) {
                     key[i] = kl;
                     key[l] = ki;
-                    const uint32_t v = val[i];
-                    val[i] = val[l];
-                    val[l] = v;
                 }
             }
             __syncthreads();
         }
     }
     for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
-        a.g_rs[g0 + i] = a.g_xyzr[val[i]];
-        a.g_rs_gp[g0 + i] = val[i];
+        const uint32_t gp = static_cast<uint32_t>(key[i]);
+        a.g_rs[g0 + i] = a.g_xyzr[gp];
+        a.g_rs_gp[g0 + i] = gp;
     }
 }
 
