@@ -75,3 +75,17 @@ def test_replica_aggregation_over_two_gloo_ranks():
     for rank, t, v in res:
         assert t == [2.0, 10.0]          # max over ranks
         assert v == pytest.approx(2 * 20 * 5 / 2.0)
+
+
+def test_roofline_constants_only_for_their_event_count():
+    """The committed per-launch ncu figures of the seeding kernel and the
+    oracle's op model are used only for a launch over the events they were
+    taken on (a 4-event run must not divide 20 events' instructions by its
+    time)."""
+    import bench
+    prof = bench.load_profile_traffic("seed_fast", 20)
+    assert prof is not None and prof["inst_issued_per_launch"] > 0
+    assert bench.load_profile_traffic("seed_fast", 4) is None
+    assert bench.load_profile_traffic("no_such_kernel", 20) is None
+    assert bench.load_op_model(20) is not None
+    assert bench.load_op_model(4) is None
