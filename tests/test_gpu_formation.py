@@ -79,3 +79,27 @@ def test_formation_then_seeding():
     ref, _ = O.seeding(formed)
     assert np.array_equal(got, ref)
     torch.cuda.synchronize()
+
+
+def test_formation_telescope_known_answer():
+    """tests/cpu/test_spacepoint_formation.cpp:82-88 on the GPU: nine planes
+    at x = 20 ... 180 mm, local axes along global y and z; (7, 2) on the first
+    plane -> (20, 7, 2), (10, 15) on the last -> (180, 10, 15)."""
+    import torch
+
+    from traccc_gb300 import seeding
+    planes = np.zeros(9, O.SURFACE_DTYPE)
+    for k, x in enumerate((20., 40., 60., 80., 100., 120., 140., 160., 180.)):
+        planes[k]["type"] = 0
+        planes[k]["rotation"] = np.array([[0, 0, 1], [1, 0, 0], [0, 1, 0]],
+                                         np.float32).reshape(-1)
+        planes[k]["translation"] = (x, 0., 0.)
+    meas = seeding.MeasurementCollection.from_numpy(dict(
+        local_position=np.array([[7., 2.], [10., 15.]], np.float32),
+        surface_link=np.array([0, 8], np.uint64)))
+    sps, k = seeding.form_spacepoints(planes, meas,
+                                      torch.tensor([2, 2], dtype=torch.uint8, device="cuda"))
+    torch.cuda.synchronize()
+    assert k == 2
+    assert np.array_equal(sps.global_.cpu().numpy()[:2],
+                          np.array([[20., 7., 2.], [180., 10., 15.]], np.float32))

@@ -12,6 +12,12 @@
   zone / remap known answers (binned neighbourhoods).
 * core/include/traccc/seeding/detail/seeding_config.hpp:120-138 -- derived
   seed-finder constants for the default config.
+* tests/cpu/test_spacepoint_formation.cpp:21-89 -- a telescope of nine planes
+  at x = 20 ... 180 mm (normals along x, local axes along global y and z): the
+  measurement (7, 2) on the first plane forms the spacepoint (20, 7, 2), the
+  measurement (10, 15) on the last plane (180, 10, 15).  detray's telescope
+  builder is not available; its plane placement is written here as a rotation
+  and a translation of the library's surface table.
 """
 import ctypes as C
 import math
@@ -172,3 +178,18 @@ def test_bad_grid_config_is_rejected():
     g.minPt = 0.01  # minHelixRadius < rMax / 2: std::domain_error in get_axes
     with pytest.raises(ValueError):
         O.get_axes(g)
+
+
+def test_spacepoint_formation_on_a_telescope():
+    planes = np.zeros(9, O.SURFACE_DTYPE)
+    for k, x in enumerate((20., 40., 60., 80., 100., 120., 140., 160., 180.)):
+        planes[k]["type"] = 0  # plane: local (u, v) -> global R (u, v, 0) + t
+        # local u -> global y, local v -> global z, local normal -> global x
+        planes[k]["rotation"] = np.array([[0, 0, 1], [1, 0, 0], [0, 1, 0]],
+                                         np.float32).reshape(-1)
+        planes[k]["translation"] = (x, 0., 0.)
+    sp = O.form_spacepoints(planes, np.array([[7., 2.], [10., 15.]], np.float32),
+                            np.array([0, 8], np.uint64), np.array([2, 2], np.uint8))
+    assert len(sp["global"]) == 2
+    assert np.array_equal(sp["global"], np.array([[20., 7., 2.], [180., 10., 15.]], np.float32))
+    assert np.array_equal(sp["measurement_index_1"], np.array([0, 1], np.uint32))
