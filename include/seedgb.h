@@ -550,13 +550,22 @@ seedgb_status seedgb_params_run_batch(seedgb_params* h, const float bfield[3],
  *   bin_sps      device, >= sps->size entries: spacepoint indices, bins in
  *                serial order, ascending index inside a bin
  *
+ * Returns SEEDGB_BAD_CONFIG, before launching anything, when the grid's phi
+ * axis cannot place every phi the finder accepts (a grid phi range much
+ * narrower than the finder's: ibin = int((phi - min) / (max - min) * n)
+ * outside [-n, 2n) at an end of the finder's range); such spacepoints would
+ * otherwise be left out of the grid.
+ *
  * Asynchronous on `stream`.  The kernel's scratch is one static device array
  * shared by every call, which keeps the last call's contents (the kernel
  * clears what must start at zero): calls that overlap on the GPU -- on two
  * streams, or from two host threads -- race and corrupt each other's result;
- * serialise them.  The first call on each device looks up the array's device
- * address (cudaGetSymbolAddress) with that device current; make that first
- * call before any stream capture.  Allocates nothing: no cudaMalloc, no
+ * serialise them.  Every call made outside stream capture looks up the
+ * array's device address (cudaGetSymbolAddress) with the current device;
+ * a call during capture reuses the address found by the last call outside
+ * capture on that device, so make a first call on each device before any
+ * stream capture (and again after a device reset).  Device ordinals of 64 or
+ * more get SEEDGB_UNSUPPORTED.  Allocates nothing: no cudaMalloc, no
  * cudaFree. */
 seedgb_status seedgb_spacepoint_binning_noalloc(
     const seedgb_seedfinder_config* finder, const seedgb_spacepoint_grid_config* grid,

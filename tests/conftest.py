@@ -10,10 +10,6 @@ if ROOT not in sys.path:
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300)")
-    # temporary files of the tests stay inside the working tree (ignored)
-    if not config.option.basetemp:
-        os.makedirs(os.path.join(ROOT, "_work"), exist_ok=True)
-        config.option.basetemp = os.path.join(ROOT, "_work", "pytest_tmp")
 
 
 def _have_gpu():

@@ -88,3 +88,22 @@ def test_invalid_arguments_are_rejected_before_device_work():
     st = L.seedgb_spacepoint_binning_noalloc(C.byref(f), C.byref(g), C.byref(v),
                                              C.c_void_p(1), C.c_void_p(1), None)
     assert st == seeding.SIZE_LIMIT
+
+
+def test_noalloc_refuses_a_grid_too_narrow_for_the_finder_before_device_work():
+    """The allocation-free binning checks on the host that the grid's
+    circular phi axis can place every phi the finder accepts; a grid range of
+    [-0.5, 0.5] against the finder's [-pi, pi] is refused (no launch, so no
+    GPU is needed), a wrapping [-2, 2] grid passes the check (and then fails
+    only for want of a device here)."""
+    L = seeding.lib()
+    f, g, _, _ = seeding.default_configs()
+    v = seeding._SpacepointView(0, 0, 1, 0, 0, 10)
+    g.phiMin, g.phiMax = -0.5, 0.5
+    st = L.seedgb_spacepoint_binning_noalloc(C.byref(f), C.byref(g), C.byref(v),
+                                             C.c_void_p(1), C.c_void_p(1), None)
+    assert st == seeding.BAD_CONFIG
+    g.phiMin, g.phiMax = -2.0, 2.0
+    st = L.seedgb_spacepoint_binning_noalloc(C.byref(f), C.byref(g), C.byref(v),
+                                             C.c_void_p(1), C.c_void_p(1), None)
+    assert st != seeding.BAD_CONFIG

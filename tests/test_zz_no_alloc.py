@@ -66,3 +66,41 @@ def test_noalloc_rejects_events_above_its_capacity():
     off = torch.zeros(1024, dtype=torch.int32, device="cuda")
     bsp = torch.zeros(n, dtype=torch.int32, device="cuda")
     assert seeding.spacepoint_binning_noalloc(f, g, sps, off, bsp) == seeding.SIZE_LIMIT
+
+
+def test_noalloc_refuses_a_grid_that_cannot_place_the_finders_phi():
+    """A grid phi range far narrower than the finder's (here [-0.5, 0.5]
+    against [-pi, pi]) cannot place every accepted spacepoint.  The handle
+    path reports that after the run (SEEDGB_BAD_CONFIG from last_status);
+    the allocation-free entry point refuses the configuration before it
+    launches anything, so it never returns SEEDGB_OK with spacepoints left
+    out of the grid."""
+    import torch
+    f, g, fl, _ = seeding.default_configs()
+    g.phiMin, g.phiMax = -0.5, 0.5
+    ev = synth.workload_event("trk1000", 23)
+    alg = seeding.TripletSeedingAlgorithm(f, g, fl)
+    alg(seeding.SpacepointCollection.from_numpy(ev))
+    torch.cuda.synchronize()
+    assert alg.last_status() == seeding.BAD_CONFIG
+    ax = seeding.get_axes(g)
+    sps = seeding.SpacepointCollection.from_numpy(ev)
+    off = torch.full((ax.phi_bins * ax.z_bins + 1,), -1, dtype=torch.int32, device="cuda")
+    bsp = torch.full((len(sps),), -1, dtype=torch.int32, device="cuda")
+    assert seeding.spacepoint_binning_noalloc(f, g, sps, off, bsp) == seeding.BAD_CONFIG
+    torch.cuda.synchronize()
+    assert int(off.max().item()) == -1  # nothing was written
+
+
+def test_noalloc_narrower_grid_that_wraps_equals_seeding_grid():
+    """A grid phi range narrower than the finder's whose circular axis still
+    wraps every accepted phi ([-2, 2] against [-pi, pi]) is accepted and
+    gives the handle path's grid, on two calls in a row."""
+    f, g, fl, _ = seeding.default_configs()
+    g.phiMin, g.phiMax = -2.0, 2.0
+    events = [synth.workload_event("trk1000", 24), synth.workload_event("trk1000", 25)]
+    got = [_noalloc_grid(f, g, ev) for ev in events]
+    for ev, (off, bsp) in zip(events, got):
+        roff, rbsp = _handle_grid(f, g, fl, ev)
+        assert np.array_equal(off, roff)
+        assert np.array_equal(bsp, rbsp)

@@ -47,8 +47,9 @@ __global__ void __launch_bounds__(kNoallocWarps * 32)
 k_bin_noalloc(DevConfig c, seedgb_spacepoint_view sps, uint8_t* scratch,
               uint32_t* bin_offsets, uint32_t* bin_sps) {
     __shared__ uint32_t tmp[33];
-    // classify() flags a grid phi range narrower than the finder's here; the
-    // spacepoints concerned are left out of the grid
+    // classify()'s status words and counters (the host has already rejected
+    // grids that cannot place every phi the finder accepts, so no status bit
+    // is raised here); cleared on every call so nothing accumulates
     unsigned long long* status = reinterpret_cast<unsigned long long*>(scratch);
     int32_t* sp_bin = reinterpret_cast<int32_t*>(scratch + kNoallocStatusBytes);
     uint32_t* whist =
@@ -59,7 +60,9 @@ k_bin_noalloc(DevConfig c, seedgb_spacepoint_view sps, uint8_t* scratch,
     const uint32_t L = (n + kNoallocWarps - 1) / kNoallocWarps;
     const uint32_t i0 = min(n, warp * L), i1 = min(n, i0 + L);
 
-    // the histograms keep the previous call's contents: clear them
+    // the status block and the histograms keep the previous call's contents:
+    // clear them (classify() runs only after the barrier)
+    if (threadIdx.x < kNoallocStatusBytes / sizeof(unsigned long long)) status[threadIdx.x] = 0;
     for (uint32_t i = threadIdx.x; i < kNoallocWarps * nb; i += blockDim.x) whist[i] = 0;
     __syncthreads();
     uint32_t* wh = whist + warp * nb;
@@ -125,16 +128,22 @@ k_bin_noalloc(DevConfig c, seedgb_spacepoint_view sps, uint8_t* scratch,
     }
 }
 
-// Device address of the scratch array, looked up once per device.
+// Device address of the scratch array per device (at most 64 devices).  It is
+// looked up again on every call made outside stream capture, so a context
+// that was reset and created again gets the new address; during capture the
+// address of the last call outside capture on this device is used.
+constexpr int kMaxDevices = 64;
 std::mutex g_mu;
-void* g_scratch_ptr[64] = {};
+void* g_scratch_ptr[kMaxDevices] = {};
 
-seedgb_status scratch_address(void** out) {
+seedgb_status scratch_address(cudaStream_t stream, void** out) {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return SEEDGB_CUDA_ERROR;
-    if (dev < 0 || dev >= 64) return SEEDGB_UNSUPPORTED;
+    if (dev < 0 || dev >= kMaxDevices) return SEEDGB_UNSUPPORTED;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(stream, &cap) != cudaSuccess) return SEEDGB_CUDA_ERROR;
     std::lock_guard<std::mutex> lock(g_mu);
-    if (!g_scratch_ptr[dev]) {
+    if (cap == cudaStreamCaptureStatusNone || !g_scratch_ptr[dev]) {
         void* p = nullptr;
         if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p)
             return SEEDGB_CUDA_ERROR;
@@ -142,6 +151,27 @@ seedgb_status scratch_address(void** out) {
     }
     *out = g_scratch_ptr[dev];
     return SEEDGB_OK;
+}
+
+// True when the grid's circular phi axis can place every phi the finder
+// accepts.  The axis maps phi to ibin = int((phi - min) / (max - min) * n)
+// and wraps ibin in [-n, 2n) (core/include/traccc/seeding/grids/axis.hpp:
+// 277-289); ibin is monotone in phi, so the two ends of the finder's range
+// (clipped to atan2f's range) decide.  A narrower grid would leave
+// spacepoints out of the grid (the handle path reports that case as
+// SEEDGB_BAD_CONFIG after the fact; this entry point refuses it up front).
+bool grid_places_finder_phi(const seedgb_seedfinder_config& f, const seedgb_grid_axes& ax) {
+    const float pi_f = 3.14159274f;  // the float nearest pi: atan2f's extreme
+    const float lo = f.phiMin > -pi_f ? f.phiMin : -pi_f;
+    const float hi = f.phiMax < pi_f ? f.phiMax : pi_f;
+    if (!(lo <= hi)) return lo > hi;  // no phi accepted (or NaN limits: refuse)
+    const float n = static_cast<float>(ax.phi_bins);
+    for (const float phi : {lo, hi}) {
+        const float v = (phi - ax.phi_min) / (ax.phi_max - ax.phi_min) * n;
+        // int(v) in [-n, 2n)  <=>  -n - 1 < v < 2n  (truncation toward zero)
+        if (!(v > -n - 1.f && v < 2.f * n)) return false;
+    }
+    return true;
 }
 
 }  // namespace
@@ -161,8 +191,9 @@ extern "C" seedgb_status seedgb_spacepoint_binning_noalloc(
     if (st != SEEDGB_OK) return st;
     const uint64_t nbins = static_cast<uint64_t>(ax.phi_bins) * ax.z_bins;
     if (ax.phi_bins == 0 || nbins > static_cast<uint64_t>(kMaxBins)) return SEEDGB_SIZE_LIMIT;
+    if (!grid_places_finder_phi(*finder, ax)) return SEEDGB_BAD_CONFIG;
     void* scratch = nullptr;
-    const seedgb_status sst = scratch_address(&scratch);
+    const seedgb_status sst = scratch_address(static_cast<cudaStream_t>(stream), &scratch);
     if (sst != SEEDGB_OK) return sst;
     seedgb_seedfilter_config flt;
     seedgb_seedfilter_config_default(&flt);
