@@ -84,7 +84,7 @@ def parse():
     p.add_argument("--no-learned", action="store_true",
                    help="skip training and timing the learned doublet filter")
     p.add_argument("--filter-events", type=int, default=FILTER_TRAIN_EVENTS)
-    p.add_argument("--profile-case", choices=["plain4", "learned4", "train", "batch64"],
+    p.add_argument("--profile-case", choices=["plain4", "plain20", "learned4", "train", "batch64"],
                    help="run one small fixed workload for an ncu capture and exit")
     return p.parse_args()
 
@@ -364,6 +364,62 @@ def run_batched(args, dev, stream, flush_buf, inputs, model=None):
                                   "max": float(frac.max())}
         rep["fallback_events"] = int(fb.sum())
     return rep, outs
+
+
+def run_trk1000(args, stream, flush_buf):
+    """The 1000-track event (trk1000, seed 0, ~10k spacepoints, 10 % noise):
+    ms per event through the per-event API (seeding then parameters), device
+    time with the L2 flushed before each event, and its parity with the
+    committed oracle outputs (tests/golden/trk1000_s0.npz): seeds bit-exact,
+    parameters within 1e-5 relative."""
+    import torch
+
+    from traccc_gb300 import seeding, synth
+    ev = synth.workload_event("trk1000", 0)
+    f, g, fl, tp = seeding.default_configs()
+    alg = seeding.TripletSeedingAlgorithm(f, g, fl)
+    est = seeding.SeedParameterEstimationAlgorithm(tp)
+    sps = seeding.SpacepointCollection.from_numpy(ev)
+    meas = seeding.MeasurementCollection.from_numpy(ev)
+    out = seeding.SeedBuffer(alg.max_seeds(len(sps)))
+    par = seeding.ParamsBuffer(out.capacity)
+    bf = (0.0, 0.0, float(f.bFieldInZ))
+    sptr = stream.cuda_stream
+
+    def one():
+        alg(sps, out, stream=sptr)
+        est(bf, meas, sps, out, par, stream=sptr)
+
+    for _ in range(max(3, args.warmup)):
+        one()
+    torch.cuda.synchronize()
+    ev_t = [torch.cuda.Event(enable_timing=True) for _ in range(2 * args.steps)]
+    for k in range(args.steps):
+        flush_buf.fill_(1)
+        ev_t[2 * k].record(stream)
+        one()
+        ev_t[2 * k + 1].record(stream)
+    torch.cuda.synchronize()
+    ms = [ev_t[2 * k].elapsed_time(ev_t[2 * k + 1]) for k in range(args.steps)]
+    gold = np.load(os.path.join(ROOT, "tests", "golden", "trk1000_s0.npz"))
+    got = out.to_numpy()
+    seeds_ok = bool(np.array_equal(got, gold["seeds"]))
+    gp, rp = par.to_numpy(), gold["params"]
+    params_ok = False
+    if seeds_ok and len(gp) == len(rp):
+        a, b = gp["params"].astype(np.float64), rp["params"].astype(np.float64)
+        d = np.abs(a - b)
+        d[:, 2] = np.abs((a[:, 2] - b[:, 2] + np.pi) % (2 * np.pi) - np.pi)
+        params_ok = bool(np.all(gp["surface_link"] == rp["surface_link"]) and
+                         np.all(d <= 1e-5 * 0.5 * (np.abs(a) + np.abs(b)) + 1e-30))
+    return {"workload": "trk1000: 1 synthetic event (seed 0), 1000 helices, pT log-U(0.5, 20) "
+                        "GeV, 10% noise, %d spacepoints" % len(sps),
+            "ms_per_event": statistics.median(ms), "ms_per_event_mean": sum(ms) / len(ms),
+            "events_per_s": 1e3 * len(ms) / sum(ms), "seeds": len(got),
+            "parity": {"seeds_bit_exact": seeds_ok, "params_within_1e-5": params_ok,
+                       "against": "tests/golden/trk1000_s0.npz (oracle outputs)"},
+            "timing": "per-event API (seedgb_seeding_run + seedgb_params_run), device "
+                      "time, L2 flushed before each event"}
 
 
 FILTER_TRAIN_EVENTS = 200
@@ -771,6 +827,8 @@ def run_gpu(args):
     e2e_s = time.perf_counter() - t0
     barrier()
 
+    trk1000 = run_trk1000(args, stream, flush_buf) if world == 1 else None
+
     learned_line = None
     batched = None
     if world == 1 and not args.no_learned:
@@ -832,7 +890,10 @@ def run_gpu(args):
     value = job_throughput(n_ev, args.steps, world, dev_s)
     e2e_value = job_throughput(n_ev, args.steps, world, e2e_s)
 
-    # roofline of the dominant kernel
+    # roofline of the dominant kernel (seed_fast).  Its binding limit is
+    # instruction issue: the headline is warp instructions issued per second
+    # against SMs x 4 schedulers x clock.  HBM (algorithmic bytes) and the
+    # reference-equivalent FP32 op rate are reported beside it.
     dom = max(kt_sum, key=kt_sum.get)
     dom_ms = kt_sum[dom] / args.steps
     n_valid, n_seeds = counters["n_valid"], counters["n_seeds"]
@@ -852,36 +913,23 @@ def run_gpu(args):
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
     achieved = ab / (dom_ms * 1e-3) / 1e9
     prof = load_profile_traffic(dom, n_ev) or {}
-    roofline = {
-        "bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak,
-        "unit": "GB/s", "frac": achieved / hbm_peak,
+    sm_mhz = clocks.get("sm_mhz") or float(peaks.get("sm_max_mhz", 2070.0))
+    n_sm = torch.cuda.get_device_properties(dev).multi_processor_count
+    hbm = {
+        "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+        "frac": achieved / hbm_peak, "algorithmic_bytes_per_launch": int(ab),
         "traffic": prof.get("dram_bytes_per_launch"),
         "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else
-                       "fallback 6800 GB/s",
-        "avg_launch_ms": dom_ms,
-        "share": kt_sum[dom] / max(1e-12, sum(step_ms)),
-        "note": "seed_fast is issue-bound, not HBM-bound: see issue_roofline",
+                       "fallback 6800 GB/s (of fallback)",
     }
-    if prof.get("inst_issued_per_launch"):
-        sm_mhz = clocks.get("sm_mhz") or 1900.0
-        n_sm = torch.cuda.get_device_properties(dev).multi_processor_count
-        peak_issue = n_sm * 4 * sm_mhz * 1e6
-        ach_issue = prof["inst_issued_per_launch"] / (dom_ms * 1e-3)
-        roofline["issue_roofline"] = {
-            "achieved_warp_inst_per_s": ach_issue, "peak_warp_inst_per_s": peak_issue,
-            "frac": ach_issue / peak_issue,
-            "source": "warp instructions issued per launch from the ncu capture in "
-                      "profiles/, launch duration measured live, peak = SMs x 4 "
-                      "schedulers x median SM clock"}
+    fp32 = None
     om = load_op_model(n_ev) if dom == "seed_fast" else None
     if om is not None:
-        sm_mhz = clocks.get("sm_mhz") or 1900.0
-        n_sm = torch.cuda.get_device_properties(dev).multi_processor_count
         peak_fma = n_sm * 128 * 2 * sm_mhz * 1e6
         ach = om["flop_seeding_total"] / (dom_ms * 1e-3)
-        roofline["fp32_op_model"] = {
-            "flop_per_launch": om["flop_seeding_total"],
-            "achieved_tflops": ach / 1e12, "peak_tflops": peak_fma / 1e12,
+        fp32 = {
+            "bound": "fp32", "flop_per_launch": om["flop_seeding_total"],
+            "achieved": ach / 1e12, "peak": peak_fma / 1e12, "unit": "TFLOP/s",
             "frac": ach / peak_fma, "frac_of_fma_free_peak": 2 * ach / peak_fma,
             "source": "profiles/op_model.json: FP32 operations of the reference's doublet "
                       "and triplet tests and lin_circles for these 20 events, counted by "
@@ -889,6 +937,27 @@ def run_gpu(args):
                       "build is FMA-free (bit-exact cuts), so half that peak is attainable; "
                       "the GPU skips most triplet tests (exact cot(theta) window), so this "
                       "is a reference-work-equivalent rate"}
+    common = {"kernel": dom, "avg_launch_ms": dom_ms,
+              "share": kt_sum[dom] / max(1e-12, sum(step_ms)),
+              "sm_mhz": sm_mhz, "sms": n_sm}
+    if prof.get("inst_issued_per_launch"):
+        peak_issue = n_sm * 4 * sm_mhz * 1e6
+        ach_issue = prof["inst_issued_per_launch"] / (dom_ms * 1e-3)
+        roofline = dict(common, **{
+            "bound": "issue", "achieved": ach_issue / 1e9, "peak": peak_issue / 1e9,
+            "unit": "G warp-instructions/s", "frac": ach_issue / peak_issue,
+            "traffic": prof.get("dram_bytes_per_launch"),
+            "inst_issued_per_launch": prof["inst_issued_per_launch"],
+            "count_source": prof.get("source"),
+            "duration": "average launch time of this run (CUDA events on the launching "
+                        "stream); peak = SMs x 4 schedulers x median SM clock of this run",
+            "hbm": hbm})
+        if fp32 is not None:
+            roofline["fp32_op_model"] = fp32
+    elif fp32 is not None:
+        roofline = dict(common, **fp32, traffic=prof.get("dram_bytes_per_launch"), hbm=hbm)
+    else:
+        roofline = dict(common, **hbm)
 
     kernels = {k: v / args.steps for k, v in kt_sum.items()}
     line = {
@@ -917,6 +986,8 @@ def run_gpu(args):
                  "triplets": counters["n_triplets"],
                  "overflow_middles": counters["n_overflow_middles"]},
     }
+    if trk1000 is not None:
+        line["trk1000"] = trk1000
     if learned_line is not None:
         line["learned"] = learned_line
     if batched is not None:
@@ -939,6 +1010,7 @@ def run_gpu(args):
 #         python bench.py --profile-case <case>
 # captures exactly those launches however many came before.  Cases:
 #   plain4    plain seeding of 4 events of the 100k-spacepoint workload
+#   plain20   the same for the bench step's 20 events
 #   learned4  the same 4 events with the learned doublet filter (trained on
 #             16 events, calibrated on 4)
 #   train     one gradient step of the filter's network on the doublets of
@@ -959,17 +1031,27 @@ def _range(torch, fn):
     torch.cuda.nvtx.range_pop()
 
 
-def case_plain4():
+def _case_plain(n):
     import torch
 
     from traccc_gb300 import seeding
-    sps = [seeding.SpacepointCollection.from_numpy(e) for e in _events(4)]
+    sps = [seeding.SpacepointCollection.from_numpy(e) for e in _events(n)]
     alg = seeding.TripletSeedingAlgorithm()
     outs = [seeding.SeedBuffer(alg.max_seeds(len(s))) for s in sps]
     for _ in range(2):
         alg.run_batch(sps, outs)
     _range(torch, lambda: alg.run_batch(sps, outs))
     assert alg.last_status() == seeding.OK
+
+
+def case_plain4():
+    _case_plain(4)
+
+
+def case_plain20():
+    # the bench step's 20 events (seeds 0-19): for single-pass counters of
+    # the exact launch the bench times
+    _case_plain(N_EVENTS)
 
 
 def _trained_model(alg):
@@ -1029,7 +1111,7 @@ def case_batch64():
     assert alg.last_status() == seeding.OK
 
 
-PROFILE_CASES = {"plain4": case_plain4, "learned4": case_learned4, "train": case_train,
+PROFILE_CASES = {"plain4": case_plain4, "plain20": case_plain20, "learned4": case_learned4, "train": case_train,
          "batch64": case_batch64}
 
 

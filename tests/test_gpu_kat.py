@@ -1,0 +1,127 @@
+"""The reference's own known answers, run on the GPU path through the C ABI.
+
+* tests/cpu/test_seeding.cpp:35-181 -- two 5-spacepoint muon events; with the
+  tests' config tweaks (deltaRMax = 100 mm, maxPtScattering = 0.5 GeV, set on
+  the finder after the grid config was copied from it) each gives exactly one
+  seed and one set of track parameters.  These are non-default finder configs,
+  so they also exercise the kernels' handling of a changed radial window and
+  pT-scattering switch.
+* tests/cpu/test_track_params_estimation.cpp:34-144 -- three spacepoints on a
+  helix (p = sqrt(2) GeV, B = 2 T, charge -1 / +1) give |p - sqrt(2)| < 2e-4
+  and the right q/p sign; the points are regenerated from the helix equation
+  (detray's helix class is not available), as the oracle's test does.
+
+Each GPU result is also compared with the oracle's on the same input
+(seeds bit-exact, parameters within 1e-5 relative).
+"""
+import math
+
+import numpy as np
+import pytest
+
+import oracle as O
+from traccc_gb300 import seeding
+
+pytestmark = pytest.mark.gpu
+
+INVALID = 0xFFFFFFFF
+B_2T = 2.0 * 0.000299792458  # 2 T in the reference's unit system
+
+CASE1 = [(36.6706, 10.6472, 104.131), (94.2191, 29.6699, 113.628),
+         (149.805, 47.9518, 122.979), (218.514, 70.3049, 134.029),
+         (275.359, 88.668, 143.378)]
+CASE2 = [(36.301, 13.1197, 106.83), (93.9366, 33.7101, 120.978),
+         (149.192, 52.0562, 134.678), (218.398, 73.1025, 151.979),
+         (275.322, 89.0663, 166.229)]
+
+
+def _event(points):
+    n = len(points)
+    return {"measurement_index_1": np.arange(n, dtype=np.uint32),
+            "measurement_index_2": np.full(n, INVALID, np.uint32),
+            "global": np.asarray(points, np.float32),
+            "z_variance": np.zeros(n, np.float32),
+            "radius_variance": np.zeros(n, np.float32),
+            "local_position": np.zeros((n, 2), np.float32),
+            "surface_link": np.zeros(n, np.uint64)}
+
+
+def _tweak(f):
+    # tests/cpu/test_seeding.cpp:43-44, after the grid config was copied
+    f.deltaRMax = 100.0
+    f.maxPtScattering = 0.5
+
+
+def _close(a, b, rel=1e-5):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return np.all(np.abs(a - b) <= rel * 0.5 * (np.abs(a) + np.abs(b)) + 1e-30)
+
+
+@pytest.mark.parametrize("points", [CASE1, CASE2], ids=["case1", "case2"])
+def test_seeding_cases_give_one_seed_on_the_gpu(points):
+    import torch
+    f, g, fl, tp = seeding.default_configs()
+    _tweak(f)
+    ev = _event(points)
+    alg = seeding.TripletSeedingAlgorithm(f, g, fl)
+    est = seeding.SeedParameterEstimationAlgorithm(tp)
+    sps = seeding.SpacepointCollection.from_numpy(ev)
+    meas = seeding.MeasurementCollection.from_numpy(ev)
+    seeds = alg(sps)
+    params = est((0.0, 0.0, B_2T), meas, sps, seeds)
+    torch.cuda.synchronize()
+    assert alg.last_status() == seeding.OK
+    got = seeds.to_numpy()
+    # ASSERT_EQ(seeds.size(), 1u) and ASSERT_EQ(bound_params.size(), 1u)
+    assert len(got) == 1
+    assert len(params) == 1
+    assert (got["bottom"][0], got["middle"][0], got["top"][0]) == (0, 1, 2)
+    # and the same seed and parameters as the oracle
+    of, og, ofl, otp = O.default_configs()
+    _tweak(of)
+    ref, _ = O.seeding(ev, of, og, ofl, phi_mode=O.PHI_CR)
+    assert np.array_equal(got, ref)
+    gp = params.to_numpy()
+    rp = O.track_params(ev, ref, (0.0, 0.0, B_2T), otp)
+    assert np.array_equal(gp["surface_link"], rp["surface_link"])
+    assert _close(gp["params"], rp["params"])
+    assert _close(gp["cov"], rp["cov"])
+
+
+def _helix_points(q, s_values):
+    """Positions at path lengths s on the helix from the origin with
+    direction (1, 0, 1)/sqrt(2), |p| = sqrt(2) GeV, in B = (0, 0, 2 T)."""
+    qop = q / math.sqrt(2.0)
+    st = 1.0 / math.sqrt(2.0)
+    w = -qop * B_2T
+    return [(st / w * math.sin(w * s), -st / w * (math.cos(w * s) - 1.0), st * s)
+            for s in s_values]
+
+
+@pytest.mark.parametrize("q", [-1.0, 1.0], ids=["negative", "positive"])
+def test_track_params_on_a_helix_on_the_gpu(q):
+    import torch
+    ev = _event(_helix_points(q, [50.0, 100.0, 150.0]))
+    _, _, _, tp = seeding.default_configs()
+    est = seeding.SeedParameterEstimationAlgorithm(tp)
+    sps = seeding.SpacepointCollection.from_numpy(ev)
+    meas = seeding.MeasurementCollection.from_numpy(ev)
+    seeds = seeding.SeedBuffer(1)
+    for col, v in ((seeds.bottom_index, 0), (seeds.middle_index, 1), (seeds.top_index, 2)):
+        col.fill_(v)
+    seeds.quality.fill_(0.0)
+    seeds.size.fill_(1)
+    params = est((0.0, 0.0, B_2T), meas, sps, seeds)
+    torch.cuda.synchronize()
+    p = params.to_numpy()
+    assert len(p) == 1
+    qop = float(p["params"][0][4])
+    # test_track_params_estimation.cpp: |p - sqrt(2) GeV| < 2e-4 GeV, q/p sign
+    assert abs(abs(q / qop) - math.sqrt(2.0)) < 2e-4
+    assert (qop < 0) == (q < 0)
+    ref = np.zeros(1, O.SEED_DTYPE)
+    ref[0] = (0, 1, 2, 0.0)
+    rp = O.track_params(ev, ref, (0.0, 0.0, B_2T), O.default_configs()[3])
+    assert _close(p["params"], rp["params"])
+    assert _close(p["cov"], rp["cov"])

@@ -9,6 +9,8 @@
   surfaces) reproduces the events' global positions, keeps measurement order
   and skips non-pixel measurements and unknown surfaces.
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -108,3 +110,39 @@ def test_oracle_formation_on_the_barrel():
     keep = np.nonzero((dims == 2) & (link < 11))[0]
     assert np.array_equal(sp2["measurement_index_1"], keep.astype(np.uint32))
     assert np.array_equal(sp2["global"], sp["global"][keep])
+
+
+MOCK = "/root/reference/tests/io/mock_data"
+
+
+@pytest.mark.skipif(not os.path.isdir(MOCK), reason="the reference's test data is not here")
+def test_csv_readers_on_the_reference_mock_event():
+    """The reference's own CSV test event (tests/io/mock_data, used by
+    tests/io/test_event_data.cpp:66-140: three particles, one hit and one
+    measurement each).  The hits become three spacepoints with the files'
+    positions (decimal -> float, correctly rounded) and measurement indices
+    0, 1, 2 through the measurement-hit-id map, as
+    io/src/csv/read_spacepoints.cpp:39-77 builds them.  The three
+    measurements keep their geometry id; their local_key column holds the raw
+    byte 0x06 (the reference's uint8_t field, read as one character), so loc0
+    and loc1 are both active (io/src/csv/make_measurement_edm.cpp:36-52) and
+    the local positions are the files' local0 / local1."""
+    sp = seeding.read_spacepoints_csv(os.path.join(MOCK, "event000000000-hits.csv"),
+                                      os.path.join(MOCK, "event000000000-measurement-simhit-map.csv"))
+    want = np.array([[39.2037048, 0.352969825, -1502.5],
+                     [31.5048428, 5.16000509, -1502.5],
+                     [90.4015808, 0.7420941, -1502.5]], np.float32)
+    assert np.array_equal(sp["global"], want)
+    assert sp["measurement_index_1"].tolist() == [0, 1, 2]
+    assert np.all(sp["measurement_index_2"] == 0xFFFFFFFF)
+    assert not sp["z_variance"].any() and not sp["radius_variance"].any()
+    m = seeding.read_measurements_csv(os.path.join(MOCK, "event000000000-measurements.csv"))
+    assert m["surface_link"].tolist() == [1224979236083738112] * 3
+    assert m["dimensions"].tolist() == [2, 2, 2]
+    assert np.array_equal(m["local_position"], np.array(
+        [[4.2657785415649414, 11.742777824401855], [2.4493119716644287, -17.223770141601562],
+         [3.1442358493804932, 21.099834442138672]], np.float32))
+    # the read columns feed the seeding path: all three are inside the
+    # default finder's z and radius range and are binned
+    off, bins, _, st = O.binning(dict(sp))
+    assert sorted(bins.tolist()) == [0, 1, 2]

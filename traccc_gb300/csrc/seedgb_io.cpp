@@ -85,6 +85,22 @@ bool to_u64(const std::string& s, uint64_t& v) {
     return end && *end == '\0' && errno != ERANGE;
 }
 
+// local_key: the reference's CSV record holds it as uint8_t
+// (io/include/traccc/io/csv/measurement.hpp:23), which its stream-based reader
+// extracts as one character whose byte value is the key -- the reference's own
+// test data stores the raw byte (tests/io/mock_data/
+// event000000000-measurements.csv: 0x06, loc0 and loc1 active).  A one-
+// character field is therefore that byte (a digit '0'..'7' gives the same
+// active bits as its decimal value); a longer field is read as a decimal key
+// up to 255 (an extension: the reference would read only its first character).
+bool to_key(const std::string& s, uint64_t& key) {
+    if (s.size() == 1) {
+        key = static_cast<unsigned char>(s[0]);
+        return true;
+    }
+    return to_u64(s, key) && key <= 255;
+}
+
 }  // namespace
 
 extern "C" {
@@ -180,8 +196,8 @@ seedgb_status seedgb_csv_read_measurements(const char* meas_path, uint64_t capac
         split(l, fields);
         uint64_t gid, key;
         float l0, l1;
-        if (fields.size() <= need || !to_u64(fields[c[0]], gid) || !to_u64(fields[c[1]], key) ||
-            !to_float(fields[c[2]], l0) || !to_float(fields[c[3]], l1) || key > 255)
+        if (fields.size() <= need || !to_u64(fields[c[0]], gid) || !to_key(fields[c[1]], key) ||
+            !to_float(fields[c[2]], l0) || !to_float(fields[c[3]], l1))
             return SEEDGB_INVALID_ARGUMENT;
         if (i < capacity) {
             // make_measurement_edm.cpp:36-52: bit 1 -> loc0, bit 2 -> loc1
