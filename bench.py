@@ -22,13 +22,14 @@ estimation (one batched launch for all events).
           bounded sample of the same events, one event per host thread
 
 Also in the JSON line (one GPU):
-  learned : the same 20-event step with the learned doublet filter, trained
-            on the GPU by the library's kernels (200 events, pileup9k per-track
-            statistics, U(500, 12000) tracks), thresholds per event-size class
-            calibrated for 99.7 % seed recall on 48 held-out events (a margin
-            above the 99.5 % target); events/s, speed-up against the plain
-            step, per-event recall, seeds outside the plain set, pruned
-            fraction, fallback events, training report
+  learned : the same 20-event step with the learned doublet filter gating
+            whole middles (a subset of the plain seeds by construction),
+            trained on the GPU by the library's kernels (200 pileup9k events),
+            gate thresholds per event-size class calibrated for 99.7 % seed
+            recall on 48 held-out events (a margin above the 99.5 % target);
+            events/s, speed-up against the plain step, per-event recall,
+            seeds outside the plain set, pruned fraction, fallback events,
+            training report
   batched : the 64-event uneven batch (5k-114k spacepoints per event) through
             the captured graph with the autotuned launch shape, plain and
             with the filter: events/s, p50/p99 batch latency (device and end
@@ -435,29 +436,41 @@ FILTER_CALIB_TARGET = 0.997
 FILTER_CALIB_MIN_EVENT = 0.995
 
 
+FILTER_TRAIN_SEED0 = 1000
+
+
 def train_filter(args):
-    """Learned doublet filter: 200 training events with pileup9k's per-track
-    statistics and U(500, 12000) tracks each (batch seed 10, so that the
-    filter sees the densities of the uneven batch), labels from the plain
-    seeder, trained with the library's kernels; thresholds and band
-    calibrated per event-size class on 48 held-out events of the same kind
-    (batch seed 20) for >= 99.7 % seed recall over each class's events (a
-    margin above the 99.5 % target for unseen events) and >= 99.5 % on each
-    of them."""
+    """Learned doublet filter (middle gate): 200 training events of the
+    100k-spacepoint workload's statistics (pileup9k, 9000 tracks, seeds
+    1000-1199, disjoint from the bench events), labels from the plain seeder,
+    trained with the library's kernels; the gate threshold and band
+    calibrated per event-size class on 48 held-out events spanning the
+    uneven batch's sizes (U(500, 12000) tracks, batch seed 20) for >= 99.7 %
+    seed recall over each class's events (a margin above the 99.5 % target
+    for unseen events) and >= 99.5 % on each of them."""
     from traccc_gb300 import learned, seeding, synth
     t0 = time.perf_counter()
-    train_ev = synth.batch_events(args.filter_events, 10)
+    train_ev = [synth.workload_event("pileup9k", FILTER_TRAIN_SEED0 + s)
+                for s in range(args.filter_events)]
     calib_ev = synth.batch_events(FILTER_CALIB_EVENTS, 20)
     gen_s = time.perf_counter() - t0
     alg = seeding.TripletSeedingAlgorithm()
     model, rep = learned.build_filter(
         alg, train_ev, calib_ev, epochs=4, target=FILTER_CALIB_TARGET, class_max=FILTER_SIZE_CLASSES,
-        min_event=FILTER_CALIB_MIN_EVENT,
-        quantiles=(0.02, 0.015, 0.01, 0.008, 0.006, 0.005, 0.004, 0.003, 0.0025, 0.002,
-                   0.0015, 0.001, 0.0005, 0.0))
+        min_event=FILTER_CALIB_MIN_EVENT)
     rep["generate_s"] = gen_s
+    rep["train_workload"] = (f"pileup9k statistics, {len(train_ev)} events (seeds "
+                             f"{FILTER_TRAIN_SEED0}-{FILTER_TRAIN_SEED0 + len(train_ev) - 1})")
+    rep["calib_workload"] = f"{FILTER_CALIB_EVENTS} uneven events (batch seed 20), size classes"
+    rep["mode"] = "middle gate"
     rep.pop("candidates", None)
     return model, rep
+
+
+def _finite(v):
+    """JSON-safe float: None for infinities (a role the filter keeps whole)."""
+    v = float(v)
+    return v if np.isfinite(v) else None
 
 
 def recall_report(plain, learned_keys):
@@ -865,9 +878,10 @@ def run_gpu(args):
             "pruned_fraction": {"mean": float(frac.mean()), "min": float(frac.min()),
                                 "max": float(frac.max())},
             "fallback_events": int(fb.sum()),
-            "threshold": [float(v) for v in model.threshold],
+            "mode": "middle gate (prune_top = SEEDGB_FILTER_GATE_MIDDLE)",
+            "threshold": [_finite(v) for v in model.threshold],
             "band": [float(v) for v in model.band],
-            "size_classes": [[int(m), [float(t) for t in th], [float(b) for b in bd]]
+            "size_classes": [[int(m), [_finite(t) for t in th], [float(b) for b in bd]]
                              for m, th, bd in (model.classes or [])],
             "training": train_rep,
         }

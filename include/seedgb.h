@@ -409,7 +409,18 @@ seedgb_status seedgb_seeding_get_tune(seedgb_seeding* h, seedgb_tune* t);
 /* fraction of the scored doublets lies outside [band[0], band[1]], the     */
 /* event is seeded again without the filter inside the same launch          */
 /* sequence (fallback).                                                      */
+/*                                                                          */
+/* prune_top = SEEDGB_FILTER_GATE_MIDDLE gates whole middles instead: a     */
+/* middle none of whose middle-top doublets reaches threshold[1] yields no  */
+/* seed (its middle-top doublets count as pruned), every other middle is   */
+/* seeded with all its doublets.  The reference selects seeds per middle   */
+/* from that middle's triplets alone (core/src/seeding/seed_finding.cpp:    */
+/* 76-116), so the gated output is a subset of the plain seeds by           */
+/* construction.                                                             */
 /* ------------------------------------------------------------------------ */
+#define SEEDGB_FILTER_KEEP 0u           /* score only */
+#define SEEDGB_FILTER_PRUNE_DOUBLETS 1u /* drop doublets below the threshold */
+#define SEEDGB_FILTER_GATE_MIDDLE 2u    /* prune_top only: gate whole middles */
 typedef struct {
     float mu[8], isd[8];
     float w1[8 * 32];   /* [input][output], rounded to bf16 when loaded */
@@ -421,7 +432,7 @@ typedef struct {
     float threshold[2];
     uint32_t n_edges;   /* <= 15 */
     float edges[15];    /* ascending radial band edges (mm) */
-    uint32_t prune_bottom, prune_top;
+    uint32_t prune_bottom, prune_top; /* SEEDGB_FILTER_* */
     float band[2];
     /* Optional per-event-size classes (n_size_classes <= 8; 0: threshold and
      * band above apply to every event).  An event with n spacepoints belongs
@@ -522,6 +533,39 @@ seedgb_status seedgb_params_run_batch(seedgb_params* h, const float bfield[3],
                                       const seedgb_seed_buffer* seeds,
                                       seedgb_params_buffer* outs, uint32_t n_events,
                                       void* stream);
+
+/* ------------------------------------------------------------------------ */
+/* Hand-off to the combinatorial Kalman filter                               */
+/* ------------------------------------------------------------------------ */
+
+/* The record the reference's track finding takes as seeds:
+ * bound_track_parameters_collection_types::buffer, whose element is detray's
+ * bound_track_parameters over the array algebra
+ * (core/include/traccc/edm/track_parameters.hpp:29-49; consumed by
+ * combinatorial_kalman_filter_algorithm at
+ * examples/run/cuda/src/full_chain_algorithm.cpp:241-247).  detray is not
+ * vendored, so this layout follows its published definition and is NOT
+ * pinned against a build of it: the bound parameter vector (a 6 x 1 matrix:
+ * loc0, loc1, phi, theta, q/p, time), the surface barcode (64 bits), then the
+ * 6 x 6 covariance as the array algebra stores matrices, an array of columns
+ * (element (row, col) at covariance[col * 6 + row]). */
+typedef struct {
+    float vector[6];
+    uint64_t barcode;
+    float covariance[36];
+} seedgb_ckf_bound_track_parameters;
+
+/* Converts a parameter buffer (seedgb_params_run / _run_batch output) into
+ * the CKF's record layout on the device, keeping the parameters device-
+ * resident: reads the count from in->size on the device, writes
+ * min(count, capacity) records to `out` (device, 16-byte aligned) and that
+ * number to *out_size (device; may be NULL).  Asynchronous on `stream`; one
+ * launch, no host synchronisation (graph-capturable like the seeding
+ * launches).  No counterpart in the reference, which estimates parameters
+ * directly in this layout. */
+seedgb_status seedgb_params_to_ckf(const seedgb_params_buffer* in,
+                                   seedgb_ckf_bound_track_parameters* out, uint32_t capacity,
+                                   uint32_t* out_size, void* stream);
 
 /* ------------------------------------------------------------------------ */
 

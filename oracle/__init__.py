@@ -297,10 +297,15 @@ class DoubletFilter(C.Structure):
                 ("prune_bottom", C.c_uint32), ("prune_top", C.c_uint32)]
 
 
+FILTER_KEEP, FILTER_PRUNE_DOUBLETS, FILTER_GATE_MIDDLE = 0, 1, 2
+
+
 def doublet_filter(model: dict, threshold, prune_bottom=True, prune_top=True):
     """A DoubletFilter from a model dict with numpy arrays mu, isd, w1 (8x32),
     b1, w2 (32x32), b2, w3 (32), b3 and edges; threshold = (middle-bottom,
-    middle-top) logit thresholds (or one for both)."""
+    middle-top) logit thresholds (or one for both).  prune_bottom / prune_top:
+    False / True (keep / drop doublets below the threshold) or a FILTER_*
+    mode (prune_top = FILTER_GATE_MIDDLE gates whole middles)."""
     f = DoubletFilter()
     def put(name, arr):
         arr = np.asarray(arr, np.float32).reshape(-1)
@@ -314,8 +319,8 @@ def doublet_filter(model: dict, threshold, prune_bottom=True, prune_top=True):
     edges = np.asarray(model["edges"], np.float32)
     f.n_edges = len(edges)
     f.edges[: len(edges)] = edges.tolist()
-    f.prune_bottom = 1 if prune_bottom else 0
-    f.prune_top = 1 if prune_top else 0
+    f.prune_bottom = int(prune_bottom)
+    f.prune_top = int(prune_top)
     return f
 
 

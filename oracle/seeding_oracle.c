@@ -701,10 +701,12 @@ float or_mlp_logit(const or_doublet_filter* f, const float feat[OR_MLP_IN]) {
 static int score_role(const or_doublet_filter* filt, int top, uint32_t spM,
                       const float m[6], const or_spacepoints* sps, vec_t* v,
                       or_doublet_rec* dump, uint64_t dump_cap, uint64_t* n_dump,
-                      uint64_t* n_scored, uint64_t* n_pruned) {
+                      uint64_t* n_scored, uint64_t* n_pruned, int* reach) {
     dbl_t* D = (dbl_t*)v->p;
     size_t w = 0;
-    const int may_prune = filt && (top ? filt->prune_top : filt->prune_bottom);
+    const uint32_t mode = filt ? (top ? filt->prune_top : filt->prune_bottom) : 0u;
+    const int may_prune = mode == 1u;
+    *reach = 0;
     for (size_t k = 0; k < v->n; ++k) {
         float ov[6], feat[OR_MLP_IN];
         load_sp(sps, D[k].sp, ov);
@@ -722,6 +724,7 @@ static int score_role(const or_doublet_filter* filt, int top, uint32_t spM,
             ++*n_dump;
         }
         (*n_scored)++;
+        if (filt && logit >= filt->threshold[top ? 1 : 0]) *reach = 1;
         if (may_prune && !(logit >= filt->threshold[top ? 1 : 0])) {
             (*n_pruned)++;
             continue;
@@ -795,11 +798,17 @@ int or_seeding_ex(const or_finder_config* fc, const or_grid_config* gc,
             if (filt || dump) {
                 /* bottoms first; a middle left without bottoms has no seeds
                  * and its tops are not scored */
+                int reach = 0;
                 score_role(filt, 0, spM, m, sps, &mb, dump, dump_cap, n_dump,
-                           &st->n_scored_mb, &st->n_pruned_mb);
+                           &st->n_scored_mb, &st->n_pruned_mb, &reach);
                 if (mb.n == 0) continue;
                 score_role(filt, 1, spM, m, sps, &mt, dump, dump_cap, n_dump,
-                           &st->n_scored_mt, &st->n_pruned_mt);
+                           &st->n_scored_mt, &st->n_pruned_mt, &reach);
+                if (filt && filt->prune_top == 2u && !reach) {
+                    /* gated middle: no seed, its middle-top doublets pruned */
+                    st->n_pruned_mt += mt.n;
+                    continue;
+                }
                 if (mt.n == 0) continue;
             }
             if (st) {

@@ -225,7 +225,10 @@ typedef struct {
     float threshold[2];               /* keep when logit >= threshold[top] */
     uint32_t n_edges;
     float edges[OR_MAX_BAND_EDGES];   /* ascending radial band edges */
-    uint32_t prune_bottom, prune_top; /* which roles the filter may drop */
+    uint32_t prune_bottom, prune_top; /* 0 keep, 1 drop doublets below the
+                                       * threshold, 2 (prune_top only) gate
+                                       * whole middles: no seed unless a
+                                       * middle-top doublet reaches it */
 } or_doublet_filter;
 
 /* One scored doublet (dump of or_seeding_ex). */

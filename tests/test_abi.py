@@ -107,3 +107,18 @@ def test_noalloc_refuses_a_grid_too_narrow_for_the_finder_before_device_work():
     st = L.seedgb_spacepoint_binning_noalloc(C.byref(f), C.byref(g), C.byref(v),
                                              C.c_void_p(1), C.c_void_p(1), None)
     assert st != seeding.BAD_CONFIG
+
+
+def test_ckf_record_layout():
+    """The CKF hand-off record: parameter vector (24 B), 64-bit barcode at
+    offset 24, 6 x 6 covariance at offset 32, 176 bytes, as declared in
+    seedgb.h (and the converter refuses null or misaligned buffers without
+    touching a device)."""
+    dt = seeding.CKF_PARAMS_DTYPE
+    assert dt.itemsize == 176
+    assert dt.fields["barcode"][1] == 24 and dt.fields["covariance"][1] == 32
+    L = seeding.lib()
+    assert L.seedgb_params_to_ckf(None, None, 0, None, None) == seeding.INVALID_ARGUMENT
+    b = seeding._ParamsBuffer(16, 4, 16)
+    assert L.seedgb_params_to_ckf(C.byref(b), C.c_void_p(24), 4, None, None) == \
+        seeding.INVALID_ARGUMENT

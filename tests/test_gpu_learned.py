@@ -196,7 +196,8 @@ def test_triplet_dump_matches_oracle(model_and_event):
     assert np.all(got[:, 3] == 0)
 
 
-@pytest.mark.parametrize("prune", [(True, True), (False, True)], ids=["both", "tops"])
+@pytest.mark.parametrize("prune", [(True, True), (False, True), (False, O.FILTER_GATE_MIDDLE)],
+                         ids=["both", "tops", "gate"])
 def test_learned_seeds_match_oracle(model_and_event, prune):
     from traccc_gb300 import seeding
     model, ev = model_and_event
@@ -227,7 +228,36 @@ def test_learned_seeds_match_oracle(model_and_event, prune):
         diff |= {k[1] for k in gk ^ rk}
         assert diff <= amb, sorted(diff - amb)[:10]
     assert abs(int(per[0, 1]) - st["n_pruned_mb"]) <= 2
-    assert abs(int(per[0, 3]) - st["n_pruned_mt"]) <= 2
+    assert abs(int(per[0, 3]) - st["n_pruned_mt"]) <= 2 * (1 if prune[1] != O.FILTER_GATE_MIDDLE
+                                                           else int(per[0, 2]))
+
+
+def test_middle_gate_is_a_subset_of_plain_seeding(model_and_event):
+    """Gating whole middles yields exactly the plain seeds of the middles it
+    keeps -- no seed outside the plain set, whatever the network -- on the
+    GPU (per event, against the GPU's plain seeds) at several thresholds."""
+    from traccc_gb300 import seeding
+    model, _ = model_and_event
+    evs = [synth.workload_event("pileup9k", 31, n_tracks=4000),
+           synth.workload_event("trk1000", 32)]
+    sps = [seeding.SpacepointCollection.from_numpy(e) for e in evs]
+    alg = seeding.TripletSeedingAlgorithm()
+    plain = [o.to_numpy() for o in alg.run_batch(sps)]
+    gated_any = False
+    for thr in (-2.0, 0.0, 1.0):
+        alg.set_filter(model.struct(threshold=(-np.inf, thr), band=(0.0, 1.0),
+                                    prune=(O.FILTER_KEEP, O.FILTER_GATE_MIDDLE)))
+        outs = alg.run_batch(sps)
+        assert alg.last_status() == seeding.OK
+        per, fb, _ = alg.filter_stats(len(sps))
+        assert not fb.any()
+        for p, o in zip(plain, outs):
+            g = o.to_numpy()
+            kept = np.isin(p["middle"], np.unique(g["middle"]))
+            # the gated seeds are the plain seeds of the kept middles, in order
+            assert np.array_equal(g, p[kept])
+            gated_any |= len(g) < len(p)
+    assert gated_any
 
 
 def test_fallback_reseeds_plain(model_and_event):

@@ -13,6 +13,13 @@ from traccc_gb300 import seeding, synth
 pytestmark = pytest.mark.gpu
 
 PARAM_TOL = 1e-5
+# The reference's angle comparison (is_same_angle.cpp) is relative to the
+# angle itself, so it is ill-conditioned near phi = 0: there both sides carry
+# the absolute float rounding (~1e-7 rad) of the direction they take the
+# angle of, and a relative 1e-5 would ask for ~1e-12 rad at phi ~ 1e-7.
+# Such angles pass within this absolute bound instead; tests count them and
+# keep them rare.
+ANGLE_ABS_TOL = 1e-6
 
 
 def run_gpu(ev, cfgs=None, exhaustive=False):
@@ -28,8 +35,10 @@ def run_gpu(ev, cfgs=None, exhaustive=False):
     return alg, sps, out, st
 
 
-def same_params(a, b, tol=PARAM_TOL):
-    """is_same_object<bound_track_parameters> semantics, vectorised."""
+def same_params(a, b, tol=PARAM_TOL, angle_abs=0.0, counts=None):
+    """is_same_object<bound_track_parameters> semantics, vectorised; with
+    angle_abs > 0 an angle also passes within that absolute difference
+    (counted in counts["angle_abs"] when counts is a dict)."""
     ok = a["surface_link"] == b["surface_link"]
     pa, pb = a["params"].astype(np.float64), b["params"].astype(np.float64)
     for k in (0, 1, 3, 4, 5):
@@ -37,8 +46,16 @@ def same_params(a, b, tol=PARAM_TOL):
     d = (pa[:, 2] - pb[:, 2] + np.pi) % (2 * np.pi) - np.pi
     mean = pb[:, 2] + 0.5 * d
     mean = (mean + np.pi) % (2 * np.pi) - np.pi
-    ok &= np.abs(d) <= tol * np.abs(mean)
-    return ok
+    rel = np.abs(d) <= tol * np.abs(mean)
+    absol = np.abs(d) <= angle_abs
+    if counts is not None:
+        counts["angle_abs"] = counts.get("angle_abs", 0) + int((ok & absol & ~rel).sum())
+        bad = ok & ~(rel | absol)
+        counts["worst_angle_diff"] = max(counts.get("worst_angle_diff", 0.0),
+                                         float(np.abs(d[~rel]).max()) if (~rel).any() else 0.0)
+        counts["bad_examples"] = counts.get("bad_examples", []) + [
+            (float(pa[i, 2]), float(pb[i, 2])) for i in np.nonzero(bad)[0][:3]]
+    return ok & (rel | absol)
 
 
 @pytest.mark.parametrize("name,seed", [("trk100", 0), ("trk100", 1), ("trk1000", 0), ("trk1000", 3)])

@@ -9,7 +9,9 @@ from the batched parameter launch the bench times, against the oracle's
 parameter estimation of the same seeds (once the seeds are known to be the
 oracle's, the oracle needs no seeding run: its parameter estimation is
 milliseconds per event): surface links exact, the six parameters and the
-covariance diagonal within 1e-5 relative (angles wrapped)."""
+covariance diagonal within 1e-5 relative (angles wrapped), with phi within
+1e-6 rad absolute where the relative comparison is ill-conditioned (phi near
+zero); those are counted and must stay rare."""
 import json
 import os
 import sys
@@ -26,7 +28,7 @@ sys.path.insert(0, os.path.join(HERE, "golden"))
 sys.path.insert(0, HERE)
 
 import make_workload_hashes as W  # noqa: E402
-from test_gpu_parity import same_params  # noqa: E402
+from test_gpu_parity import ANGLE_ABS_TOL, same_params  # noqa: E402
 
 
 def test_full_workloads_match_the_oracle_digests():
@@ -62,16 +64,21 @@ def _params_match_oracle(events, sps, seed_outs):
     pouts = est.run_batch(bf, meas, sps, seed_outs)
     torch.cuda.synchronize()
     n_all = 0
+    counts = {}
     for e, (ev, so, po) in enumerate(zip(events, seed_outs, pouts)):
         gp = po.to_numpy()
         rp = oracle.track_params(ev, so.to_numpy(), bf)
         assert len(gp) == len(rp) == len(so), e
-        ok = same_params(gp, rp)
+        ok = same_params(gp, rp, angle_abs=ANGLE_ABS_TOL, counts=counts)
         dg = np.diagonal(gp["cov"].reshape(-1, 6, 6), axis1=1, axis2=2).astype(np.float64)
         dr = np.diagonal(rp["cov"].reshape(-1, 6, 6), axis1=1, axis2=2).astype(np.float64)
         ok &= np.all(np.abs(dg - dr) <= 1e-5 * 0.5 * (np.abs(dg) + np.abs(dr)), axis=1)
         off = gp["cov"].reshape(-1, 6, 6) * (1 - np.eye(6, dtype=np.float32))
         ok &= ~off.reshape(len(gp), -1).any(axis=1)
-        assert ok.all(), (e, np.nonzero(~ok)[0][:10])
+        assert ok.all(), (e, np.nonzero(~ok)[0][:10], counts)
         n_all += len(gp)
     assert n_all > 1_000_000
+    # phi near zero (relative comparison ill-conditioned): rare
+    assert counts["angle_abs"] <= 1e-4 * n_all, counts
+    print(f"{n_all} parameter sets; {counts['angle_abs']} phi within {ANGLE_ABS_TOL} rad "
+          f"absolute only (largest such difference {counts['worst_angle_diff']:.3g} rad)")

@@ -156,3 +156,31 @@ def test_pruning_is_monotone(trk1000_event):
         recalls.append(len(pk & set(zip(s["bottom"], s["middle"], s["top"]))) / len(pk))
     assert fracs[0] < fracs[1] < fracs[2]
     assert recalls[0] >= recalls[1] >= recalls[2]
+
+
+def test_middle_gate_keeps_exactly_the_plain_seeds_of_kept_middles(trk1000_event):
+    """Gating whole middles (prune_top = FILTER_GATE_MIDDLE): a middle is
+    seeded, unpruned, iff one of its middle-top doublets reaches the
+    threshold; the reference selects seeds per middle from that middle's
+    triplets alone (core/src/seeding/seed_finding.cpp:76-116), so the output
+    is the plain seeds of the kept middles -- a subset by construction --
+    for any network and threshold."""
+    p, norm = _model(8)
+    _, _, d = O.seeding_ex(trk1000_event, filt=O.doublet_filter(_model_dict(p, norm), -np.inf),
+                           dump=True)
+    plain, _ = O.seeding(trk1000_event)
+    tops = d[d["top"] == 1]
+    for q in (0.2, 0.5, 0.8):
+        th = float(np.quantile(tops["logit"], q))
+        f = O.doublet_filter(_model_dict(p, norm), (-np.inf, th), prune_bottom=O.FILTER_KEEP,
+                             prune_top=O.FILTER_GATE_MIDDLE)
+        s, st, _ = O.seeding_ex(trk1000_event, filt=f)
+        best = {}
+        for m, lg in zip(tops["middle"].tolist(), tops["logit"].tolist()):
+            best[m] = max(best.get(m, -np.inf), lg)
+        kept = np.array([best.get(m, -np.inf) >= th for m in plain["middle"].tolist()])
+        assert np.array_equal(s, plain[kept])
+        assert 0 < len(s) < len(plain)
+        gated = [m for m, b in best.items() if b < th]
+        n_gated_tops = int(np.isin(tops["middle"], gated).sum())
+        assert st["n_pruned_mt"] == n_gated_tops and st["n_pruned_mb"] == 0

@@ -604,6 +604,8 @@ seedgb_status seedgb_seeding_set_filter(seedgb_seeding* h, const seedgb_doublet_
         return SEEDGB_OK;
     }
     if (f->n_edges > 15 || !(f->band[0] <= f->band[1])) return SEEDGB_INVALID_ARGUMENT;
+    if (f->prune_bottom > SEEDGB_FILTER_PRUNE_DOUBLETS || f->prune_top > SEEDGB_FILTER_GATE_MIDDLE)
+        return SEEDGB_INVALID_ARGUMENT;
     for (int i = 0; i < 8; ++i)
         if (!std::isfinite(f->mu[i]) || !std::isfinite(f->isd[i])) return SEEDGB_INVALID_ARGUMENT;
     for (uint32_t i = 1; i < f->n_edges; ++i)

@@ -1139,10 +1139,15 @@ __device__ MiddleResult process_middle(const DevConfig& c, const Arena& a,
         mlp_load_regs(*c.mlp, lane, R);
         uint32_t* xs = ws.bstart;
         float* lg = reinterpret_cast<float*>(ws.bstart + 128);
-        const bool prune = c.mlp_prune_top != 0;
+        // mlp_prune_top: 1 drops the doublets below the threshold; 2 gates
+        // the whole middle (it yields no seed unless one of its middle-top
+        // doublets reaches the threshold, and then runs unpruned)
+        const bool prune = c.mlp_prune_top == SEEDGB_FILTER_PRUNE_DOUBLETS;
+        const bool gate = c.mlp_prune_top == SEEDGB_FILTER_GATE_MIDDLE;
         const float thr = filter_threshold(c, a, ev, 1);
         const uint32_t mid_idx = a.dump ? a.g_idx[gm] : 0u;
         uint32_t w = 0;
+        bool reach = false;
         for (uint32_t base = 0; base < n_mt; base += 32) {
             const uint32_t i = base + lane;
             const bool valid = i < n_mt;
@@ -1161,6 +1166,7 @@ __device__ MiddleResult process_middle(const DevConfig& c, const Arena& a,
             const float logit =
                 score_chunk<true>(c, a, R, x, valid, xs, lg, ev, mid_idx, oth, lane, lt);
             const bool keep = valid && (!prune || logit >= thr);
+            reach |= valid && logit >= thr;
             const uint32_t mask = __ballot_sync(0xffffffffu, keep);
             if (keep) {
                 const uint32_t k = w + __popc(mask & lt);
@@ -1179,6 +1185,7 @@ __device__ MiddleResult process_middle(const DevConfig& c, const Arena& a,
             w += __popc(mask);
             __syncwarp();
         }
+        if (gate && !__any_sync(0xffffffffu, reach)) w = 0;  // gated: no seed
         if (lane == 0) {
             atomicAdd(&a.ev_filter[4 * ev + 2], n_mt);
             atomicAdd(&a.ev_filter[4 * ev + 3], n_mt - w);

@@ -1,10 +1,15 @@
 """Learned doublet filter: data, training and calibration on the GPU.
 
 The filter (seedgb_doublet_filter, include/seedgb.h) scores every doublet of
-a middle spacepoint that has both roles with an MLP 8 -> 32 -> 32 -> 1 and
-drops the doublets below a per-role threshold before triplet finding; the
-plain cuts still run on every survivor.  Everything here runs through the
-seeding library's own kernels:
+a middle spacepoint that has both roles with an MLP 8 -> 32 -> 32 -> 1.  By
+default it gates whole middles: a middle none of whose middle-top doublets
+reaches the threshold yields no seed, every other middle is seeded with all
+its doublets and the plain cuts.  The reference selects seeds per middle
+from that middle's triplets alone, so the output is a subset of the plain
+seeds by construction.  (The older mode, dropping single doublets below a
+per-role threshold, changes the surviving middles' seed weights and ranks
+and so can emit seeds outside the plain set.)  Everything here runs through
+the seeding library's own kernels:
 
 * ``collect``   -- plain seeding of training events with the doublet dump on;
                    label = the doublet appears in an accepted seed (middle and
@@ -14,10 +19,14 @@ seeding library's own kernels:
 * ``train``     -- mini-batch Adam on the weighted logistic loss with the
                    library's forward/backward kernels (bf16 operands, fp32
                    accumulate on the tensor cores, fp32 master weights).
-* ``calibrate`` -- per-role thresholds at a common quantile of the positive
-                   doublets' logits, the most aggressive quantile whose seed
-                   recall against plain seeding is >= the target over the
-                   held-out events (or on every one of them); the
+* ``calibrate`` -- middle gate: the highest threshold on a middle's best
+                   middle-top logit whose seed recall against plain seeding
+                   is >= the target over the held-out events and >= a floor on
+                   every one of them, read off exactly from one scored plain
+                   run (the gated seeds are the plain seeds of the kept
+                   middles), then confirmed by a gated run; doublet pruning:
+                   per-role thresholds at a common quantile of the positive
+                   doublets' logits, checked by seeding runs.  The
                    pruned-fraction band is the range seen on those events,
                    widened by a margin.
 
@@ -50,11 +59,11 @@ class FilterModel:
     edges: np.ndarray             # fp32 radial band edges
     threshold: tuple = (-np.inf, -np.inf)
     band: tuple = (0.0, 1.0)
-    # middle-top doublets only by default: their features come with the
-    # lin_circles the seeder computes anyway, and pruning them shrinks the
-    # triplet search of every middle-bottom doublet
-    prune_bottom: bool = False
-    prune_top: bool = True
+    # seeding.FILTER_* modes per role.  Default: gate middles on their
+    # middle-top doublets (whose features come with the lin_circles the
+    # seeder computes anyway); middle-bottom doublets are not scored
+    prune_bottom: int = seeding.FILTER_KEEP
+    prune_top: int = seeding.FILTER_GATE_MIDDLE
     # per-event-size classes: [(max spacepoints, (thr bottom, thr top),
     # (band lo, band hi)), ...] ascending, or None
     classes: list = None
@@ -79,8 +88,8 @@ class FilterModel:
         f.n_edges = len(e)
         f.edges[: len(e)] = e.tolist()
         pb, pt = (self.prune_bottom, self.prune_top) if prune is None else prune
-        f.prune_bottom = 1 if pb else 0
-        f.prune_top = 1 if pt else 0
+        f.prune_bottom = int(pb)
+        f.prune_top = int(pt)
         b = self.band if band is None else band
         f.band[0] = float(b[0])
         f.band[1] = float(b[1])
@@ -100,7 +109,8 @@ class FilterModel:
         np.savez(path, params=self.params, norm=self.norm, edges=self.edges,
                  threshold=np.asarray(self.threshold, np.float32),
                  band=np.asarray(self.band, np.float32),
-                 prune=np.asarray([self.prune_bottom, self.prune_top], np.uint8), classes=cl)
+                 prune=np.asarray([int(self.prune_bottom), int(self.prune_top)], np.uint8),
+                 classes=cl)
 
     @classmethod
     def load(cls, path):
@@ -109,8 +119,8 @@ class FilterModel:
                   for r in z["classes"]] if "classes" in z.files else []
             return cls(z["params"].astype(np.float32), z["norm"].astype(np.float32),
                        z["edges"].astype(np.float32), tuple(float(v) for v in z["threshold"]),
-                       tuple(float(v) for v in z["band"]), bool(z["prune"][0]),
-                       bool(z["prune"][1]), cl or None)
+                       tuple(float(v) for v in z["band"]), int(z["prune"][0]),
+                       int(z["prune"][1]), cl or None)
 
 
 def init_params(seed=0) -> np.ndarray:
@@ -128,7 +138,7 @@ def scoring_model(edges=None) -> FilterModel:
     """A filter that scores (for the dump) but prunes nothing."""
     return FilterModel(init_params(), np.concatenate([np.zeros(8), np.ones(8)]).astype(np.float32),
                        band_edges() if edges is None else np.asarray(edges, np.float32),
-                       prune_bottom=False, prune_top=False)
+                       prune_bottom=seeding.FILTER_KEEP, prune_top=seeding.FILTER_KEEP)
 
 
 def _key(torch, ev, mid, other):
@@ -342,14 +352,107 @@ def compare(plain, learned):
     return np.asarray(rec), np.asarray(out)
 
 
+def middle_scores(torch, rec, outs):
+    """Per middle with both roles, from a scored plain run's doublet records
+    and seeds: (event, best middle-top logit, plain seed count, middle-top
+    doublet count), numpy arrays."""
+    words = rec.view(torch.int32)
+    role = words[:, 2].to(torch.int64) & 0xffffffff
+    top = (role & 1).bool()
+    ev = (role >> 1)[top]
+    mid = (words[:, 0].to(torch.int64) & 0xffffffff)[top]
+    logit = rec.view(torch.float32)[:, 11][top]
+    key = (ev << 32) | mid
+    ukey, inv = torch.unique(key, return_inverse=True)
+    best = torch.full((len(ukey),), -float("inf"), dtype=torch.float32, device=rec.device)
+    best = best.scatter_reduce(0, inv, logit, reduce="amax", include_self=True)
+    n_mt = torch.bincount(inv, minlength=len(ukey))
+    seeds = torch.zeros(len(ukey), dtype=torch.int64, device=rec.device)
+    for e, o in enumerate(outs):
+        n = int(o.size.item())
+        if n == 0:
+            continue
+        sk = (torch.full((n,), e, dtype=torch.int64, device=rec.device) << 32) | (
+            o.middle_index[:n].to(torch.int64) & 0xffffffff)
+        pos = torch.searchsorted(ukey, sk)
+        hit = (pos < len(ukey)) & (ukey[pos.clamp_max(len(ukey) - 1)] == sk)
+        seeds.index_add_(0, pos[hit], torch.ones(int(hit.sum().item()), dtype=torch.int64,
+                                                   device=rec.device))
+    return ((ukey >> 32).cpu().numpy(), best.cpu().numpy(), seeds.cpu().numpy(),
+            n_mt.cpu().numpy())
+
+
+def gate_recall(ev, best, seeds, n_mt, n_events, thr):
+    """Exact per-event seed recall and pruned fraction of the middle gate at
+    threshold `thr` (the kept middles keep exactly their plain seeds)."""
+    kept = best >= thr
+    tot = np.bincount(ev, weights=seeds, minlength=n_events)
+    keep = np.bincount(ev, weights=seeds * kept, minlength=n_events)
+    mt = np.bincount(ev, weights=n_mt, minlength=n_events)
+    gated = np.bincount(ev, weights=n_mt * ~kept, minlength=n_events)
+    rec = np.where(tot > 0, keep / np.maximum(tot, 1), 1.0)
+    return rec, keep.sum() / max(tot.sum(), 1), gated / np.maximum(mt, 1)
+
+
+def calibrate_gate(alg, model: FilterModel, events, target=0.995, margin=0.05, log=None,
+                   min_event=0.0, **_):
+    """Middle-gate threshold and pruned-fraction band on held-out events: the
+    highest threshold on a middle's best middle-top logit whose exact seed
+    recall (read off one scored plain run) is >= `target` over all held-out
+    seeds and >= `min_event` on every event; then one gated run confirms the
+    recall and that no seed lies outside the plain set."""
+    import torch
+    dev = torch.device("cuda", torch.cuda.current_device())
+    sps = _device_events(torch, events, dev)
+    outs, rec = run_dump(alg, sps, model)
+    plain = seed_keys(outs)
+    ev, best, seeds, n_mt = middle_scores(torch, rec, outs)
+    cand = np.unique(best[seeds > 0])
+    lo, hi = 0, len(cand) - 1          # recall is non-increasing in the threshold
+    chosen = -np.inf
+    while lo <= hi:
+        mid = (lo + hi) // 2
+        r, agg, _ = gate_recall(ev, best, seeds, n_mt, len(events), cand[mid])
+        if agg >= target and r.min() >= min_event:
+            chosen = float(cand[mid])
+            lo = mid + 1
+        else:
+            hi = mid - 1
+    r, agg, frac = gate_recall(ev, best, seeds, n_mt, len(events), chosen)
+    thr = (-np.inf, chosen)
+    alg.set_filter(model.struct(threshold=thr, band=(0.0, 1.0)))
+    louts = alg.run_batch(sps)
+    per, _, _ = alg.filter_stats(len(sps))
+    alg.set_filter(None)
+    rr, oo = compare(plain, seed_keys(louts))
+    frac_run = pruned_fraction(per)
+    c = {"threshold": thr, "recall": float(agg), "min_recall": float(r.min()),
+         "mean_recall": float(r.mean()), "pruned_fraction": [float(frac.min()), float(frac.max())],
+         "mean_pruned_fraction": float(frac.mean()),
+         "gated_run": {"min_recall": float(rr.min()), "outside": int(oo.sum()),
+                       "mean_pruned_fraction": float(frac_run.mean())},
+         "middles": int(len(best)), "middles_gated": int((best < chosen).sum())}
+    if log:
+        log(f"gate threshold {chosen:.4f}: recall {agg:.5f} (event min {r.min():.5f}), "
+            f"gated run min {rr.min():.5f} outside {oo.sum()}, pruned {frac.mean():.4f}")
+    b = (max(0.0, float(frac.min()) - margin), min(1.0, float(frac.max()) + margin))
+    return dataclasses.replace(model, threshold=thr, band=b), {"chosen": c, "band": b}
+
+
 def calibrate(alg, model: FilterModel, events, target=0.995, margin=0.05,
               quantiles=(0.02, 0.015, 0.01, 0.007, 0.005, 0.003, 0.002, 0.001, 0.0005),
               log=None, criterion="total", min_event=0.0):
-    """Thresholds and pruned-fraction band on held-out events (numpy dicts):
-    the most aggressive quantile whose seed recall against plain seeding
-    reaches `target` over all held-out seeds (criterion "total") or on every
-    event ("event"), and `min_event` on every event.  Returns (model with
-    threshold/band set, report)."""
+    """Thresholds and pruned-fraction band on held-out events (numpy dicts).
+    Middle gate: calibrate_gate.  Doublet pruning: the most aggressive
+    quantile whose seed recall against plain seeding reaches `target` over
+    all held-out seeds (criterion "total") or on every event ("event"), and
+    `min_event` on every event.  Returns (model with threshold/band set,
+    report)."""
+    if model.prune_top == seeding.FILTER_GATE_MIDDLE:
+        if criterion == "event":
+            min_event = max(min_event, target)
+        return calibrate_gate(alg, model, events, target=target, margin=margin, log=log,
+                              min_event=min_event)
     import torch
     dev = torch.device("cuda", torch.cuda.current_device())
     sps = _device_events(torch, events, dev)

@@ -111,6 +111,10 @@ class Tune(C.Structure):
                 self.ctas_per_sm)
 
 
+# seedgb_doublet_filter.prune_bottom / prune_top modes
+FILTER_KEEP, FILTER_PRUNE_DOUBLETS, FILTER_GATE_MIDDLE = 0, 1, 2
+
+
 class DoubletFilter(C.Structure):
     """seedgb_doublet_filter: the learned doublet filter's network, input
     standardisation, per-role thresholds, radial band edges and the
@@ -149,6 +153,10 @@ PARAMS_DTYPE = np.dtype([("surface_link", "<u8"), ("params", "<f4", (6,)),
                          ("cov", "<f4", (36,))])
 SEED_DTYPE = np.dtype([("bottom", "<u4"), ("middle", "<u4"), ("top", "<u4"),
                        ("quality", "<f4")])
+# seedgb_ckf_bound_track_parameters: the CKF's record (parameter vector,
+# surface barcode, covariance as an array of columns)
+CKF_PARAMS_DTYPE = np.dtype([("vector", "<f4", (6,)), ("barcode", "<u8"),
+                             ("covariance", "<f4", (36,))])
 
 
 class SeedingError(RuntimeError):
@@ -258,6 +266,8 @@ def lib():
                                               P(_SpacepointView), P(_SeedBuffer),
                                               P(_ParamsBuffer), C.c_uint32, vp]
         L.seedgb_params_run_batch.restype = C.c_int
+        L.seedgb_params_to_ckf.argtypes = [P(_ParamsBuffer), vp, C.c_uint32, vp, vp]
+        L.seedgb_params_to_ckf.restype = C.c_int
         L.seedgb_spacepoint_binning_noalloc.argtypes = [
             P(SeedfinderConfig), P(SpacepointGridConfig), P(_SpacepointView), vp, vp, vp]
         L.seedgb_spacepoint_binning_noalloc.restype = C.c_int
@@ -434,6 +444,27 @@ class ParamsBuffer:
 # ---------------------------------------------------------------------------
 # Algorithms
 # ---------------------------------------------------------------------------
+
+
+def params_to_ckf(params: "ParamsBuffer", out=None, out_size=None, stream=None):
+    """The parameters of `params` in the combinatorial Kalman filter's record
+    layout (seedgb_params_to_ckf), device-resident: returns (out, out_size),
+    a uint8 CUDA tensor of capacity x 176 bytes (CKF_PARAMS_DTYPE records)
+    and an int32 device count."""
+    torch = _torch()
+    dev = params.data.device
+    cap = params.capacity
+    if out is None:
+        out = torch.empty(max(1, cap) * CKF_PARAMS_DTYPE.itemsize, dtype=torch.uint8,
+                          device=dev)
+    if out_size is None:
+        out_size = torch.zeros(1, dtype=torch.int32, device=dev)
+    cap_out = out.numel() // CKF_PARAMS_DTYPE.itemsize
+    b = params.buf()
+    _check(lib().seedgb_params_to_ckf(C.byref(b), C.c_void_p(out.data_ptr()), cap_out,
+                                      C.c_void_p(out_size.data_ptr()), _stream_ptr(stream)),
+           "seedgb_params_to_ckf")
+    return out, out_size
 
 
 def spacepoint_binning_noalloc(finder_config, grid_config, spacepoints, bin_offsets,
