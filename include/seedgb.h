@@ -389,6 +389,23 @@ typedef struct {
 seedgb_status seedgb_seeding_set_tune(seedgb_seeding* h, const seedgb_tune* t);
 seedgb_status seedgb_seeding_get_tune(seedgb_seeding* h, seedgb_tune* t);
 
+/* The autotuner (no counterpart in the reference): for the batch `events`
+ * (device views; seeds into `outs`), sets each candidate shape (NULL: the
+ * default grid of 3 x 3 x 4 x 2 shapes -- warps {8, 12, 16}, middles per item
+ * {64, 256, 1024}, neighbourhood {1536, 2048, 2560, 3072}, CTAs per SM
+ * {1, 2}), captures the graph for the batch and times `reps` launches with
+ * CUDA events on `stream` (median, after one warm-up launch).  Shapes that do
+ * not fit in shared memory, or that are clamped to a shape already measured,
+ * are skipped (times_ms[i] = -1; times_ms may be NULL, else n_candidates --
+ * or 72 for the default grid -- entries).  Leaves the fastest shape set (and
+ * in *best) with the graph captured for the batch.  Every measured launch
+ * must end with status OK.  Synchronises `stream`. */
+seedgb_status seedgb_seeding_autotune(seedgb_seeding* h, const seedgb_spacepoint_view* events,
+                                      uint32_t n_events, seedgb_seed_buffer* outs,
+                                      const seedgb_tune* candidates, uint32_t n_candidates,
+                                      uint32_t reps, seedgb_tune* best, float* times_ms,
+                                      void* stream);
+
 /* ------------------------------------------------------------------------ */
 /* Learned doublet filter.  No counterpart in the reference.                 */
 /*                                                                          */
@@ -474,6 +491,52 @@ seedgb_status seedgb_seeding_filter_stats(seedgb_seeding* h, uint32_t n_events,
                                           uint32_t* per_event, uint8_t* fell_back,
                                           uint64_t* n_records, uint64_t* n_triplet_records,
                                           void* stream);
+
+/* Host drivers of the filter for C++ callers (no counterpart in the
+ * reference).  Training: plain seeding of the events on this handle, in
+ * passes of events_per_pass, with the doublet dump on; every middle-top
+ * doublet of a middle with both roles is a sample, labelled 1 when it is the
+ * (middle, top) pair of an accepted seed; all positives and a share
+ * neg_keep of the negatives (chosen by a hash of seed, event, middle and
+ * partner) are kept; inputs standardised over the samples; He-uniform
+ * initial weights; `epochs` epochs of mini-batch Adam (lr, 0.9, 0.999, 1e-8)
+ * on the weighted logistic loss (positives weighted by the negative /
+ * positive ratio) with seedgb_mlp_grad / seedgb_mlp_adam, the samples
+ * shuffled every epoch.  The same events, configuration and seed give the
+ * same network bit for bit.  *out receives the network, the band edges,
+ * thresholds -inf, band [0, 1] and prune_top = SEEDGB_FILTER_GATE_MIDDLE.
+ * loss_per_epoch (may be NULL): `epochs` mean losses.  Allocates its own
+ * device buffers and synchronises `stream`. */
+typedef struct {
+    uint32_t epochs;          /* >= 1, e.g. 4 */
+    uint32_t batch;           /* samples per step, e.g. 16384 */
+    float learning_rate;      /* e.g. 3e-3 */
+    float neg_keep;           /* share of the negative doublets kept, e.g. 0.05 */
+    uint64_t seed;
+    uint32_t events_per_pass; /* events seeded per dump pass, e.g. 8 */
+} seedgb_filter_train_config;
+seedgb_status seedgb_filter_train(seedgb_seeding* h, const seedgb_spacepoint_view* events,
+                                  uint32_t n_events, const float* band_edges, uint32_t n_edges,
+                                  const seedgb_filter_train_config* cfg,
+                                  seedgb_doublet_filter* out, float* loss_per_epoch,
+                                  void* stream);
+
+/* Calibration of the middle gate on held-out events: one scored plain run
+ * gives every middle's best middle-top logit and plain seed count, from
+ * which the gate's seed recall at any threshold follows exactly (a gated run
+ * keeps precisely the plain seeds of the middles it keeps).  Per size class
+ * (class_max ascending, n_classes <= 8; 0: one class), the highest threshold
+ * whose recall over the class's events is >= target and >= min_event on each
+ * of them; the band is the class's range of gated middle-top fractions
+ * widened by `margin`.  *f (the network, in) gets thresholds, bands, size
+ * classes and prune_top = SEEDGB_FILTER_GATE_MIDDLE.  recall_out /
+ * pruned_out (may be NULL): per event, the calibrated recall and gated
+ * fraction.  Synchronises `stream`. */
+seedgb_status seedgb_filter_calibrate_gate(seedgb_seeding* h, const seedgb_spacepoint_view* events,
+                                           uint32_t n_events, const uint32_t* class_max,
+                                           uint32_t n_classes, float target, float min_event,
+                                           float margin, seedgb_doublet_filter* f,
+                                           float* recall_out, float* pruned_out, void* stream);
 
 /* Training and stand-alone inference of the network on the tensor cores.
  * params: device fp32 block of seedgb_mlp_num_params() values laid out as

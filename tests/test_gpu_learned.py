@@ -291,29 +291,58 @@ def test_fallback_reseeds_plain(model_and_event):
 
 
 def test_training_gains_over_untrained():
+    """What the trained network gains over the method without it: at the
+    same per-event seed recall the trained gate drops far more middle-top
+    doublets (whole middles) than the same gate with an untrained network,
+    and the gated seeds stay a subset of the plain ones."""
     import torch
 
     from traccc_gb300 import learned, seeding
     alg = seeding.TripletSeedingAlgorithm()
     train_ev = [synth.workload_event("pileup9k", 500 + s, n_tracks=3000) for s in range(6)]
     calib_ev = [synth.workload_event("pileup9k", 600 + s, n_tracks=3000) for s in range(3)]
-    data = learned.collect(alg, train_ev, neg_keep=0.1)
-    assert data.n_positive > 0 and len(data.labels) > data.n_positive
-    params, norm, hist = learned.train(data, epochs=3)
-    assert hist[-1] < hist[0]
-    trained = learned.FilterModel(params, norm, learned.band_edges())
-    untrained = learned.FilterModel(learned.init_params(1), norm, learned.band_edges())
-    m1, r1 = learned.calibrate(alg, trained, calib_ev, target=0.99, criterion="event")
-    m0, r0 = learned.calibrate(alg, untrained, calib_ev, target=0.99, criterion="event",
-                               quantiles=(0.2, 0.1, 0.05, 0.02, 0.01, 0.005, 0.002, 0.001,
-                                          0.0005, 0.0001, 0.0))
-    f1 = np.mean(r1["chosen"]["pruned_fraction"])
-    f0 = np.mean(r0["chosen"]["pruned_fraction"])
-    assert r1["chosen"]["min_recall"] >= 0.99
-    # small training set: the trained network prunes several times more
-    # doublets than an untrained one at the same recall (~0.11 vs ~0.015)
-    assert f1 > 0.06 and f1 > 3 * f0 + 0.02, (f1, f0)
-    torch.cuda.synchronize()
+    dev = torch.device("cuda")
+    tr = [seeding.SpacepointCollection.from_numpy(e, device=dev) for e in train_ev]
+    ca = [seeding.SpacepointCollection.from_numpy(e, device=dev) for e in calib_ev]
+    f, loss = alg.train_filter(tr, learned.band_edges(), epochs=3, neg_keep=0.1)
+    assert loss[-1] < loss[0]
+    untrained = learned.FilterModel(learned.init_params(1), learned.FilterModel.from_struct(f).norm,
+                                    learned.band_edges()).struct()
+    f1, r1, g1 = alg.calibrate_gate(f, ca, target=0.99, min_event=0.99)
+    f0, r0, g0 = alg.calibrate_gate(untrained, ca, target=0.99, min_event=0.99)
+    assert r1.min() >= 0.99 and r0.min() >= 0.99
+    assert g1.mean() > 2 * g0.mean() + 0.01, (g1.mean(), g0.mean())
+    # the calibrated gate on the same events: the recall it promised, no
+    # seed outside the plain set
+    plain = learned.seed_keys(alg.run_batch(ca))
+    alg.set_filter(f1)
+    gated = learned.seed_keys(alg.run_batch(ca))
+    alg.set_filter(None)
+    rec, out = learned.compare(plain, gated)
+    assert out.sum() == 0
+    assert np.allclose(rec, r1, atol=1e-6)
+
+
+def test_library_training_is_reproducible():
+    """seedgb_filter_train twice on the same events gives the same network
+    bit for bit (dump records ordered, negatives sampled by a hash, seeded
+    shuffles, fixed-order gradient sums)."""
+    import torch
+
+    from traccc_gb300 import learned, seeding
+    alg = seeding.TripletSeedingAlgorithm()
+    evs = [seeding.SpacepointCollection.from_numpy(synth.workload_event("trk1000", 40 + s,
+                                                                        n_tracks=2000),
+                                                   device=torch.device("cuda"))
+           for s in range(3)]
+    a, la = alg.train_filter(evs, learned.band_edges(), epochs=2, batch=4096, neg_keep=0.2,
+                             events_per_pass=2)
+    b, lb = alg.train_filter(evs, learned.band_edges(), epochs=2, batch=4096, neg_keep=0.2,
+                             events_per_pass=2)
+    ma, mb = learned.FilterModel.from_struct(a), learned.FilterModel.from_struct(b)
+    assert np.array_equal(ma.params, mb.params) and np.array_equal(ma.norm, mb.norm)
+    assert la == lb
+    assert a.prune_top == seeding.FILTER_GATE_MIDDLE
 
 
 def test_size_classes_apply_per_event(model_and_event):

@@ -10,9 +10,10 @@ fewer warps).
 
 For a batch, every candidate is set, the graph is captured for the batch's
 size, and the captured launch is timed with CUDA events on the launching
-stream (median of ``reps`` after one warm-up launch).  The best shape is
-stored in a JSON table keyed by the batch's mean-spacepoints-per-event
-bucket, so a later process looks it up instead of searching again:
+stream (median of ``reps`` after one warm-up launch) -- the library's own
+search, seedgb_seeding_autotune, which C++ callers use directly.  The best
+shape is stored in a JSON table keyed by the batch's mean-spacepoints-per-
+event bucket, so a later process looks it up instead of searching again:
 
     table = autotune.load(path)
     shape = autotune.lookup(table, mean_sp)      # None: not tuned yet
@@ -25,7 +26,6 @@ import itertools
 import json
 import math
 import os
-import statistics
 
 from . import seeding
 
@@ -48,53 +48,19 @@ def bucket(mean_sp: float) -> str:
     return f"le{b}"
 
 
-def _time_graph(alg, events, outs, stream, reps):
-    import torch
-    alg.graph_launch(events, outs, stream=stream.cuda_stream)
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2 * reps)]
-    times = []
-    for r in range(reps):
-        ev[2 * r].record(stream)
-        alg.graph_launch(events, outs, stream=stream.cuda_stream)
-        ev[2 * r + 1].record(stream)
-    stream.synchronize()
-    for r in range(reps):
-        times.append(ev[2 * r].elapsed_time(ev[2 * r + 1]))
-    return statistics.median(times)
-
-
 def tune(alg, events, outs=None, shapes=None, reps=3, stream=None):
-    """Search the launch shapes for this batch.  Returns (best shape,
-    report); leaves the best shape set and the graph captured for the
-    batch's size.  Every candidate must end with status OK."""
+    """Search the launch shapes for this batch (seedgb_seeding_autotune).
+    Returns (best shape, report sorted by time); leaves the best shape set
+    and the graph captured for the batch's size."""
     import torch
     stream = stream or torch.cuda.current_stream()
     outs = outs or [seeding.SeedBuffer(alg.max_seeds(len(e)), device=e.global_.device)
                     for e in events]
-    total_sp = sum(len(e) for e in events)
-    report = []
-    best = None
-    for shape in shapes or candidates():
-        try:
-            eff = alg.set_tune(*shape)
-        except seeding.SeedingError:
-            continue  # does not fit in shared memory
-        if any(r["shape"] == list(eff) for r in report):
-            continue  # clamped to a shape already measured
-        alg.graph_create(len(events), total_sp)
-        ms = _time_graph(alg, events, outs, stream, reps)
-        st = alg.last_status(stream.cuda_stream)
-        if st != seeding.OK:
-            raise seeding.SeedingError(st, f"tuning shape {eff}")
-        report.append({"shape": list(eff), "ms": ms})
-        if best is None or ms < best[1]:
-            best = (tuple(eff), ms)
-    if best is None:
-        raise RuntimeError("no launch shape fits this device")
-    alg.set_tune(*best[0])
-    alg.graph_create(len(events), total_sp)
-    report.sort(key=lambda r: r["ms"])
-    return best[0], report
+    best, times = alg.autotune(events, outs, candidates=shapes or candidates(), reps=reps,
+                               stream=stream.cuda_stream)
+    report = sorted(({"shape": list(sh), "ms": ms} for sh, ms in times if ms is not None),
+                    key=lambda r: r["ms"])
+    return tuple(best), report
 
 
 def load(path: str) -> dict:

@@ -113,6 +113,24 @@ class FilterModel:
                  classes=cl)
 
     @classmethod
+    def from_struct(cls, f: seeding.DoubletFilter) -> "FilterModel":
+        """The model of a seedgb_doublet_filter (as the library's training and
+        calibration drivers return it)."""
+        params = np.concatenate([np.asarray(f.w1, np.float32), np.asarray(f.b1, np.float32),
+                                 np.asarray(f.w2, np.float32), np.asarray(f.b2, np.float32),
+                                 np.asarray(f.w3, np.float32),
+                                 np.asarray([f.b3], np.float32)])
+        norm = np.concatenate([np.asarray(f.mu, np.float32), np.asarray(f.isd, np.float32)])
+        edges = np.asarray(f.edges[: f.n_edges], np.float32)
+        classes = [(int(f.size_class_max[k]),
+                    (float(f.size_class_threshold[k][0]), float(f.size_class_threshold[k][1])),
+                    (float(f.size_class_band[k][0]), float(f.size_class_band[k][1])))
+                   for k in range(f.n_size_classes)]
+        return cls(params, norm, edges, (float(f.threshold[0]), float(f.threshold[1])),
+                   (float(f.band[0]), float(f.band[1])), int(f.prune_bottom), int(f.prune_top),
+                   classes or None)
+
+    @classmethod
     def load(cls, path):
         with np.load(path) as z:
             cl = [(int(r[0]), (float(r[1]), float(r[2])), (float(r[3]), float(r[4])))
@@ -530,9 +548,16 @@ def calibrate_classes(alg, model: FilterModel, events, class_max, target=0.995, 
 
 def build_filter(alg, train_events, calib_events, epochs=3, neg_keep=0.05, target=0.995,
                  seed=0, log=None, quantiles=None, label="seed", criterion="total",
-                 class_max=None, min_event=0.0):
+                 class_max=None, min_event=0.0, impl="library"):
     """collect -> train -> calibrate (per size class when class_max is
-    given).  Returns (model, report)."""
+    given).  Returns (model, report).  impl "library": the library's C++
+    drivers (seedgb_filter_train, seedgb_filter_calibrate_gate; middle gate,
+    seed labels); impl "torch": the orchestration below (torch tensors as
+    device buffers around the same kernels), which also serves the doublet-
+    pruning mode and the triplet label."""
+    if impl == "library":
+        return _build_filter_library(alg, train_events, calib_events, epochs, neg_keep, target,
+                                     seed, class_max, min_event)
     import torch
     t0 = time.perf_counter()
     data = collect(alg, train_events, neg_keep=neg_keep, seed=seed, label=label)
@@ -557,4 +582,30 @@ def build_filter(alg, train_events, calib_events, epochs=3, neg_keep=0.05, targe
                 "doublets_seen": data.n_doublets, "positives": data.n_positive,
                 "samples": int(len(data.labels)), "epochs": epochs, "loss": hist,
                 "collect_s": t1 - t0, "train_s": t2 - t1, "calibrate_s": t3 - t2})
+    return model, rep
+
+
+def _build_filter_library(alg, train_events, calib_events, epochs, neg_keep, target, seed,
+                          class_max, min_event):
+    import torch
+    dev = torch.device("cuda", torch.cuda.current_device())
+    t0 = time.perf_counter()
+    tr = _device_events(torch, train_events, dev)
+    f, loss = alg.train_filter(tr, band_edges(), epochs=epochs, neg_keep=neg_keep, seed=seed)
+    del tr
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    ca = _device_events(torch, calib_events, dev)
+    f, rec, frac = alg.calibrate_gate(f, ca, class_max=tuple(class_max or ()), target=target,
+                                      min_event=min_event)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    model = FilterModel.from_struct(f)
+    rep = {"impl": "library (seedgb_filter_train, seedgb_filter_calibrate_gate)",
+           "label": "seed", "mode": "middle gate", "train_events": len(train_events),
+           "calib_events": len(calib_events), "epochs": epochs, "loss": loss,
+           "calib_recall": {"min": float(rec.min()), "mean": float(rec.mean())},
+           "calib_gated_fraction": {"min": float(frac.min()), "mean": float(frac.mean()),
+                                    "max": float(frac.max())},
+           "train_s": t1 - t0, "calibrate_s": t2 - t1}
     return model, rep

@@ -111,6 +111,12 @@ class Tune(C.Structure):
                 self.ctas_per_sm)
 
 
+class FilterTrainConfig(C.Structure):
+    """seedgb_filter_train_config."""
+    _fields_ = [("epochs", C.c_uint32), ("batch", C.c_uint32), ("learning_rate", C.c_float),
+                ("neg_keep", C.c_float), ("seed", C.c_uint64), ("events_per_pass", C.c_uint32)]
+
+
 # seedgb_doublet_filter.prune_bottom / prune_top modes
 FILTER_KEEP, FILTER_PRUNE_DOUBLETS, FILTER_GATE_MIDDLE = 0, 1, 2
 
@@ -254,6 +260,19 @@ def lib():
         L.seedgb_mlp_adam.argtypes = [vp, vp, vp, vp, C.c_uint32, C.c_uint32, C.c_float,
                                       C.c_float, C.c_float, C.c_float, vp]
         L.seedgb_mlp_adam.restype = C.c_int
+        L.seedgb_seeding_autotune.argtypes = [vp, P(_SpacepointView), C.c_uint32, P(_SeedBuffer),
+                                              P(Tune), C.c_uint32, C.c_uint32, P(Tune),
+                                              P(C.c_float), vp]
+        L.seedgb_seeding_autotune.restype = C.c_int
+        L.seedgb_filter_train.argtypes = [vp, P(_SpacepointView), C.c_uint32, P(C.c_float),
+                                          C.c_uint32, P(FilterTrainConfig), P(DoubletFilter),
+                                          P(C.c_float), vp]
+        L.seedgb_filter_train.restype = C.c_int
+        L.seedgb_filter_calibrate_gate.argtypes = [vp, P(_SpacepointView), C.c_uint32,
+                                                   P(C.c_uint32), C.c_uint32, C.c_float,
+                                                   C.c_float, C.c_float, P(DoubletFilter),
+                                                   P(C.c_float), P(C.c_float), vp]
+        L.seedgb_filter_calibrate_gate.restype = C.c_int
         L.seedgb_params_create.argtypes = [P(TrackParamsEstimationConfig), P(vp)]
         L.seedgb_params_create.restype = C.c_int
         L.seedgb_params_destroy.argtypes = [vp]
@@ -571,6 +590,63 @@ class TripletSeedingAlgorithm:
         t = Tune()
         _check(lib().seedgb_seeding_get_tune(self._h, C.byref(t)), "seedgb_seeding_get_tune")
         return t.astuple()
+
+    def autotune(self, events, outs, candidates=None, reps=3, stream=None):
+        """The library's autotuner (seedgb_seeding_autotune) on this batch:
+        returns (best shape, [(shape, ms or None if skipped), ...]) and leaves
+        the best shape set with the graph captured."""
+        n = len(events)
+        ev = (_SpacepointView * n)(*[e.view() for e in events])
+        bufs = (_SeedBuffer * n)(*[o.buf() for o in outs])
+        shapes = list(candidates) if candidates is not None else None
+        nc = len(shapes) if shapes is not None else 72
+        cand = (Tune * nc)(*[Tune(*sh) for sh in shapes]) if shapes is not None else None
+        times = (C.c_float * nc)()
+        best = Tune()
+        _check(lib().seedgb_seeding_autotune(self._h, ev, n, bufs, cand, len(shapes or []),
+                                             reps, C.byref(best), times, _stream_ptr(stream)),
+               "seedgb_seeding_autotune")
+        if shapes is None:
+            shapes = [(w, m, nb, c) for w in (8, 12, 16) for m in (64, 256, 1024)
+                      for nb in (1536, 2048, 2560, 3072) for c in (1, 2)]
+        return best.astuple(), [(tuple(sh), (float(t) if t >= 0 else None))
+                                for sh, t in zip(shapes, times)]
+
+    def train_filter(self, events, band_edges, epochs=4, batch=16384, lr=3e-3, neg_keep=0.05,
+                     seed=0, events_per_pass=8, stream=None):
+        """The library's filter training (seedgb_filter_train) on device
+        events: returns (DoubletFilter with prune_top = FILTER_GATE_MIDDLE,
+        mean loss per epoch)."""
+        n = len(events)
+        ev = (_SpacepointView * n)(*[e.view() for e in events])
+        edges = np.ascontiguousarray(band_edges, np.float32)
+        cfg = FilterTrainConfig(epochs, batch, lr, neg_keep, seed, events_per_pass)
+        out = DoubletFilter()
+        loss = (C.c_float * epochs)()
+        _check(lib().seedgb_filter_train(self._h, ev, n,
+                                         edges.ctypes.data_as(C.POINTER(C.c_float)), len(edges),
+                                         C.byref(cfg), C.byref(out), loss, _stream_ptr(stream)),
+               "seedgb_filter_train")
+        return out, [float(v) for v in loss]
+
+    def calibrate_gate(self, filt: "DoubletFilter", events, class_max=(), target=0.997,
+                       min_event=0.995, margin=0.05, stream=None):
+        """The library's gate calibration (seedgb_filter_calibrate_gate):
+        returns (calibrated DoubletFilter, per-event recall, per-event gated
+        fraction)."""
+        n = len(events)
+        ev = (_SpacepointView * n)(*[e.view() for e in events])
+        cm = (C.c_uint32 * max(1, len(class_max)))(*[min(int(c), 0xFFFFFFFF)
+                                                      for c in class_max])
+        f = DoubletFilter()
+        C.memmove(C.byref(f), C.byref(filt), C.sizeof(DoubletFilter))
+        rec = (C.c_float * n)()
+        frac = (C.c_float * n)()
+        _check(lib().seedgb_filter_calibrate_gate(self._h, ev, n, cm, len(class_max), target,
+                                                  min_event, margin, C.byref(f), rec, frac,
+                                                  _stream_ptr(stream)),
+               "seedgb_filter_calibrate_gate")
+        return f, np.asarray(rec, np.float64), np.asarray(frac, np.float64)
 
     def set_filter(self, filt: "DoubletFilter | None"):
         """Install the learned doublet filter (None: plain seeding)."""
