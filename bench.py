@@ -413,8 +413,8 @@ def run_trk1000(args, stream, flush_buf):
         d[:, 2] = np.abs((a[:, 2] - b[:, 2] + np.pi) % (2 * np.pi) - np.pi)
         params_ok = bool(np.all(gp["surface_link"] == rp["surface_link"]) and
                          np.all(d <= 1e-5 * 0.5 * (np.abs(a) + np.abs(b)) + 1e-30))
-    return {"workload": "trk1000: 1 synthetic event (seed 0), 1000 helices, pT log-U(0.5, 20) "
-                        "GeV, 10% noise, %d spacepoints" % len(sps),
+    return {"workload": f"trk1000: 1 synthetic event (seed 0), 1000 helices, pT log-U(0.5, 20) "
+                        f"GeV, 10% noise, {len(sps)} spacepoints",
             "ms_per_event": statistics.median(ms), "ms_per_event_mean": sum(ms) / len(ms),
             "events_per_s": 1e3 * len(ms) / sum(ms), "seeds": len(got),
             "parity": {"seeds_bit_exact": seeds_ok, "params_within_1e-5": params_ok,

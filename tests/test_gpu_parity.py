@@ -15,11 +15,12 @@ pytestmark = pytest.mark.gpu
 PARAM_TOL = 1e-5
 # The reference's angle comparison (is_same_angle.cpp) is relative to the
 # angle itself, so it is ill-conditioned near phi = 0: there both sides carry
-# the absolute float rounding (~1e-7 rad) of the direction they take the
-# angle of, and a relative 1e-5 would ask for ~1e-12 rad at phi ~ 1e-7.
-# Such angles pass within this absolute bound instead; tests count them and
-# keep them rare.
-ANGLE_ABS_TOL = 1e-6
+# the absolute float rounding of the direction they take the angle of, and a
+# relative 1e-5 would ask for ~1e-12 rad at phi ~ 1e-7.  Such angles pass
+# within this absolute bound instead; tests count them and keep them rare (on
+# the 1.03 M parameter sets of the 100k-spacepoint bench events: 2, the
+# largest difference 1.9e-9 rad).
+ANGLE_ABS_TOL = 1e-8
 
 
 def run_gpu(ev, cfgs=None, exhaustive=False):

@@ -10,7 +10,7 @@ parameter estimation of the same seeds (once the seeds are known to be the
 oracle's, the oracle needs no seeding run: its parameter estimation is
 milliseconds per event): surface links exact, the six parameters and the
 covariance diagonal within 1e-5 relative (angles wrapped), with phi within
-1e-6 rad absolute where the relative comparison is ill-conditioned (phi near
+1e-8 rad absolute where the relative comparison is ill-conditioned (phi near
 zero); those are counted and must stay rare."""
 import json
 import os
