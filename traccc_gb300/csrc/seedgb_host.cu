@@ -95,10 +95,11 @@ struct SeedSet {
     }
 };
 
-// Scored plain seeding of events [e0, e1): the sorted top-doublet records
-// and, per event, the set of plain seeds' (middle, top) keys.
+// Scored plain seeding of events [e0, e1): the top-doublet records (in the
+// order the GPU found them) and, per event, the set of plain seeds'
+// (middle, top) keys.
 struct Scored {
-    std::vector<DumpRec> tops;                       // role 1 only, sorted
+    std::vector<DumpRec> tops;                       // role 1 only
     std::vector<std::unordered_set<uint64_t>> seeds;  // per event of the pass
     std::vector<std::unordered_map<uint32_t, uint32_t>> seeds_per_middle;
 };
@@ -136,11 +137,6 @@ seedgb_status scored_pass(seedgb_seeding* h, const seedgb_doublet_filter& scorin
     out.tops.clear();
     for (const DumpRec& r : all)
         if (r.role_event & 1u) out.tops.push_back(r);
-    std::sort(out.tops.begin(), out.tops.end(), [](const DumpRec& a, const DumpRec& b) {
-        if (a.role_event != b.role_event) return a.role_event < b.role_event;
-        if (a.middle != b.middle) return a.middle < b.middle;
-        return a.other < b.other;
-    });
     std::vector<uint32_t> sizes(n);
     SEEDGB_CUDA(cudaMemcpy(sizes.data(), ss.sizes.p, 4 * n, cudaMemcpyDeviceToHost));
     out.seeds.assign(n, {});
@@ -290,6 +286,9 @@ seedgb_status seedgb_filter_train(seedgb_seeding* h, const seedgb_spacepoint_vie
         const uint32_t n = std::min(per_pass, n_events - e0);
         Scored sc;
         SEEDGB_TRY(scored_pass(h, scoring, events + e0, n, 8, rec, sc, s));
+        // keep the positives and a hashed share of the negatives, then put
+        // the kept samples in (event, middle, partner) order
+        std::vector<std::pair<const DumpRec*, bool>> kept;
         for (const DumpRec& r : sc.tops) {
             const uint32_t e = r.role_event >> 1;
             const bool pos = sc.seeds[e].count(mt_key(r.middle, r.other)) != 0;
@@ -297,10 +296,18 @@ seedgb_status seedgb_filter_train(seedgb_seeding* h, const seedgb_spacepoint_vie
                 (static_cast<uint64_t>(e0 + e) << 42) ^ (static_cast<uint64_t>(r.middle) << 21) ^
                 r.other));
             const double u = static_cast<double>(hsh >> 11) * 0x1p-53;
-            if (!pos && !(u < cfg->neg_keep)) continue;
-            feats.insert(feats.end(), r.feat, r.feat + 8);
-            labels.push_back(pos ? 1.f : 0.f);
-            n_pos += pos;
+            if (pos || u < cfg->neg_keep) kept.emplace_back(&r, pos);
+        }
+        std::sort(kept.begin(), kept.end(), [](const auto& a, const auto& b) {
+            if (a.first->role_event != b.first->role_event)
+                return a.first->role_event < b.first->role_event;
+            if (a.first->middle != b.first->middle) return a.first->middle < b.first->middle;
+            return a.first->other < b.first->other;
+        });
+        for (const auto& k : kept) {
+            feats.insert(feats.end(), k.first->feat, k.first->feat + 8);
+            labels.push_back(k.second ? 1.f : 0.f);
+            n_pos += k.second;
         }
     }
     const uint64_t n64 = labels.size();
@@ -411,20 +418,21 @@ seedgb_status seedgb_filter_calibrate_gate(seedgb_seeding* h, const seedgb_space
         const uint32_t n = std::min(per_pass, n_events - e0);
         Scored sc;
         SEEDGB_TRY(scored_pass(h, scoring, events + e0, n, 8, rec, sc, s));
-        for (size_t i = 0; i < sc.tops.size();) {
-            const DumpRec& r = sc.tops[i];
-            Mid m{e0 + (r.role_event >> 1), -INFINITY, 0, 0};
-            size_t j = i;
-            for (; j < sc.tops.size() && sc.tops[j].role_event == r.role_event &&
-                   sc.tops[j].middle == r.middle; ++j) {
-                m.best = std::max(m.best, sc.tops[j].logit);
-                ++m.n_mt;
+        // group by (event, middle); the result does not depend on the order
+        std::unordered_map<uint64_t, Mid> by_mid;
+        by_mid.reserve(sc.tops.size() / 16 + 16);
+        for (const DumpRec& r : sc.tops) {
+            const uint32_t e = r.role_event >> 1;
+            auto ins = by_mid.emplace(mt_key(e, r.middle), Mid{e0 + e, -INFINITY, 0, 0});
+            Mid& m = ins.first->second;
+            if (ins.second) {
+                const auto it = sc.seeds_per_middle[e].find(r.middle);
+                m.seeds = it == sc.seeds_per_middle[e].end() ? 0u : it->second;
             }
-            const auto it = sc.seeds_per_middle[r.role_event >> 1].find(r.middle);
-            m.seeds = it == sc.seeds_per_middle[r.role_event >> 1].end() ? 0u : it->second;
-            mids.push_back(m);
-            i = j;
+            m.best = std::max(m.best, r.logit);
+            ++m.n_mt;
         }
+        for (const auto& kv : by_mid) mids.push_back(kv.second);
     }
     const uint32_t nc = std::max(1u, n_classes);
     auto class_of = [&](uint32_t e) {

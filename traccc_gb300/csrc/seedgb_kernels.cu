@@ -1148,9 +1148,14 @@ __device__ MiddleResult process_middle(const DevConfig& c, const Arena& a,
         const uint32_t mid_idx = a.dump ? a.g_idx[gm] : 0u;
         uint32_t w = 0;
         bool reach = false;
+        // gate: once a doublet of the middle reaches the threshold the middle
+        // is kept whatever the rest score, so the remaining chunks are not
+        // scored (unless every score is recorded); warp-uniform
+        bool decided = false;
         for (uint32_t base = 0; base < n_mt; base += 32) {
             const uint32_t i = base + lane;
             const bool valid = i < n_mt;
+            const bool score = !(gate && decided && !a.dump);
             uint32_t p = 0, hp = 0, oth = 0;
             LinCircle l{};
             float x[kMlpIn] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
@@ -1160,13 +1165,15 @@ __device__ MiddleResult process_middle(const DevConfig& c, const Arena& a,
                 const float2 vo = any_var ? a.g_var[nb.gpos(hp)] : make_float2(0.f, 0.f);
                 const float4 o = nb.get(p);
                 l = lin_circle_cs(true, M, cosPhiM, sinPhiM, vM, o, vo);
-                mlp_features(c.mlp_edges, c.mlp_n_edges, M, o, l.cot, l.s, l.Zo, x);
+                if (score) mlp_features(c.mlp_edges, c.mlp_n_edges, M, o, l.cot, l.s, l.Zo, x);
                 if (a.dump) oth = a.g_idx[nb.gpos(hp)];
             }
             const float logit =
-                score_chunk<true>(c, a, R, x, valid, xs, lg, ev, mid_idx, oth, lane, lt);
+                score ? score_chunk<true>(c, a, R, x, valid, xs, lg, ev, mid_idx, oth, lane, lt)
+                      : thr;
             const bool keep = valid && (!prune || logit >= thr);
             reach |= valid && logit >= thr;
+            if (gate) decided = __any_sync(0xffffffffu, reach);
             const uint32_t mask = __ballot_sync(0xffffffffu, keep);
             if (keep) {
                 const uint32_t k = w + __popc(mask & lt);
