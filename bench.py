@@ -438,6 +438,41 @@ FILTER_CALIB_TARGET = 0.998
 FILTER_CALIB_MIN_EVENT = 0.997
 
 
+def run_formation(args, stream, meas, n_sp_total):
+    """Spacepoint formation in front of the step (seedgb_form_spacepoints:
+    the 20 events' measurements on the synthetic barrel's cylinder surfaces
+    -> spacepoints): device time per step, the upper bound of what fusing
+    formation into binning could save (fusion would remove only the
+    spacepoint columns' write and re-read, 28 + 12 bytes per spacepoint)."""
+    import torch
+
+    from traccc_gb300 import seeding, synth
+    surf = np.zeros(len(synth.LAYER_RADII) + 1, seeding.SURFACE_DTYPE)
+    for layer, r in enumerate(synth.LAYER_RADII):
+        surf[layer + 1]["type"] = seeding.SURFACE_CYLINDER
+        surf[layer + 1]["radius"] = r
+        surf[layer + 1]["rotation"] = np.eye(3, dtype=np.float32).reshape(-1)
+    sptr = stream.cuda_stream
+    for m in meas:
+        seeding.form_spacepoints(surf, m, stream=sptr)
+    ev_t = [torch.cuda.Event(enable_timing=True) for _ in range(2 * len(meas))]
+    reps, total_ms, formed = max(1, min(args.steps, 5)), 0.0, 0
+    for _ in range(reps):
+        for i, m in enumerate(meas):
+            ev_t[2 * i].record(stream)
+            _, k = seeding.form_spacepoints(surf, m, stream=sptr)
+            ev_t[2 * i + 1].record(stream)
+            formed += k
+        torch.cuda.synchronize()
+        total_ms += sum(ev_t[2 * i].elapsed_time(ev_t[2 * i + 1]) for i in range(len(meas)))
+    ms = total_ms / reps
+    return {"ms_per_step": ms, "events": len(meas), "spacepoints_formed": formed // reps,
+            "fusion_saving_bound_bytes": 40 * n_sp_total,
+            "timing": "device time of the per-event formation calls (one kernel sequence each: "
+                      "count, scan, write), summed over the step's events, mean of "
+                      f"{reps} repetitions"}
+
+
 FILTER_TRAIN_SEED0 = 1000
 
 
@@ -868,6 +903,7 @@ def run_gpu(args):
     barrier()
 
     trk1000 = run_trk1000(args, stream, flush_buf) if world == 1 else None
+    formation = run_formation(args, stream, meas, total) if world == 1 else None
 
     learned_line = None
     batched = None
@@ -1030,6 +1066,8 @@ def run_gpu(args):
     }
     if trk1000 is not None:
         line["trk1000"] = trk1000
+    if formation is not None:
+        line["formation"] = formation
     if learned_line is not None:
         line["learned"] = learned_line
     if batched is not None:
