@@ -11,6 +11,12 @@
  *  seedgb::seed_parameter_estimation_algorithm <- traccc::cuda::seed_parameter_estimation_algorithm
  *      operator():  device/common/include/traccc/seeding/device/
  *                   seed_parameter_estimation_algorithm.hpp:48-67
+ *  seedgb::to_ckf   the parameters in the record layout the track finding
+ *                   takes (examples/run/cuda/src/full_chain_algorithm.cpp:
+ *                   241-247), device-resident
+ *  triplet_seeding_algorithm::autotune / train_filter / calibrate_gate /
+ *                   set_filter: the library's launch-shape search and learned
+ *                   doublet filter (no counterpart in the reference)
  *
  * Header-only, C++17, needs cuda_runtime.h for the device buffers.  Errors
  * are exceptions as in the reference: std::domain_error for a rejected
@@ -150,6 +156,44 @@ private:
     uint32_t capacity_;
 };
 
+/* The parameters in the track finding's record layout, with a device
+ * count (bound_track_parameters_collection_types::buffer). */
+class ckf_params_buffer {
+public:
+    explicit ckf_params_buffer(uint32_t capacity) : data(capacity), size(1), capacity_(capacity) {}
+    uint32_t capacity() const { return capacity_; }
+    std::vector<seedgb_ckf_bound_track_parameters> to_host(cudaStream_t stream) const {
+        uint32_t n = 0;
+        if (cudaMemcpyAsync(&n, size.data(), sizeof n, cudaMemcpyDeviceToHost, stream) !=
+                cudaSuccess ||
+            cudaStreamSynchronize(stream) != cudaSuccess)
+            throw std::runtime_error("ckf parameter size copy failed");
+        n = n < capacity_ ? n : capacity_;
+        std::vector<seedgb_ckf_bound_track_parameters> out(n);
+        if (n && (cudaMemcpyAsync(out.data(), data.data(), sizeof(out[0]) * n,
+                                  cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
+                  cudaStreamSynchronize(stream) != cudaSuccess))
+            throw std::runtime_error("ckf parameter copy failed");
+        return out;
+    }
+
+    device_buffer<seedgb_ckf_bound_track_parameters> data;
+    device_buffer<uint32_t> size;
+
+private:
+    uint32_t capacity_;
+};
+
+/* Hands estimated parameters to the track finding: one launch on `stream`,
+ * no host synchronisation. */
+inline ckf_params_buffer to_ckf(const track_params_buffer& params, cudaStream_t stream) {
+    const seedgb_params_buffer in = params.view();
+    ckf_params_buffer out(in.capacity);
+    check(seedgb_params_to_ckf(&in, out.data.data(), in.capacity, out.size.data(), stream),
+          "to_ckf");
+    return out;
+}
+
 /* traccc::cuda::triplet_seeding_algorithm. */
 class triplet_seeding_algorithm {
 public:
@@ -191,6 +235,53 @@ public:
     /* Device status of the last call (synchronises the stream). */
     void check_status() const {
         check(seedgb_seeding_last_status(h_, stream_), "triplet_seeding_algorithm status");
+    }
+
+    /* Launch-shape search on a representative batch (candidates empty: the
+     * library's default grid); leaves the fastest shape set. */
+    seedgb_tune autotune(const std::vector<seedgb_spacepoint_view>& events,
+                         const std::vector<seedgb_tune>& candidates = {},
+                         uint32_t reps = 3) {
+        std::vector<seed_collection_buffer> out;
+        std::vector<seedgb_seed_buffer> views;
+        for (const auto& e : events) {
+            out.emplace_back(capacity(e.size));
+            views.push_back(out.back().view());
+        }
+        seedgb_tune best{};
+        check(seedgb_seeding_autotune(h_, events.data(), static_cast<uint32_t>(events.size()),
+                                      views.data(),
+                                      candidates.empty() ? nullptr : candidates.data(),
+                                      static_cast<uint32_t>(candidates.size()), reps, &best,
+                                      nullptr, stream_),
+              "autotune");
+        return best;
+    }
+
+    /* The learned doublet filter: training on these events' plain seeds,
+     * gate calibration on held-out events, installation (nullptr: plain). */
+    seedgb_doublet_filter train_filter(const std::vector<seedgb_spacepoint_view>& events,
+                                       const std::vector<float>& band_edges,
+                                       const seedgb_filter_train_config& cfg) {
+        seedgb_doublet_filter f{};
+        check(seedgb_filter_train(h_, events.data(), static_cast<uint32_t>(events.size()),
+                                  band_edges.data(), static_cast<uint32_t>(band_edges.size()),
+                                  &cfg, &f, nullptr, stream_),
+              "train_filter");
+        return f;
+    }
+    void calibrate_gate(seedgb_doublet_filter& f, const std::vector<seedgb_spacepoint_view>& events,
+                        const std::vector<uint32_t>& class_max, float target, float min_event,
+                        float margin = 0.05f) {
+        check(seedgb_filter_calibrate_gate(h_, events.data(),
+                                           static_cast<uint32_t>(events.size()),
+                                           class_max.empty() ? nullptr : class_max.data(),
+                                           static_cast<uint32_t>(class_max.size()), target,
+                                           min_event, margin, &f, nullptr, nullptr, stream_),
+              "calibrate_gate");
+    }
+    void set_filter(const seedgb_doublet_filter* f) {
+        check(seedgb_seeding_set_filter(h_, f), "set_filter");
     }
     seedgb_seeding* handle() const { return h_; }
 

@@ -13,6 +13,10 @@
 //   parameters seedgb_bound_track_parameters[n_seeds],
 //   uint32 batch seed counts [2] (the same event twice through the batch call;
 //   the batch's parameters, one launch, must equal the single call's: exit 4)
+// Also: the parameters handed to the track finding's layout round-trip every
+// field (exit 5); the autotuner picks one of its candidates (exit 6); a
+// filter trained and gate-calibrated on the event keeps a subset of the
+// plain seeds (exit 7).
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -94,6 +98,50 @@ int main(int argc, char** argv) {
             if (h.size() != hp.size() ||
                 (!h.empty() && std::memcmp(h.data(), hp.data(), sizeof(h[0]) * h.size()) != 0))
                 return 4;
+        }
+        // the CKF hand-off: vector, barcode, column-major covariance
+        {
+            const auto ckf = seedgb::to_ckf(pars, stream).to_host(stream);
+            if (ckf.size() != hp.size()) return 5;
+            for (std::size_t i = 0; i < ckf.size(); ++i) {
+                if (std::memcmp(ckf[i].vector, hp[i].params, sizeof hp[i].params) != 0 ||
+                    ckf[i].barcode != hp[i].surface_link)
+                    return 5;
+                for (int r = 0; r < 6; ++r)
+                    for (int c = 0; c < 6; ++c)
+                        if (std::memcmp(&ckf[i].covariance[c * 6 + r], &hp[i].cov[r * 6 + c],
+                                        4) != 0)
+                            return 5;
+            }
+        }
+        // the autotuner on a two-event batch, two candidate shapes
+        {
+            seedgb::triplet_seeding_algorithm tuned(finder, grid, filter, stream);
+            const std::vector<seedgb_tune> cand{{8, 256, 2048, 1}, {12, 64, 2048, 1}};
+            const seedgb_tune best = tuned.autotune({sps, sps}, cand, 2);
+            if (!((best.warps_per_cta == 8 && best.middles_per_item == 256) ||
+                  (best.warps_per_cta == 12 && best.middles_per_item == 64)))
+                return 6;
+            tuned.check_status();
+        }
+        // the learned filter: train, calibrate the gate, seed a subset
+        {
+            seedgb::triplet_seeding_algorithm learned(finder, grid, filter, stream);
+            const seedgb_filter_train_config cfg{2, 4096, 3e-3f, 0.2f, 7u, 1};
+            seedgb_doublet_filter f =
+                learned.train_filter({sps}, {52.f, 94.f, 144.f, 216.f, 310.f, 430.f}, cfg);
+            learned.calibrate_gate(f, {sps}, {}, 0.99f, 0.99f);
+            learned.set_filter(&f);
+            const auto gated = learned(sps).to_host(stream);
+            learned.check_status();
+            learned.set_filter(nullptr);
+            std::size_t j = 0;  // gated seeds appear in the plain seeds, in order
+            for (const auto& g : gated) {
+                while (j < hs.size() && std::memcmp(&hs[j], &g, sizeof g) != 0) ++j;
+                if (j == hs.size()) return 7;
+                ++j;
+            }
+            if (gated.empty() || gated.size() > hs.size()) return 7;
         }
         // a rejected configuration is a std::domain_error, as in the reference
         bool threw = false;

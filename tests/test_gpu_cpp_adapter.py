@@ -2,7 +2,9 @@
 triplet_seeding_algorithm / seed_parameter_estimation_algorithm surface)
 compiled against the library and run like traccc's examples run theirs:
 same seeds and parameters as the oracle, the batch call gives the same seeds,
-and a rejected configuration throws std::domain_error."""
+a rejected configuration throws std::domain_error; and the C++ surface of the
+additions (the CKF hand-off, the autotuner, filter training and gate
+calibration) works from C++ alone."""
 import os
 import shutil
 import subprocess
