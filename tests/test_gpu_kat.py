@@ -125,3 +125,24 @@ def test_track_params_on_a_helix_on_the_gpu(q):
     rp = O.track_params(ev, ref, (0.0, 0.0, B_2T), O.default_configs()[3])
     assert _close(p["params"], rp["params"])
     assert _close(p["cov"], rp["cov"])
+
+
+def test_empty_and_all_invalid_events_give_no_seeds():
+    """The reference returns an empty seed buffer for an event without
+    spacepoints (device/common/src/seeding/triplet_seeding_algorithm.cpp:
+    74-77) and finds no seed when binning rejects every spacepoint; the
+    library returns zero seeds (status OK), zero parameters and an empty
+    hand-off to the track finding in both cases."""
+    import torch
+    f, g, fl, tp = seeding.default_configs()
+    alg = seeding.TripletSeedingAlgorithm(f, g, fl)
+    est = seeding.SeedParameterEstimationAlgorithm(tp)
+    outside = _event([(900.0, 10.0, 5.0), (950.0, 12.0, 6.0), (10.0, 1.0, 1500.0)])  # r, z cuts
+    for ev in (_event(np.zeros((0, 3), np.float32)), outside):
+        sps = seeding.SpacepointCollection.from_numpy(ev)
+        seeds = alg(sps)
+        par = est((0.0, 0.0, B_2T), seeding.MeasurementCollection.from_numpy(ev), sps, seeds)
+        ckf, n = seeding.params_to_ckf(par)
+        torch.cuda.synchronize()
+        assert alg.last_status() == seeding.OK
+        assert len(seeds) == 0 and len(par) == 0 and int(n.item()) == 0

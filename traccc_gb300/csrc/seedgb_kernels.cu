@@ -996,6 +996,55 @@ __device__ __noinline__ uint32_t filter_bottoms(const DevConfig& c, const Arena&
     return w;
 }
 
+// The middle gate inside the plain seeding routine: true when one of the
+// middle's middle-top doublets (neighbourhood positions q[0..n)) has a logit
+// >= its event's threshold.  Features and network as in the scoring
+// instantiation (the lin_circle's cot, s and Zo do not depend on the
+// variances; the network's fragments are read from memory rather than held in
+// registers, with the same operands and mma order, so the same logits),
+// stopping at the first chunk of 32 that decides.  Out of line, so that the
+// routine's hot loops keep their registers and instruction-cache footprint.
+// xs: 128 words, lg: 32 floats of warp scratch.
+template <int MODE>
+__device__ __noinline__ bool gate_keeps_middle(const DevConfig& c, const Arena& a,
+                                               const NbViewT<MODE>& nb, const float4 M,
+                                               const uint16_t* q, uint32_t n_mt,
+                                               uint32_t* xs, float* lg, uint32_t ev,
+                                               uint32_t lane) {
+    const float thr = filter_threshold(c, a, ev, 1);
+    const float cosPhiM = M.x / M.w, sinPhiM = M.y / M.w;
+    const float2 zero2 = make_float2(0.f, 0.f);
+    for (uint32_t base = 0; base < n_mt; base += 32) {
+        const uint32_t i = base + lane;
+        const bool valid = i < n_mt;
+        uint32_t pk[4] = {0u, 0u, 0u, 0u};
+        if (valid) {
+            const float4 o = nb.get(q[i]);
+            const LinCircle l = lin_circle_cs(true, M, cosPhiM, sinPhiM, zero2, o, zero2);
+            float x[kMlpIn];
+            mlp_features(c.mlp_edges, c.mlp_n_edges, M, o, l.cot, l.s, l.Zo, x);
+            mlp_pack_inputs(c.mlp_mu, c.mlp_isd, x, pk);
+        }
+        *reinterpret_cast<uint4*>(xs + 4 * lane) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+        __syncwarp();
+#pragma unroll 1
+        for (uint32_t tt = 0; tt < 2; ++tt) {
+            float lo, hi;
+            mlp_tile16(*c.mlp, xs + 64 * tt, lane, lo, hi);
+            if ((lane & 3) == 0) {
+                const uint32_t g = lane >> 2;
+                lg[16 * tt + g] = lo;
+                lg[16 * tt + g + 8] = hi;
+            }
+        }
+        __syncwarp();
+        const bool reach = valid && lg[lane] >= thr;
+        __syncwarp();
+        if (__any_sync(0xffffffffu, reach)) return true;
+    }
+    return false;
+}
+
 // Seeds of one middle spacepoint, following host seed_finding::operator()
 // (core/src/seeding/seed_finding.cpp:69-118) with triplet_finding
 // (triplet_finding.hpp:60-183) and seed_filtering (seed_filtering.cpp:28-123).
@@ -1005,7 +1054,8 @@ __device__ __noinline__ uint32_t filter_bottoms(const DevConfig& c, const Arena&
 // VAR: read the spacepoint variances.  With VAR false every variance term is
 // zero (valid when no spacepoint of the batch has a variance); the results
 // are the same as with VAR true on such a batch, without the variance loads.
-template <int MODE, bool SCORE, bool VAR, int CAPB, int CAPT, int CAPLC, int CAPCT>
+template <int MODE, bool SCORE, bool VAR, int CAPB, int CAPT, int CAPLC, int CAPCT,
+          bool GATE = false>
 __device__ MiddleResult process_middle(const DevConfig& c, const Arena& a,
                                        const NbViewT<MODE>& nb, const uint32_t gm,
                                        const bool check_r,
@@ -1127,6 +1177,23 @@ __device__ MiddleResult process_middle(const DevConfig& c, const Arena& a,
         }
     }
     if (n_mt > CAPLC) { res.status = 1; return res; }
+    if constexpr (!SCORE && GATE) {
+        // learned middle gate, the scoring instantiation's decision, before
+        // any middle-top work (the cot-bucket tables are free scratch here)
+        const bool keep = gate_keeps_middle(c, a, nb, M, ws.qt, n_mt, ws.bstart,
+                                            reinterpret_cast<float*>(ws.bstart + 128), ev,
+                                            lane);
+        if (lane == 0) {
+            atomicAdd(&a.ev_filter[4 * ev + 2], n_mt);
+            if (!keep) atomicAdd(&a.ev_filter[4 * ev + 3], n_mt);
+        }
+        __syncwarp();
+        if (!keep) {
+            res.n_mt = 0;
+            if (lane == 0) a.seed_cnt[gm] = 0;
+            return res;
+        }
+    }
 
     // -- middle-top lin_circles (list order) and a counting sort by cot(theta)
     const float cosPhiM = M.x / M.w, sinPhiM = M.y / M.w;
@@ -1649,7 +1716,7 @@ __host__ __device__ constexpr size_t fast_scratch_offset(uint32_t nb_cap) {
 // kScoreWarps warps per CTA, so that each thread keeps 168 registers (14
 // warps would force 128 and spill: 11 % slower than 12).
 constexpr int kScoreWarps = 12;
-template <bool SCORE, bool VAR>
+template <bool SCORE, bool VAR, bool GATE = false>
 __device__ __forceinline__ void seed_fast_items(const DevConfig& c, const Arena& a, uint32_t mpi,
                                                 uint32_t nb_cap, uint32_t pass) {
     extern __shared__ __align__(128) uint8_t smem[];
@@ -1748,7 +1815,7 @@ __device__ __forceinline__ void seed_fast_items(const DevConfig& c, const Arena&
                 if (lane == 0) push_overflow(a, gm);
                 continue;
             }
-            const MiddleResult r = process_middle<kNbShared, SCORE, VAR, 512, 1024, 216, 128>(
+            const MiddleResult r = process_middle<kNbShared, SCORE, VAR, 512, 1024, 216, 128, GATE>(
                 c, a, nb, gm, true, nb_minr, nb_maxr, e, ws);
             if (lane == 0) {
                 if (r.status) push_overflow(a, gm);
@@ -1762,11 +1829,14 @@ __device__ __forceinline__ void seed_fast_items(const DevConfig& c, const Arena&
 // The fast seeding kernel: one branch on the batch's variance flag (set by
 // binning) picks the body; without variances the body carries no variance
 // loads (3 % faster on the 100k-spacepoint events).
-template <bool SCORE>
+// GATE: the learned middle gate inside the plain routine (pass 0 with a filter
+// that only gates middles); a separate instantiation, so that the plain
+// kernel's registers and code stay those of plain seeding.
+template <bool SCORE, bool GATE = false>
 __global__ void __launch_bounds__(SCORE ? kScoreWarps * 32 : 512)
     k_seed_fast(DevConfig c, Arena a, uint32_t mpi, uint32_t nb_cap, uint32_t pass) {
-    if (a.counters[kAnyVariance] != 0) seed_fast_items<SCORE, true>(c, a, mpi, nb_cap, pass);
-    else seed_fast_items<SCORE, false>(c, a, mpi, nb_cap, pass);
+    if (a.counters[kAnyVariance] != 0) seed_fast_items<SCORE, true, GATE>(c, a, mpi, nb_cap, pass);
+    else seed_fast_items<SCORE, false, GATE>(c, a, mpi, nb_cap, pass);
 }
 
 // General path, for the middles the fast kernel hands over (neighbourhood not
@@ -1787,7 +1857,8 @@ __host__ __device__ constexpr size_t general_warp_bytes() {
     return (kGeneralSegBytes + sizeof(Scratch) + 127) & ~static_cast<size_t>(127);
 }
 
-template <bool SCORE, bool VAR, bool LAST, int CAPB, int CAPT, int CAPLC, int CAPCT>
+template <bool SCORE, bool VAR, bool LAST, int CAPB, int CAPT, int CAPLC, int CAPCT,
+          bool GATE = false>
 __device__ __forceinline__ void general_middles(const DevConfig& c, const Arena& a,
                                                 uint32_t pass) {
     using Scratch = WarpScratch<CAPB, CAPT, CAPLC, CAPCT>;
@@ -1862,12 +1933,12 @@ __device__ __forceinline__ void general_middles(const DevConfig& c, const Arena&
                 const uint32_t base = seg_g[0];
                 NbViewT<kNbGlobalRs> nb{a.g_rs + base, nullptr, a.g_rs_gp + base, base,
                                         a.g_xyzr, seg_pos, seg_g, nseg, size};
-                r = process_middle<kNbGlobalRs, SCORE, VAR, CAPB, CAPT, CAPLC, CAPCT>(
+                r = process_middle<kNbGlobalRs, SCORE, VAR, CAPB, CAPT, CAPLC, CAPCT, GATE>(
                     c, a, nb, gm, false, 0.f, 0.f, e, ws);
             } else {
                 NbViewT<kNbHost> nb{nullptr, nullptr, nullptr, 0u, a.g_xyzr, seg_pos, seg_g,
                                     nseg, size};
-                r = process_middle<kNbHost, SCORE, VAR, CAPB, CAPT, CAPLC, CAPCT>(
+                r = process_middle<kNbHost, SCORE, VAR, CAPB, CAPT, CAPLC, CAPCT, GATE>(
                     c, a, nb, gm, false, 0.f, 0.f, e, ws);
             }
         }
@@ -1891,19 +1962,19 @@ __device__ __forceinline__ void general_middles(const DevConfig& c, const Arena&
 // Middle tier: larger capacities than the fast kernel's, as many warps as fit
 // (9 with its 23.4 KiB per warp; the launch bound leaves it the registers).
 constexpr int kMidMaxWarps = 10;
-template <bool SCORE>
+template <bool SCORE, bool GATE = false>
 __global__ void __launch_bounds__(kMidMaxWarps * 32) k_seed_mid(DevConfig c, Arena a, uint32_t pass) {
     if (a.counters[kAnyVariance] != 0)
-        general_middles<SCORE, true, false, 1024, 1024, 512, 256>(c, a, pass);
+        general_middles<SCORE, true, false, 1024, 1024, 512, 256, GATE>(c, a, pass);
     else
-        general_middles<SCORE, false, false, 1024, 1024, 512, 256>(c, a, pass);
+        general_middles<SCORE, false, false, 1024, 1024, 512, 256, GATE>(c, a, pass);
 }
 
 // Last tier: one warp per CTA with large capacities; always with the
 // variance terms (exact for zero variances too; very few middles get here).
-template <bool SCORE>
+template <bool SCORE, bool GATE = false>
 __global__ void __launch_bounds__(32) k_seed_slow(DevConfig c, Arena a, uint32_t pass) {
-    general_middles<SCORE, true, true, 8192, 8192, 4096, 2048>(c, a, pass);
+    general_middles<SCORE, true, true, 8192, 8192, 4096, 2048, GATE>(c, a, pass);
 }
 
 // Events whose pruned fraction (of all scored doublets) leaves the filter's
@@ -2198,11 +2269,11 @@ cudaError_t prepare_kernels() {
     int dev = -1;
     cudaError_t err = cudaGetDevice(&dev);
     if (err != cudaSuccess || dev == done_for) return err;
-    for (auto k : {k_seed_fast<false>, k_seed_fast<true>}) {
+    for (auto k : {k_seed_fast<false>, k_seed_fast<true>, k_seed_fast<false, true>}) {
         if (err == cudaSuccess)
             err = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
     }
-    for (auto k : {k_seed_slow<false>, k_seed_slow<true>}) {
+    for (auto k : {k_seed_slow<false>, k_seed_slow<true>, k_seed_slow<false, true>}) {
         if (err == cudaSuccess)
             err = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        static_cast<int>(slow_kernel_smem()));
@@ -2213,6 +2284,10 @@ cudaError_t prepare_kernels() {
     if (err == cudaSuccess)
         err = cudaFuncSetAttribute(k_seed_mid<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    static_cast<int>(mid_kernel_smem(true)));
+    if (err == cudaSuccess)
+        err = cudaFuncSetAttribute(k_seed_mid<false, true>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   static_cast<int>(mid_kernel_smem(false)));
     if (err == cudaSuccess) done_for = dev;
     return err;
 }
@@ -2252,7 +2327,24 @@ cudaError_t launch_seeding(const DevConfig& cfg, const Arena& a, const BatchHead
     const uint32_t mpi = static_cast<uint32_t>(tp.middles_per_item);
     const uint32_t nbc = static_cast<uint32_t>(tp.nb_cap);
     const dim3 fgrid(num_sms * tp.ctas_per_sm), fblock(tp.fast_warps * 32);
-    if (cfg.mlp) {
+    // a filter that only gates middles (and records nothing) runs inside the
+    // plain routine (GATE instantiation), which keeps the plain kernel's warps
+    const bool plain_gate = cfg.mlp && cfg.mlp_prune_top == SEEDGB_FILTER_GATE_MIDDLE &&
+                            cfg.mlp_prune_bottom == SEEDGB_FILTER_KEEP && !a.dump && !a.tdump;
+    if (plain_gate) {
+        k_seed_fast<false, true><<<fgrid, fblock, fsm, stream>>>(cfg, a, mpi, nbc, 0u);
+        mark(6);
+        k_seed_mid<false, true><<<num_sms, mid_kernel_warps(false) * 32, mid_kernel_smem(false),
+                                   stream>>>(cfg, a, 0u);
+        mark(7);
+        k_seed_slow<false, true><<<num_sms, 32, ssm, stream>>>(cfg, a, 0u);
+        // fallback: events whose gated fraction left the band, without the gate
+        k_filter_mark<<<(grid.n_events + 255) / 256, 256, 0, stream>>>(cfg, a);
+        k_seed_fast<false><<<fgrid, fblock, fsm, stream>>>(cfg, a, mpi, nbc, 1u);
+        k_seed_mid<false><<<num_sms, mid_kernel_warps(false) * 32, mid_kernel_smem(false),
+                             stream>>>(cfg, a, 1u);
+        k_seed_slow<false><<<num_sms, 32, ssm, stream>>>(cfg, a, 1u);
+    } else if (cfg.mlp) {
         TuneParams ts = tp;
         ts.fast_warps = std::min(tp.fast_warps, kScoreWarps);
         k_seed_fast<true><<<fgrid, ts.fast_warps * 32, fast_kernel_smem(ts), stream>>>(
