@@ -1030,7 +1030,7 @@ __device__ __noinline__ bool gate_keeps_middle(const DevConfig& c, const Arena& 
 #pragma unroll 1
         for (uint32_t tt = 0; tt < 2; ++tt) {
             float lo, hi;
-            mlp_tile16(*c.mlp, xs + 64 * tt, lane, lo, hi);
+            mlp_tile16_lean(*c.mlp, xs + 64 * tt, lane, lo, hi);
             if ((lane & 3) == 0) {
                 const uint32_t g = lane >> 2;
                 lg[16 * tt + g] = lo;

@@ -159,6 +159,64 @@ __device__ __forceinline__ void mlp_tile16(const MlpFrag& f, const uint32_t* xs,
     hi = o[2];
 }
 
+// mlp_tile16 computed two output n-tiles at a time, so that few fragments and
+// accumulators are live at once (for code that calls it with many registers
+// of its own live).  Same operands, same mma sequence per output element,
+// hence the same logits.
+__device__ __forceinline__ void mlp_tile16_lean(const MlpFrag& f, const uint32_t* xs,
+                                                uint32_t lane, float& lo, float& hi) {
+    const uint32_t g = lane >> 2, t = lane & 3;
+    const uint32_t a[4] = {xs[4 * g + t], xs[4 * (g + 8) + t], 0u, 0u};
+    uint32_t a2[2][4], a3[2][4];
+#pragma unroll 1
+    for (int ks = 0; ks < 2; ++ks) {
+        float h0[4], h1[4];
+        const int n0 = 2 * ks, n1 = 2 * ks + 1;
+        h0[0] = h0[2] = f.b1[n0 * 8 + 2 * t];
+        h0[1] = h0[3] = f.b1[n0 * 8 + 2 * t + 1];
+        h1[0] = h1[2] = f.b1[n1 * 8 + 2 * t];
+        h1[1] = h1[3] = f.b1[n1 * 8 + 2 * t + 1];
+        const uint2 b0 = f.w1[n0][lane], b1 = f.w1[n1][lane];
+        mma_bf16(h0, a, b0.x, b0.y);
+        mma_bf16(h1, a, b1.x, b1.y);
+        const uint32_t p0 = pack_bf16(fmaxf(h0[0], 0.f), fmaxf(h0[1], 0.f));
+        const uint32_t p1 = pack_bf16(fmaxf(h0[2], 0.f), fmaxf(h0[3], 0.f));
+        const uint32_t p2 = pack_bf16(fmaxf(h1[0], 0.f), fmaxf(h1[1], 0.f));
+        const uint32_t p3 = pack_bf16(fmaxf(h1[2], 0.f), fmaxf(h1[3], 0.f));
+        if (ks == 0) { a2[0][0] = p0; a2[0][1] = p1; a2[0][2] = p2; a2[0][3] = p3; }
+        else { a2[1][0] = p0; a2[1][1] = p1; a2[1][2] = p2; a2[1][3] = p3; }
+    }
+#pragma unroll 1
+    for (int ks = 0; ks < 2; ++ks) {
+        float h0[4], h1[4];
+        const int n0 = 2 * ks, n1 = 2 * ks + 1;
+        h0[0] = h0[2] = f.b2[n0 * 8 + 2 * t];
+        h0[1] = h0[3] = f.b2[n0 * 8 + 2 * t + 1];
+        h1[0] = h1[2] = f.b2[n1 * 8 + 2 * t];
+        h1[1] = h1[3] = f.b2[n1 * 8 + 2 * t + 1];
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            const uint2 b0 = f.w2[k][n0][lane], b1 = f.w2[k][n1][lane];
+            mma_bf16(h0, a2[k], b0.x, b0.y);
+            mma_bf16(h1, a2[k], b1.x, b1.y);
+        }
+        const uint32_t p0 = pack_bf16(fmaxf(h0[0], 0.f), fmaxf(h0[1], 0.f));
+        const uint32_t p1 = pack_bf16(fmaxf(h0[2], 0.f), fmaxf(h0[3], 0.f));
+        const uint32_t p2 = pack_bf16(fmaxf(h1[0], 0.f), fmaxf(h1[1], 0.f));
+        const uint32_t p3 = pack_bf16(fmaxf(h1[2], 0.f), fmaxf(h1[3], 0.f));
+        if (ks == 0) { a3[0][0] = p0; a3[0][1] = p1; a3[0][2] = p2; a3[0][3] = p3; }
+        else { a3[1][0] = p0; a3[1][1] = p1; a3[1][2] = p2; a3[1][3] = p3; }
+    }
+    float o[4] = {t == 0 ? f.b3 : 0.f, 0.f, t == 0 ? f.b3 : 0.f, 0.f};
+#pragma unroll
+    for (int ks = 0; ks < 2; ++ks) {
+        const uint2 b = f.w3[ks][lane];
+        mma_bf16(o, a3[ks], b.x, b.y);
+    }
+    lo = o[0];
+    hi = o[2];
+}
+
 // The network held in registers by one warp (per-lane B fragments and the
 // biases of the lane's output columns), for loops over many tiles.
 struct MlpRegs {
