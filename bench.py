@@ -440,11 +440,14 @@ FILTER_CALIB_MIN_EVENT = 0.998
 
 
 def run_formation(args, stream, meas, n_sp_total):
-    """Spacepoint formation in front of the step (seedgb_form_spacepoints:
-    the 20 events' measurements on the synthetic barrel's cylinder surfaces
-    -> spacepoints): device time per step, the upper bound of what fusing
-    formation into binning could save (fusion would remove only the
-    spacepoint columns' write and re-read, 28 + 12 bytes per spacepoint)."""
+    """Spacepoint formation in front of the step: the 20 events' measurements
+    on the synthetic barrel's cylinder surfaces -> spacepoints, device time
+    per step (i) in one launch sequence for all events on a device-resident
+    surface table (seedgb_formation_run_batch) and (ii) event by event
+    (seedgb_form_spacepoints, which uploads the surface table and finishes
+    each call before returning).  Fusing formation into binning would save
+    at most the spacepoint columns' write and re-read (28 + 12 bytes per
+    spacepoint), which the batched figure bounds."""
     import torch
 
     from traccc_gb300 import seeding, synth
@@ -454,24 +457,38 @@ def run_formation(args, stream, meas, n_sp_total):
         surf[layer + 1]["radius"] = r
         surf[layer + 1]["rotation"] = np.eye(3, dtype=np.float32).reshape(-1)
     sptr = stream.cuda_stream
+    reps = max(1, min(args.steps, 5))
+    # (i) batched
+    form = seeding.SpacepointFormationAlgorithm(surf)
+    outs, counts = form.run_batch(meas, stream=sptr)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    batched = []
+    for _ in range(reps):
+        e0.record(stream)
+        form.run_batch(meas, outs=outs, stream=sptr)
+        e1.record(stream)
+        e1.synchronize()
+        batched.append(e0.elapsed_time(e1))
+    formed = int(counts.sum().item())
+    # (ii) event by event
     for m in meas:
         seeding.form_spacepoints(surf, m, stream=sptr)
     ev_t = [torch.cuda.Event(enable_timing=True) for _ in range(2 * len(meas))]
-    reps, total_ms, formed = max(1, min(args.steps, 5)), 0.0, 0
+    per_event = 0.0
     for _ in range(reps):
         for i, m in enumerate(meas):
             ev_t[2 * i].record(stream)
-            _, k = seeding.form_spacepoints(surf, m, stream=sptr)
+            seeding.form_spacepoints(surf, m, stream=sptr)
             ev_t[2 * i + 1].record(stream)
-            formed += k
         torch.cuda.synchronize()
-        total_ms += sum(ev_t[2 * i].elapsed_time(ev_t[2 * i + 1]) for i in range(len(meas)))
-    ms = total_ms / reps
-    return {"ms_per_step": ms, "events": len(meas), "spacepoints_formed": formed // reps,
-            "fusion_saving_bound_bytes": 40 * n_sp_total,
-            "timing": "device time of the per-event formation calls (one kernel sequence each: "
-                      "count, scan, write), summed over the step's events, mean of "
-                      f"{reps} repetitions"}
+        per_event += sum(ev_t[2 * i].elapsed_time(ev_t[2 * i + 1]) for i in range(len(meas)))
+    return {"batched_ms_per_step": statistics.median(batched),
+            "per_event_calls_ms_per_step": per_event / reps, "events": len(meas),
+            "spacepoints_formed": formed, "fusion_saving_bound_bytes": 40 * n_sp_total,
+            "timing": "device time, CUDA events on the launching stream; batched: one "
+                      "seedgb_formation_run_batch call for the step's events (median of "
+                      f"{reps}); per event: the seedgb_form_spacepoints calls summed over the "
+                      f"events (mean of {reps})"}
 
 
 FILTER_TRAIN_SEED0 = 1000

@@ -318,6 +318,39 @@ seedgb_status seedgb_form_spacepoints(const seedgb_surface* surfaces_host, uint3
                                       float* z_variance, float* radius_variance,
                                       uint32_t* n_out, void* stream);
 
+/* Spacepoint formation for many events per call, without host
+ * synchronisation: the surface table is uploaded once, at creation, and
+ * stays on the device; each batch is one launch sequence (descriptor copy
+ * from pinned memory, count, scan, write) over all its events.  Same
+ * spacepoints, in the same order, as seedgb_form_spacepoints per event.  No
+ * counterpart in the reference, whose algorithm forms one event per call
+ * (silicon_pixel_spacepoint_formation.hpp:31-60). */
+typedef struct {
+    uint32_t* measurement_index_1;
+    uint32_t* measurement_index_2;
+    float* global;          /* x, y, z interleaved */
+    float* z_variance;
+    float* radius_variance;
+    uint32_t capacity;      /* >= the event's measurement count */
+    uint32_t* size;         /* device: spacepoints formed */
+} seedgb_spacepoint_buffer;
+
+typedef struct seedgb_formation seedgb_formation;
+seedgb_status seedgb_formation_create(const seedgb_surface* surfaces_host, uint32_t n_surfaces,
+                                      seedgb_formation** out);
+seedgb_status seedgb_formation_destroy(seedgb_formation* h);
+/* Element e of each array belongs to event e; dimensions may be NULL (all
+ * measurements 2-dimensional), else an array of n_events device pointers
+ * (each may be NULL).  Asynchronous on `stream`; the descriptors travel
+ * through two pinned slots used in turn (a call waits only for the copy of
+ * the call before the previous one).  SEEDGB_INVALID_ARGUMENT when an
+ * output's capacity is below its event's measurement count; SEEDGB_SIZE_LIMIT
+ * above 65535 events.  One stream per handle. */
+seedgb_status seedgb_formation_run_batch(seedgb_formation* h, const seedgb_measurement_view* meas,
+                                         const uint8_t* const* dimensions,
+                                         seedgb_spacepoint_buffer* outs, uint32_t n_events,
+                                         void* stream);
+
 /* ------------------------------------------------------------------------ */
 /* CSV input (traccc's on-disk event format)                                 */
 /* ------------------------------------------------------------------------ */

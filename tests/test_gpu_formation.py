@@ -103,3 +103,47 @@ def test_formation_telescope_known_answer():
     assert k == 2
     assert np.array_equal(sps.global_.cpu().numpy()[:2],
                           np.array([[20., 7., 2.], [180., 10., 15.]], np.float32))
+
+
+def test_batched_formation_equals_per_event_calls():
+    """seedgb_formation_run_batch (surface table resident on the device, one
+    launch sequence for the batch) forms the same spacepoints, in the same
+    order and with the same counts, as seedgb_form_spacepoints event by
+    event -- with mixed surfaces, pixel / strip dimensions, unknown surfaces
+    and an empty event in the batch -- on two batches in a row (the two
+    descriptor slots)."""
+    import torch
+
+    from traccc_gb300 import seeding
+    surf = _surfaces()
+    rng = np.random.default_rng(3)
+    events, dims = [], []
+    for s in range(4):
+        ev = synth.workload_event("trk1000", 30 + s)
+        n = len(ev["global"])
+        link = np.asarray(ev["surface_link"], np.uint64).copy()
+        link[rng.choice(n, 200, replace=False)] = rng.integers(11, 16, 200)
+        link[rng.choice(n, 30, replace=False)] = 1000
+        d = np.full(n, 2, np.uint8)
+        d[rng.choice(n, 100, replace=False)] = 1
+        events.append(dict(local_position=ev["local_position"], surface_link=link))
+        dims.append(d)
+    events.insert(2, dict(local_position=np.zeros((0, 2), np.float32),
+                          surface_link=np.zeros(0, np.uint64)))
+    dims.insert(2, np.zeros(0, np.uint8))
+    meas = [seeding.MeasurementCollection.from_numpy(e) for e in events]
+    ddims = [torch.from_numpy(d).cuda() for d in dims]
+    alg = seeding.SpacepointFormationAlgorithm(surf)
+    for _ in range(2):
+        outs, counts = alg.run_batch(meas, ddims)
+        torch.cuda.synchronize()
+        counts = counts.cpu().numpy()
+        for e, (m, d, o) in enumerate(zip(meas, ddims, outs)):
+            ref, k = seeding.form_spacepoints(surf, m, d)
+            assert counts[e] == k
+            for col in ("measurement_index_1", "measurement_index_2", "global_", "z_variance",
+                        "radius_variance"):
+                a = getattr(o, col)[:k].cpu().numpy()
+                b = getattr(ref, col)[:k].cpu().numpy()
+                assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), (e, col)
+    assert counts[2] == 0

@@ -137,6 +137,13 @@ class DoubletFilter(C.Structure):
                 ("size_class_band", (C.c_float * 2) * 8)]
 
 
+class _SpacepointBuffer(C.Structure):
+    _fields_ = [("measurement_index_1", C.c_void_p), ("measurement_index_2", C.c_void_p),
+                ("global_", C.c_void_p), ("z_variance", C.c_void_p),
+                ("radius_variance", C.c_void_p), ("capacity", C.c_uint32),
+                ("size", C.c_void_p)]
+
+
 class _ParamsBuffer(C.Structure):
     _fields_ = [("data", C.c_void_p), ("capacity", C.c_uint32),
                 ("size", C.c_void_p)]
@@ -244,6 +251,13 @@ def lib():
         L.seedgb_form_spacepoints.argtypes = [vp, C.c_uint32, P(_MeasurementView), vp, vp, vp,
                                               vp, vp, vp, vp, vp]
         L.seedgb_form_spacepoints.restype = C.c_int
+        L.seedgb_formation_create.argtypes = [vp, C.c_uint32, P(vp)]
+        L.seedgb_formation_create.restype = C.c_int
+        L.seedgb_formation_destroy.argtypes = [vp]
+        L.seedgb_formation_destroy.restype = C.c_int
+        L.seedgb_formation_run_batch.argtypes = [vp, P(_MeasurementView), vp,
+                                                 P(_SpacepointBuffer), C.c_uint32, vp]
+        L.seedgb_formation_run_batch.restype = C.c_int
         L.seedgb_csv_rows.argtypes = [C.c_char_p]
         L.seedgb_csv_rows.restype = C.c_int64
         L.seedgb_csv_read_spacepoints.argtypes = [C.c_char_p, C.c_char_p, C.c_uint64, vp, vp,
@@ -748,6 +762,59 @@ def form_spacepoints(surfaces, measurements: MeasurementCollection, dimensions=N
     return SpacepointCollection(cols.measurement_index_1[:k], cols.measurement_index_2[:k],
                                 cols.global_[:k], cols.z_variance[:k],
                                 cols.radius_variance[:k]), k
+
+
+class SpacepointFormationAlgorithm:
+    """Spacepoint formation of many events per call on a device-resident
+    surface table (seedgb_formation_*): the same spacepoints as
+    form_spacepoints per event, one launch sequence per batch, no host
+    synchronisation."""
+
+    def __init__(self, surfaces):
+        self.surfaces = np.ascontiguousarray(surfaces, SURFACE_DTYPE)
+        self._h = C.c_void_p()
+        _check(lib().seedgb_formation_create(
+            self.surfaces.ctypes.data if len(self.surfaces) else None, len(self.surfaces),
+            C.byref(self._h)), "seedgb_formation_create")
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and h.value and _lib is not None:
+            _lib.seedgb_formation_destroy(h)
+            self._h = C.c_void_p()
+
+    def run_batch(self, measurements, dimensions=None, outs=None, stream=None):
+        """Returns (list of SpacepointCollection with room for every
+        measurement, int32 device tensor of the per-event counts).  Slice
+        each collection by its count before seeding it."""
+        torch = _torch()
+        n = len(measurements)
+        if n == 0:
+            return [], None
+        dev = measurements[0].local_position.device
+        if outs is None:
+            outs = []
+            for m in measurements:
+                k = len(m.surface_link)
+                outs.append(SpacepointCollection(
+                    torch.empty(k, dtype=torch.int32, device=dev),
+                    torch.empty(k, dtype=torch.int32, device=dev),
+                    torch.empty((k, 3), dtype=torch.float32, device=dev),
+                    torch.empty(k, dtype=torch.float32, device=dev),
+                    torch.empty(k, dtype=torch.float32, device=dev)))
+        counts = torch.zeros(n, dtype=torch.int32, device=dev)
+        mv = (_MeasurementView * n)(*[m.view() for m in measurements])
+        ob = (_SpacepointBuffer * n)(*[_SpacepointBuffer(
+            o.measurement_index_1.data_ptr(), o.measurement_index_2.data_ptr(),
+            o.global_.data_ptr(), o.z_variance.data_ptr(), o.radius_variance.data_ptr(),
+            len(o.measurement_index_1), counts.data_ptr() + 4 * e) for e, o in enumerate(outs)])
+        dims = None
+        if dimensions is not None:
+            dims = (C.c_void_p * n)(*[d.data_ptr() if d is not None else None
+                                      for d in dimensions])
+        _check(lib().seedgb_formation_run_batch(self._h, mv, dims, ob, n, _stream_ptr(stream)),
+               "seedgb_formation_run_batch")
+        return outs, counts
 
 
 def read_spacepoints_csv(hits_path, meas_hit_map_path=None) -> dict:
