@@ -1001,10 +1001,12 @@ __device__ __noinline__ uint32_t filter_bottoms(const DevConfig& c, const Arena&
 // >= its event's threshold.  Features and network as in the scoring
 // instantiation (the lin_circle's cot, s and Zo do not depend on the
 // variances; the network's fragments are read from memory rather than held in
-// registers, with the same operands and mma order, so the same logits),
-// stopping at the first chunk of 32 that decides.  Out of line, so that the
-// routine's hot loops keep their registers and instruction-cache footprint.
-// xs: 128 words, lg: 32 floats of warp scratch.
+// registers, with the same operands and mma order, so the same logits).
+// Doublets are scored 16 at a time (one network tile, lanes 0-15 computing
+// the features), stopping at the first tile that decides.  Out of line and
+// with rolled loops, so that the routine's hot loops keep their registers and
+// the instruction cache its footprint.  xs: 64 words, lg: 16 floats of warp
+// scratch.
 template <int MODE>
 __device__ __noinline__ bool gate_keeps_middle(const DevConfig& c, const Arena& a,
                                                const NbViewT<MODE>& nb, const float4 M,
@@ -1014,31 +1016,37 @@ __device__ __noinline__ bool gate_keeps_middle(const DevConfig& c, const Arena& 
     const float thr = filter_threshold(c, a, ev, 1);
     const float cosPhiM = M.x / M.w, sinPhiM = M.y / M.w;
     const float2 zero2 = make_float2(0.f, 0.f);
-    for (uint32_t base = 0; base < n_mt; base += 32) {
-        const uint32_t i = base + lane;
-        const bool valid = i < n_mt;
-        uint32_t pk[4] = {0u, 0u, 0u, 0u};
-        if (valid) {
-            const float4 o = nb.get(q[i]);
-            const LinCircle l = lin_circle_cs(true, M, cosPhiM, sinPhiM, zero2, o, zero2);
-            float x[kMlpIn];
-            mlp_features(c.mlp_edges, c.mlp_n_edges, M, o, l.cot, l.s, l.Zo, x);
-            mlp_pack_inputs(c.mlp_mu, c.mlp_isd, x, pk);
-        }
-        *reinterpret_cast<uint4*>(xs + 4 * lane) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
-        __syncwarp();
+    uint32_t bm = 0;  // band of the middle spacepoint
 #pragma unroll 1
-        for (uint32_t tt = 0; tt < 2; ++tt) {
-            float lo, hi;
-            mlp_tile16_lean(*c.mlp, xs + 64 * tt, lane, lo, hi);
-            if ((lane & 3) == 0) {
-                const uint32_t g = lane >> 2;
-                lg[16 * tt + g] = lo;
-                lg[16 * tt + g + 8] = hi;
+    for (uint32_t e = 0; e < c.mlp_n_edges; ++e) bm += c.mlp_edges[e] <= M.w ? 1u : 0u;
+#pragma unroll 1
+    for (uint32_t base = 0; base < n_mt; base += 16) {
+        const uint32_t i = base + lane;
+        const bool valid = lane < 16 && i < n_mt;
+        if (lane < 16) {
+            uint32_t pk[4] = {0u, 0u, 0u, 0u};
+            if (valid) {
+                const float4 o = nb.get(q[i]);
+                const LinCircle l = lin_circle_cs(true, M, cosPhiM, sinPhiM, zero2, o, zero2);
+                uint32_t bo = 0;
+#pragma unroll 1
+                for (uint32_t e = 0; e < c.mlp_n_edges; ++e) bo += c.mlp_edges[e] <= o.w ? 1u : 0u;
+                const float x[kMlpIn] = {M.w, M.z, o.w - M.w, o.z - M.z, l.cot, l.s, l.Zo,
+                                         static_cast<float>(bm * (c.mlp_n_edges + 1) + bo)};
+                mlp_pack_inputs(c.mlp_mu, c.mlp_isd, x, pk);
             }
+            *reinterpret_cast<uint4*>(xs + 4 * lane) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
         }
         __syncwarp();
-        const bool reach = valid && lg[lane] >= thr;
+        float lo, hi;
+        mlp_tile16_lean(*c.mlp, xs, lane, lo, hi);
+        if ((lane & 3) == 0) {
+            const uint32_t g = lane >> 2;
+            lg[g] = lo;
+            lg[g + 8] = hi;
+        }
+        __syncwarp();
+        const bool reach = valid && lg[lane & 15] >= thr;
         __syncwarp();
         if (__any_sync(0xffffffffu, reach)) return true;
     }
