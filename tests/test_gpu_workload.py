@@ -4,8 +4,9 @@ batch through the captured graph -- against the oracle's, through the
 committed per-event digests (tests/golden/workload_hashes.json): seed count
 and SHA-256 of the seed bytes, 2.9 M seeds in all.
 
-Then the track parameters of all 1.03 M seeds of the 20-event bench step,
-from the batched parameter launch the bench times, against the oracle's
+Then the track parameters of all seeds of both workloads (1.03 M of the
+20-event bench step, 1.9 M of the batch), from the batched parameter launch
+the bench times, against the oracle's
 parameter estimation of the same seeds (once the seeds are known to be the
 oracle's, the oracle needs no seeding run: its parameter estimation is
 milliseconds per event): surface links exact, the six parameters and the
@@ -51,8 +52,7 @@ def test_full_workloads_match_the_oracle_digests():
             got = o.to_numpy()
             assert len(got) == g["n_seeds"], (name, e)
             assert W.seed_digest(got) == g["seeds"], (name, e)
-        if name == "pileup9k":
-            _params_match_oracle(events, sps, outs)
+        _params_match_oracle(events, sps, outs)
 
 
 def _params_match_oracle(events, sps, seed_outs):
@@ -77,7 +77,7 @@ def _params_match_oracle(events, sps, seed_outs):
         ok &= ~off.reshape(len(gp), -1).any(axis=1)
         assert ok.all(), (e, np.nonzero(~ok)[0][:10], counts)
         n_all += len(gp)
-    assert n_all > 1_000_000
+    assert n_all > 500_000
     # phi near zero (relative comparison ill-conditioned): rare
     assert counts["angle_abs"] <= 1e-4 * n_all, counts
     print(f"{n_all} parameter sets; {counts['angle_abs']} phi within {ANGLE_ABS_TOL} rad "
