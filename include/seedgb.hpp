@@ -11,6 +11,9 @@
  *  seedgb::seed_parameter_estimation_algorithm <- traccc::cuda::seed_parameter_estimation_algorithm
  *      operator():  device/common/include/traccc/seeding/device/
  *                   seed_parameter_estimation_algorithm.hpp:48-67
+ *  seedgb::spacepoint_formation_algorithm  measurements -> spacepoints for
+ *                   many events per call (core/src/seeding/
+ *                   silicon_pixel_spacepoint_formation.hpp:31-60 per event)
  *  seedgb::to_ckf   the parameters in the record layout the track finding
  *                   takes (examples/run/cuda/src/full_chain_algorithm.cpp:
  *                   241-247), device-resident
@@ -193,6 +196,77 @@ inline ckf_params_buffer to_ckf(const track_params_buffer& params, cudaStream_t 
           "to_ckf");
     return out;
 }
+
+/* Spacepoint collection buffer with room for `capacity` spacepoints and a
+ * device count (edm::spacepoint_collection::buffer). */
+class spacepoint_collection_buffer {
+public:
+    explicit spacepoint_collection_buffer(uint32_t capacity)
+        : measurement_index_1(capacity), measurement_index_2(capacity), global(3ull * capacity),
+          z_variance(capacity), radius_variance(capacity), size(1), capacity_(capacity) {}
+    seedgb_spacepoint_buffer buffer() const {
+        return seedgb_spacepoint_buffer{measurement_index_1.data(), measurement_index_2.data(),
+                                        global.data(), z_variance.data(), radius_variance.data(),
+                                        capacity_, size.data()};
+    }
+    /* A view of the first n spacepoints (n: the count, read back by the caller). */
+    seedgb_spacepoint_view view(uint32_t n) const {
+        return seedgb_spacepoint_view{measurement_index_1.data(), measurement_index_2.data(),
+                                      global.data(), z_variance.data(), radius_variance.data(), n};
+    }
+    uint32_t count(cudaStream_t stream) const {
+        uint32_t n = 0;
+        if (cudaMemcpyAsync(&n, size.data(), sizeof n, cudaMemcpyDeviceToHost, stream) !=
+                cudaSuccess ||
+            cudaStreamSynchronize(stream) != cudaSuccess)
+            throw std::runtime_error("spacepoint count copy failed");
+        return n;
+    }
+
+    device_buffer<uint32_t> measurement_index_1, measurement_index_2;
+    device_buffer<float> global, z_variance, radius_variance;
+    device_buffer<uint32_t> size;
+
+private:
+    uint32_t capacity_;
+};
+
+/* traccc::host::silicon_pixel_spacepoint_formation_algorithm on the device, for
+ * many events per call: the surface table uploaded once. */
+class spacepoint_formation_algorithm {
+public:
+    spacepoint_formation_algorithm(const std::vector<seedgb_surface>& surfaces,
+                                   cudaStream_t stream)
+        : stream_(stream) {
+        check(seedgb_formation_create(surfaces.empty() ? nullptr : surfaces.data(),
+                                      static_cast<uint32_t>(surfaces.size()), &h_),
+              "spacepoint_formation_algorithm");
+    }
+    spacepoint_formation_algorithm(const spacepoint_formation_algorithm&) = delete;
+    spacepoint_formation_algorithm& operator=(const spacepoint_formation_algorithm&) = delete;
+    ~spacepoint_formation_algorithm() { seedgb_formation_destroy(h_); }
+
+    /* One buffer per event (room for all its measurements); asynchronous. */
+    std::vector<spacepoint_collection_buffer> operator()(
+        const std::vector<seedgb_measurement_view>& measurements) const {
+        std::vector<spacepoint_collection_buffer> out;
+        std::vector<seedgb_spacepoint_buffer> bufs;
+        out.reserve(measurements.size());
+        for (const auto& m : measurements) {
+            out.emplace_back(m.size > 0 ? m.size : 1u);
+            bufs.push_back(out.back().buffer());
+        }
+        if (!measurements.empty())
+            check(seedgb_formation_run_batch(h_, measurements.data(), nullptr, bufs.data(),
+                                             static_cast<uint32_t>(measurements.size()), stream_),
+                  "spacepoint_formation_algorithm()");
+        return out;
+    }
+
+private:
+    cudaStream_t stream_;
+    seedgb_formation* h_ = nullptr;
+};
 
 /* traccc::cuda::triplet_seeding_algorithm. */
 class triplet_seeding_algorithm {
