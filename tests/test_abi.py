@@ -122,3 +122,26 @@ def test_ckf_record_layout():
     b = seeding._ParamsBuffer(16, 4, 16)
     assert L.seedgb_params_to_ckf(C.byref(b), C.c_void_p(24), 4, None, None) == \
         seeding.INVALID_ARGUMENT
+
+
+def test_batched_formation_arguments_are_checked_before_device_work():
+    """seedgb_formation_run_batch refuses, before touching a device, a batch
+    above 65535 events and an output whose capacity is below its event's
+    measurement count (a handle without surfaces needs no device)."""
+    L = seeding.lib()
+    assert L.seedgb_formation_run_batch(None, None, None, None, 1, None) == \
+        seeding.INVALID_ARGUMENT
+    assert L.seedgb_formation_destroy(None) == seeding.INVALID_ARGUMENT
+    bad = C.c_void_p()
+    assert L.seedgb_formation_create(None, 3, C.byref(bad)) == seeding.INVALID_ARGUMENT
+    h = C.c_void_p()
+    assert L.seedgb_formation_create(None, 0, C.byref(h)) == seeding.OK
+    m = seeding._MeasurementView(16, 16, 10)
+    small = seeding._SpacepointBuffer(16, 16, 16, 16, 16, 9, 16)
+    assert L.seedgb_formation_run_batch(h, C.byref(m), None, C.byref(small), 1, None) == \
+        seeding.INVALID_ARGUMENT
+    n = 65536
+    ms = (seeding._MeasurementView * n)()
+    outs = (seeding._SpacepointBuffer * n)()
+    assert L.seedgb_formation_run_batch(h, ms, None, outs, n, None) == seeding.SIZE_LIMIT
+    L.seedgb_formation_destroy(h)
