@@ -294,13 +294,14 @@ class DoubletFilter(C.Structure):
                 ("w3", C.c_float * MLP_H), ("b3", C.c_float),
                 ("threshold", C.c_float * 2), ("n_edges", C.c_uint32),
                 ("edges", C.c_float * MAX_BAND_EDGES),
-                ("prune_bottom", C.c_uint32), ("prune_top", C.c_uint32)]
+                ("prune_bottom", C.c_uint32), ("prune_top", C.c_uint32),
+                ("gate_max_tops", C.c_uint32)]
 
 
 FILTER_KEEP, FILTER_PRUNE_DOUBLETS, FILTER_GATE_MIDDLE = 0, 1, 2
 
 
-def doublet_filter(model: dict, threshold, prune_bottom=True, prune_top=True):
+def doublet_filter(model: dict, threshold, prune_bottom=True, prune_top=True, gate_max_tops=0):
     """A DoubletFilter from a model dict with numpy arrays mu, isd, w1 (8x32),
     b1, w2 (32x32), b2, w3 (32), b3 and edges; threshold = (middle-bottom,
     middle-top) logit thresholds (or one for both).  prune_bottom / prune_top:
@@ -321,6 +322,7 @@ def doublet_filter(model: dict, threshold, prune_bottom=True, prune_top=True):
     f.edges[: len(edges)] = edges.tolist()
     f.prune_bottom = int(prune_bottom)
     f.prune_top = int(prune_top)
+    f.gate_max_tops = int(gate_max_tops)
     return f
 
 

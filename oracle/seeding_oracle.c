@@ -804,7 +804,8 @@ int or_seeding_ex(const or_finder_config* fc, const or_grid_config* gc,
                 if (mb.n == 0) continue;
                 score_role(filt, 1, spM, m, sps, &mt, dump, dump_cap, n_dump,
                            &st->n_scored_mt, &st->n_pruned_mt, &reach);
-                if (filt && filt->prune_top == 2u && !reach) {
+                if (filt && filt->prune_top == 2u && !reach &&
+                    (filt->gate_max_tops == 0u || mt.n <= filt->gate_max_tops)) {
                     /* gated middle: no seed, its middle-top doublets pruned */
                     st->n_pruned_mt += mt.n;
                     continue;

@@ -229,6 +229,8 @@ typedef struct {
                                        * threshold, 2 (prune_top only) gate
                                        * whole middles: no seed unless a
                                        * middle-top doublet reaches it */
+    uint32_t gate_max_tops;           /* gate: middles with more middle-top
+                                       * doublets are kept (0: no limit) */
 } or_doublet_filter;
 
 /* One scored doublet (dump of or_seeding_ex). */

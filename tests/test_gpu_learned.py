@@ -48,7 +48,8 @@ def _oracle_filter(model, threshold, prune=(True, True)):
     w1, b1, w2, b2, w3, b3 = R.unpack(p)
     d = dict(mu=model.norm[:8], isd=model.norm[8:], w1=w1, b1=b1, w2=w2, b2=b2, w3=w3, b3=b3,
              edges=model.edges)
-    return O.doublet_filter(d, threshold, prune_bottom=prune[0], prune_top=prune[1])
+    return O.doublet_filter(d, threshold, prune_bottom=prune[0], prune_top=prune[1],
+                            gate_max_tops=model.gate_max_tops)
 
 
 def test_forward_matches_reference():
@@ -305,9 +306,10 @@ def test_training_gains_over_untrained():
     tr = [seeding.SpacepointCollection.from_numpy(e, device=dev) for e in train_ev]
     ca = [seeding.SpacepointCollection.from_numpy(e, device=dev) for e in calib_ev]
     f, loss = alg.train_filter(tr, learned.band_edges(), epochs=3, neg_keep=0.1)
-    assert loss[-1] < loss[0]
+    assert loss[-1] < loss[0] and f.gate_max_tops == 32
+    f.gate_max_tops = 0  # every middle scored: the comparison measures the network
     untrained = learned.FilterModel(learned.init_params(1), learned.FilterModel.from_struct(f).norm,
-                                    learned.band_edges()).struct()
+                                    learned.band_edges(), gate_max_tops=0).struct()
     f1, r1, g1 = alg.calibrate_gate(f, ca, target=0.99, min_event=0.99)
     f0, r0, g0 = alg.calibrate_gate(untrained, ca, target=0.99, min_event=0.99)
     assert r1.min() >= 0.99 and r0.min() >= 0.99
@@ -362,7 +364,8 @@ def test_size_classes_apply_per_event(model_and_event):
     sps = [seeding.SpacepointCollection.from_numpy(e) for e in (small, large)]
     alg = seeding.TripletSeedingAlgorithm()
     m = dataclasses.replace(model, classes=[(20000, (-np.inf, np.inf), (0.0, 1.0)),
-                                            (1 << 31, (-np.inf, -np.inf), (0.0, 1.0))])
+                                            (1 << 31, (-np.inf, -np.inf), (0.0, 1.0))],
+                            gate_max_tops=0)
     alg.set_filter(m.struct())
     outs = alg.run_batch(sps)
     assert alg.last_status() == seeding.OK
@@ -371,7 +374,8 @@ def test_size_classes_apply_per_event(model_and_event):
     assert np.array_equal(outs[1].to_numpy(), plain_l) and per[1, 3] == 0
     # the small class's band excludes "everything pruned": it falls back
     m2 = dataclasses.replace(model, classes=[(20000, (-np.inf, np.inf), (0.0, 0.5)),
-                                             (1 << 31, (-np.inf, -np.inf), (0.0, 1.0))])
+                                             (1 << 31, (-np.inf, -np.inf), (0.0, 1.0))],
+                             gate_max_tops=0)
     alg.set_filter(m2.struct())
     outs = alg.run_batch(sps)
     _, fb, _ = alg.filter_stats(2)

@@ -184,3 +184,24 @@ def test_middle_gate_keeps_exactly_the_plain_seeds_of_kept_middles(trk1000_event
         gated = [m for m, b in best.items() if b < th]
         n_gated_tops = int(np.isin(tops["middle"], gated).sum())
         assert st["n_pruned_mt"] == n_gated_tops and st["n_pruned_mb"] == 0
+
+
+def test_middle_gate_size_limit_keeps_large_middles(trk1000_event):
+    """With gate_max_tops = K the gate scores only middles with at most K
+    middle-top doublets; larger middles keep all their plain seeds even when
+    no doublet reaches the threshold (here: a threshold nothing reaches)."""
+    p, norm = _model(9)
+    _, _, d = O.seeding_ex(trk1000_event, filt=O.doublet_filter(_model_dict(p, norm), -np.inf),
+                           dump=True)
+    plain, _ = O.seeding(trk1000_event)
+    tops = d[d["top"] == 1]
+    n_mt = np.bincount(tops["middle"], minlength=len(trk1000_event["global"]))
+    K = 8
+    f = O.doublet_filter(_model_dict(p, norm), (-np.inf, np.inf), prune_bottom=O.FILTER_KEEP,
+                         prune_top=O.FILTER_GATE_MIDDLE, gate_max_tops=K)
+    s, st, _ = O.seeding_ex(trk1000_event, filt=f)
+    kept = n_mt[plain["middle"]] > K
+    assert np.array_equal(s, plain[kept])
+    assert 0 < len(s) < len(plain)
+    assert st["n_pruned_mt"] == int(n_mt[(n_mt > 0) & (n_mt <= K)][
+        np.isin(np.nonzero((n_mt > 0) & (n_mt <= K))[0], np.unique(tops["middle"]))].sum())

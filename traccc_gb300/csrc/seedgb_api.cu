@@ -631,6 +631,7 @@ seedgb_status seedgb_seeding_set_filter(seedgb_seeding* h, const seedgb_doublet_
     for (uint32_t i = 0; i < 15; ++i) h->dc.mlp_edges[i] = i < f->n_edges ? f->edges[i] : 0.f;
     h->dc.mlp_prune_bottom = f->prune_bottom;
     h->dc.mlp_prune_top = f->prune_top;
+    h->dc.mlp_gate_max_tops = f->gate_max_tops;
     if (f->n_size_classes > 8) return SEEDGB_INVALID_ARGUMENT;
     h->dc.mlp_n_classes = f->n_size_classes;
     for (uint32_t k = 0; k < 8; ++k) {

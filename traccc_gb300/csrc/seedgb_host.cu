@@ -71,6 +71,9 @@ struct DumpRec {
 static_assert(sizeof(DumpRec) == 48, "doublet record");
 
 constexpr uint32_t kParams = 8 * 32 + 32 + 32 * 32 + 32 + 32 + 1;  // 1377
+// Middles with more middle-top doublets than this are kept unscored by the
+// gate a training run returns (seedgb_doublet_filter.gate_max_tops).
+constexpr uint32_t kDefaultGateMaxTops = 32;
 
 // Per-event seed buffers sized like the seeding path's maximum.
 struct SeedSet {
@@ -385,6 +388,7 @@ seedgb_status seedgb_filter_train(seedgb_seeding* h, const seedgb_spacepoint_vie
     SEEDGB_CUDA(cudaMemcpy(P.data(), dP.p, 4ull * kParams, cudaMemcpyDeviceToHost));
     scoring_filter(P.data(), norm, band_edges, n_edges, *out);
     out->prune_top = SEEDGB_FILTER_GATE_MIDDLE;
+    out->gate_max_tops = kDefaultGateMaxTops;
     return SEEDGB_OK;
 }
 
@@ -442,6 +446,8 @@ seedgb_status seedgb_filter_calibrate_gate(seedgb_seeding* h, const seedgb_space
     };
     // exact recall and gated share per event at threshold thr (class k)
     std::vector<double> tot(n_events), keep(n_events), mt(n_events), gated(n_events);
+    const uint32_t max_tops = f->gate_max_tops;
+    const auto gateable = [&](const Mid& m) { return max_tops == 0 || m.n_mt <= max_tops; };
     auto evaluate = [&](uint32_t k, float thr) {
         std::fill(tot.begin(), tot.end(), 0.0);
         std::fill(keep.begin(), keep.end(), 0.0);
@@ -449,7 +455,7 @@ seedgb_status seedgb_filter_calibrate_gate(seedgb_seeding* h, const seedgb_space
         std::fill(gated.begin(), gated.end(), 0.0);
         for (const Mid& m : mids) {
             if (class_of(m.ev) != k) continue;
-            const bool kept = m.best >= thr;
+            const bool kept = !gateable(m) || m.best >= thr;
             tot[m.ev] += m.seeds;
             keep[m.ev] += kept ? m.seeds : 0;
             mt[m.ev] += m.n_mt;
@@ -463,7 +469,7 @@ seedgb_status seedgb_filter_calibrate_gate(seedgb_seeding* h, const seedgb_space
     for (uint32_t k = 0; k < nc; ++k) {
         std::vector<float> cand;
         for (const Mid& m : mids)
-            if (class_of(m.ev) == k && m.seeds > 0) cand.push_back(m.best);
+            if (class_of(m.ev) == k && m.seeds > 0 && gateable(m)) cand.push_back(m.best);
         std::sort(cand.begin(), cand.end());
         cand.erase(std::unique(cand.begin(), cand.end()), cand.end());
         float chosen = -INFINITY;

@@ -111,6 +111,7 @@ struct DevConfig {
     uint32_t mlp_class_max[8];
     float mlp_class_thr[8][2];
     float mlp_class_band[8][2];
+    uint32_t mlp_gate_max_tops;  // middle gate: larger middles kept unscored (0: none)
 };
 
 // One event of a batch, as the kernels see it.

@@ -1187,10 +1187,12 @@ __device__ MiddleResult process_middle(const DevConfig& c, const Arena& a,
     if (n_mt > CAPLC) { res.status = 1; return res; }
     if constexpr (!SCORE && GATE) {
         // learned middle gate, the scoring instantiation's decision, before
-        // any middle-top work (the cot-bucket tables are free scratch here)
-        const bool keep = gate_keeps_middle(c, a, nb, M, ws.qt, n_mt, ws.bstart,
-                                            reinterpret_cast<float*>(ws.bstart + 128), ev,
-                                            lane);
+        // any middle-top work (the cot-bucket tables are free scratch here);
+        // middles above the gate's size limit are kept unscored
+        const bool keep =
+            (c.mlp_gate_max_tops != 0 && n_mt > c.mlp_gate_max_tops) ||
+            gate_keeps_middle(c, a, nb, M, ws.qt, n_mt, ws.bstart,
+                              reinterpret_cast<float*>(ws.bstart + 128), ev, lane);
         if (lane == 0) {
             atomicAdd(&a.ev_filter[4 * ev + 2], n_mt);
             if (!keep) atomicAdd(&a.ev_filter[4 * ev + 3], n_mt);
@@ -1267,7 +1269,10 @@ __device__ MiddleResult process_middle(const DevConfig& c, const Arena& a,
             w += __popc(mask);
             __syncwarp();
         }
-        if (gate && !__any_sync(0xffffffffu, reach)) w = 0;  // gated: no seed
+        // gated (no seed) unless the middle is too large to be gated
+        if (gate && (c.mlp_gate_max_tops == 0 || n_mt <= c.mlp_gate_max_tops) &&
+            !__any_sync(0xffffffffu, reach))
+            w = 0;
         if (lane == 0) {
             atomicAdd(&a.ev_filter[4 * ev + 2], n_mt);
             atomicAdd(&a.ev_filter[4 * ev + 3], n_mt - w);

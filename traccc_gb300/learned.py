@@ -67,6 +67,9 @@ class FilterModel:
     # per-event-size classes: [(max spacepoints, (thr bottom, thr top),
     # (band lo, band hi)), ...] ascending, or None
     classes: list = None
+    # middle gate: middles with more middle-top doublets are kept unscored
+    # (0: no limit); nearly every middle without a seed is small
+    gate_max_tops: int = 32
 
     def struct(self, threshold=None, band=None, prune=None) -> seeding.DoubletFilter:
         """The C struct, optionally with other thresholds / band / pruning
@@ -93,6 +96,7 @@ class FilterModel:
         b = self.band if band is None else band
         f.band[0] = float(b[0])
         f.band[1] = float(b[1])
+        f.gate_max_tops = int(self.gate_max_tops)
         if self.classes and threshold is None and band is None:
             f.n_size_classes = len(self.classes)
             for k, (mx, th_k, band_k) in enumerate(self.classes):
@@ -110,7 +114,7 @@ class FilterModel:
                  threshold=np.asarray(self.threshold, np.float32),
                  band=np.asarray(self.band, np.float32),
                  prune=np.asarray([int(self.prune_bottom), int(self.prune_top)], np.uint8),
-                 classes=cl)
+                 classes=cl, gate_max_tops=np.asarray(int(self.gate_max_tops), np.uint32))
 
     @classmethod
     def from_struct(cls, f: seeding.DoubletFilter) -> "FilterModel":
@@ -128,7 +132,7 @@ class FilterModel:
                    for k in range(f.n_size_classes)]
         return cls(params, norm, edges, (float(f.threshold[0]), float(f.threshold[1])),
                    (float(f.band[0]), float(f.band[1])), int(f.prune_bottom), int(f.prune_top),
-                   classes or None)
+                   classes or None, int(f.gate_max_tops))
 
     @classmethod
     def load(cls, path):
@@ -138,7 +142,8 @@ class FilterModel:
             return cls(z["params"].astype(np.float32), z["norm"].astype(np.float32),
                        z["edges"].astype(np.float32), tuple(float(v) for v in z["threshold"]),
                        tuple(float(v) for v in z["band"]), int(z["prune"][0]),
-                       int(z["prune"][1]), cl or None)
+                       int(z["prune"][1]), cl or None,
+                       int(z["gate_max_tops"]) if "gate_max_tops" in z.files else 0)
 
 
 def init_params(seed=0) -> np.ndarray:
@@ -400,10 +405,11 @@ def middle_scores(torch, rec, outs):
             n_mt.cpu().numpy())
 
 
-def gate_recall(ev, best, seeds, n_mt, n_events, thr):
+def gate_recall(ev, best, seeds, n_mt, n_events, thr, max_tops=0):
     """Exact per-event seed recall and pruned fraction of the middle gate at
-    threshold `thr` (the kept middles keep exactly their plain seeds)."""
-    kept = best >= thr
+    threshold `thr` (the kept middles keep exactly their plain seeds; middles
+    above max_tops middle-top doublets are kept unscored)."""
+    kept = (best >= thr) | ((n_mt > max_tops) if max_tops else False)
     tot = np.bincount(ev, weights=seeds, minlength=n_events)
     keep = np.bincount(ev, weights=seeds * kept, minlength=n_events)
     mt = np.bincount(ev, weights=n_mt, minlength=n_events)
@@ -425,18 +431,19 @@ def calibrate_gate(alg, model: FilterModel, events, target=0.995, margin=0.05, l
     outs, rec = run_dump(alg, sps, model)
     plain = seed_keys(outs)
     ev, best, seeds, n_mt = middle_scores(torch, rec, outs)
-    cand = np.unique(best[seeds > 0])
+    mx = int(model.gate_max_tops)
+    cand = np.unique(best[(seeds > 0) & ((n_mt <= mx) if mx else True)])
     lo, hi = 0, len(cand) - 1          # recall is non-increasing in the threshold
     chosen = -np.inf
     while lo <= hi:
         mid = (lo + hi) // 2
-        r, agg, _ = gate_recall(ev, best, seeds, n_mt, len(events), cand[mid])
+        r, agg, _ = gate_recall(ev, best, seeds, n_mt, len(events), cand[mid], mx)
         if agg >= target and r.min() >= min_event:
             chosen = float(cand[mid])
             lo = mid + 1
         else:
             hi = mid - 1
-    r, agg, frac = gate_recall(ev, best, seeds, n_mt, len(events), chosen)
+    r, agg, frac = gate_recall(ev, best, seeds, n_mt, len(events), chosen, mx)
     thr = (-np.inf, chosen)
     alg.set_filter(model.struct(threshold=thr, band=(0.0, 1.0)))
     louts = alg.run_batch(sps)

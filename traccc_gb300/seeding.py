@@ -134,7 +134,7 @@ class DoubletFilter(C.Structure):
                 ("prune_top", C.c_uint32), ("band", C.c_float * 2),
                 ("n_size_classes", C.c_uint32), ("size_class_max", C.c_uint32 * 8),
                 ("size_class_threshold", (C.c_float * 2) * 8),
-                ("size_class_band", (C.c_float * 2) * 8)]
+                ("size_class_band", (C.c_float * 2) * 8), ("gate_max_tops", C.c_uint32)]
 
 
 class _SpacepointBuffer(C.Structure):
