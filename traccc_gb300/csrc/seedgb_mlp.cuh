@@ -194,7 +194,7 @@ __device__ __forceinline__ void mlp_tile16_lean(const MlpFrag& f, const uint32_t
         h0[1] = h0[3] = f.b2[n0 * 8 + 2 * t + 1];
         h1[0] = h1[2] = f.b2[n1 * 8 + 2 * t];
         h1[1] = h1[3] = f.b2[n1 * 8 + 2 * t + 1];
-#pragma unroll
+#pragma unroll 1
         for (int k = 0; k < 2; ++k) {
             const uint2 b0 = f.w2[k][n0][lane], b1 = f.w2[k][n1][lane];
             mma_bf16(h0, a2[k], b0.x, b0.y);
@@ -208,7 +208,7 @@ __device__ __forceinline__ void mlp_tile16_lean(const MlpFrag& f, const uint32_t
         else { a3[1][0] = p0; a3[1][1] = p1; a3[1][2] = p2; a3[1][3] = p3; }
     }
     float o[4] = {t == 0 ? f.b3 : 0.f, 0.f, t == 0 ? f.b3 : 0.f, 0.f};
-#pragma unroll
+#pragma unroll 1
     for (int ks = 0; ks < 2; ++ks) {
         const uint2 b = f.w3[ks][lane];
         mma_bf16(o, a3[ks], b.x, b.y);
