@@ -720,6 +720,126 @@ seedgb_status seedgb_spacepoint_binning_noalloc(
     const seedgb_spacepoint_view* sps, uint32_t* bin_offsets, uint32_t* bin_sps,
     void* stream);
 
+/* ------------------------------------------------------------------------ */
+/* GBTS seeding (graph-based track seeding)                                  */
+/* ------------------------------------------------------------------------ */
+
+/* traccc::gbts_seedfinder_config (core/include/traccc/gbts_seeding/
+ * gbts_seeding_config.hpp:67-276): the per-kernel parameter structs
+ * flattened in declaration order, the config's scalars, then the bit layout
+ * of the measurements' surface barcode (volume = (link >> volume_shift) &
+ * (2^volume_bits - 1), surface index likewise; the defaults are detray's
+ * barcode layout, volume in bits 52-63 and surface index in bits 27-47). */
+typedef struct {
+    /* gbts_sort_nodes_params */
+    float tMin_slope, offset, tMax_min, tMax_correction, tMax_slope, maxTau;
+    int32_t useTauLUT;
+    float tau_lut_inv_bin;
+    uint32_t tauLutSize;
+    /* gbts_make_graph_edges_params */
+    float minDeltaRadius, min_z0, max_z0, maxOuterRadius, tau_roi, cut_zMinU, cut_zMaxU,
+        max_Kappa, low_Kappa_d0, high_Kappa_d0;
+    /* gbts_match_graph_edges_params */
+    float cut_dphi_max, cut_dcurv_max, cut_tau_ratio_max;
+    /* gbts_dphi_window_params */
+    float min_delta_phi, dphi_coeff, min_delta_phi_low_dr, dphi_coeff_low_dr,
+        low_dr_threshold;
+    /* gbts_count_spacepoints_by_layer_params */
+    float type1_max_width;
+    int32_t doTauCut;
+    /* gbts_fit_segments_params */
+    float sigmaMS, radLen, sigma_x, sigma_y, weight_x, weight_y, maxDChi2_x, maxDChi2_y,
+        add_hit, qual_scale, inv_max_curvature;
+    /* gbts_convert_seeds_params */
+    int32_t use_dropout;
+    float dropout_dcurv_m, force_dropout_max_curv_m, best_hit_frac, tight_bid_cot_threshold;
+    /* gbts_seedfinder_config scalars */
+    uint32_t n_phi_bins, max_num_neighbours, minLevel, max_edges_factor, edge_bidding_rounds;
+    /* surface barcode layout */
+    uint32_t volume_shift, volume_bits, index_shift, index_bits;
+} seedgb_gbts_config;
+
+/* One layer of gbts_layerInfo (gbts_seeding_config.hpp:24-44): type (0
+ * barrel, 1 / 2 end-caps), first eta bin and number of eta bins, minimum eta
+ * and eta bin width. */
+typedef struct {
+    int32_t type;
+    uint32_t eta_bin0, n_eta_bins;
+    float min_eta, eta_bin_width;
+} seedgb_gbts_layer;
+
+/* One (detray geometry id, layer) pair of the geometry-id binning. */
+typedef struct {
+    uint64_t barcode;
+    int32_t layer;
+} seedgb_gbts_geoid;
+
+/* The reference's defaults (gbts_seeding_config.hpp member initialisers). */
+void seedgb_gbts_config_default(seedgb_gbts_config* c);
+
+typedef struct seedgb_gbts seedgb_gbts;
+
+/* Replaces gbts_seedfinder_config::setLinkingScheme(binTables, layerInfo,
+ * geoIDBinning, minPt) (core/src/gbts_seeding/gbts_seeding_config.cpp:19-142)
+ * followed by the construction of traccc::cuda::gbts_seeding_algorithm(config,
+ * mr, copy, stream) (device/cuda/include/traccc/cuda/gbts_seeding/
+ * gbts_seeding_algorithm.hpp).  `bin_pairs` holds n_pairs (bin1, bin2) pairs,
+ * the linked layer-eta bins already unrolled; `tau_lut` (n_tau_lut floats,
+ * a multiple of 5) is used when config->useTauLUT is set, else may be NULL.
+ * The pT-dependent cuts of the config are scaled by 900 MeV / min_pt (MeV),
+ * as setLinkingScheme does.  SEEDGB_BAD_CONFIG where setLinkingScheme returns
+ * false, and for tables the kernels cannot index (a layer index outside the
+ * layer table, a bin pair outside the eta bins, a malformed tau table). */
+seedgb_status seedgb_gbts_create(const seedgb_gbts_config* config,
+                                 const seedgb_gbts_layer* layers, uint32_t n_layers,
+                                 const uint32_t* bin_pairs, uint32_t n_pairs,
+                                 const seedgb_gbts_geoid* geoids, uint32_t n_geoids,
+                                 float min_pt, const float* tau_lut, uint32_t n_tau_lut,
+                                 seedgb_gbts** out);
+seedgb_status seedgb_gbts_destroy(seedgb_gbts* h);
+
+/* The config after setLinkingScheme's scaling, and the sizes of the derived
+ * tables (eta bins, volume map entries, surface map entries). */
+seedgb_status seedgb_gbts_get_config(const seedgb_gbts* h, seedgb_gbts_config* config,
+                                     uint32_t* n_eta_bins, uint32_t* n_volumes,
+                                     uint32_t* n_surfaces);
+
+/* Replaces edm::seed_collection::buffer operator()(spacepoints, measurements)
+ * (device/common/include/traccc/gbts_seeding/device/gbts_seeding_algorithm.
+ * hpp:94-96).  surface_link / diameter: device measurement columns (n_meas
+ * entries) indexed by the spacepoints' measurement_index_1.  Seeds (bottom =
+ * innermost, top = outermost spacepoint, quality = the path's fit quality)
+ * are written in a canonical order: by seed proposal (path-store order), up
+ * to three per proposal in the reference's emission order; the reference's
+ * own order depends on its atomics.  Enqueued on `stream`; the call waits
+ * once for the device in the middle (to size the path store, as the
+ * reference reads its path counts back) and returns with the rest in flight.
+ * A seed buffer smaller than the result is filled to capacity and the status
+ * reports SEEDGB_CAPACITY_OVERFLOW. */
+seedgb_status seedgb_gbts_run(seedgb_gbts* h, const seedgb_spacepoint_view* sps,
+                              const uint64_t* surface_link, const float* diameter,
+                              uint32_t n_meas, seedgb_seed_buffer* out, void* stream);
+
+/* Synchronise `stream` and return the device status of the last run. */
+seedgb_status seedgb_gbts_last_status(seedgb_gbts* h, void* stream);
+
+/* Counters of the last run (synchronises the handle's last stream): nodes,
+ * edges created, edge connections, connected edges, terminus edges, path
+ * store entries below the terminus edges, seed proposals, proposals rejected
+ * by the bidding, seeds. */
+#define SEEDGB_GBTS_N_COUNTERS 9u
+seedgb_status seedgb_gbts_counters(seedgb_gbts* h, uint64_t* counters);
+
+/* The reference's GBTS configuration directory (examples/options/src/
+ * track_gbts_seeding.cpp:158-226): geoidBinning.txt, binTables.txt and
+ * layerInfo.txt.  Call with NULL arrays to get the counts, then with arrays
+ * of at least those sizes; bin_pairs gets 2 * n_pairs entries.  SEEDGB_
+ * INVALID_ARGUMENT when a file is missing or malformed. */
+seedgb_status seedgb_gbts_read_config_dir(const char* dir, seedgb_gbts_layer* layers,
+                                          uint32_t* n_layers, uint32_t* bin_pairs,
+                                          uint32_t* n_pairs, seedgb_gbts_geoid* geoids,
+                                          uint32_t* n_geoids);
+
 const char* seedgb_status_string(seedgb_status s);
 uint32_t seedgb_abi_version(void);
 

@@ -23,13 +23,14 @@ PHI_CR = 1
 
 def build(force: bool = False) -> str:
     """Compile the oracle with gcc (-O2 -ffp-contract=off) into oracle/_lib."""
-    src = os.path.join(_HERE, "seeding_oracle.c")
+    srcs = [os.path.join(_HERE, f) for f in ("seeding_oracle.c", "gbts_oracle.c")]
+    deps = srcs + [os.path.join(_HERE, f) for f in ("seeding_oracle.h", "gbts_oracle.h")]
     if (not force and os.path.exists(_LIB_PATH)
-            and os.path.getmtime(_LIB_PATH) >= os.path.getmtime(src)):
+            and all(os.path.getmtime(_LIB_PATH) >= os.path.getmtime(d) for d in deps)):
         return _LIB_PATH
     os.makedirs(os.path.dirname(_LIB_PATH), exist_ok=True)
     cmd = ["gcc", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fPIC",
-           "-std=c11", "-D_GNU_SOURCE", "-shared", "-o", _LIB_PATH, src, "-lm"]
+           "-std=c11", "-D_GNU_SOURCE", "-shared", "-o", _LIB_PATH] + srcs + ["-lm"]
     subprocess.run(cmd, check=True)
     return _LIB_PATH
 
@@ -418,3 +419,129 @@ def track_params(ev, seeds, bfield, tp=None):
     if rc:
         raise RuntimeError(f"or_track_params failed {rc}")
     return out[: len(seeds)].copy()
+
+
+# ---------------------------------------------------------------------------
+# GBTS seeding (gbts_oracle.c)
+# ---------------------------------------------------------------------------
+_GBTS_FLOATS_1 = ("tMin_slope", "offset", "tMax_min", "tMax_correction", "tMax_slope", "maxTau")
+_GBTS_FLOATS_2 = ("minDeltaRadius", "min_z0", "max_z0", "maxOuterRadius", "tau_roi",
+                  "cut_zMinU", "cut_zMaxU", "max_Kappa", "low_Kappa_d0", "high_Kappa_d0",
+                  "cut_dphi_max", "cut_dcurv_max", "cut_tau_ratio_max", "min_delta_phi",
+                  "dphi_coeff", "min_delta_phi_low_dr", "dphi_coeff_low_dr",
+                  "low_dr_threshold", "type1_max_width")
+_GBTS_FLOATS_3 = ("sigmaMS", "radLen", "sigma_x", "sigma_y", "weight_x", "weight_y",
+                  "maxDChi2_x", "maxDChi2_y", "add_hit", "qual_scale", "inv_max_curvature")
+_GBTS_FLOATS_4 = ("dropout_dcurv_m", "force_dropout_max_curv_m", "best_hit_frac",
+                  "tight_bid_cot_threshold")
+_GBTS_UINTS = ("n_phi_bins", "max_num_neighbours", "minLevel", "max_edges_factor",
+               "edge_bidding_rounds", "volume_shift", "volume_bits", "index_shift",
+               "index_bits")
+
+
+class GbtsConfig(C.Structure):
+    """or_gbts_config: gbts_seedfinder_config's parameters, flattened."""
+    _fields_ = ([(n, C.c_float) for n in _GBTS_FLOATS_1]
+                + [("useTauLUT", C.c_int32), ("tau_lut_inv_bin", C.c_float),
+                   ("tauLutSize", C.c_uint32)]
+                + [(n, C.c_float) for n in _GBTS_FLOATS_2]
+                + [("doTauCut", C.c_int32)]
+                + [(n, C.c_float) for n in _GBTS_FLOATS_3]
+                + [("use_dropout", C.c_int32)]
+                + [(n, C.c_float) for n in _GBTS_FLOATS_4]
+                + [(n, C.c_uint32) for n in _GBTS_UINTS])
+
+
+class GbtsTables(C.Structure):
+    _fields_ = [("n_layers", C.c_uint32), ("layer_type", C.c_void_p),
+                ("eta_bin0", C.c_void_p), ("n_eta", C.c_void_p), ("min_eta", C.c_void_p),
+                ("eta_width", C.c_void_p), ("n_pairs", C.c_uint32), ("pairs", C.c_void_p),
+                ("n_volumes", C.c_uint32), ("volume_map", C.c_void_p),
+                ("n_surfaces", C.c_uint32), ("surface_map", C.c_void_p),
+                ("n_tau_lut", C.c_uint32), ("tau_lut", C.c_void_p),
+                ("n_eta_bins", C.c_uint32)]
+
+
+GBTS_COUNTERS = ("nodes", "edges", "connections", "connected_edges", "terminus", "paths",
+                 "props", "rejected", "seeds")
+
+
+def _gbts_lib():
+    L = lib()
+    if not hasattr(L, "_gbts_ready"):
+        P = C.POINTER
+        L.or_gbts_config_default.argtypes = [P(GbtsConfig)]
+        L.or_gbts_linking.argtypes = [P(GbtsConfig), C.c_float, C.c_void_p, C.c_void_p,
+                                      C.c_uint32, C.c_void_p, C.c_uint32, P(C.c_uint32),
+                                      C.c_void_p, C.c_uint32, P(C.c_uint32)]
+        L.or_gbts_linking.restype = C.c_int
+        L.or_gbts_run.argtypes = [P(GbtsConfig), P(GbtsTables), C.c_uint32, C.c_void_p,
+                                  C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p,
+                                  C.c_uint64, P(C.c_uint64), C.c_void_p]
+        L.or_gbts_run.restype = C.c_int
+        L._gbts_ready = True
+    return L
+
+
+def gbts_config_default():
+    c = GbtsConfig()
+    _gbts_lib().or_gbts_config_default(C.byref(c))
+    return c
+
+
+def gbts_linking(cfg, geoid, min_pt=900.0):
+    """setLinkingScheme on a copy of `cfg`: (scaled config, volume map,
+    surface map [n, 2])."""
+    L = _gbts_lib()
+    c = GbtsConfig()
+    C.memmove(C.byref(c), C.byref(cfg), C.sizeof(GbtsConfig))
+    ids = np.ascontiguousarray(geoid["barcode"], np.uint64)
+    lay = np.ascontiguousarray(geoid["layer"], np.int16)
+    vcap = 2 * (1 << int(cfg.volume_bits)) if cfg.volume_bits <= 15 else 1 << 16
+    vmap = np.zeros(vcap, np.int16)
+    smap = np.zeros(2 * (len(ids) + 1), np.uint32)
+    nv, ns = C.c_uint32(0), C.c_uint32(0)
+    rc = L.or_gbts_linking(C.byref(c), min_pt, ids.ctypes.data, lay.ctypes.data, len(ids),
+                           vmap.ctypes.data, vcap, C.byref(nv), smap.ctypes.data,
+                           len(ids) + 1, C.byref(ns))
+    if rc:
+        raise RuntimeError("or_gbts_linking rejected the geometry binning")
+    return c, vmap[: nv.value].copy(), smap[: 2 * ns.value].reshape(-1, 2).copy()
+
+
+def gbts(ev, surface_link, diameter, layers, pairs, geoid, cfg=None, min_pt=900.0,
+         tau_lut=None):
+    """GBTS seeding of one event: (seeds in SEED_DTYPE, counters dict)."""
+    L = _gbts_lib()
+    if cfg is None:
+        cfg = gbts_config_default()
+    c, vmap, smap = gbts_linking(cfg, geoid, min_pt)
+    ltype = np.ascontiguousarray(layers["type"], np.int8)
+    bin0 = np.ascontiguousarray(layers["eta_bin0"], np.uint32)
+    neta = np.ascontiguousarray(layers["n_eta_bins"], np.uint32)
+    meta = np.ascontiguousarray(layers["min_eta"], np.float32)
+    weta = np.ascontiguousarray(layers["eta_bin_width"], np.float32)
+    prs = np.ascontiguousarray(pairs, np.uint32).reshape(-1)
+    lut = np.ascontiguousarray(tau_lut if tau_lut is not None else np.zeros(1), np.float32)
+    smap_flat = np.ascontiguousarray(smap.reshape(-1), np.uint32)
+    t = GbtsTables(len(ltype), ltype.ctypes.data, bin0.ctypes.data, neta.ctypes.data,
+                   meta.ctypes.data, weta.ctypes.data, len(prs) // 2, prs.ctypes.data,
+                   len(vmap), vmap.ctypes.data, len(smap), smap_flat.ctypes.data,
+                   0 if tau_lut is None else len(lut), lut.ctypes.data,
+                   int((bin0 + neta).max()) if len(bin0) else 0)
+    g = np.ascontiguousarray(ev["global"], np.float32)
+    mi = np.ascontiguousarray(ev["measurement_index_1"], np.uint32)
+    link = np.ascontiguousarray(surface_link, np.uint64)
+    dia = np.ascontiguousarray(diameter, np.float32)
+    cap = max(64, 3 * len(g))
+    out = np.zeros(cap, SEED_DTYPE)
+    n = C.c_uint64(0)
+    ctr = np.zeros(len(GBTS_COUNTERS), np.uint64)
+    rc = L.or_gbts_run(C.byref(c), C.byref(t), len(g), g.ctypes.data, mi.ctypes.data,
+                       len(link), link.ctypes.data, dia.ctypes.data, out.ctypes.data, cap,
+                       C.byref(n), ctr.ctypes.data)
+    if rc == 1:
+        raise RuntimeError("or_gbts_run: seed capacity exceeded")
+    if rc not in (0, 2):
+        raise RuntimeError(f"or_gbts_run failed {rc}")
+    return out[: n.value].copy(), dict(zip(GBTS_COUNTERS, (int(v) for v in ctr)))

@@ -1,0 +1,135 @@
+"""GBTS seeding on the GPU against the oracle: identical seeds (indices and
+quality bits, in the same canonical order) and identical counters, on clean
+and dense events, with the edge budget binding and not, with end-cap layer
+types and the tau lookup table, at another pT threshold; plus empty events,
+events with no usable spacepoint, bad measurement indices and a seed
+buffer too small."""
+import numpy as np
+import pytest
+
+import oracle as O
+from traccc_gb300 import gbts, synth
+
+pytestmark = pytest.mark.gpu
+
+
+def _run(ev, link, dia, layers, pairs, geoid, cfg=None, min_pt=900.0, tau_lut=None, cap=None):
+    import torch
+
+    from traccc_gb300 import seeding
+    alg = gbts.GbtsSeedingAlgorithm(cfg, layers, pairs, geoid, min_pt=min_pt, tau_lut=tau_lut)
+    sps = seeding.SpacepointCollection.from_numpy(ev)
+    meas = seeding.MeasurementCollection.from_numpy(dict(surface_link=link, diameter=dia))
+    out = seeding.SeedBuffer(cap if cap is not None else alg.max_seeds(len(ev["global"])))
+    alg(sps, meas, out)
+    torch.cuda.synchronize()
+    return alg, out
+
+
+def _compare(ev, link, dia, layers, pairs, geoid, cfg=None, min_pt=900.0, tau_lut=None):
+    alg, out = _run(ev, link, dia, layers, pairs, geoid, cfg, min_pt, tau_lut)
+    assert alg.last_status() == 0
+    ref, rctr = O.gbts(ev, link, dia, layers, pairs, geoid,
+                       cfg=None if cfg is None else _oracle_cfg(cfg), min_pt=min_pt,
+                       tau_lut=tau_lut)
+    got = out.to_numpy()
+    assert alg.counters() == rctr
+    assert len(got) == len(ref)
+    for k in ("bottom", "middle", "top"):
+        assert np.array_equal(got[k], ref[k]), k
+    assert np.array_equal(got["quality"].view(np.uint32), ref["quality"].view(np.uint32))
+    return got, rctr
+
+
+def _oracle_cfg(cfg):
+    import ctypes as C
+    o = O.GbtsConfig()
+    C.memmove(C.byref(o), C.byref(cfg), C.sizeof(o))
+    return o
+
+
+@pytest.mark.parametrize("name,seed", [("trk100", 0), ("trk1000", 0), ("trk1000", 5)])
+def test_gbts_matches_oracle(name, seed):
+    layers, pairs, geoid = synth.gbts_geometry()
+    ev = synth.workload_event(name, seed)
+    link, dia = synth.gbts_measurements(ev, seed)
+    got, ctr = _compare(ev, link, dia, layers, pairs, geoid)
+    assert ctr["seeds"] > 0
+
+
+def test_gbts_dense_event_full_and_capped_edge_budget():
+    """100k spacepoints: with max_edges_factor 40 the graph is complete; with
+    the reference default (10) the edge budget binds and the first edges in
+    the canonical order are kept."""
+    layers, pairs, geoid = synth.gbts_geometry()
+    ev = synth.workload_event("pileup9k", 0)
+    link, dia = synth.gbts_measurements(ev)
+    for factor in (40, 10):
+        cfg = gbts.config_default()
+        cfg.max_edges_factor = factor
+        got, ctr = _compare(ev, link, dia, layers, pairs, geoid, cfg=cfg)
+        if factor == 10:
+            assert ctr["edges"] > 10 * ctr["nodes"]
+        assert ctr["seeds"] > 0
+
+
+def test_gbts_lower_pt_threshold():
+    layers, pairs, geoid = synth.gbts_geometry()
+    ev = synth.workload_event("trk1000", 2)
+    link, dia = synth.gbts_measurements(ev, 2)
+    _compare(ev, link, dia, layers, pairs, geoid, min_pt=500.0)
+
+
+def test_gbts_endcap_types_and_tau_table():
+    """Layers of type 1 / 2 (wide clusters on type 1 dropped, diameters
+    replaced by -type under doTauCut), then the tau window from a lookup
+    table instead of the linear formula."""
+    layers, pairs, geoid = synth.gbts_geometry()
+    layers = layers.copy()
+    layers["type"][7] = 1
+    layers["type"][9] = 2
+    ev = synth.workload_event("trk1000", 4)
+    link, dia = synth.gbts_measurements(ev, 4)
+    _compare(ev, link, dia, layers, pairs, geoid)
+    cfg = gbts.config_default()
+    cfg.useTauLUT = 1
+    cfg.tau_lut_inv_bin = 20.0
+    n_bins = 16
+    lut = np.zeros(5 * n_bins, np.float32)
+    for b in range(n_bins):
+        w = (b + 1) / 20.0
+        lut[5 * b:5 * b + 5] = (w, max(0.0, 6.5 * (w - 0.25)), 1.8 + 6.5 * w, -1.0, -1.0)
+    cfg.tauLutSize = len(lut) - 5
+    _compare(ev, link, dia, layers, pairs, geoid, cfg=cfg, tau_lut=lut)
+
+
+def test_gbts_empty_and_unmapped_events():
+    layers, pairs, geoid = synth.gbts_geometry()
+    ev = synth.workload_event("trk100", 1)
+    link, dia = synth.gbts_measurements(ev)
+    # every barcode in a volume the binning does not know
+    bad = (np.uint64(4000) << np.uint64(52)) | (link & np.uint64((1 << 52) - 1))
+    alg, out = _run(ev, bad, dia, layers, pairs, geoid)
+    assert alg.last_status() == 0 and len(out.to_numpy()) == 0
+    assert alg.counters()["nodes"] == 0
+    z = {k: v[:0] for k, v in ev.items()}
+    alg, out = _run(z, link[:0], dia[:0], layers, pairs, geoid)
+    assert alg.last_status() == 0 and len(out.to_numpy()) == 0
+
+
+def test_gbts_bad_measurement_index_and_small_buffer():
+    layers, pairs, geoid = synth.gbts_geometry()
+    ev = synth.workload_event("trk100", 2)
+    link, dia = synth.gbts_measurements(ev, 2)
+    ref, _ = O.gbts(ev, link, dia, layers, pairs, geoid)
+    alg, out = _run(ev, link, dia, layers, pairs, geoid, cap=10)
+    assert alg.last_status() == 4  # SEEDGB_CAPACITY_OVERFLOW
+    got = out.to_numpy()
+    assert len(got) == 10
+    assert np.array_equal(got["top"], ref["top"][:10])
+    ev2 = dict(ev)
+    mi = ev["measurement_index_1"].copy()
+    mi[5] = 10 ** 6
+    ev2["measurement_index_1"] = mi
+    alg, out = _run(ev2, link, dia, layers, pairs, geoid)
+    assert alg.last_status() == 6  # SEEDGB_INVALID_ARGUMENT

@@ -20,7 +20,7 @@ REPO = os.path.dirname(HERE)
 INCLUDE = os.path.join(REPO, "include")
 
 CUDA_SOURCES = ["seedgb_kernels.cu", "seedgb_api.cu", "seedgb_noalloc.cu", "seedgb_learned.cu",
-                "seedgb_formation.cu", "seedgb_handoff.cu", "seedgb_host.cu"]
+                "seedgb_formation.cu", "seedgb_handoff.cu", "seedgb_host.cu", "seedgb_gbts.cu"]
 HOST_SOURCES = ["seedgb_config.cpp", "seedgb_io.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

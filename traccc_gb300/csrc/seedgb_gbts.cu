@@ -1,0 +1,1659 @@
+// GBTS seeding (graph-based track seeding) on the GB300.
+//
+// The reference's GBTS chain (device/common/src/gbts_seeding/
+// gbts_seeding_algorithm.cpp, kernels in device/common/include/traccc/
+// gbts_seeding/device/impl) builds a graph of spacepoint pairs (edges) between
+// linked layer-eta bins, links edges that continue each other, finds the
+// longest chains with a cellular automaton, fits every chain with a Kalman
+// filter and resolves shared edges and hits by bidding.  Its results depend on
+// the order in which its atomics land in several places; this library
+// computes the same chain in one fixed order, so results are reproducible and
+// equal to the CPU oracle bit for bit:
+//   - nodes of one (eta, phi) cell in ascending spacepoint index;
+//   - edges by (work item, outer node, inner node), each work item a bin pair
+//     with a bin-1 chunk of at most 128 nodes, 128 threads per item taking the
+//     outer nodes t, t + 128, ... with the reference's sliding-window state;
+//   - every node's outgoing edges in ascending edge index;
+//   - connected edges numbered in ascending edge index (a scan, not atomics);
+//   - terminus edges in ascending connected-edge index, the path store as a
+//     depth-first pre-order walk below each terminus edge;
+//   - seed proposals in path-store order, seeds by proposal.
+// Ordered outputs come from count / scan / write passes; the bidding's
+// outcome does not depend on the order of its atomics once each round's
+// bidders are fixed before it starts (the reference decides that inside the
+// racing kernel).
+//
+// Layout in HBM: one arena sized from the event's spacepoint count (nodes,
+// edges up to max_edges_factor x nodes, the graph rows, the automaton's
+// levels) and one sized from the path count, which the host reads back once
+// in the middle of the run (the reference reads its counters back six times).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <string>
+#include <vector>
+
+#include "seedgb.h"
+
+namespace {
+
+constexpr uint32_t kMaxCca = 15u;       // gbts_consts::max_cca_iter
+constexpr uint32_t kNodeBuffer = 128u;  // gbts_consts::node_buffer_length
+constexpr int kEdgeThreads = 128;       // threads of one edge work item
+constexpr int kThreads = 256;
+constexpr int kScanThreads = 1024;
+constexpr uint32_t kScanTile = 4u * kScanThreads;
+constexpr float kPi = 3.14159265358979323846f;
+constexpr float kTwoPi = 2.0f * kPi;
+constexpr uint32_t kInvalid = 0xFFFFFFFFu;
+constexpr int32_t kPathCountLimit = 1 << 30;
+
+// device-resident sizes and status of one run
+enum Size : uint32_t {
+    S_NODES = 0,
+    S_ITEMS,
+    S_EDGES_MADE,
+    S_CONN,
+    S_CONNECTED,
+    S_TERMINUS,
+    S_PATHS,
+    S_PROPS,
+    S_REJECTED,
+    S_SEEDS,
+    S_STATUS,
+    S_BAD_INPUT,
+    S_TMP,
+    S_COUNT
+};
+
+struct Tables {
+    seedgb_gbts_config c;
+    uint32_t n_layers, n_eta, n_pairs, n_volumes, n_surfaces, n_tau_lut;
+    const int8_t* layer_type;
+    const uint32_t* eta_bin0;
+    const uint32_t* n_eta_l;
+    const float* min_eta;
+    const float* eta_width;
+    const uint32_t* pairs;
+    const int16_t* vmap;
+    const uint32_t* smap;
+    const float* tau_lut;
+};
+
+// work buffers of one run
+struct Work {
+    // spacepoints
+    float4* red;
+    float* sp_phi;
+    uint32_t* sp_cell;
+    // cells and nodes
+    uint32_t *cell_cnt, *cell_off, *cell_cur;
+    uint32_t* node_sp;
+    float4* node_p;
+    float* node_phi;
+    uint32_t* view;
+    float* rads;
+    // work items
+    uint32_t *item_cnt, *item_off;
+    uint4* items;
+    float* item_dphi;
+    uint32_t *item_ecnt, *item_ebase;
+    // edges
+    uint32_t *e_in, *e_out;
+    float4* e_p;
+    uint32_t *out_cnt, *lstart, *lcur, *links;
+    uint8_t* nnei;
+    uint32_t *nei, *kept, *kbase;
+    // graph and automaton
+    uint32_t* graph;
+    uint8_t* levels;
+    int8_t* active;
+    int32_t* opx;
+    int16_t* opy;
+    uint32_t *tflag, *tidx, *tpaths, *pbase;
+    unsigned long long *ebid, *hbid;
+    uint32_t* tile;
+    // path-sized buffers
+    int2* store;
+    uint32_t *term_edge, *term_pos;
+    uint32_t *fflag, *fidx;
+    int32_t* fqual;
+    int2* props;
+    int8_t* ambi;
+    uint8_t* bidder;
+    uint32_t *ecount, *eoff;
+    uint4* seeds3;
+    uint32_t* tile_b;
+    // sizes
+    uint32_t* sz;
+    uint64_t ecap;  // edge capacity (max_edges_factor x spacepoints)
+    uint64_t pcap;  // path store capacity
+};
+
+__device__ __forceinline__ void set_status(uint32_t* sz, uint32_t s) { atomicMax(&sz[S_STATUS], s); }
+
+__device__ __forceinline__ uint64_t field(uint64_t v, uint32_t shift, uint32_t bits) {
+    const uint64_t m = bits >= 64 ? ~0ull : ((1ull << bits) - 1ull);
+    return shift >= 64 ? 0 : ((v >> shift) & m);
+}
+
+// std::min / std::max as the reference calls them (comparison based)
+__device__ __forceinline__ float smin(float a, float b) { return (b < a) ? b : a; }
+__device__ __forceinline__ float smax(float a, float b) { return (a < b) ? b : a; }
+
+// correctly rounded float atan2 / log: the double-precision result rounded
+__device__ __forceinline__ float cr_atan2f(float y, float x) {
+    return static_cast<float>(atan2(static_cast<double>(y), static_cast<double>(x)));
+}
+__device__ __forceinline__ float cr_logf(float x) {
+    return static_cast<float>(log(static_cast<double>(x)));
+}
+
+// traccc::detail::wrap_phi (core/include/traccc/utils/trigonometric_helpers.hpp:18-38)
+__device__ __forceinline__ float wrap_phi(float phi) {
+    const float diff = phi - (-kPi);
+    return ((0 <= diff) && (diff < kTwoPi)) ? phi : (phi - kTwoPi * floorf(diff / kTwoPi));
+}
+
+__device__ __forceinline__ uint32_t load_n(const uint32_t* n_dev, uint32_t n_host, uint32_t add) {
+    return n_dev ? *n_dev + add : n_host;
+}
+
+// ---------------------------------------------------------------------------
+// Exclusive scan of n values (n on the host or in device memory): out[i] =
+// sum of in[0, i), out[n] = total, *total_dst = total.  Three launches over a
+// grid sized for the capacity; blocks past n exit.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* total) {
+    __shared__ uint32_t ws[32];
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t incl = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t x = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= static_cast<uint32_t>(o)) incl += x;
+    }
+    if (lane == 31) ws[warp] = incl;
+    __syncthreads();
+    const uint32_t nw = blockDim.x >> 5;
+    if (warp == 0) {
+        uint32_t s = lane < nw ? ws[lane] : 0u;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t x = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= static_cast<uint32_t>(o)) s += x;
+        }
+        if (lane < nw) ws[lane] = s;
+    }
+    __syncthreads();
+    const uint32_t before = warp ? ws[warp - 1] : 0u;
+    *total = ws[nw - 1];
+    __syncthreads();
+    return before + incl - v;
+}
+
+__global__ void __launch_bounds__(kScanThreads)
+k_scan_tile(const uint32_t* in, uint32_t* out, const uint32_t* n_dev, uint32_t n_host,
+            uint32_t add, uint32_t* tile) {
+    const uint32_t n = load_n(n_dev, n_host, add);
+    const uint32_t base = blockIdx.x * kScanTile;
+    if (base >= n) {
+        if (threadIdx.x == 0) tile[blockIdx.x] = 0;
+        return;
+    }
+    uint32_t v[4];
+    uint32_t s = 0;
+    for (int j = 0; j < 4; ++j) {
+        const uint32_t i = base + 4u * threadIdx.x + j;
+        v[j] = i < n ? in[i] : 0u;
+        s += v[j];
+    }
+    uint32_t total;
+    uint32_t run = block_exclusive_scan(s, &total);
+    for (int j = 0; j < 4; ++j) {
+        const uint32_t i = base + 4u * threadIdx.x + j;
+        if (i < n) out[i] = run;
+        run += v[j];
+    }
+    if (threadIdx.x == 0) tile[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(kScanThreads)
+k_scan_sums(uint32_t* tile, uint32_t n_tiles, uint32_t* tile_total) {
+    __shared__ uint32_t carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (uint32_t b = 0; b < n_tiles; b += blockDim.x) {
+        const uint32_t i = b + threadIdx.x;
+        const uint32_t v = i < n_tiles ? tile[i] : 0u;
+        uint32_t tot;
+        const uint32_t ex = block_exclusive_scan(v, &tot);
+        if (i < n_tiles) tile[i] = carry + ex;
+        __syncthreads();
+        if (threadIdx.x == 0) carry += tot;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *tile_total = carry;
+}
+
+__global__ void __launch_bounds__(kScanThreads)
+k_scan_add(uint32_t* out, const uint32_t* n_dev, uint32_t n_host, uint32_t add,
+           const uint32_t* tile, const uint32_t* tile_total, uint32_t* total_dst) {
+    const uint32_t n = load_n(n_dev, n_host, add);
+    const uint32_t base = blockIdx.x * kScanTile;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        out[n] = *tile_total;
+        if (total_dst) *total_dst = *tile_total;
+    }
+    if (base >= n) return;
+    const uint32_t off = tile[blockIdx.x];
+    for (int j = 0; j < 4; ++j) {
+        const uint32_t i = base + 4u * threadIdx.x + j;
+        if (i < n) out[i] += off;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Nodes: gbts_count_spacepoints_by_layer, gbts_bin_spacepoints,
+// gbts_sort_nodes, gbts_find_minmax_radius
+// ---------------------------------------------------------------------------
+
+// layer, eta bin, phi bin of every spacepoint
+// (gbts_count_spacepoints_by_layer.ipp:32-113, gbts_bin_spacepoints.ipp:27-107)
+__global__ void __launch_bounds__(kThreads)
+k_classify(Tables T, seedgb_spacepoint_view sps, const uint64_t* link, const float* diam,
+           uint32_t n_meas, Work w) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= sps.size) return;
+    const seedgb_gbts_config& c = T.c;
+    const float x = sps.global[3 * i], y = sps.global[3 * i + 1], z = sps.global[3 * i + 2];
+    w.red[i] = make_float4(x, y, z, static_cast<float>(-CHAR_MAX - 1));
+    w.sp_cell[i] = kInvalid;
+    const uint32_t m = sps.measurement_index_1[i];
+    if (m >= n_meas) {
+        atomicAdd(&w.sz[S_BAD_INPUT], 1u);
+        return;
+    }
+    const uint64_t lk = link[m];
+    const uint32_t volume = static_cast<uint32_t>(field(lk, c.volume_shift, c.volume_bits));
+    const int16_t begin_or_bin = (volume < T.n_volumes) ? T.vmap[volume] : SHRT_MAX;
+    if (begin_or_bin == SHRT_MAX) return;
+    uint32_t layer = 0u;
+    if (begin_or_bin < 0) {
+        const uint32_t sidx = static_cast<uint32_t>(field(lk, c.index_shift, c.index_bits));
+        for (uint32_t s = static_cast<uint32_t>(-1 * (begin_or_bin + 1)); s < T.n_surfaces; s++) {
+            if (T.smap[2 * s] == sidx) {
+                layer = T.smap[2 * s + 1];
+                break;
+            }
+        }
+    } else {
+        layer = static_cast<uint32_t>(begin_or_bin);
+    }
+    if (layer >= T.n_layers) return;
+    float d = diam[m];
+    const int type = static_cast<int>(T.layer_type[layer]);
+    if (type == 1 && d > c.type1_max_width) return;
+    d = (c.doTauCut && type != 0) ? static_cast<float>(-1 * type) : d;
+    w.red[i].w = d;
+    const uint32_t bin0 = T.eta_bin0[layer];
+    const uint32_t nb = T.n_eta_l[layer];
+    uint32_t eta_index;
+    if (nb == 1u) {
+        eta_index = bin0;
+    } else {
+        const float r = sqrtf(x * x + y * y);
+        const float t1 = z / r;
+        const float eta = -cr_logf(sqrtf(1.0f + t1 * t1) - t1);
+        const uint32_t bi = static_cast<uint32_t>(
+            smax(0.0f, smin((eta - T.min_eta[layer]) / T.eta_width[layer],
+                            static_cast<float>(nb - 1u))));
+        eta_index = bin0 + bi;
+    }
+    const float inv_slice = 1.0f / (kTwoPi / static_cast<float>(c.n_phi_bins));
+    const float phi = cr_atan2f(y, x);
+    uint32_t pb = static_cast<uint32_t>((phi + kPi) * inv_slice);
+    if (pb >= c.n_phi_bins) pb -= c.n_phi_bins;
+    const uint32_t cell = pb + c.n_phi_bins * eta_index;
+    w.sp_phi[i] = phi;
+    w.sp_cell[i] = cell;
+    atomicAdd(&w.cell_cnt[cell], 1u);
+}
+
+__global__ void __launch_bounds__(kThreads) k_scatter(uint32_t n_sp, Work w) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_sp) return;
+    const uint32_t cell = w.sp_cell[i];
+    if (cell == kInvalid) return;
+    w.node_sp[w.cell_off[cell] + atomicAdd(&w.cell_cur[cell], 1u)] = i;
+}
+
+// the nodes of a cell in ascending spacepoint index (insertion sort per cell)
+__global__ void __launch_bounds__(kThreads) k_sort_cells(uint32_t n_cells, Work w) {
+    const uint32_t cidx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (cidx >= n_cells) return;
+    const uint32_t b = w.cell_off[cidx], e = w.cell_off[cidx + 1];
+    for (uint32_t i = b + 1; i < e; ++i) {
+        const uint32_t v = w.node_sp[i];
+        uint32_t j = i;
+        while (j > b && w.node_sp[j - 1] > v) {
+            w.node_sp[j] = w.node_sp[j - 1];
+            --j;
+        }
+        w.node_sp[j] = v;
+    }
+}
+
+// gbts_sort_nodes.ipp:24-101: (tau_min, tau_max, r, z) and phi of each node
+__global__ void __launch_bounds__(kThreads) k_node_params(Tables T, Work w) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= w.sz[S_NODES]) return;
+    const seedgb_gbts_config& ap = T.c;
+    const uint32_t s = w.node_sp[k];
+    const float4 sp = w.red[s];
+    const float r = sqrtf(sp.x * sp.x + sp.y * sp.y);
+    float min_tau = 0.0f;
+    float max_tau = ap.maxTau;
+    if (sp.w > 0) {
+        if (ap.useTauLUT) {
+            const int tau_bin = 5 * static_cast<int>(floorf(ap.tau_lut_inv_bin * sp.w) - 1.0f);
+            if (tau_bin > -1 && tau_bin < static_cast<int>(ap.tauLutSize)) {
+                min_tau = T.tau_lut[static_cast<uint32_t>(tau_bin) + 1u];
+                max_tau = T.tau_lut[static_cast<uint32_t>(tau_bin) + 2u];
+            }
+            if (max_tau < 0.0f) max_tau = ap.maxTau;
+            if (min_tau < 0.0f) min_tau = 0.0f;
+        } else {
+            min_tau = ap.tMin_slope * (sp.w - ap.offset);
+            max_tau = ap.tMax_min + ap.tMax_correction / (sp.w + ap.offset) +
+                      ap.tMax_slope * (sp.w - ap.offset);
+        }
+    }
+    w.node_p[k] = make_float4(min_tau, max_tau, r, sp.z);
+    w.node_phi[k] = w.sp_phi[s];
+}
+
+// node ranges of the eta bins and their radius range
+// (gbts_find_minmax_radius.ipp:21-54); one warp per eta bin
+__global__ void __launch_bounds__(kThreads) k_eta_bins(uint32_t n_eta, uint32_t n_phi, Work w) {
+    const uint32_t e = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t lane = threadIdx.x & 31;
+    if (e >= n_eta) return;
+    const uint32_t b = w.cell_off[e * n_phi], en = w.cell_off[(e + 1) * n_phi];
+    float mn = 1e8f, mx = -1e8f;
+    for (uint32_t k = b + lane; k < en; k += 32) {
+        const float r = w.node_p[k].z;
+        mx = fmaxf(r, mx);
+        mn = fminf(r, mn);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+    }
+    if (lane == 0) {
+        w.view[2 * e] = b;
+        w.view[2 * e + 1] = en;
+        w.rads[2 * e] = mn;
+        w.rads[2 * e + 1] = mx;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Work items (gbts_seeding_algorithm.cpp:215-283): bin pairs with their phi
+// window, bin 1 split into chunks of 128 nodes
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ bool pair_window(const Tables& T, const Work& w, uint32_t p,
+                                            uint32_t& chunks, float& dphi) {
+    const uint32_t bin1 = T.pairs[2 * p], bin2 = T.pairs[2 * p + 1];
+    const uint32_t b1 = w.view[2 * bin1], e1 = w.view[2 * bin1 + 1];
+    chunks = 0;
+    if (b1 == e1 || w.view[2 * bin2] == w.view[2 * bin2 + 1]) return false;
+    const float rb1 = w.rads[2 * bin1];
+    const float rb2 = w.rads[2 * bin2 + 1];
+    const float maxDeltaR = fabsf(rb2 - rb1);
+    const seedgb_gbts_config& c = T.c;
+    dphi = c.min_delta_phi + c.dphi_coeff * maxDeltaR;
+    if (maxDeltaR < c.low_dr_threshold) dphi = c.min_delta_phi_low_dr + c.dphi_coeff_low_dr * maxDeltaR;
+    chunks = (e1 - b1 + kNodeBuffer - 1u) / kNodeBuffer;
+    return true;
+}
+
+__global__ void __launch_bounds__(kThreads) k_items_count(Tables T, Work w) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= T.n_pairs) return;
+    uint32_t chunks;
+    float dphi;
+    pair_window(T, w, p, chunks, dphi);
+    w.item_cnt[p] = chunks;
+}
+
+__global__ void __launch_bounds__(kThreads) k_items_fill(Tables T, Work w) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= T.n_pairs) return;
+    uint32_t chunks;
+    float dphi;
+    if (!pair_window(T, w, p, chunks, dphi)) return;
+    const uint32_t bin1 = T.pairs[2 * p], bin2 = T.pairs[2 * p + 1];
+    const uint32_t b1 = w.view[2 * bin1], e1 = w.view[2 * bin1 + 1];
+    const uint32_t o = w.item_off[p];
+    for (uint32_t j = 0; j < chunks; ++j) {
+        const uint32_t b = b1 + j * kNodeBuffer;
+        const uint32_t e = (e1 - b > kNodeBuffer) ? b + kNodeBuffer : e1;
+        w.items[o + j] = make_uint4(b, e, w.view[2 * bin2], w.view[2 * bin2 + 1]);
+        w.item_dphi[o + j] = dphi;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Edges (gbts_make_graph_edges.ipp:31-239)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ bool edge_test(float4 np1, float4 np2, float phi1, float phi2,
+                                          float deltaPhi, const seedgb_gbts_config& ap,
+                                          float4& out) {
+    const float dr = np2.z - np1.z;
+    if (dr < ap.minDeltaRadius) return false;
+    const float dz = np2.w - np1.w;
+    const float tau = dz / dr;
+    const float ftau = fabsf(tau);
+    if ((ftau < np2.x) || (ftau > np2.y)) return false;
+    if ((ftau < np1.x) || (ftau > np1.y)) return false;
+    const float z0 = np1.w - np1.z * tau;
+    if ((z0 < ap.min_z0) || (z0 > ap.max_z0)) return false;
+    const float zouter = z0 + ap.maxOuterRadius * tau;
+    if (zouter < ap.cut_zMinU || zouter > ap.cut_zMaxU) return false;
+    const float dphi = wrap_phi(phi2 - phi1);
+    if (fabsf(dphi) > deltaPhi) return false;
+    const float curv = dphi / dr;
+    const float d0_for_max_curv = np1.z * np2.z * (fabsf(curv) - ap.max_Kappa);
+    const float d0_max = (ftau < 4.0f) ? ap.low_Kappa_d0 : ap.high_Kappa_d0;
+    if (d0_for_max_curv > d0_max) return false;
+    out = make_float4(sqrtf(1.0f + tau * tau) - tau, curv, phi2 + curv * np2.z,
+                      phi1 + curv * np1.z);
+    return true;
+}
+
+struct ItemCtx {
+    uint32_t b1, n1, b2;
+    float dphi, phi0, phiN, pbw, brk;
+};
+
+// one outer node of a work item: the reference's window walk with the
+// thread's sliding start (last_n1) and stop flag (done); counts the edges, and
+// writes them from `pos` on when WRITE
+template <bool WRITE>
+__device__ __forceinline__ uint32_t walk(const ItemCtx& it, uint32_t n2Idx, uint32_t& last_n1,
+                                         bool& done, const float* s_phi, const float4* s_np,
+                                         const Work& w, const seedgb_gbts_config& c,
+                                         uint64_t pos, uint64_t cap) {
+    const uint32_t g2 = it.b2 + n2Idx;
+    const float phi2 = w.node_phi[g2];
+    uint32_t n1Idx = last_n1;
+    float min_phi1 = phi2 - it.dphi;
+    float max_phi1 = phi2 + it.dphi;
+    if (min_phi1 < -kPi) min_phi1 += kTwoPi;
+    if (max_phi1 > kPi) max_phi1 -= kTwoPi;
+    const bool boundary = max_phi1 < min_phi1;
+    max_phi1 += it.pbw;
+    min_phi1 -= it.pbw;
+    if (!boundary) {
+        if (it.phi0 > max_phi1) return 0;
+        if (it.phiN < min_phi1) {
+            if (it.phi0 > it.brk) done = true;
+            return 0;
+        }
+    } else {
+        if (it.phi0 < max_phi1) {
+            n1Idx = 0u;
+        } else if (it.phiN < min_phi1) {
+            return 0;
+        }
+    }
+    const float4 np2 = w.node_p[g2];
+    uint32_t cnt = 0;
+    for (; n1Idx < it.n1; n1Idx++) {
+        const float phi1 = s_phi[n1Idx];
+        if (!boundary) {
+            if (phi1 > max_phi1) break;
+            if (phi1 < min_phi1) continue;
+        } else if (phi1 > max_phi1 && phi1 < min_phi1) {
+            continue;
+        }
+        last_n1 = n1Idx;
+        float4 ep;
+        if (edge_test(s_np[n1Idx], np2, phi1, phi2, it.dphi, c, ep)) {
+            if (WRITE) {
+                const uint64_t q = pos + cnt;
+                if (q < cap) {
+                    w.e_in[q] = it.b1 + n1Idx;
+                    w.e_out[q] = g2;
+                    w.e_p[q] = ep;
+                    atomicAdd(&w.out_cnt[it.b1 + n1Idx], 1u);
+                }
+            }
+            ++cnt;
+        }
+    }
+    return cnt;
+}
+
+template <bool WRITE>
+__global__ void __launch_bounds__(kEdgeThreads) k_edges(Tables T, Work w) {
+    __shared__ float s_phi[kNodeBuffer];
+    __shared__ float4 s_np[kNodeBuffer];
+    __shared__ uint32_t s_red[kEdgeThreads / 32];
+    const uint32_t t = threadIdx.x;
+    const uint32_t n_items = w.sz[S_ITEMS];
+    const uint64_t by_nodes = static_cast<uint64_t>(T.c.max_edges_factor) * w.sz[S_NODES];
+    const uint64_t cap = by_nodes < w.ecap ? by_nodes : w.ecap;
+    for (uint32_t item = blockIdx.x; item < n_items; item += gridDim.x) {
+        const uint4 r = w.items[item];
+        ItemCtx it;
+        it.b1 = r.x;
+        it.n1 = r.y - r.x;
+        it.b2 = r.z;
+        const uint32_t n2 = r.w - r.z;
+        it.dphi = w.item_dphi[item];
+        __syncthreads();
+        if (t < it.n1) {
+            s_np[t] = w.node_p[it.b1 + t];
+            s_phi[t] = w.node_phi[it.b1 + t];
+        }
+        __syncthreads();
+        it.phi0 = s_phi[0];
+        it.phiN = s_phi[it.n1 - 1u];
+        it.pbw = kTwoPi / static_cast<float>(T.c.n_phi_bins);
+        it.brk = it.dphi + it.pbw - kPi;
+        uint32_t last_n1 = 0u;
+        bool done = false;
+        if (!WRITE) {
+            uint32_t cnt = 0;
+            for (uint32_t n2Idx = t; n2Idx < n2 && !done; n2Idx += kEdgeThreads)
+                cnt += walk<false>(it, n2Idx, last_n1, done, s_phi, s_np, w, T.c, 0, 0);
+            for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+            if ((t & 31) == 0) s_red[t >> 5] = cnt;
+            __syncthreads();
+            if (t == 0) {
+                uint32_t s = 0;
+                for (int k = 0; k < kEdgeThreads / 32; ++k) s += s_red[k];
+                w.item_ecnt[item] = s;
+            }
+        } else {
+            uint64_t base = w.item_ebase[item];
+            for (uint32_t r0 = 0; r0 < n2; r0 += kEdgeThreads) {
+                const uint32_t n2Idx = r0 + t;
+                const uint32_t l0 = last_n1;
+                const bool d0 = done;
+                uint32_t c = 0;
+                if (!done && n2Idx < n2)
+                    c = walk<false>(it, n2Idx, last_n1, done, s_phi, s_np, w, T.c, 0, 0);
+                uint32_t tot;
+                const uint32_t off = block_exclusive_scan(c, &tot);
+                last_n1 = l0;
+                done = d0;
+                if (!done && n2Idx < n2)
+                    walk<true>(it, n2Idx, last_n1, done, s_phi, s_np, w, T.c, base + off, cap);
+                base += tot;
+            }
+        }
+    }
+}
+
+// gbts_link_graph_edges.ipp:22-44: the edges leaving each node (by inner node)
+__global__ void __launch_bounds__(kThreads) k_link_fill(Work w, uint32_t n_edges) {
+    const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n_edges) return;
+    const uint32_t n1 = w.e_in[e];
+    w.links[w.lstart[n1] + atomicAdd(&w.lcur[n1], 1u)] = e;
+}
+
+__global__ void __launch_bounds__(kThreads) k_link_sort(Work w) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= w.sz[S_NODES]) return;
+    const uint32_t b = w.lstart[k], e = w.lstart[k + 1];
+    for (uint32_t i = b + 1; i < e; ++i) {
+        const uint32_t v = w.links[i];
+        uint32_t j = i;
+        while (j > b && w.links[j - 1] > v) {
+            w.links[j] = w.links[j - 1];
+            --j;
+        }
+        w.links[j] = v;
+    }
+}
+
+// gbts_match_graph_edges.ipp:29-118
+__global__ void __launch_bounds__(kThreads) k_match(Tables T, Work w, uint32_t n_edges) {
+    const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n_edges) return;
+    const seedgb_gbts_config& c = T.c;
+    const uint32_t M = c.max_num_neighbours;
+    const uint32_t shared_node = w.e_out[e];
+    const uint32_t link_begin = w.lstart[shared_node];
+    const uint32_t nLinks = w.lstart[shared_node + 1] - link_begin;
+    uint32_t num_nei = 0;
+    if (nLinks != 0u) {
+        const float4 p1 = w.e_p[e];
+        const float uat_2 = 1.0f / p1.x;
+        const float Phi2 = p1.z;
+        const float curv2 = p1.y;
+        for (uint32_t k = 0u; k < nLinks; k++) {
+            if (num_nei >= M) break;
+            const uint32_t e2 = w.links[link_begin + k];
+            const float4 p2 = w.e_p[e2];
+            const float tau_ratio = p2.x * uat_2 - 1.0f;
+            if (fabsf(tau_ratio) > c.cut_tau_ratio_max) continue;
+            const float dPhi = wrap_phi(Phi2 - p2.w);
+            if (fabsf(dPhi) > c.cut_dphi_max) continue;
+            const float dcurv = curv2 - p2.y;
+            if (fabsf(dcurv) > c.cut_dcurv_max) continue;
+            w.nei[static_cast<uint64_t>(M) * e + num_nei] = e2;
+            w.kept[e2] = 1u;
+            ++num_nei;
+        }
+    }
+    w.nnei[e] = static_cast<uint8_t>(num_nei);
+    if (num_nei != 0) {
+        w.kept[e] = 1u;
+        atomicAdd(&w.sz[S_CONN], num_nei);
+    }
+}
+
+// gbts_compress_graph.ipp:22-68: rows [outer sp, inner sp, nNei, neighbours]
+__global__ void __launch_bounds__(kThreads) k_compress(Tables T, Work w, uint32_t n_edges) {
+    const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n_edges || !w.kept[e]) return;
+    const uint32_t M = T.c.max_num_neighbours;
+    uint32_t* row = w.graph + static_cast<uint64_t>(3u + M) * w.kbase[e];
+    row[0] = w.node_sp[w.e_out[e]];
+    row[1] = w.node_sp[w.e_in[e]];
+    const uint32_t nn = w.nnei[e];
+    row[2] = nn;
+    for (uint32_t k = 0; k < nn; ++k) row[3 + k] = w.kbase[w.nei[static_cast<uint64_t>(M) * e + k]];
+}
+
+// ---------------------------------------------------------------------------
+// Longest chains: gbts_run_cca_iteration.ipp:23-101 (one launch per iteration)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kThreads) k_cca(Tables T, Work w, uint32_t iter) {
+    const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= w.sz[S_CONNECTED]) return;
+    if (iter != 0 && w.active[e] != static_cast<int8_t>(iter)) return;
+    const uint32_t esz = 3u + T.c.max_num_neighbours;
+    const uint32_t* row = w.graph + static_cast<uint64_t>(esz) * e;
+    const uint32_t toggle = iter % 2;
+    const uint8_t* lload = w.levels + toggle * w.ecap;
+    uint8_t* lstore = w.levels + (1u - toggle) * w.ecap;
+    const uint32_t nN = row[2];
+    uint8_t next_level = lload[e];
+    bool change = false;
+    for (uint32_t k = 0; k < nN; k++) {
+        const uint8_t f = lload[row[3 + k]];
+        if (next_level == f) {
+            next_level = static_cast<uint8_t>(f + 1);
+            change = true;
+            break;
+        }
+    }
+    if (change) {
+        if (iter == kMaxCca - 1) {
+            w.opy[e] = -1;
+            w.active[e] = -1;
+        } else {
+            w.active[e] = static_cast<int8_t>(iter + 1u);
+        }
+    } else {
+        w.active[e] = -1;
+        int64_t out_paths = 0;
+        for (uint32_t k = 0; k < nN; ++k) {
+            const uint32_t n = row[3 + k];
+            if (next_level == 1 + w.levels[n]) out_paths += 1 + w.opx[n];
+            w.opy[n] = -1;
+        }
+        if (out_paths > kPathCountLimit) {
+            out_paths = kPathCountLimit;
+            set_status(w.sz, SEEDGB_CAPACITY_OVERFLOW);
+        }
+        w.opx[e] = static_cast<int32_t>(out_paths);
+        w.opy[e] = static_cast<int16_t>((next_level >= T.c.minLevel) - 1);
+    }
+    lstore[e] = next_level;
+}
+
+// gbts_count_terminus_edges.ipp:22-46
+__global__ void __launch_bounds__(kThreads) k_term_flags(Work w) {
+    const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= w.sz[S_CONNECTED]) return;
+    const bool t = w.opy[e] != -1;
+    w.tflag[e] = t ? 1u : 0u;
+    w.tpaths[e] = t ? static_cast<uint32_t>(w.opx[e]) : 0u;
+}
+
+// gbts_add_terminus_to_path_store.ipp:21-44
+__global__ void __launch_bounds__(kThreads) k_term_fill(Work w) {
+    const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= w.sz[S_CONNECTED] || !w.tflag[e]) return;
+    const uint32_t ti = w.tidx[e];
+    w.store[ti] = make_int2(static_cast<int>(e), -1);
+    w.term_edge[ti] = e;
+    w.term_pos[ti] = w.sz[S_TERMINUS] + w.pbase[e];
+}
+
+// gbts_fill_path_store.ipp:24-163 as a depth-first pre-order walk below each
+// terminus edge: the children of an entry are its neighbours one level down
+__global__ void __launch_bounds__(kThreads) k_dfs(Tables T, Work w) {
+    const uint32_t ti = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ti >= w.sz[S_TERMINUS]) return;
+    const uint32_t esz = 3u + T.c.max_num_neighbours;
+    const uint64_t end = static_cast<uint64_t>(w.sz[S_TERMINUS]) + w.sz[S_PATHS];
+    uint32_t se[kMaxCca + 2], sk[kMaxCca + 2];
+    int32_t si[kMaxCca + 2];
+    uint64_t pos = w.term_pos[ti];
+    int d = 0;
+    se[0] = w.term_edge[ti];
+    si[0] = static_cast<int32_t>(ti);
+    sk[0] = 0;
+    while (d >= 0) {
+        const uint32_t e = se[d];
+        const uint32_t* row = w.graph + static_cast<uint64_t>(esz) * e;
+        if (sk[d] >= row[2]) {
+            --d;
+            continue;
+        }
+        const uint32_t n = row[3 + sk[d]++];
+        if (w.levels[e] != w.levels[n] + 1) continue;
+        if (pos >= end || d + 1 > static_cast<int>(kMaxCca)) {
+            set_status(w.sz, SEEDGB_CAPACITY_OVERFLOW);
+            break;
+        }
+        w.store[pos] = make_int2(static_cast<int>(n), si[d]);
+        ++d;
+        se[d] = n;
+        si[d] = static_cast<int32_t>(pos);
+        sk[d] = 0;
+        ++pos;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Kalman fit of the paths (gbts_fit_segments.ipp:37-335)
+// ---------------------------------------------------------------------------
+struct EdgeState {
+    float X[3], Y[2];
+    float c, s, refX, refY;
+    float J;
+    bool head_type;
+    float Cx[6];
+    float Cy[3];
+    __device__ __forceinline__ float& cx(int i, int j) { return Cx[i + j + 1 * (i != 0) * (j != 0)]; }
+    __device__ __forceinline__ float cx(int i, int j) const { return Cx[i + j + 1 * (i != 0) * (j != 0)]; }
+    __device__ __forceinline__ float& cy(int i, int j) { return Cy[i + j]; }
+    __device__ __forceinline__ float cy(int i, int j) const { return Cy[i + j]; }
+};
+
+__device__ __forceinline__ void state_init(EdgeState& st, float4 n1, float4 n2) {
+    st.J = 0.0f;
+    st.head_type = (n1.w < 0);
+    const float dx = n1.x - n2.x;
+    const float dy = n1.y - n2.y;
+    const float L = sqrtf(dx * dx + dy * dy);
+    const float r1 = sqrtf(n1.x * n1.x + n1.y * n1.y);
+    const float r2 = sqrtf(n2.x * n2.x + n2.y * n2.y);
+    st.s = dy / L;
+    st.c = dx / L;
+    st.refX = n2.x * st.c + n2.y * st.s;
+    st.refY = r2;
+    st.X[0] = -n2.x * st.s + n2.y * st.c;
+    st.X[1] = 0.0f;
+    st.X[2] = 0.0f;
+    st.Y[0] = n2.z;
+    st.Y[1] = (n1.z - n2.z) / (r1 - r2);
+    for (int i = 0; i < 6; ++i) st.Cx[i] = 0.0f;
+    for (int i = 0; i < 3; ++i) st.Cy[i] = 0.0f;
+    st.cx(0, 0) = 0.25f;
+    st.cx(1, 1) = 0.001f;
+    st.cx(2, 2) = 0.001f;
+    st.cy(0, 0) = 1.5f;
+    st.cy(1, 1) = 0.001f;
+}
+
+__device__ bool kalman_update(EdgeState& nt, const EdgeState& ts, float4 node,
+                              const seedgb_gbts_config& p) {
+    const float tau2 = ts.Y[1] * ts.Y[1];
+    const float invSin2 = 1 + tau2;
+    const float lenCorr = (node.w != -1) ? invSin2 : invSin2 / tau2;
+    const float minPtFrac = fabsf(ts.X[2]) * p.inv_max_curvature;
+    const float corrMS = p.sigmaMS * minPtFrac;
+    const float sigma2 = p.radLen * lenCorr * corrMS * corrMS;
+    const float m_Cx11 = ts.cx(1, 1) + sigma2;
+    const float m_Cy11 = ts.cy(1, 1) + sigma2;
+    const float r = sqrtf(node.x * node.x + node.y * node.y);
+    nt.refX = node.x * ts.c + node.y * ts.s;
+    const float mx = -node.x * ts.s + node.y * ts.c;
+    nt.refY = r;
+    const float my = node.z;
+    const float A = nt.refX - ts.refX;
+    const float B = (0.5f) * A * A;
+    const float dr = nt.refY - ts.refY;
+    nt.X[0] = ts.X[0] + ts.X[1] * A + ts.X[2] * B;
+    nt.X[1] = ts.X[1] + ts.X[2] * A;
+    nt.X[2] = ts.X[2];
+    nt.cx(0, 0) = ts.cx(0, 0) + 2 * ts.cx(0, 1) * A + 2 * ts.cx(0, 2) * B + A * m_Cx11 * A +
+                  2 * A * ts.cx(1, 2) * B + B * ts.cx(2, 2) * B;
+    nt.cx(0, 1) = ts.cx(0, 1) + m_Cx11 * A + ts.cx(1, 2) * B + ts.cx(0, 2) * A +
+                  A * ts.cx(1, 2) * A + A * ts.cx(2, 2) * B;
+    nt.cx(0, 2) = ts.cx(0, 2) + ts.cx(1, 2) * A + ts.cx(2, 2) * B;
+    nt.cx(1, 1) = m_Cx11 + 2 * A * ts.cx(1, 2) + A * ts.cx(2, 2) * A;
+    nt.cx(1, 2) = ts.cx(1, 2) + ts.cx(2, 2) * A;
+    nt.cx(2, 2) = ts.cx(2, 2);
+    nt.Y[0] = ts.Y[0] + ts.Y[1] * dr;
+    nt.Y[1] = ts.Y[1];
+    nt.cy(0, 0) = ts.cy(0, 0) + 2 * ts.cy(0, 1) * dr + dr * m_Cy11 * dr;
+    nt.cy(0, 1) = ts.cy(0, 1) + dr * m_Cy11;
+    nt.cy(1, 1) = m_Cy11;
+    const float resid_x = mx - nt.X[0];
+    const float resid_y = my - nt.Y[0];
+    float sigma_rz = 0;
+    if (!ts.head_type) {
+        sigma_rz = p.sigma_y;
+    } else {
+        sigma_rz = p.sigma_y * ts.Y[1];
+    }
+    const float inv_Dx = nt.cx(0, 0) + p.sigma_x * p.sigma_x;
+    const float Dx = 1 / inv_Dx;
+    const float Dy = 1 / (nt.cy(0, 0) + sigma_rz * sigma_rz);
+    const float dchi2_x = resid_x * resid_x * Dx;
+    const float dchi2_y = resid_y * resid_y * Dy;
+    if (dchi2_x > p.maxDChi2_x || dchi2_y > p.maxDChi2_y) return false;
+    nt.J = ts.J + (p.add_hit - dchi2_x * p.weight_x - dchi2_y * p.weight_y);
+    for (int i = 0; i < 3; i++) nt.X[i] += Dx * nt.cx(0, i) * resid_x;
+    if (fabsf(nt.X[2]) * p.inv_max_curvature > 1.0f) return false;
+    for (int i = 0; i < 2; i++) nt.Y[i] += Dx * nt.cy(0, i) * resid_y;
+    const float z0 = nt.Y[0] - nt.refY * ts.Y[1];
+    if (fabsf(z0) > p.max_z0) return false;
+    nt.cx(2, 2) = Dx * (nt.cx(2, 2) * inv_Dx - nt.cx(0, 2) * nt.cx(0, 2));
+    nt.cx(1, 2) = Dx * (nt.cx(1, 2) * inv_Dx - nt.cx(0, 1) * nt.cx(0, 2));
+    nt.cx(1, 1) = Dx * (nt.cx(1, 1) * inv_Dx - nt.cx(0, 1) * nt.cx(0, 1));
+    nt.cx(0, 2) = Dx * (nt.cx(0, 2) * inv_Dx - nt.cx(0, 0) * nt.cx(0, 2));
+    nt.cx(0, 1) = Dx * (nt.cx(0, 1) * inv_Dx - nt.cx(0, 0) * nt.cx(0, 1));
+    nt.cx(0, 0) *= Dx * (p.sigma_x * p.sigma_x);
+    nt.cy(1, 1) -= Dy * nt.cy(0, 1) * nt.cy(0, 1);
+    nt.cy(0, 1) -= Dy * nt.cy(0, 0) * nt.cy(0, 1);
+    nt.cy(0, 0) -= Dy * nt.cy(0, 0) * nt.cy(0, 0);
+    nt.c = ts.c;
+    nt.s = ts.s;
+    nt.head_type = (node.w < 0);
+    return true;
+}
+
+__global__ void __launch_bounds__(kThreads) k_fit(Tables T, Work w) {
+    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= w.sz[S_PATHS]) return;
+    const seedgb_gbts_config& c = T.c;
+    const uint32_t esz = 3u + c.max_num_neighbours;
+    const uint32_t path_idx = w.sz[S_TERMINUS] + q;
+    unsigned length = 1;
+    bool toggle = false;
+    EdgeState s1, s2;
+    int2 path = w.store[path_idx];
+    const uint32_t* row = w.graph + static_cast<uint64_t>(esz) * static_cast<uint32_t>(path.x);
+    state_init(s1, w.red[row[1]], w.red[row[0]]);
+    s2 = s1;
+    while (path.y >= 0) {
+        path = w.store[path.y];
+        const float4 nd = w.red[w.graph[static_cast<uint64_t>(esz) * static_cast<uint32_t>(path.x) + 1]];
+        if (toggle) {
+            if (!kalman_update(s1, s2, nd, c)) {
+                s1 = s2;
+                break;
+            }
+        } else if (!kalman_update(s2, s1, nd, c)) {
+            break;
+        }
+        toggle = !toggle;
+        length++;
+    }
+    const bool ok = length >= c.minLevel;
+    w.fflag[q] = ok ? 1u : 0u;
+    w.fqual[q] = toggle ? static_cast<int>(c.qual_scale * s2.J) : static_cast<int>(c.qual_scale * s1.J);
+}
+
+__global__ void __launch_bounds__(kThreads) k_props(Work w) {
+    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= w.sz[S_PATHS] || !w.fflag[q]) return;
+    const uint32_t P = w.fidx[q];
+    w.props[P] = make_int2(w.fqual[q], static_cast<int>(w.sz[S_TERMINUS] + q));
+    w.ambi[P] = 0;
+    w.bidder[P] = 1;
+}
+
+// ---------------------------------------------------------------------------
+// Bidding (gbts_create_seed_candidate.ipp:22-58, gbts_rebid_seeds_for_edges.
+// ipp:23-62, gbts_reset_edge_bids.ipp:22-69).  Each round's bidders are fixed
+// by k_round before the bids (value 2 = bidding this round); a bid kernel only
+// ever writes -1, so the outcome does not depend on the order of the atomics.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned long long bid_of(int2 prop, uint32_t P) {
+    return (static_cast<unsigned long long>(static_cast<uint32_t>(prop.x)) << 32) |
+           static_cast<unsigned long long>(P);
+}
+
+__global__ void __launch_bounds__(kThreads) k_bid(Work w, int depth) {
+    const uint32_t P = blockIdx.x * blockDim.x + threadIdx.x;
+    if (P >= w.sz[S_PROPS] || !w.bidder[P]) return;
+    const int2 prop = w.props[P];
+    const unsigned long long seed_bid = bid_of(prop, P);
+    int2 path = make_int2(0, prop.y);
+    int d = depth;
+    while (path.y >= 0 && d != 0) {
+        path = w.store[path.y];
+        d--;
+        const unsigned long long comp = atomicMax(&w.ebid[path.x], seed_bid);
+        if (comp > seed_bid) {
+            w.ambi[P] = -1;
+        } else if (comp != 0) {
+            w.ambi[comp & 0xFFFFFFFFull] = -1;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) k_round(Work w, int first) {
+    const uint32_t P = blockIdx.x * blockDim.x + threadIdx.x;
+    if (P >= w.sz[S_PROPS]) return;
+    const int8_t a = w.ambi[P];
+    uint8_t b = 0;
+    if (first) {
+        if (a == 0) {
+            w.ambi[P] = 2;
+            b = 1;
+        } else {
+            w.ambi[P] = -2;
+        }
+    } else if (a == 1) {
+        w.ambi[P] = 2;
+        b = 1;
+    }
+    w.bidder[P] = b;
+}
+
+__global__ void __launch_bounds__(kThreads) k_reset(Work w) {
+    const uint32_t P = blockIdx.x * blockDim.x + threadIdx.x;
+    if (P >= w.sz[S_PROPS]) return;
+    const int8_t a = w.ambi[P];
+    if (a == 2) {
+        w.ambi[P] = 0;
+        return;
+    }
+    if (a != -1) return;
+    bool good = true;
+    int2 path = make_int2(0, w.props[P].y);
+    while (path.y >= 0) {
+        path = w.store[path.y];
+        const int8_t best = w.ambi[w.ebid[path.x] & 0xFFFFFFFFull];
+        if (best == 0 || best == 2) {
+            good = false;
+            break;
+        }
+    }
+    w.ambi[P] = good ? 1 : -2;
+}
+
+// gbts_bid_seeds_for_hits.ipp:23-70
+__global__ void __launch_bounds__(kThreads) k_hit_bids(Tables T, Work w) {
+    const uint32_t P = blockIdx.x * blockDim.x + threadIdx.x;
+    if (P >= w.sz[S_PROPS]) return;
+    if (w.ambi[P] == -2) {
+        atomicAdd(&w.sz[S_REJECTED], 1u);
+        return;
+    }
+    const uint32_t esz = 3u + T.c.max_num_neighbours;
+    const int2 prop = w.props[P];
+    const unsigned long long b = bid_of(prop, P);
+    int2 path = make_int2(0, prop.y);
+    while (path.y >= 0) {
+        path = w.store[path.y];
+        atomicMax(&w.hbid[w.graph[static_cast<uint64_t>(esz) * static_cast<uint32_t>(path.x)]], b);
+    }
+    atomicMax(&w.hbid[w.graph[static_cast<uint64_t>(esz) * static_cast<uint32_t>(path.x) + 1]], b);
+}
+
+// gbts_estimate_seed_params (gbts_convert_seeds.ipp:33-67)
+__device__ __forceinline__ float2 estimate_seed_params(const float4 sps[3]) {
+    float u[2], v[2];
+    const float x0 = sps[1].x;
+    const float y0 = sps[1].y;
+    const float r0 = sqrtf(x0 * x0 + y0 * y0);
+    const float cosA = x0 / r0;
+    const float sinA = y0 / r0;
+    for (unsigned k = 0; k < 2; k++) {
+        const unsigned i = (k == 1) ? 2u : k;
+        const float dx = sps[i].x - x0;
+        const float dy = sps[i].y - y0;
+        const float r2_inv = 1.0f / (dx * dx + dy * dy);
+        const float xn = dx * cosA + dy * sinA;
+        const float yn = -dx * sinA + dy * cosA;
+        u[k] = xn * r2_inv;
+        v[k] = yn * r2_inv;
+    }
+    const float du = u[0] - u[1];
+    if (du == 0.0f) return make_float2(0.0f, 0.0f);
+    const float A = (v[0] - v[1]) / du;
+    const float B = v[1] - A * u[1];
+    const float curv = 1000.0f * B / sqrtf(1 + A * A);
+    const float cot_t = (sps[2].z - sps[1].z) / (sqrtf(sps[2].x * sps[2].x + sps[2].y * sps[2].y) - r0);
+    return make_float2(curv, cot_t);
+}
+
+// gbts_convert_seeds.ipp:72-194: up to three seeds per surviving proposal
+__global__ void __launch_bounds__(kThreads) k_convert(Tables T, Work w) {
+    const uint32_t P = blockIdx.x * blockDim.x + threadIdx.x;
+    if (P >= w.sz[S_PROPS]) return;
+    w.ecount[P] = 0;
+    if (w.ambi[P] == -2) return;
+    const seedgb_gbts_config& c = T.c;
+    const uint32_t esz = 3u + c.max_num_neighbours;
+    uint32_t nodes[kMaxCca + 1];
+    int size = 0;
+    signed char best_for_hit = 0;
+    const int2 prop = w.props[P];
+    int2 path = make_int2(0, prop.y);
+    while (path.y >= 0 && size < static_cast<int>(kMaxCca)) {
+        path = w.store[path.y];
+        nodes[size++] = w.graph[static_cast<uint64_t>(esz) * static_cast<uint32_t>(path.x)];
+        best_for_hit = static_cast<signed char>(best_for_hit + (P == (w.hbid[nodes[size - 1]] & 0xFFFFFFFFull)));
+    }
+    nodes[size++] = w.graph[static_cast<uint64_t>(esz) * static_cast<uint32_t>(path.x) + 1];
+    best_for_hit = static_cast<signed char>(best_for_hit + (P == (w.hbid[nodes[size - 1]] & 0xFFFFFFFFull)));
+    if (best_for_hit < c.best_hit_frac * static_cast<float>(size)) return;
+    int diff_code = 0;
+    bool force_dropout = false;
+    if (c.use_dropout) {
+        float4 sps[3] = {w.red[nodes[size - 1]], w.red[nodes[(size - 1) / 2 + 1]], w.red[nodes[0]]};
+        const float2 c1 = estimate_seed_params(sps);
+        sps[1] = w.red[nodes[(size - 1) / 2]];
+        const float2 c2 = estimate_seed_params(sps);
+        sps[0] = w.red[nodes[size - 2]];
+        const float2 c3 = estimate_seed_params(sps);
+        if ((best_for_hit < size - 1) & (fabsf(c1.y + c2.y + c3.y) < 3.0f * c.tight_bid_cot_threshold) &
+            (size < 5))
+            return;
+        const float d0 = fabsf(c1.x - c2.x), d1 = fabsf(c2.x - c3.x), d2 = fabsf(c1.x - c3.x);
+        diff_code = 4 * (d0 < c.dropout_dcurv_m) + 2 * (d1 < c.dropout_dcurv_m) + (d2 < c.dropout_dcurv_m);
+        force_dropout = fabsf(c1.x + c2.x + c3.x) < 3.0f * c.force_dropout_max_curv_m;
+        force_dropout |= (fabsf(c1.y + c2.y + c3.y) < 3.0f * c.tight_bid_cot_threshold) & (diff_code == 0);
+    }
+    const uint32_t qbits = __float_as_uint(static_cast<float>(prop.x));
+    uint32_t ne = 0;
+    uint4* o = w.seeds3 + 3ull * P;
+    if (((diff_code != 3) & (diff_code != 6)) | force_dropout)
+        o[ne++] = make_uint4(nodes[size - 1], nodes[(size - 1) / 2 + 1], nodes[0], qbits);
+    if ((diff_code == 1) | (diff_code == 6))
+        o[ne++] = make_uint4(nodes[size - 1], nodes[(size - 1) / 2], nodes[0], qbits);
+    if ((diff_code == 2) | (diff_code == 3) | (diff_code == 4) | force_dropout)
+        o[ne++] = make_uint4(nodes[size - 2], nodes[(size - 1) / 2], nodes[0], qbits);
+    w.ecount[P] = ne;
+}
+
+__global__ void __launch_bounds__(kThreads) k_seeds_out(Work w, seedgb_seed_buffer out) {
+    const uint32_t P = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t n = w.sz[S_PROPS];
+    if (P == 0) {
+        const uint32_t tot = w.sz[S_SEEDS];
+        *out.size = tot < out.capacity ? tot : out.capacity;
+        if (tot > out.capacity) set_status(w.sz, SEEDGB_CAPACITY_OVERFLOW);
+    }
+    if (P >= n) return;
+    const uint32_t ne = w.ecount[P];
+    const uint32_t o = w.eoff[P];
+    for (uint32_t k = 0; k < ne; ++k) {
+        if (o + k >= out.capacity) break;
+        const uint4 s = w.seeds3[3ull * P + k];
+        out.bottom_index[o + k] = s.x;
+        out.middle_index[o + k] = s.y;
+        out.top_index[o + k] = s.z;
+        out.quality[o + k] = __uint_as_float(s.w);
+    }
+}
+
+__global__ void k_empty_out(seedgb_seed_buffer out) { *out.size = 0; }
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+uint64_t field_h(uint64_t v, uint32_t shift, uint32_t bits) {
+    const uint64_t m = bits >= 64 ? ~0ull : ((1ull << bits) - 1ull);
+    return shift >= 64 ? 0 : ((v >> shift) & m);
+}
+
+struct DevBlock {
+    void* p = nullptr;
+    size_t bytes = 0;
+    ~DevBlock() {
+        if (p) cudaFree(p);
+    }
+    bool ensure(size_t need) {
+        if (need <= bytes) return true;
+        if (p) {
+            cudaDeviceSynchronize();
+            cudaFree(p);
+            p = nullptr;
+            bytes = 0;
+        }
+        if (cudaMalloc(&p, need) != cudaSuccess) return false;
+        bytes = need;
+        return true;
+    }
+};
+
+struct Carver {
+    char* base;
+    size_t off = 0;
+    template <class T>
+    T* take(uint64_t n) {
+        off = (off + 255) & ~size_t(255);
+        T* r = reinterpret_cast<T*>(base ? base + off : nullptr);
+        off += sizeof(T) * static_cast<size_t>(n ? n : 1);
+        return r;
+    }
+};
+
+}  // namespace
+
+struct seedgb_gbts {
+    seedgb_gbts_config cfg;
+    uint32_t n_layers = 0, n_eta = 0, n_pairs = 0, n_volumes = 0, n_surfaces = 0, n_tau = 0;
+    uint32_t max_first_degree = 0;
+    // device tables
+    int8_t* d_type = nullptr;
+    uint32_t *d_bin0 = nullptr, *d_neta = nullptr, *d_pairs = nullptr, *d_smap = nullptr;
+    float *d_min_eta = nullptr, *d_width = nullptr, *d_lut = nullptr;
+    int16_t* d_vmap = nullptr;
+    DevBlock arena_a, arena_b;
+    uint32_t* d_sz = nullptr;
+    uint32_t* h_sz = nullptr;  // pinned
+    cudaStream_t last = nullptr;
+    Work w{};
+    uint64_t a_sp = 0, a_e = 0;
+};
+
+namespace {
+
+Tables tables_of(const seedgb_gbts* h) {
+    Tables T;
+    T.c = h->cfg;
+    T.n_layers = h->n_layers;
+    T.n_eta = h->n_eta;
+    T.n_pairs = h->n_pairs;
+    T.n_volumes = h->n_volumes;
+    T.n_surfaces = h->n_surfaces;
+    T.n_tau_lut = h->n_tau;
+    T.layer_type = h->d_type;
+    T.eta_bin0 = h->d_bin0;
+    T.n_eta_l = h->d_neta;
+    T.min_eta = h->d_min_eta;
+    T.eta_width = h->d_width;
+    T.pairs = h->d_pairs;
+    T.vmap = h->d_vmap;
+    T.smap = h->d_smap;
+    T.tau_lut = h->d_lut;
+    return T;
+}
+
+uint32_t blocks(uint64_t n, int threads = kThreads) {
+    return static_cast<uint32_t>(std::max<uint64_t>(1, (n + threads - 1) / threads));
+}
+
+// exclusive scan helper: n on the device (n_dev + add) or the host; grid for `cap`
+void scan(const uint32_t* in, uint32_t* out, const uint32_t* n_dev, uint32_t n_host, uint32_t add,
+          uint64_t cap, uint32_t* tile, uint32_t* tile_total, uint32_t* total_dst, cudaStream_t s) {
+    const uint32_t tiles = static_cast<uint32_t>(std::max<uint64_t>(1, (cap + kScanTile - 1) / kScanTile));
+    k_scan_tile<<<tiles, kScanThreads, 0, s>>>(in, out, n_dev, n_host, add, tile);
+    k_scan_sums<<<1, kScanThreads, 0, s>>>(tile, tiles, tile_total);
+    k_scan_add<<<tiles, kScanThreads, 0, s>>>(out, n_dev, n_host, add, tile, tile_total, total_dst);
+}
+
+// carve the spacepoint-sized arena (base == nullptr: measure only)
+size_t carve_a(seedgb_gbts* h, char* base, uint64_t n_sp, uint64_t items_cap, Work& w) {
+    const uint64_t N = std::max<uint64_t>(n_sp, 1);
+    const uint64_t E = std::max<uint64_t>(1, static_cast<uint64_t>(h->cfg.max_edges_factor) * N);
+    const uint64_t M = h->cfg.max_num_neighbours;
+    const uint64_t cells = static_cast<uint64_t>(h->n_eta) * h->cfg.n_phi_bins;
+    const uint64_t scan_cap = std::max<uint64_t>({E + 1, N + 1, cells + 1, items_cap + 1, h->n_pairs + 1ull});
+    Carver cv{base};
+    w.red = cv.take<float4>(N);
+    w.sp_phi = cv.take<float>(N);
+    w.sp_cell = cv.take<uint32_t>(N);
+    w.cell_cnt = cv.take<uint32_t>(cells + 1);
+    w.cell_off = cv.take<uint32_t>(cells + 1);
+    w.cell_cur = cv.take<uint32_t>(cells + 1);
+    w.node_sp = cv.take<uint32_t>(N);
+    w.node_p = cv.take<float4>(N);
+    w.node_phi = cv.take<float>(N);
+    w.view = cv.take<uint32_t>(2ull * h->n_eta);
+    w.rads = cv.take<float>(2ull * h->n_eta);
+    w.item_cnt = cv.take<uint32_t>(h->n_pairs + 1ull);
+    w.item_off = cv.take<uint32_t>(h->n_pairs + 1ull);
+    w.items = cv.take<uint4>(items_cap);
+    w.item_dphi = cv.take<float>(items_cap);
+    w.item_ecnt = cv.take<uint32_t>(items_cap + 1);
+    w.item_ebase = cv.take<uint32_t>(items_cap + 1);
+    w.e_in = cv.take<uint32_t>(E);
+    w.e_out = cv.take<uint32_t>(E);
+    w.e_p = cv.take<float4>(E);
+    w.out_cnt = cv.take<uint32_t>(N + 1);
+    w.lstart = cv.take<uint32_t>(N + 1);
+    w.lcur = cv.take<uint32_t>(N + 1);
+    w.links = cv.take<uint32_t>(E);
+    w.nnei = cv.take<uint8_t>(E);
+    w.nei = cv.take<uint32_t>(M * E);
+    w.kept = cv.take<uint32_t>(E);
+    w.kbase = cv.take<uint32_t>(E + 1);
+    w.graph = cv.take<uint32_t>((3 + M) * E);
+    w.levels = cv.take<uint8_t>(2 * E);
+    w.active = cv.take<int8_t>(E);
+    w.opx = cv.take<int32_t>(E);
+    w.opy = cv.take<int16_t>(E);
+    w.tflag = cv.take<uint32_t>(E);
+    w.tidx = cv.take<uint32_t>(E + 1);
+    w.tpaths = cv.take<uint32_t>(E);
+    w.pbase = cv.take<uint32_t>(E + 1);
+    w.ebid = cv.take<unsigned long long>(E);
+    w.hbid = cv.take<unsigned long long>(N);
+    w.tile = cv.take<uint32_t>(scan_cap / kScanTile + 4);
+    w.ecap = E;
+    return cv.off + 256;
+}
+
+size_t carve_b(char* base, uint64_t n_term, uint64_t n_paths, Work& w) {
+    const uint64_t S = std::max<uint64_t>(1, n_term + n_paths);
+    const uint64_t P = std::max<uint64_t>(1, n_paths);
+    Carver cv{base};
+    w.store = cv.take<int2>(S);
+    w.term_edge = cv.take<uint32_t>(std::max<uint64_t>(1, n_term));
+    w.term_pos = cv.take<uint32_t>(std::max<uint64_t>(1, n_term));
+    w.fflag = cv.take<uint32_t>(P);
+    w.fidx = cv.take<uint32_t>(P + 1);
+    w.fqual = cv.take<int32_t>(P);
+    w.props = cv.take<int2>(P);
+    w.ambi = cv.take<int8_t>(P);
+    w.bidder = cv.take<uint8_t>(P);
+    w.ecount = cv.take<uint32_t>(P);
+    w.eoff = cv.take<uint32_t>(P + 1);
+    w.seeds3 = cv.take<uint4>(3 * P);
+    w.tile_b = cv.take<uint32_t>((P + 1) / kScanTile + 4);
+    w.pcap = S;
+    return cv.off + 256;
+}
+
+// gbts_seedfinder_config::setLinkingScheme (core/src/gbts_seeding/
+// gbts_seeding_config.cpp:19-142): descending barcodes; one volume -> one
+// layer, or -(first surface-map entry + 1) when its surfaces lie on several
+// layers; a (UINT_MAX, -1) sentinel ends the walk; the volume map is
+// (largest volume + 1) zeros followed by as many SHRT_MAX entries.
+bool linking(seedgb_gbts_config& c, float minPt, const seedgb_gbts_geoid* geoids, uint32_t n,
+             std::vector<int16_t>& vmap, std::vector<uint32_t>& smap) {
+    if (n == 0) return false;
+    std::vector<std::pair<uint64_t, int16_t>> g(n);
+    for (uint32_t i = 0; i < n; ++i) g[i] = {geoids[i].barcode, static_cast<int16_t>(geoids[i].layer)};
+    std::stable_sort(g.begin(), g.end(), [](const auto& a, const auto& b) { return a.first > b.first; });
+    const uint32_t largest = static_cast<uint32_t>(field_h(g[0].first, c.volume_shift, c.volume_bits));
+    if (largest >= SHRT_MAX) return false;
+    int16_t current_volume = static_cast<int16_t>(largest);
+    bool layer_change = false;
+    int16_t current_layer = g[0].second;
+    g.emplace_back(static_cast<uint64_t>(UINT_MAX), static_cast<int16_t>(-1));
+    std::vector<std::pair<int16_t, uint32_t>> vol_bins;
+    std::vector<std::pair<uint32_t, uint32_t>> in_volume;
+    smap.clear();
+    for (const auto& gp : g) {
+        const int16_t vol = static_cast<int16_t>(field_h(gp.first, c.volume_shift, c.volume_bits));
+        if (current_volume != vol) {
+            int16_t bin = current_layer;
+            if (layer_change) {
+                bin = static_cast<int16_t>(-1 * static_cast<int16_t>(smap.size() / 2 + 1));
+                for (const auto& s : in_volume) {
+                    smap.push_back(s.first);
+                    smap.push_back(s.second);
+                }
+            }
+            vol_bins.emplace_back(bin, static_cast<uint32_t>(static_cast<uint16_t>(current_volume)));
+            current_volume = vol;
+            current_layer = gp.second;
+            layer_change = false;
+            in_volume.clear();
+        }
+        layer_change |= (current_layer != gp.second);
+        in_volume.emplace_back(static_cast<uint32_t>(field_h(gp.first, c.index_shift, c.index_bits)),
+                               static_cast<uint32_t>(static_cast<int32_t>(gp.second)));
+    }
+    vmap.assign(largest + 1, 0);
+    vmap.insert(vmap.end(), largest + 1, static_cast<int16_t>(SHRT_MAX));
+    for (const auto& vb : vol_bins)
+        if (vb.second < vmap.size()) vmap[vb.second] = vb.first;
+    if (smap.size() / 2 > SHRT_MAX) return false;
+    const float ptScale = 900.0f / minPt;
+    c.min_delta_phi *= ptScale;
+    c.dphi_coeff *= ptScale;
+    c.min_delta_phi_low_dr *= ptScale;
+    c.dphi_coeff_low_dr *= ptScale;
+    c.max_Kappa *= ptScale;
+    return true;
+}
+
+template <class T>
+bool upload(T** dst, const T* src, size_t n) {
+    if (cudaMalloc(reinterpret_cast<void**>(dst), sizeof(T) * std::max<size_t>(n, 1)) != cudaSuccess)
+        return false;
+    if (n && cudaMemcpy(*dst, src, sizeof(T) * n, cudaMemcpyHostToDevice) != cudaSuccess) return false;
+    return true;
+}
+
+void free_tables(seedgb_gbts* h) {
+    cudaFree(h->d_type);
+    cudaFree(h->d_bin0);
+    cudaFree(h->d_neta);
+    cudaFree(h->d_pairs);
+    cudaFree(h->d_smap);
+    cudaFree(h->d_min_eta);
+    cudaFree(h->d_width);
+    cudaFree(h->d_lut);
+    cudaFree(h->d_vmap);
+    cudaFree(h->d_sz);
+    if (h->h_sz) cudaFreeHost(h->h_sz);
+}
+
+}  // namespace
+
+extern "C" void seedgb_gbts_config_default(seedgb_gbts_config* c) {
+    std::memset(c, 0, sizeof(*c));
+    c->tMin_slope = 6.7f;
+    c->offset = 0.2f;
+    c->tMax_min = 1.6f;
+    c->tMax_correction = 0.15f;
+    c->tMax_slope = 6.1f;
+    c->maxTau = 36.0f;
+    c->minDeltaRadius = 2.0f;
+    c->min_z0 = -160.0f;
+    c->max_z0 = 160.0f;
+    c->maxOuterRadius = 350.0f;
+    c->tau_roi = 45.0f;
+    c->cut_zMinU = c->min_z0 - c->maxOuterRadius * c->tau_roi;
+    c->cut_zMaxU = c->max_z0 + c->maxOuterRadius * c->tau_roi;
+    c->max_Kappa = 3.75e-4f;
+    c->cut_dphi_max = 0.012f;
+    c->cut_dcurv_max = 0.001f;
+    c->cut_tau_ratio_max = 0.01f;
+    c->min_delta_phi = 0.015f;
+    c->dphi_coeff = 2.2e-4f;
+    c->min_delta_phi_low_dr = 0.002f;
+    c->dphi_coeff_low_dr = 4.33e-4f;
+    c->low_dr_threshold = 60.0f;
+    c->type1_max_width = 0.2f;
+    c->doTauCut = 1;
+    c->sigmaMS = 0.016f;
+    c->radLen = 0.025f;
+    c->sigma_x = 0.08f;
+    c->sigma_y = 0.25f;
+    c->weight_x = 0.5f;
+    c->weight_y = 0.5f;
+    c->maxDChi2_x = 5.0f;
+    c->maxDChi2_y = 6.0f;
+    c->add_hit = 14.0f;
+    c->qual_scale = 0.01f * static_cast<float>(INT_MAX) / (c->add_hit * static_cast<float>(kMaxCca));
+    c->inv_max_curvature = 900.0f;
+    c->use_dropout = 1;
+    c->dropout_dcurv_m = 0.007f;
+    c->force_dropout_max_curv_m = 0.03f;
+    c->best_hit_frac = 0.49f;
+    c->tight_bid_cot_threshold = 1.0f;
+    c->n_phi_bins = 128;
+    c->max_num_neighbours = 10;
+    c->minLevel = 3;
+    c->max_edges_factor = 10;
+    c->edge_bidding_rounds = 5;
+    c->volume_shift = 52;
+    c->volume_bits = 12;
+    c->index_shift = 27;
+    c->index_bits = 21;
+}
+
+extern "C" seedgb_status seedgb_gbts_create(const seedgb_gbts_config* config,
+                                            const seedgb_gbts_layer* layers, uint32_t n_layers,
+                                            const uint32_t* bin_pairs, uint32_t n_pairs,
+                                            const seedgb_gbts_geoid* geoids, uint32_t n_geoids,
+                                            float min_pt, const float* tau_lut, uint32_t n_tau_lut,
+                                            seedgb_gbts** out) {
+    if (!config || !out || (n_layers && !layers) || (n_pairs && !bin_pairs) ||
+        (n_geoids && !geoids))
+        return SEEDGB_INVALID_ARGUMENT;
+    *out = nullptr;
+    seedgb_gbts_config c = *config;
+    if (n_layers == 0 || c.n_phi_bins == 0 || c.max_num_neighbours == 0 ||
+        c.max_num_neighbours > 255 || c.max_edges_factor == 0 || !(min_pt > 0.0f))
+        return SEEDGB_BAD_CONFIG;
+    if (c.useTauLUT && (!tau_lut || n_tau_lut % 5 != 0 || c.tauLutSize > n_tau_lut))
+        return SEEDGB_BAD_CONFIG;
+    std::vector<int16_t> vmap;
+    std::vector<uint32_t> smap;
+    if (!linking(c, min_pt, geoids, n_geoids, vmap, smap)) return SEEDGB_BAD_CONFIG;
+    for (uint32_t i = 0; i < n_geoids; ++i)
+        if (geoids[i].layer < 0 || static_cast<uint32_t>(geoids[i].layer) >= n_layers)
+            return SEEDGB_BAD_CONFIG;
+    uint32_t n_eta = 0;
+    std::vector<int8_t> type(n_layers);
+    std::vector<uint32_t> bin0(n_layers), neta(n_layers);
+    std::vector<float> mine(n_layers), width(n_layers);
+    for (uint32_t l = 0; l < n_layers; ++l) {
+        if (layers[l].n_eta_bins == 0) return SEEDGB_BAD_CONFIG;
+        type[l] = static_cast<int8_t>(layers[l].type);
+        bin0[l] = layers[l].eta_bin0;
+        neta[l] = layers[l].n_eta_bins;
+        mine[l] = layers[l].min_eta;
+        width[l] = layers[l].eta_bin_width;
+        n_eta = std::max(n_eta, layers[l].eta_bin0 + layers[l].n_eta_bins);
+    }
+    if (static_cast<uint64_t>(n_eta) * c.n_phi_bins >= 0xFFFFFFF0ull) return SEEDGB_BAD_CONFIG;
+    std::vector<uint32_t> deg(n_eta, 0);
+    for (uint32_t p = 0; p < n_pairs; ++p) {
+        if (bin_pairs[2 * p] >= n_eta || bin_pairs[2 * p + 1] >= n_eta) return SEEDGB_BAD_CONFIG;
+        deg[bin_pairs[2 * p]]++;
+    }
+    auto* h = new seedgb_gbts();
+    h->cfg = c;
+    h->n_layers = n_layers;
+    h->n_eta = n_eta;
+    h->n_pairs = n_pairs;
+    h->n_volumes = static_cast<uint32_t>(vmap.size());
+    h->n_surfaces = static_cast<uint32_t>(smap.size() / 2);
+    h->n_tau = c.useTauLUT ? n_tau_lut : 0;
+    h->max_first_degree = n_eta ? *std::max_element(deg.begin(), deg.end()) : 0;
+    std::vector<float> lut(tau_lut && c.useTauLUT ? tau_lut : nullptr,
+                           tau_lut && c.useTauLUT ? tau_lut + n_tau_lut : nullptr);
+    const bool ok = upload(&h->d_type, type.data(), type.size()) &&
+                    upload(&h->d_bin0, bin0.data(), bin0.size()) &&
+                    upload(&h->d_neta, neta.data(), neta.size()) &&
+                    upload(&h->d_min_eta, mine.data(), mine.size()) &&
+                    upload(&h->d_width, width.data(), width.size()) &&
+                    upload(&h->d_pairs, bin_pairs, 2ull * n_pairs) &&
+                    upload(&h->d_vmap, vmap.data(), vmap.size()) &&
+                    upload(&h->d_smap, smap.data(), smap.size()) &&
+                    upload(&h->d_lut, lut.data(), lut.size()) &&
+                    cudaMalloc(reinterpret_cast<void**>(&h->d_sz), sizeof(uint32_t) * S_COUNT) == cudaSuccess &&
+                    cudaMallocHost(reinterpret_cast<void**>(&h->h_sz), sizeof(uint32_t) * S_COUNT) == cudaSuccess;
+    if (!ok) {
+        free_tables(h);
+        delete h;
+        return SEEDGB_CUDA_ERROR;
+    }
+    std::memset(h->h_sz, 0, sizeof(uint32_t) * S_COUNT);
+    cudaMemset(h->d_sz, 0, sizeof(uint32_t) * S_COUNT);
+    *out = h;
+    return SEEDGB_OK;
+}
+
+extern "C" seedgb_status seedgb_gbts_destroy(seedgb_gbts* h) {
+    if (!h) return SEEDGB_INVALID_ARGUMENT;
+    cudaDeviceSynchronize();
+    free_tables(h);
+    delete h;
+    return SEEDGB_OK;
+}
+
+extern "C" seedgb_status seedgb_gbts_get_config(const seedgb_gbts* h, seedgb_gbts_config* config,
+                                                uint32_t* n_eta_bins, uint32_t* n_volumes,
+                                                uint32_t* n_surfaces) {
+    if (!h) return SEEDGB_INVALID_ARGUMENT;
+    if (config) *config = h->cfg;
+    if (n_eta_bins) *n_eta_bins = h->n_eta;
+    if (n_volumes) *n_volumes = h->n_volumes;
+    if (n_surfaces) *n_surfaces = h->n_surfaces;
+    return SEEDGB_OK;
+}
+
+extern "C" seedgb_status seedgb_gbts_run(seedgb_gbts* h, const seedgb_spacepoint_view* sps,
+                                         const uint64_t* surface_link, const float* diameter,
+                                         uint32_t n_meas, seedgb_seed_buffer* out, void* stream) {
+    if (!h || !sps || !out || !out->size || (sps->size && (!sps->global || !sps->measurement_index_1)) ||
+        (n_meas && (!surface_link || !diameter)) ||
+        (out->capacity && (!out->bottom_index || !out->middle_index || !out->top_index || !out->quality)))
+        return SEEDGB_INVALID_ARGUMENT;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    h->last = s;
+    if (cudaMemsetAsync(h->d_sz, 0, sizeof(uint32_t) * S_COUNT, s) != cudaSuccess) return SEEDGB_CUDA_ERROR;
+    const uint32_t n_sp = sps->size;
+    if (n_sp == 0) {
+        k_empty_out<<<1, 1, 0, s>>>(*out);
+        return cudaGetLastError() == cudaSuccess ? SEEDGB_OK : SEEDGB_CUDA_ERROR;
+    }
+    const uint64_t items_cap = static_cast<uint64_t>(h->n_pairs) +
+                               static_cast<uint64_t>(h->max_first_degree) * ((n_sp + kNodeBuffer - 1) / kNodeBuffer);
+    if (n_sp > h->a_sp || items_cap > h->a_e) {
+        Work tmp{};
+        const size_t need = carve_a(h, nullptr, n_sp, items_cap, tmp);
+        if (!h->arena_a.ensure(need)) return SEEDGB_CUDA_ERROR;
+        h->a_sp = n_sp;
+        h->a_e = items_cap;
+    }
+    Work& w = h->w;
+    carve_a(h, static_cast<char*>(h->arena_a.p), h->a_sp, h->a_e, w);
+    w.sz = h->d_sz;
+    const Tables T = tables_of(h);
+    const uint64_t N = n_sp;
+    const uint64_t E = w.ecap;  // edge capacity: max_edges_factor x arena spacepoints
+    const uint32_t cells = h->n_eta * h->cfg.n_phi_bins;
+    uint32_t* tile_total = h->d_sz + S_TMP;
+    // nodes
+    cudaMemsetAsync(w.cell_cnt, 0, sizeof(uint32_t) * (cells + 1ull), s);
+    cudaMemsetAsync(w.cell_cur, 0, sizeof(uint32_t) * (cells + 1ull), s);
+    k_classify<<<blocks(N), kThreads, 0, s>>>(T, *sps, surface_link, diameter, n_meas, w);
+    scan(w.cell_cnt, w.cell_off, nullptr, cells, 0, cells + 1ull, w.tile, tile_total, h->d_sz + S_NODES, s);
+    k_scatter<<<blocks(N), kThreads, 0, s>>>(n_sp, w);
+    k_sort_cells<<<blocks(cells), kThreads, 0, s>>>(cells, w);
+    k_node_params<<<blocks(N), kThreads, 0, s>>>(T, w);
+    k_eta_bins<<<blocks(32ull * h->n_eta), kThreads, 0, s>>>(h->n_eta, h->cfg.n_phi_bins, w);
+    // work items
+    k_items_count<<<blocks(h->n_pairs), kThreads, 0, s>>>(T, w);
+    scan(w.item_cnt, w.item_off, nullptr, h->n_pairs, 0, h->n_pairs + 1ull, w.tile, tile_total,
+         h->d_sz + S_ITEMS, s);
+    k_items_fill<<<blocks(h->n_pairs), kThreads, 0, s>>>(T, w);
+    // edges: count per item, scan, write in canonical order
+    const uint32_t edge_grid = 152u * 16u;
+    k_edges<false><<<edge_grid, kEdgeThreads, 0, s>>>(T, w);
+    scan(w.item_ecnt, w.item_ebase, h->d_sz + S_ITEMS, 0, 0, h->a_e + 1, w.tile, tile_total,
+         h->d_sz + S_EDGES_MADE, s);
+    cudaMemsetAsync(w.out_cnt, 0, sizeof(uint32_t) * (N + 1), s);
+    k_edges<true><<<edge_grid, kEdgeThreads, 0, s>>>(T, w);
+    // the edges leaving each node: offsets by inner node
+    scan(w.out_cnt, w.lstart, h->d_sz + S_NODES, 0, 0, N + 1, w.tile, tile_total, nullptr, s);
+    cudaMemsetAsync(w.lcur, 0, sizeof(uint32_t) * (N + 1), s);
+    // first sync: kept edge count, nodes
+    if (cudaMemcpyAsync(h->h_sz, h->d_sz, sizeof(uint32_t) * S_COUNT, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+        return SEEDGB_CUDA_ERROR;
+    const uint64_t nodes = h->h_sz[S_NODES];
+    const uint64_t made = h->h_sz[S_EDGES_MADE];
+    const uint32_t n_edges = static_cast<uint32_t>(
+        std::min<uint64_t>({made, static_cast<uint64_t>(h->cfg.max_edges_factor) * nodes, E}));
+    if (n_edges == 0) {
+        k_empty_out<<<1, 1, 0, s>>>(*out);
+        return cudaGetLastError() == cudaSuccess ? SEEDGB_OK : SEEDGB_CUDA_ERROR;
+    }
+    k_link_fill<<<blocks(n_edges), kThreads, 0, s>>>(w, n_edges);
+    k_link_sort<<<blocks(nodes), kThreads, 0, s>>>(w);
+    cudaMemsetAsync(w.kept, 0, sizeof(uint32_t) * n_edges, s);
+    k_match<<<blocks(n_edges), kThreads, 0, s>>>(T, w, n_edges);
+    scan(w.kept, w.kbase, nullptr, n_edges, 0, n_edges + 1ull, w.tile, tile_total, h->d_sz + S_CONNECTED, s);
+    k_compress<<<blocks(n_edges), kThreads, 0, s>>>(T, w, n_edges);
+    // automaton over the connected edges (at most n_edges)
+    cudaMemsetAsync(w.levels, 1, static_cast<size_t>(2 * E), s);
+    for (uint32_t it = 0; it < kMaxCca; ++it) k_cca<<<blocks(n_edges), kThreads, 0, s>>>(T, w, it);
+    k_term_flags<<<blocks(n_edges), kThreads, 0, s>>>(w);
+    scan(w.tflag, w.tidx, h->d_sz + S_CONNECTED, 0, 0, n_edges + 1ull, w.tile, tile_total, h->d_sz + S_TERMINUS, s);
+    scan(w.tpaths, w.pbase, h->d_sz + S_CONNECTED, 0, 0, n_edges + 1ull, w.tile, tile_total, h->d_sz + S_PATHS, s);
+    // second sync: the path store's size
+    if (cudaMemcpyAsync(h->h_sz, h->d_sz, sizeof(uint32_t) * S_COUNT, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+        return SEEDGB_CUDA_ERROR;
+    const uint64_t n_term = h->h_sz[S_TERMINUS], n_paths = h->h_sz[S_PATHS];
+    if (n_term == 0 || n_paths == 0) {
+        k_empty_out<<<1, 1, 0, s>>>(*out);
+        return cudaGetLastError() == cudaSuccess ? SEEDGB_OK : SEEDGB_CUDA_ERROR;
+    }
+    {
+        Work tmp{};
+        const size_t need = carve_b(nullptr, n_term, n_paths, tmp);
+        if (!h->arena_b.ensure(need)) return SEEDGB_CUDA_ERROR;
+        carve_b(static_cast<char*>(h->arena_b.p), n_term, n_paths, w);
+    }
+    k_term_fill<<<blocks(n_edges), kThreads, 0, s>>>(w);
+    k_dfs<<<blocks(n_term), kThreads, 0, s>>>(T, w);
+    k_fit<<<blocks(n_paths), kThreads, 0, s>>>(T, w);
+    scan(w.fflag, w.fidx, h->d_sz + S_PATHS, 0, 0, n_paths + 1, w.tile_b, tile_total, h->d_sz + S_PROPS, s);
+    k_props<<<blocks(n_paths), kThreads, 0, s>>>(w);
+    // bidding: the fit's one-edge bids, then the rounds
+    cudaMemsetAsync(w.ebid, 0, sizeof(unsigned long long) * n_edges, s);
+    k_bid<<<blocks(n_paths), kThreads, 0, s>>>(w, 1);
+    for (uint32_t r = 0; r < h->cfg.edge_bidding_rounds; ++r) {
+        cudaMemsetAsync(w.ebid, 0, sizeof(unsigned long long) * n_edges, s);
+        k_round<<<blocks(n_paths), kThreads, 0, s>>>(w, r == 0 ? 1 : 0);
+        k_bid<<<blocks(n_paths), kThreads, 0, s>>>(w, -1);
+        k_reset<<<blocks(n_paths), kThreads, 0, s>>>(w);
+    }
+    cudaMemsetAsync(w.hbid, 0, sizeof(unsigned long long) * N, s);
+    k_hit_bids<<<blocks(n_paths), kThreads, 0, s>>>(T, w);
+    k_convert<<<blocks(n_paths), kThreads, 0, s>>>(T, w);
+    scan(w.ecount, w.eoff, h->d_sz + S_PROPS, 0, 0, n_paths + 1, w.tile_b, tile_total, h->d_sz + S_SEEDS, s);
+    k_seeds_out<<<blocks(n_paths), kThreads, 0, s>>>(w, *out);
+    return cudaGetLastError() == cudaSuccess ? SEEDGB_OK : SEEDGB_CUDA_ERROR;
+}
+
+extern "C" seedgb_status seedgb_gbts_last_status(seedgb_gbts* h, void* stream) {
+    if (!h) return SEEDGB_INVALID_ARGUMENT;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (cudaMemcpyAsync(h->h_sz, h->d_sz, sizeof(uint32_t) * S_COUNT, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+        return SEEDGB_CUDA_ERROR;
+    if (h->h_sz[S_BAD_INPUT]) return SEEDGB_INVALID_ARGUMENT;
+    return static_cast<seedgb_status>(h->h_sz[S_STATUS]);
+}
+
+extern "C" seedgb_status seedgb_gbts_counters(seedgb_gbts* h, uint64_t* counters) {
+    if (!h || !counters) return SEEDGB_INVALID_ARGUMENT;
+    if (cudaMemcpyAsync(h->h_sz, h->d_sz, sizeof(uint32_t) * S_COUNT, cudaMemcpyDeviceToHost, h->last) != cudaSuccess ||
+        cudaStreamSynchronize(h->last) != cudaSuccess)
+        return SEEDGB_CUDA_ERROR;
+    const uint32_t* z = h->h_sz;
+    counters[0] = z[S_NODES];
+    counters[1] = z[S_EDGES_MADE];
+    counters[2] = z[S_CONN];
+    counters[3] = z[S_CONNECTED];
+    counters[4] = z[S_TERMINUS];
+    counters[5] = z[S_PATHS];
+    counters[6] = z[S_PROPS];
+    counters[7] = z[S_REJECTED];
+    counters[8] = z[S_SEEDS];
+    return SEEDGB_OK;
+}

@@ -214,3 +214,110 @@ seedgb_status seedgb_csv_read_measurements(const char* meas_path, uint64_t capac
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// The GBTS configuration directory, whitespace-separated like the reference's
+// stream reads (examples/options/src/track_gbts_seeding.cpp:158-226):
+//   geoidBinning.txt  n, then n x (barcode, layer)
+//   binTables.txt     n, then n x (bin1, bin2)
+//   layerInfo.txt     n, then n x (type, first eta bin, eta bins, min eta, eta bin width)
+// ---------------------------------------------------------------------------
+namespace {
+
+class Tokens {
+public:
+    explicit Tokens(const std::string& path) {
+        FILE* f = std::fopen(path.c_str(), "rb");
+        if (!f) return;
+        ok_ = true;
+        std::string cur;
+        int c;
+        while ((c = std::fgetc(f)) != EOF) {
+            if (c == ' ' || c == '\t' || c == '\n' || c == '\r') {
+                if (!cur.empty()) toks_.push_back(cur);
+                cur.clear();
+            } else {
+                cur.push_back(static_cast<char>(c));
+            }
+        }
+        if (!cur.empty()) toks_.push_back(cur);
+        std::fclose(f);
+    }
+    bool ok() const { return ok_; }
+    bool u64(uint64_t& v) {
+        if (i_ >= toks_.size()) return false;
+        const char* s = toks_[i_].c_str();
+        if (*s == '-') return false;
+        char* end = nullptr;
+        errno = 0;
+        v = std::strtoull(s, &end, 10);
+        return errno == 0 && end && *end == '\0' && (++i_, true);
+    }
+    bool i64(int64_t& v) {
+        if (i_ >= toks_.size()) return false;
+        char* end = nullptr;
+        errno = 0;
+        v = std::strtoll(toks_[i_].c_str(), &end, 10);
+        return errno == 0 && end && *end == '\0' && (++i_, true);
+    }
+    bool f32(float& v) {
+        if (i_ >= toks_.size()) return false;
+        char* end = nullptr;
+        errno = 0;
+        v = std::strtof(toks_[i_].c_str(), &end);
+        return errno == 0 && end && *end == '\0' && (++i_, true);
+    }
+
+private:
+    std::vector<std::string> toks_;
+    size_t i_ = 0;
+    bool ok_ = false;
+};
+
+}  // namespace
+
+extern "C" seedgb_status seedgb_gbts_read_config_dir(const char* dir, seedgb_gbts_layer* layers,
+                                                     uint32_t* n_layers, uint32_t* bin_pairs,
+                                                     uint32_t* n_pairs, seedgb_gbts_geoid* geoids,
+                                                     uint32_t* n_geoids) {
+    if (!dir || !n_layers || !n_pairs || !n_geoids) return SEEDGB_INVALID_ARGUMENT;
+    const std::string d(dir);
+    Tokens g(d + "/geoidBinning.txt"), b(d + "/binTables.txt"), l(d + "/layerInfo.txt");
+    if (!g.ok() || !b.ok() || !l.ok()) return SEEDGB_INVALID_ARGUMENT;
+    uint64_t ng, nb, nl;
+    if (!g.u64(ng) || !b.u64(nb) || !l.u64(nl) || ng > 0xFFFFFFFFull || nb > 0xFFFFFFFFull ||
+        nl > 0xFFFFFFFFull)
+        return SEEDGB_INVALID_ARGUMENT;
+    const bool fill = layers && bin_pairs && geoids;
+    if (fill && (*n_layers < nl || *n_pairs < nb || *n_geoids < ng)) return SEEDGB_INVALID_ARGUMENT;
+    for (uint64_t i = 0; i < ng; ++i) {
+        uint64_t id;
+        int64_t layer;
+        if (!g.u64(id) || !g.i64(layer) || layer < INT16_MIN || layer > INT16_MAX)
+            return SEEDGB_INVALID_ARGUMENT;
+        if (fill) geoids[i] = seedgb_gbts_geoid{id, static_cast<int32_t>(layer)};
+    }
+    for (uint64_t i = 0; i < nb; ++i) {
+        uint64_t b1, b2;
+        if (!b.u64(b1) || !b.u64(b2) || b1 > 0xFFFFFFFFull || b2 > 0xFFFFFFFFull)
+            return SEEDGB_INVALID_ARGUMENT;
+        if (fill) {
+            bin_pairs[2 * i] = static_cast<uint32_t>(b1);
+            bin_pairs[2 * i + 1] = static_cast<uint32_t>(b2);
+        }
+    }
+    for (uint64_t i = 0; i < nl; ++i) {
+        uint64_t type, b0, n;
+        float mn, wd;
+        if (!l.u64(type) || !l.u64(b0) || !l.u64(n) || !l.f32(mn) || !l.f32(wd) || type > 255 ||
+            b0 > 0xFFFFFFFFull || n > 0xFFFFFFFFull)
+            return SEEDGB_INVALID_ARGUMENT;
+        if (fill)
+            layers[i] = seedgb_gbts_layer{static_cast<int32_t>(static_cast<int8_t>(type)),
+                                          static_cast<uint32_t>(b0), static_cast<uint32_t>(n), mn, wd};
+    }
+    *n_geoids = static_cast<uint32_t>(ng);
+    *n_pairs = static_cast<uint32_t>(nb);
+    *n_layers = static_cast<uint32_t>(nl);
+    return SEEDGB_OK;
+}

@@ -398,21 +398,29 @@ class SpacepointCollection:
 
 
 class MeasurementCollection:
-    """The measurement columns parameter estimation reads: local_position
-    (M, 2 f32) and surface_link (u64, stored as int64)."""
+    """The measurement columns the path reads: local_position (M, 2 f32),
+    surface_link (u64, stored as int64) and, for GBTS seeding, the cluster
+    diameter (M f32, optional)."""
 
-    def __init__(self, local_position, surface_link):
+    def __init__(self, local_position, surface_link, diameter=None):
         self.local_position = local_position
         self.surface_link = surface_link
+        self.diameter = diameter
 
     @classmethod
     def from_numpy(cls, ev, device="cuda"):
         torch = _torch()
-        lp = torch.from_numpy(np.ascontiguousarray(ev["local_position"], np.float32)
-                              .reshape(-1, 2)).to(device)
         sl = torch.from_numpy(np.ascontiguousarray(ev["surface_link"], np.uint64)
                               .view(np.int64)).to(device)
-        return cls(lp, sl)
+        if "local_position" in ev:
+            lp = torch.from_numpy(np.ascontiguousarray(ev["local_position"], np.float32)
+                                  .reshape(-1, 2)).to(device)
+        else:
+            lp = torch.zeros((sl.shape[0], 2), dtype=torch.float32, device=device)
+        dia = None
+        if "diameter" in ev:
+            dia = torch.from_numpy(np.ascontiguousarray(ev["diameter"], np.float32)).to(device)
+        return cls(lp, sl, dia)
 
     def view(self) -> _MeasurementView:
         return _MeasurementView(self.local_position.data_ptr(),
