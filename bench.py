@@ -86,7 +86,8 @@ def parse():
     p.add_argument("--no-learned", action="store_true",
                    help="skip training and timing the learned doublet filter")
     p.add_argument("--filter-events", type=int, default=FILTER_TRAIN_EVENTS)
-    p.add_argument("--profile-case", choices=["plain4", "plain20", "learned4", "train", "batch64"],
+    p.add_argument("--profile-case", choices=["plain4", "plain20", "learned4", "train", "batch64",
+                                              "gbts1"],
                    help="run one small fixed workload for an ncu capture and exit")
     return p.parse_args()
 
@@ -489,6 +490,92 @@ def run_formation(args, stream, meas, n_sp_total):
                       "seedgb_formation_run_batch call for the step's events (median of "
                       f"{reps}); per event: the seedgb_form_spacepoints calls summed over the "
                       f"events (mean of {reps})"}
+
+
+GBTS_EDGES_FACTOR = 40
+
+
+def gbts_setup(events):
+    """GBTS on the synthetic barrel: layer table, linked eta bins and
+    geometry-id binning from synth.gbts_geometry (10 barrel layers, 0.2 eta
+    bins), the reference's default cuts at min_pt 900 MeV with
+    max_edges_factor 40 (the reference default of 10 truncates the graph of
+    a 100k-spacepoint event of this 10-layer detector), per-measurement
+    barcodes and cluster diameters from synth.gbts_measurements."""
+    from traccc_gb300 import gbts, seeding, synth
+    layers, pairs, geoid = synth.gbts_geometry()
+    cfg = gbts.config_default()
+    cfg.max_edges_factor = GBTS_EDGES_FACTOR
+    alg = gbts.GbtsSeedingAlgorithm(cfg, layers, pairs, geoid, min_pt=900.0)
+    data, host = [], []
+    for s, ev in enumerate(events):
+        link, dia = synth.gbts_measurements(ev, s)
+        host.append((ev, link, dia))
+        data.append((seeding.SpacepointCollection.from_numpy(ev),
+                     seeding.MeasurementCollection.from_numpy(dict(surface_link=link,
+                                                                   diameter=dia))))
+    outs = [seeding.SeedBuffer(alg.max_seeds(len(ev["global"]))) for ev in events]
+    return alg, data, outs, host, (layers, pairs, geoid, cfg)
+
+
+def run_gbts(args, stream, flush_buf, events):
+    """GBTS seeding (the alternative seeder on the same spacepoints) of the
+    step's 20 events, one seedgb_gbts_run call per event: events/s over the
+    timed steps (CUDA events on the launching stream around each step,
+    which include the two waits per call for the path-store size), the first
+    event's seeds against the oracle, and the oracle's own time for one
+    event on one host thread."""
+    import torch
+
+    import oracle
+    alg, data, outs, host, (layers, pairs, geoid, cfg) = gbts_setup(events)
+    sptr = stream.cuda_stream
+
+    def step():
+        for (sp, m), o in zip(data, outs):
+            alg(sp, m, o, stream=sptr)
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    steps = max(1, min(args.steps, 10))
+    ms = []
+    for _ in range(steps):
+        flush_buf.fill_(1)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        step()
+        e1.record(stream)
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    counters = alg.counters()  # of the last event
+    status = alg.last_status(stream=sptr)
+    got = outs[0].to_numpy()
+    ev, link, dia = host[0]
+    oc = oracle.GbtsConfig()
+    import ctypes as C
+    C.memmove(C.byref(oc), C.byref(cfg), C.sizeof(oc))
+    t0 = time.perf_counter()
+    ref, rctr = oracle.gbts(ev, link, dia, layers, pairs, geoid, cfg=oc, min_pt=900.0)
+    cpu_s = time.perf_counter() - t0
+    same = bool(len(got) == len(ref) and all(np.array_equal(got[k], ref[k]) for k in
+                                             ("bottom", "middle", "top")) and
+                np.array_equal(got["quality"].view(np.uint32), ref["quality"].view(np.uint32)))
+    n_ev = len(events)
+    med = statistics.median(ms)
+    return {"workload": f"pileup9k: the step's {n_ev} events; GBTS on the synthetic barrel "
+                        f"(10 layers, 0.2 eta bins, {len(pairs)} linked bin pairs), reference "
+                        f"default cuts at min_pt 900 MeV, max_edges_factor {GBTS_EDGES_FACTOR}",
+            "value": 1e3 * n_ev / med, "unit": "events/s", "ms_per_step": med,
+            "ms_per_event": med / n_ev, "status": int(status),
+            "last_event_counters": counters,
+            "parity": {"event0_seeds_bit_exact": same, "seeds": len(got),
+                       "oracle_seeds": len(ref), "against": "the C oracle (parity unpinned: "
+                                                            "the reference has no GBTS tests)"},
+            "cpu_oracle": {"s_per_event": cpu_s, "events_per_s": 1.0 / cpu_s, "cores": 1,
+                           "sample": "event 0, one host thread"},
+            "timing": f"median of {steps} steps, each the {n_ev} per-event calls back to back "
+                      "on one stream, L2 flushed before each step; CUDA events on the stream"}
 
 
 FILTER_TRAIN_SEED0 = 1000
@@ -922,6 +1009,7 @@ def run_gpu(args):
 
     trk1000 = run_trk1000(args, stream, flush_buf) if world == 1 else None
     formation = run_formation(args, stream, meas, total) if world == 1 else None
+    gbts_line = run_gbts(args, stream, flush_buf, events) if world == 1 else None
 
     learned_line = None
     batched = None
@@ -1086,6 +1174,8 @@ def run_gpu(args):
         line["trk1000"] = trk1000
     if formation is not None:
         line["formation"] = formation
+    if gbts_line is not None:
+        line["gbts"] = gbts_line
     if learned_line is not None:
         line["learned"] = learned_line
     if batched is not None:
@@ -1114,6 +1204,7 @@ def run_gpu(args):
 #   train     one gradient step of the filter's network on the doublets of
 #             4 events (the tensor-core training kernel)
 #   batch64   one graph launch of the 64-event uneven batch
+#   gbts1     GBTS seeding of one event of the 100k-spacepoint workload
 # ---------------------------------------------------------------------------
 
 def _events(n, seed0=0):
@@ -1209,8 +1300,19 @@ def case_batch64():
     assert alg.last_status() == seeding.OK
 
 
-PROFILE_CASES = {"plain4": case_plain4, "plain20": case_plain20, "learned4": case_learned4, "train": case_train,
-         "batch64": case_batch64}
+def case_gbts1():
+    import torch
+    alg, data, outs, _, _ = gbts_setup(_events(1))
+    (sp, m), o = data[0], outs[0]
+    for _ in range(2):
+        alg(sp, m, o)
+    _range(torch, lambda: alg(sp, m, o))
+    assert alg.last_status() == 0
+    print(alg.counters())
+
+
+PROFILE_CASES = {"plain4": case_plain4, "plain20": case_plain20, "learned4": case_learned4,
+                 "train": case_train, "batch64": case_batch64, "gbts1": case_gbts1}
 
 
 def main():

@@ -6,8 +6,9 @@
  * one canonical order wherever the reference's output depends on the order
  * in which its atomics land:
  *   - nodes of one (eta, phi) cell in ascending spacepoint index;
- *   - edges by (work item, outer node, inner node), work items in bin-table
- *     order, each bin-1 chunk of at most 128 nodes its own work item;
+ *   - edges by (work item, thread, outer node, inner node): work items in
+ *     bin-table order, each bin-1 chunk of at most 128 nodes its own work
+ *     item; 128 threads per item, thread t taking outer nodes t, t + 128, ...;
  *   - the edges leaving a node in ascending edge index; the first
  *     max_num_neighbours matches kept;
  *   - connected edges numbered in ascending edge index;
@@ -408,8 +409,8 @@ static void push(u32vec* v, uint32_t x) {
 
 /* one work item of gbts_make_graph_edges (gbts_make_graph_edges.ipp:104-239):
  * 128 threads, thread t taking the outer nodes t, t + 128, ... with its own
- * sliding-window start; the candidates found are recorded per outer node in
- * inner-node order */
+ * sliding-window start; edges in thread order, then outer node, then inner
+ * node (the order the thread finds them in) */
 static void make_edges_item(const or_gbts_config* c, const f4* np, const float* nphi,
                             uint32_t b1, uint32_t e1, uint32_t b2, uint32_t e2, float deltaPhi,
                             u32vec* en1, u32vec* en2, u32vec* ep) {
@@ -418,10 +419,6 @@ static void make_edges_item(const or_gbts_config* c, const f4* np, const float* 
     const float phiN = nphi[b1 + n1 - 1u];
     const float phi_bin_width = TWO_PI_F / (float)c->n_phi_bins;
     const float break_threshold = deltaPhi + phi_bin_width - PI_F;
-    /* per outer node: the inner nodes it pairs with, in the thread's order */
-    u32vec* per = (u32vec*)calloc(n2 ? n2 : 1, sizeof(u32vec));
-    float (*prm)[4] = NULL;
-    size_t nprm = 0, cprm = 0;
     for (uint32_t t = 0; t < EDGE_THREADS; ++t) {
         uint32_t last_n1 = 0u;
         for (uint32_t n2Idx = t; n2Idx < n2; n2Idx += EDGE_THREADS) {
@@ -460,33 +457,17 @@ static void make_edges_item(const or_gbts_config* c, const f4* np, const float* 
                 last_n1 = n1Idx;
                 float e[4];
                 if (edge_candidate(np[b1 + n1Idx], np2, phi1, phi2, deltaPhi, c, e)) {
-                    if (nprm == cprm) {
-                        cprm = cprm ? 2 * cprm : 256;
-                        prm = (float (*)[4])realloc(prm, cprm * sizeof(*prm));
+                    push(en1, b1 + n1Idx);
+                    push(en2, g2);
+                    for (int q = 0; q < 4; ++q) {
+                        uint32_t bits;
+                        memcpy(&bits, &e[q], 4);
+                        push(ep, bits);
                     }
-                    memcpy(prm[nprm], e, sizeof(e));
-                    push(&per[n2Idx], b1 + n1Idx);
-                    push(&per[n2Idx], (uint32_t)nprm);
-                    ++nprm;
                 }
             }
         }
     }
-    for (uint32_t k = 0; k < n2; ++k) {
-        for (size_t j = 0; j < per[k].n; j += 2) {
-            push(en1, per[k].data[j]);
-            push(en2, b2 + k);
-            const float* e = prm[per[k].data[j + 1]];
-            for (int q = 0; q < 4; ++q) {
-                uint32_t bits;
-                memcpy(&bits, &e[q], 4);
-                push(ep, bits);
-            }
-        }
-        free(per[k].data);
-    }
-    free(per);
-    free(prm);
 }
 
 int or_gbts_run(const or_gbts_config* c, const or_gbts_tables* t, uint32_t n_sp,

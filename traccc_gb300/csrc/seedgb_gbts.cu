@@ -49,16 +49,23 @@ constexpr int kEdgeThreads = 128;       // threads of one edge work item
 constexpr int kThreads = 256;
 constexpr int kScanThreads = 1024;
 constexpr uint32_t kScanTile = 4u * kScanThreads;
+constexpr uint64_t kSmallScan = 1u << 14;  // one-block scan up to this capacity
 constexpr float kPi = 3.14159265358979323846f;
 constexpr float kTwoPi = 2.0f * kPi;
 constexpr uint32_t kInvalid = 0xFFFFFFFFu;
 constexpr int32_t kPathCountLimit = 1 << 30;
+constexpr uint32_t kGrid = 152u * 8u;  // grid-stride kernels: 8 blocks per SM
+
+#define GRID_STRIDE(i, n) \
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < (n); i += gridDim.x * blockDim.x)
 
 // device-resident sizes and status of one run
 enum Size : uint32_t {
     S_NODES = 0,
     S_ITEMS,
+    S_SLOTS,
     S_EDGES_MADE,
+    S_EDGES,
     S_CONN,
     S_CONNECTED,
     S_TERMINUS,
@@ -103,11 +110,11 @@ struct Work {
     uint32_t *item_cnt, *item_off;
     uint4* items;
     float* item_dphi;
-    uint32_t *item_ecnt, *item_ebase;
+    uint32_t *item_tcnt, *item_toff;  // edges per (item, thread) and their offsets
     // edges
     uint32_t *e_in, *e_out;
     float4* e_p;
-    uint32_t *out_cnt, *lstart, *lcur, *links;
+    uint32_t *out_cnt, *lstart, *lcur, *links, *links_tmp;
     uint8_t* nnei;
     uint32_t *nei, *kept, *kbase;
     // graph and automaton
@@ -238,6 +245,39 @@ k_scan_sums(uint32_t* tile, uint32_t n_tiles, uint32_t* tile_total) {
         __syncthreads();
     }
     if (threadIdx.x == 0) *tile_total = carry;
+}
+
+// the whole scan in one block (small inputs): rounds of 4 x 1024 values
+__global__ void __launch_bounds__(kScanThreads)
+k_scan_small(const uint32_t* in, uint32_t* out, const uint32_t* n_dev, uint32_t n_host,
+             uint32_t add, uint32_t* total_dst) {
+    __shared__ uint32_t carry;
+    const uint32_t n = load_n(n_dev, n_host, add);
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (uint32_t base = 0; base < n; base += kScanTile) {
+        uint32_t v[4];
+        uint32_t sum = 0;
+        for (int j = 0; j < 4; ++j) {
+            const uint32_t i = base + 4u * threadIdx.x + j;
+            v[j] = i < n ? in[i] : 0u;
+            sum += v[j];
+        }
+        uint32_t total;
+        uint32_t run = carry + block_exclusive_scan(sum, &total);
+        for (int j = 0; j < 4; ++j) {
+            const uint32_t i = base + 4u * threadIdx.x + j;
+            if (i < n) out[i] = run;
+            run += v[j];
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) carry += total;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        out[n] = carry;
+        if (total_dst) *total_dst = carry;
+    }
 }
 
 __global__ void __launch_bounds__(kScanThreads)
@@ -488,7 +528,7 @@ template <bool WRITE>
 __device__ __forceinline__ uint32_t walk(const ItemCtx& it, uint32_t n2Idx, uint32_t& last_n1,
                                          bool& done, const float* s_phi, const float4* s_np,
                                          const Work& w, const seedgb_gbts_config& c,
-                                         uint64_t pos, uint64_t cap) {
+                                         uint64_t pos, uint64_t cap, uint32_t* s_cnt) {
     const uint32_t g2 = it.b2 + n2Idx;
     const float phi2 = w.node_phi[g2];
     uint32_t n1Idx = last_n1;
@@ -531,7 +571,7 @@ __device__ __forceinline__ uint32_t walk(const ItemCtx& it, uint32_t n2Idx, uint
                     w.e_in[q] = it.b1 + n1Idx;
                     w.e_out[q] = g2;
                     w.e_p[q] = ep;
-                    atomicAdd(&w.out_cnt[it.b1 + n1Idx], 1u);
+                    atomicAdd(&s_cnt[n1Idx], 1u);
                 }
             }
             ++cnt;
@@ -540,13 +580,19 @@ __device__ __forceinline__ uint32_t walk(const ItemCtx& it, uint32_t n2Idx, uint
     return cnt;
 }
 
+// Edges of one work item, thread t taking the outer nodes t, t + 128, ...
+// with the reference's sliding-window state; an item's edges in thread order,
+// then outer node, then inner node.  The count pass records each thread's
+// edge count; after one scan over (item, thread) the write pass walks again
+// and writes from the thread's offset, no barrier inside the item.
 template <bool WRITE>
 __global__ void __launch_bounds__(kEdgeThreads) k_edges(Tables T, Work w) {
     __shared__ float s_phi[kNodeBuffer];
     __shared__ float4 s_np[kNodeBuffer];
-    __shared__ uint32_t s_red[kEdgeThreads / 32];
+    __shared__ uint32_t s_cnt[kNodeBuffer];  // edges per inner node of the chunk
     const uint32_t t = threadIdx.x;
     const uint32_t n_items = w.sz[S_ITEMS];
+    if (!WRITE && blockIdx.x == 0 && t == 0) w.sz[S_SLOTS] = n_items * kEdgeThreads;
     const uint64_t by_nodes = static_cast<uint64_t>(T.c.max_edges_factor) * w.sz[S_NODES];
     const uint64_t cap = by_nodes < w.ecap ? by_nodes : w.ecap;
     for (uint32_t item = blockIdx.x; item < n_items; item += gridDim.x) {
@@ -562,6 +608,7 @@ __global__ void __launch_bounds__(kEdgeThreads) k_edges(Tables T, Work w) {
             s_np[t] = w.node_p[it.b1 + t];
             s_phi[t] = w.node_phi[it.b1 + t];
         }
+        s_cnt[t] = 0;
         __syncthreads();
         it.phi0 = s_phi[0];
         it.phiN = s_phi[it.n1 - 1u];
@@ -569,66 +616,60 @@ __global__ void __launch_bounds__(kEdgeThreads) k_edges(Tables T, Work w) {
         it.brk = it.dphi + it.pbw - kPi;
         uint32_t last_n1 = 0u;
         bool done = false;
+        const uint64_t slot = static_cast<uint64_t>(item) * kEdgeThreads + t;
+        uint64_t pos = WRITE ? w.item_toff[slot] : 0;
+        uint32_t cnt = 0;
+        for (uint32_t n2Idx = t; n2Idx < n2 && !done; n2Idx += kEdgeThreads)
+            cnt += walk<WRITE>(it, n2Idx, last_n1, done, s_phi, s_np, w, T.c, pos + cnt, cap, s_cnt);
         if (!WRITE) {
-            uint32_t cnt = 0;
-            for (uint32_t n2Idx = t; n2Idx < n2 && !done; n2Idx += kEdgeThreads)
-                cnt += walk<false>(it, n2Idx, last_n1, done, s_phi, s_np, w, T.c, 0, 0);
-            for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
-            if ((t & 31) == 0) s_red[t >> 5] = cnt;
-            __syncthreads();
-            if (t == 0) {
-                uint32_t s = 0;
-                for (int k = 0; k < kEdgeThreads / 32; ++k) s += s_red[k];
-                w.item_ecnt[item] = s;
-            }
+            w.item_tcnt[slot] = cnt;
         } else {
-            uint64_t base = w.item_ebase[item];
-            for (uint32_t r0 = 0; r0 < n2; r0 += kEdgeThreads) {
-                const uint32_t n2Idx = r0 + t;
-                const uint32_t l0 = last_n1;
-                const bool d0 = done;
-                uint32_t c = 0;
-                if (!done && n2Idx < n2)
-                    c = walk<false>(it, n2Idx, last_n1, done, s_phi, s_np, w, T.c, 0, 0);
-                uint32_t tot;
-                const uint32_t off = block_exclusive_scan(c, &tot);
-                last_n1 = l0;
-                done = d0;
-                if (!done && n2Idx < n2)
-                    walk<true>(it, n2Idx, last_n1, done, s_phi, s_np, w, T.c, base + off, cap);
-                base += tot;
-            }
+            __syncthreads();
+            if (t < it.n1 && s_cnt[t]) atomicAdd(&w.out_cnt[it.b1 + t], s_cnt[t]);
         }
     }
 }
 
-// gbts_link_graph_edges.ipp:22-44: the edges leaving each node (by inner node)
-__global__ void __launch_bounds__(kThreads) k_link_fill(Work w, uint32_t n_edges) {
-    const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= n_edges) return;
-    const uint32_t n1 = w.e_in[e];
-    w.links[w.lstart[n1] + atomicAdd(&w.lcur[n1], 1u)] = e;
+// gbts_link_graph_edges.ipp:22-44: the edges leaving each node (by inner
+// node), first in arrival order ...
+// (the kept edges: min(made, max_edges_factor x nodes, capacity))
+__global__ void k_edges_kept(Tables T, Work w) {
+    const uint64_t by_nodes = static_cast<uint64_t>(T.c.max_edges_factor) * w.sz[S_NODES];
+    uint64_t n = w.sz[S_EDGES_MADE];
+    if (by_nodes < n) n = by_nodes;
+    if (w.ecap < n) n = w.ecap;
+    w.sz[S_EDGES] = static_cast<uint32_t>(n);
 }
 
+__global__ void __launch_bounds__(kThreads) k_link_fill(Work w) {
+    GRID_STRIDE(e, w.sz[S_EDGES]) {
+        const uint32_t n1 = w.e_in[e];
+        w.links_tmp[w.lstart[n1] + atomicAdd(&w.lcur[n1], 1u)] = e;
+        w.kept[e] = 0u;
+    }
+}
+
+// ... then in ascending edge index: one warp per node, each edge placed at
+// its rank (the edge indices of a list are distinct)
 __global__ void __launch_bounds__(kThreads) k_link_sort(Work w) {
-    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= w.sz[S_NODES]) return;
-    const uint32_t b = w.lstart[k], e = w.lstart[k + 1];
-    for (uint32_t i = b + 1; i < e; ++i) {
-        const uint32_t v = w.links[i];
-        uint32_t j = i;
-        while (j > b && w.links[j - 1] > v) {
-            w.links[j] = w.links[j - 1];
-            --j;
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t n = w.sz[S_NODES];
+    for (uint32_t k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; k < n;
+         k += (gridDim.x * blockDim.x) >> 5) {
+        const uint32_t b = w.lstart[k], L = w.lstart[k + 1] - b;
+        const uint32_t* src = w.links_tmp + b;
+        for (uint32_t i = lane; i < L; i += 32) {
+            const uint32_t v = src[i];
+            uint32_t r = 0;
+            for (uint32_t j = 0; j < L; ++j) r += src[j] < v;
+            w.links[b + r] = v;
         }
-        w.links[j] = v;
     }
 }
 
 // gbts_match_graph_edges.ipp:29-118
-__global__ void __launch_bounds__(kThreads) k_match(Tables T, Work w, uint32_t n_edges) {
-    const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= n_edges) return;
+__global__ void __launch_bounds__(kThreads) k_match(Tables T, Work w) {
+    GRID_STRIDE(e, w.sz[S_EDGES]) {
     const seedgb_gbts_config& c = T.c;
     const uint32_t M = c.max_num_neighbours;
     const uint32_t shared_node = w.e_out[e];
@@ -660,28 +701,30 @@ __global__ void __launch_bounds__(kThreads) k_match(Tables T, Work w, uint32_t n
         w.kept[e] = 1u;
         atomicAdd(&w.sz[S_CONN], num_nei);
     }
+    }
 }
 
 // gbts_compress_graph.ipp:22-68: rows [outer sp, inner sp, nNei, neighbours]
-__global__ void __launch_bounds__(kThreads) k_compress(Tables T, Work w, uint32_t n_edges) {
-    const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= n_edges || !w.kept[e]) return;
-    const uint32_t M = T.c.max_num_neighbours;
-    uint32_t* row = w.graph + static_cast<uint64_t>(3u + M) * w.kbase[e];
-    row[0] = w.node_sp[w.e_out[e]];
-    row[1] = w.node_sp[w.e_in[e]];
-    const uint32_t nn = w.nnei[e];
-    row[2] = nn;
-    for (uint32_t k = 0; k < nn; ++k) row[3 + k] = w.kbase[w.nei[static_cast<uint64_t>(M) * e + k]];
+__global__ void __launch_bounds__(kThreads) k_compress(Tables T, Work w) {
+    GRID_STRIDE(e, w.sz[S_EDGES]) {
+        if (!w.kept[e]) continue;
+        const uint32_t M = T.c.max_num_neighbours;
+        uint32_t* row = w.graph + static_cast<uint64_t>(3u + M) * w.kbase[e];
+        row[0] = w.node_sp[w.e_out[e]];
+        row[1] = w.node_sp[w.e_in[e]];
+        const uint32_t nn = w.nnei[e];
+        row[2] = nn;
+        for (uint32_t k = 0; k < nn; ++k)
+            row[3 + k] = w.kbase[w.nei[static_cast<uint64_t>(M) * e + k]];
+    }
 }
 
 // ---------------------------------------------------------------------------
 // Longest chains: gbts_run_cca_iteration.ipp:23-101 (one launch per iteration)
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kThreads) k_cca(Tables T, Work w, uint32_t iter) {
-    const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= w.sz[S_CONNECTED]) return;
-    if (iter != 0 && w.active[e] != static_cast<int8_t>(iter)) return;
+    GRID_STRIDE(e, w.sz[S_CONNECTED]) {
+    if (iter != 0 && w.active[e] != static_cast<int8_t>(iter)) continue;
     const uint32_t esz = 3u + T.c.max_num_neighbours;
     const uint32_t* row = w.graph + static_cast<uint64_t>(esz) * e;
     const uint32_t toggle = iter % 2;
@@ -721,25 +764,27 @@ __global__ void __launch_bounds__(kThreads) k_cca(Tables T, Work w, uint32_t ite
         w.opy[e] = static_cast<int16_t>((next_level >= T.c.minLevel) - 1);
     }
     lstore[e] = next_level;
+    }
 }
 
 // gbts_count_terminus_edges.ipp:22-46
 __global__ void __launch_bounds__(kThreads) k_term_flags(Work w) {
-    const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= w.sz[S_CONNECTED]) return;
-    const bool t = w.opy[e] != -1;
-    w.tflag[e] = t ? 1u : 0u;
-    w.tpaths[e] = t ? static_cast<uint32_t>(w.opx[e]) : 0u;
+    GRID_STRIDE(e, w.sz[S_CONNECTED]) {
+        const bool t = w.opy[e] != -1;
+        w.tflag[e] = t ? 1u : 0u;
+        w.tpaths[e] = t ? static_cast<uint32_t>(w.opx[e]) : 0u;
+    }
 }
 
 // gbts_add_terminus_to_path_store.ipp:21-44
 __global__ void __launch_bounds__(kThreads) k_term_fill(Work w) {
-    const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= w.sz[S_CONNECTED] || !w.tflag[e]) return;
-    const uint32_t ti = w.tidx[e];
-    w.store[ti] = make_int2(static_cast<int>(e), -1);
-    w.term_edge[ti] = e;
-    w.term_pos[ti] = w.sz[S_TERMINUS] + w.pbase[e];
+    GRID_STRIDE(e, w.sz[S_CONNECTED]) {
+        if (!w.tflag[e]) continue;
+        const uint32_t ti = w.tidx[e];
+        w.store[ti] = make_int2(static_cast<int>(e), -1);
+        w.term_edge[ti] = e;
+        w.term_pos[ti] = w.sz[S_TERMINUS] + w.pbase[e];
+    }
 }
 
 // gbts_fill_path_store.ipp:24-163 as a depth-first pre-order walk below each
@@ -1209,6 +1254,10 @@ uint32_t blocks(uint64_t n, int threads = kThreads) {
 // exclusive scan helper: n on the device (n_dev + add) or the host; grid for `cap`
 void scan(const uint32_t* in, uint32_t* out, const uint32_t* n_dev, uint32_t n_host, uint32_t add,
           uint64_t cap, uint32_t* tile, uint32_t* tile_total, uint32_t* total_dst, cudaStream_t s) {
+    if (cap <= kSmallScan) {
+        k_scan_small<<<1, kScanThreads, 0, s>>>(in, out, n_dev, n_host, add, total_dst);
+        return;
+    }
     const uint32_t tiles = static_cast<uint32_t>(std::max<uint64_t>(1, (cap + kScanTile - 1) / kScanTile));
     k_scan_tile<<<tiles, kScanThreads, 0, s>>>(in, out, n_dev, n_host, add, tile);
     k_scan_sums<<<1, kScanThreads, 0, s>>>(tile, tiles, tile_total);
@@ -1221,7 +1270,8 @@ size_t carve_a(seedgb_gbts* h, char* base, uint64_t n_sp, uint64_t items_cap, Wo
     const uint64_t E = std::max<uint64_t>(1, static_cast<uint64_t>(h->cfg.max_edges_factor) * N);
     const uint64_t M = h->cfg.max_num_neighbours;
     const uint64_t cells = static_cast<uint64_t>(h->n_eta) * h->cfg.n_phi_bins;
-    const uint64_t scan_cap = std::max<uint64_t>({E + 1, N + 1, cells + 1, items_cap + 1, h->n_pairs + 1ull});
+    const uint64_t scan_cap =
+        std::max<uint64_t>({E + 1, N + 1, cells + 1, items_cap * kEdgeThreads + 1, h->n_pairs + 1ull});
     Carver cv{base};
     w.red = cv.take<float4>(N);
     w.sp_phi = cv.take<float>(N);
@@ -1238,8 +1288,8 @@ size_t carve_a(seedgb_gbts* h, char* base, uint64_t n_sp, uint64_t items_cap, Wo
     w.item_off = cv.take<uint32_t>(h->n_pairs + 1ull);
     w.items = cv.take<uint4>(items_cap);
     w.item_dphi = cv.take<float>(items_cap);
-    w.item_ecnt = cv.take<uint32_t>(items_cap + 1);
-    w.item_ebase = cv.take<uint32_t>(items_cap + 1);
+    w.item_tcnt = cv.take<uint32_t>(items_cap * kEdgeThreads + 1);
+    w.item_toff = cv.take<uint32_t>(items_cap * kEdgeThreads + 1);
     w.e_in = cv.take<uint32_t>(E);
     w.e_out = cv.take<uint32_t>(E);
     w.e_p = cv.take<float4>(E);
@@ -1247,6 +1297,7 @@ size_t carve_a(seedgb_gbts* h, char* base, uint64_t n_sp, uint64_t items_cap, Wo
     w.lstart = cv.take<uint32_t>(N + 1);
     w.lcur = cv.take<uint32_t>(N + 1);
     w.links = cv.take<uint32_t>(E);
+    w.links_tmp = cv.take<uint32_t>(E);
     w.nnei = cv.take<uint8_t>(E);
     w.nei = cv.take<uint32_t>(M * E);
     w.kept = cv.take<uint32_t>(E);
@@ -1559,44 +1610,35 @@ extern "C" seedgb_status seedgb_gbts_run(seedgb_gbts* h, const seedgb_spacepoint
     scan(w.item_cnt, w.item_off, nullptr, h->n_pairs, 0, h->n_pairs + 1ull, w.tile, tile_total,
          h->d_sz + S_ITEMS, s);
     k_items_fill<<<blocks(h->n_pairs), kThreads, 0, s>>>(T, w);
-    // edges: count per item, scan, write in canonical order
+    // edges: count per (item, thread), scan, write
     const uint32_t edge_grid = 152u * 16u;
     k_edges<false><<<edge_grid, kEdgeThreads, 0, s>>>(T, w);
-    scan(w.item_ecnt, w.item_ebase, h->d_sz + S_ITEMS, 0, 0, h->a_e + 1, w.tile, tile_total,
-         h->d_sz + S_EDGES_MADE, s);
+    scan(w.item_tcnt, w.item_toff, h->d_sz + S_SLOTS, 0, 0, h->a_e * kEdgeThreads + 1, w.tile,
+         tile_total, h->d_sz + S_EDGES_MADE, s);
     cudaMemsetAsync(w.out_cnt, 0, sizeof(uint32_t) * (N + 1), s);
     k_edges<true><<<edge_grid, kEdgeThreads, 0, s>>>(T, w);
-    // the edges leaving each node: offsets by inner node
+    // the edges leaving each node: offsets by inner node, lists in ascending
+    // edge index; every kernel from here to the path store reads its size
+    // from device memory (grid-stride launches), so nothing waits on the host
     scan(w.out_cnt, w.lstart, h->d_sz + S_NODES, 0, 0, N + 1, w.tile, tile_total, nullptr, s);
     cudaMemsetAsync(w.lcur, 0, sizeof(uint32_t) * (N + 1), s);
-    // first sync: kept edge count, nodes
-    if (cudaMemcpyAsync(h->h_sz, h->d_sz, sizeof(uint32_t) * S_COUNT, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-        cudaStreamSynchronize(s) != cudaSuccess)
-        return SEEDGB_CUDA_ERROR;
-    const uint64_t nodes = h->h_sz[S_NODES];
-    const uint64_t made = h->h_sz[S_EDGES_MADE];
-    const uint32_t n_edges = static_cast<uint32_t>(
-        std::min<uint64_t>({made, static_cast<uint64_t>(h->cfg.max_edges_factor) * nodes, E}));
-    if (n_edges == 0) {
-        k_empty_out<<<1, 1, 0, s>>>(*out);
-        return cudaGetLastError() == cudaSuccess ? SEEDGB_OK : SEEDGB_CUDA_ERROR;
-    }
-    k_link_fill<<<blocks(n_edges), kThreads, 0, s>>>(w, n_edges);
-    k_link_sort<<<blocks(nodes), kThreads, 0, s>>>(w);
-    cudaMemsetAsync(w.kept, 0, sizeof(uint32_t) * n_edges, s);
-    k_match<<<blocks(n_edges), kThreads, 0, s>>>(T, w, n_edges);
-    scan(w.kept, w.kbase, nullptr, n_edges, 0, n_edges + 1ull, w.tile, tile_total, h->d_sz + S_CONNECTED, s);
-    k_compress<<<blocks(n_edges), kThreads, 0, s>>>(T, w, n_edges);
-    // automaton over the connected edges (at most n_edges)
+    k_edges_kept<<<1, 1, 0, s>>>(T, w);
+    k_link_fill<<<blocks(E), kThreads, 0, s>>>(w);
+    k_link_sort<<<kGrid, kThreads, 0, s>>>(w);
+    k_match<<<blocks(E), kThreads, 0, s>>>(T, w);
+    scan(w.kept, w.kbase, h->d_sz + S_EDGES, 0, 0, E + 1, w.tile, tile_total, h->d_sz + S_CONNECTED, s);
+    k_compress<<<blocks(E), kThreads, 0, s>>>(T, w);
+    // automaton over the connected edges
     cudaMemsetAsync(w.levels, 1, static_cast<size_t>(2 * E), s);
-    for (uint32_t it = 0; it < kMaxCca; ++it) k_cca<<<blocks(n_edges), kThreads, 0, s>>>(T, w, it);
-    k_term_flags<<<blocks(n_edges), kThreads, 0, s>>>(w);
-    scan(w.tflag, w.tidx, h->d_sz + S_CONNECTED, 0, 0, n_edges + 1ull, w.tile, tile_total, h->d_sz + S_TERMINUS, s);
-    scan(w.tpaths, w.pbase, h->d_sz + S_CONNECTED, 0, 0, n_edges + 1ull, w.tile, tile_total, h->d_sz + S_PATHS, s);
-    // second sync: the path store's size
+    for (uint32_t it = 0; it < kMaxCca; ++it) k_cca<<<kGrid, kThreads, 0, s>>>(T, w, it);
+    k_term_flags<<<kGrid, kThreads, 0, s>>>(w);
+    scan(w.tflag, w.tidx, h->d_sz + S_CONNECTED, 0, 0, E + 1, w.tile, tile_total, h->d_sz + S_TERMINUS, s);
+    scan(w.tpaths, w.pbase, h->d_sz + S_CONNECTED, 0, 0, E + 1, w.tile, tile_total, h->d_sz + S_PATHS, s);
+    // the one wait: the path store's size
     if (cudaMemcpyAsync(h->h_sz, h->d_sz, sizeof(uint32_t) * S_COUNT, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
         cudaStreamSynchronize(s) != cudaSuccess)
         return SEEDGB_CUDA_ERROR;
+    const uint64_t n_edges = h->h_sz[S_EDGES];
     const uint64_t n_term = h->h_sz[S_TERMINUS], n_paths = h->h_sz[S_PATHS];
     if (n_term == 0 || n_paths == 0) {
         k_empty_out<<<1, 1, 0, s>>>(*out);
@@ -1608,7 +1650,7 @@ extern "C" seedgb_status seedgb_gbts_run(seedgb_gbts* h, const seedgb_spacepoint
         if (!h->arena_b.ensure(need)) return SEEDGB_CUDA_ERROR;
         carve_b(static_cast<char*>(h->arena_b.p), n_term, n_paths, w);
     }
-    k_term_fill<<<blocks(n_edges), kThreads, 0, s>>>(w);
+    k_term_fill<<<kGrid, kThreads, 0, s>>>(w);
     k_dfs<<<blocks(n_term), kThreads, 0, s>>>(T, w);
     k_fit<<<blocks(n_paths), kThreads, 0, s>>>(T, w);
     scan(w.fflag, w.fidx, h->d_sz + S_PATHS, 0, 0, n_paths + 1, w.tile_b, tile_total, h->d_sz + S_PROPS, s);
