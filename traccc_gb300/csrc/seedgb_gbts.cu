@@ -27,6 +27,7 @@
 // edges up to max_edges_factor x nodes, the graph rows, the automaton's
 // levels) and one sized from the path count, which the host reads back once
 // in the middle of the run (the reference reads its counters back six times).
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -41,6 +42,8 @@
 
 #include "seedgb.h"
 
+namespace cg = cooperative_groups;
+
 namespace {
 
 constexpr uint32_t kMaxCca = 15u;       // gbts_consts::max_cca_iter
@@ -49,7 +52,6 @@ constexpr int kEdgeThreads = 128;       // threads of one edge work item
 constexpr int kThreads = 256;
 constexpr int kScanThreads = 1024;
 constexpr uint32_t kScanTile = 4u * kScanThreads;
-constexpr uint64_t kSmallScan = 1u << 14;  // one-block scan up to this capacity
 constexpr float kPi = 3.14159265358979323846f;
 constexpr float kTwoPi = 2.0f * kPi;
 constexpr uint32_t kInvalid = 0xFFFFFFFFu;
@@ -75,7 +77,6 @@ enum Size : uint32_t {
     S_SEEDS,
     S_STATUS,
     S_BAD_INPUT,
-    S_TMP,
     S_COUNT
 };
 
@@ -125,7 +126,7 @@ struct Work {
     int16_t* opy;
     uint32_t *tflag, *tidx, *tpaths, *pbase;
     unsigned long long *ebid, *hbid;
-    uint32_t* tile;
+    unsigned long long* tstate;  // scan tile states
     // path-sized buffers
     int2* store;
     uint32_t *term_edge, *term_pos;
@@ -136,7 +137,7 @@ struct Work {
     uint8_t* bidder;
     uint32_t *ecount, *eoff;
     uint4* seeds3;
-    uint32_t* tile_b;
+    unsigned long long* tstate_b;
     // sizes
     uint32_t* sz;
     uint64_t ecap;  // edge capacity (max_edges_factor x spacepoints)
@@ -203,97 +204,78 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* t
     return before + incl - v;
 }
 
+// Single-pass scan with decoupled look-back: each block takes the next tile
+// id from a running ticket (so every tile before it is already running),
+// scans its tile, publishes the tile's sum, then walks back over earlier
+// tiles' published sums until one holds an inclusive prefix.  A tile state
+// is (epoch:30, flag:2, value:32); states of another scan (epoch) read as
+// not yet published.  The wait for a predecessor is bounded: past the limit
+// the run's status becomes SEEDGB_TIMEOUT.
+constexpr uint32_t kFlagAggregate = 1u, kFlagPrefix = 2u;
+constexpr uint32_t kSpinLimit = 1u << 22;
+
+__device__ __forceinline__ unsigned long long tile_word(uint32_t epoch, uint32_t flag, uint32_t v) {
+    return (static_cast<unsigned long long>(epoch & 0x3FFFFFFFu) << 34) |
+           (static_cast<unsigned long long>(flag) << 32) | v;
+}
+
 __global__ void __launch_bounds__(kScanThreads)
-k_scan_tile(const uint32_t* in, uint32_t* out, const uint32_t* n_dev, uint32_t n_host,
-            uint32_t add, uint32_t* tile) {
+k_scan(const uint32_t* in, uint32_t* out, const uint32_t* n_dev, uint32_t n_host, uint32_t add,
+       unsigned long long* state, unsigned long long* ticket, unsigned long long ticket_base,
+       uint32_t epoch, uint32_t* total_dst, uint32_t* sz) {
+    __shared__ uint32_t s_tile, s_prefix;
+    if (threadIdx.x == 0) s_tile = static_cast<uint32_t>(atomicAdd(ticket, 1ull) - ticket_base);
+    __syncthreads();
+    const uint32_t tile = s_tile;
     const uint32_t n = load_n(n_dev, n_host, add);
-    const uint32_t base = blockIdx.x * kScanTile;
-    if (base >= n) {
-        if (threadIdx.x == 0) tile[blockIdx.x] = 0;
-        return;
-    }
+    const uint32_t n_tiles = n ? (n + kScanTile - 1) / kScanTile : 1u;
+    if (tile >= n_tiles) return;
+    const uint32_t base = tile * kScanTile;
     uint32_t v[4];
-    uint32_t s = 0;
+    uint32_t sum = 0;
     for (int j = 0; j < 4; ++j) {
         const uint32_t i = base + 4u * threadIdx.x + j;
         v[j] = i < n ? in[i] : 0u;
-        s += v[j];
+        sum += v[j];
     }
     uint32_t total;
-    uint32_t run = block_exclusive_scan(s, &total);
+    uint32_t run = block_exclusive_scan(sum, &total);
+    if (threadIdx.x == 0) {
+        uint32_t prefix = 0;
+        if (tile != 0) {
+            atomicExch(&state[tile], tile_word(epoch, kFlagAggregate, total));
+            const unsigned long long want = epoch & 0x3FFFFFFFu;
+            int j = static_cast<int>(tile) - 1;
+            uint32_t spins = 0;
+            while (j >= 0) {
+                const unsigned long long sv = *reinterpret_cast<volatile unsigned long long*>(&state[j]);
+                const uint32_t flag = static_cast<uint32_t>(sv >> 32) & 3u;
+                if ((sv >> 34) != want || flag == 0u) {
+                    if (++spins > kSpinLimit) {
+                        set_status(sz, SEEDGB_TIMEOUT);
+                        break;
+                    }
+                    __nanosleep(64);
+                    continue;
+                }
+                prefix += static_cast<uint32_t>(sv);
+                if (flag == kFlagPrefix) break;
+                --j;
+            }
+        }
+        atomicExch(&state[tile], tile_word(epoch, kFlagPrefix, prefix + total));
+        s_prefix = prefix;
+        if (tile == n_tiles - 1u) {
+            out[n] = prefix + total;
+            if (total_dst) *total_dst = prefix + total;
+        }
+    }
+    __syncthreads();
+    run += s_prefix;
     for (int j = 0; j < 4; ++j) {
         const uint32_t i = base + 4u * threadIdx.x + j;
         if (i < n) out[i] = run;
         run += v[j];
-    }
-    if (threadIdx.x == 0) tile[blockIdx.x] = total;
-}
-
-__global__ void __launch_bounds__(kScanThreads)
-k_scan_sums(uint32_t* tile, uint32_t n_tiles, uint32_t* tile_total) {
-    __shared__ uint32_t carry;
-    if (threadIdx.x == 0) carry = 0;
-    __syncthreads();
-    for (uint32_t b = 0; b < n_tiles; b += blockDim.x) {
-        const uint32_t i = b + threadIdx.x;
-        const uint32_t v = i < n_tiles ? tile[i] : 0u;
-        uint32_t tot;
-        const uint32_t ex = block_exclusive_scan(v, &tot);
-        if (i < n_tiles) tile[i] = carry + ex;
-        __syncthreads();
-        if (threadIdx.x == 0) carry += tot;
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) *tile_total = carry;
-}
-
-// the whole scan in one block (small inputs): rounds of 4 x 1024 values
-__global__ void __launch_bounds__(kScanThreads)
-k_scan_small(const uint32_t* in, uint32_t* out, const uint32_t* n_dev, uint32_t n_host,
-             uint32_t add, uint32_t* total_dst) {
-    __shared__ uint32_t carry;
-    const uint32_t n = load_n(n_dev, n_host, add);
-    if (threadIdx.x == 0) carry = 0;
-    __syncthreads();
-    for (uint32_t base = 0; base < n; base += kScanTile) {
-        uint32_t v[4];
-        uint32_t sum = 0;
-        for (int j = 0; j < 4; ++j) {
-            const uint32_t i = base + 4u * threadIdx.x + j;
-            v[j] = i < n ? in[i] : 0u;
-            sum += v[j];
-        }
-        uint32_t total;
-        uint32_t run = carry + block_exclusive_scan(sum, &total);
-        for (int j = 0; j < 4; ++j) {
-            const uint32_t i = base + 4u * threadIdx.x + j;
-            if (i < n) out[i] = run;
-            run += v[j];
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) carry += total;
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) {
-        out[n] = carry;
-        if (total_dst) *total_dst = carry;
-    }
-}
-
-__global__ void __launch_bounds__(kScanThreads)
-k_scan_add(uint32_t* out, const uint32_t* n_dev, uint32_t n_host, uint32_t add,
-           const uint32_t* tile, const uint32_t* tile_total, uint32_t* total_dst) {
-    const uint32_t n = load_n(n_dev, n_host, add);
-    const uint32_t base = blockIdx.x * kScanTile;
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        out[n] = *tile_total;
-        if (total_dst) *total_dst = *tile_total;
-    }
-    if (base >= n) return;
-    const uint32_t off = tile[blockIdx.x];
-    for (int j = 0; j < 4; ++j) {
-        const uint32_t i = base + 4u * threadIdx.x + j;
-        if (i < n) out[i] += off;
     }
 }
 
@@ -722,7 +704,7 @@ __global__ void __launch_bounds__(kThreads) k_compress(Tables T, Work w) {
 // ---------------------------------------------------------------------------
 // Longest chains: gbts_run_cca_iteration.ipp:23-101 (one launch per iteration)
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kThreads) k_cca(Tables T, Work w, uint32_t iter) {
+__device__ __forceinline__ void cca_step(const Tables& T, const Work& w, uint32_t iter) {
     GRID_STRIDE(e, w.sz[S_CONNECTED]) {
     if (iter != 0 && w.active[e] != static_cast<int8_t>(iter)) continue;
     const uint32_t esz = 3u + T.c.max_num_neighbours;
@@ -764,6 +746,15 @@ __global__ void __launch_bounds__(kThreads) k_cca(Tables T, Work w, uint32_t ite
         w.opy[e] = static_cast<int16_t>((next_level >= T.c.minLevel) - 1);
     }
     lstore[e] = next_level;
+    }
+}
+
+// the fifteen iterations in one cooperative launch, a grid barrier between them
+__global__ void __launch_bounds__(kThreads) k_cca_all(Tables T, Work w) {
+    cg::grid_group g = cg::this_grid();
+    for (uint32_t iter = 0; iter < kMaxCca; ++iter) {
+        cca_step(T, w, iter);
+        g.sync();
     }
 }
 
@@ -978,91 +969,121 @@ __global__ void __launch_bounds__(kThreads) k_props(Work w) {
 // ---------------------------------------------------------------------------
 // Bidding (gbts_create_seed_candidate.ipp:22-58, gbts_rebid_seeds_for_edges.
 // ipp:23-62, gbts_reset_edge_bids.ipp:22-69).  Each round's bidders are fixed
-// by k_round before the bids (value 2 = bidding this round); a bid kernel only
-// ever writes -1, so the outcome does not depend on the order of the atomics.
+// before the bids (value 2 = bidding this round); a bid phase only ever
+// writes -1, so the outcome does not depend on the order of the atomics.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ unsigned long long bid_of(int2 prop, uint32_t P) {
     return (static_cast<unsigned long long>(static_cast<uint32_t>(prop.x)) << 32) |
            static_cast<unsigned long long>(P);
 }
 
-__global__ void __launch_bounds__(kThreads) k_bid(Work w, int depth) {
-    const uint32_t P = blockIdx.x * blockDim.x + threadIdx.x;
-    if (P >= w.sz[S_PROPS] || !w.bidder[P]) return;
-    const int2 prop = w.props[P];
-    const unsigned long long seed_bid = bid_of(prop, P);
-    int2 path = make_int2(0, prop.y);
-    int d = depth;
-    while (path.y >= 0 && d != 0) {
-        path = w.store[path.y];
-        d--;
-        const unsigned long long comp = atomicMax(&w.ebid[path.x], seed_bid);
-        if (comp > seed_bid) {
-            w.ambi[P] = -1;
-        } else if (comp != 0) {
-            w.ambi[comp & 0xFFFFFFFFull] = -1;
+__device__ __forceinline__ void bid_step(const Work& w, int depth) {
+    GRID_STRIDE(P, w.sz[S_PROPS]) {
+        if (!w.bidder[P]) continue;
+        const int2 prop = w.props[P];
+        const unsigned long long seed_bid = bid_of(prop, P);
+        int2 path = make_int2(0, prop.y);
+        int d = depth;
+        while (path.y >= 0 && d != 0) {
+            path = w.store[path.y];
+            d--;
+            const unsigned long long comp = atomicMax(&w.ebid[path.x], seed_bid);
+            if (comp > seed_bid) {
+                w.ambi[P] = -1;
+            } else if (comp != 0) {
+                w.ambi[comp & 0xFFFFFFFFull] = -1;
+            }
         }
     }
 }
 
-__global__ void __launch_bounds__(kThreads) k_round(Work w, int first) {
-    const uint32_t P = blockIdx.x * blockDim.x + threadIdx.x;
-    if (P >= w.sz[S_PROPS]) return;
-    const int8_t a = w.ambi[P];
-    uint8_t b = 0;
-    if (first) {
-        if (a == 0) {
+// who bids in this round: the first round every proposal still 0 (best on
+// its outermost edge), later rounds the "maybe" ones (1); value 2 marks a
+// bidder until its round's reset
+__device__ __forceinline__ void round_step(const Work& w, bool first) {
+    GRID_STRIDE(P, w.sz[S_PROPS]) {
+        const int8_t a = w.ambi[P];
+        uint8_t b = 0;
+        if (first) {
+            if (a == 0) {
+                w.ambi[P] = 2;
+                b = 1;
+            } else {
+                w.ambi[P] = -2;
+            }
+        } else if (a == 1) {
             w.ambi[P] = 2;
             b = 1;
-        } else {
-            w.ambi[P] = -2;
         }
-    } else if (a == 1) {
-        w.ambi[P] = 2;
-        b = 1;
+        w.bidder[P] = b;
     }
-    w.bidder[P] = b;
 }
 
-__global__ void __launch_bounds__(kThreads) k_reset(Work w) {
-    const uint32_t P = blockIdx.x * blockDim.x + threadIdx.x;
-    if (P >= w.sz[S_PROPS]) return;
-    const int8_t a = w.ambi[P];
-    if (a == 2) {
-        w.ambi[P] = 0;
-        return;
-    }
-    if (a != -1) return;
-    bool good = true;
-    int2 path = make_int2(0, w.props[P].y);
-    while (path.y >= 0) {
-        path = w.store[path.y];
-        const int8_t best = w.ambi[w.ebid[path.x] & 0xFFFFFFFFull];
-        if (best == 0 || best == 2) {
-            good = false;
-            break;
+__device__ __forceinline__ void reset_step(const Work& w) {
+    GRID_STRIDE(P, w.sz[S_PROPS]) {
+        const int8_t a = w.ambi[P];
+        if (a == 2) {
+            w.ambi[P] = 0;
+            continue;
         }
+        if (a != -1) continue;
+        bool good = true;
+        int2 path = make_int2(0, w.props[P].y);
+        while (path.y >= 0) {
+            path = w.store[path.y];
+            const int8_t best = w.ambi[w.ebid[path.x] & 0xFFFFFFFFull];
+            if (best == 0 || best == 2) {
+                good = false;
+                break;
+            }
+        }
+        w.ambi[P] = good ? 1 : -2;
     }
-    w.ambi[P] = good ? 1 : -2;
 }
 
 // gbts_bid_seeds_for_hits.ipp:23-70
-__global__ void __launch_bounds__(kThreads) k_hit_bids(Tables T, Work w) {
-    const uint32_t P = blockIdx.x * blockDim.x + threadIdx.x;
-    if (P >= w.sz[S_PROPS]) return;
-    if (w.ambi[P] == -2) {
-        atomicAdd(&w.sz[S_REJECTED], 1u);
-        return;
-    }
+__device__ __forceinline__ void hit_step(const Tables& T, const Work& w) {
     const uint32_t esz = 3u + T.c.max_num_neighbours;
-    const int2 prop = w.props[P];
-    const unsigned long long b = bid_of(prop, P);
-    int2 path = make_int2(0, prop.y);
-    while (path.y >= 0) {
-        path = w.store[path.y];
-        atomicMax(&w.hbid[w.graph[static_cast<uint64_t>(esz) * static_cast<uint32_t>(path.x)]], b);
+    GRID_STRIDE(P, w.sz[S_PROPS]) {
+        if (w.ambi[P] == -2) {
+            atomicAdd(&w.sz[S_REJECTED], 1u);
+            continue;
+        }
+        const int2 prop = w.props[P];
+        const unsigned long long b = bid_of(prop, P);
+        int2 path = make_int2(0, prop.y);
+        while (path.y >= 0) {
+            path = w.store[path.y];
+            atomicMax(&w.hbid[w.graph[static_cast<uint64_t>(esz) * static_cast<uint32_t>(path.x)]], b);
+        }
+        atomicMax(&w.hbid[w.graph[static_cast<uint64_t>(esz) * static_cast<uint32_t>(path.x) + 1]], b);
     }
-    atomicMax(&w.hbid[w.graph[static_cast<uint64_t>(esz) * static_cast<uint32_t>(path.x) + 1]], b);
+}
+
+__device__ __forceinline__ void zero64(unsigned long long* p, uint64_t n) {
+    for (uint64_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = 0ull;
+}
+
+// the fit's bids on each proposal's outermost edge, the rounds of edge
+// bidding and the hit bids, in one cooperative launch
+__global__ void __launch_bounds__(kThreads)
+k_bidding(Tables T, Work w, uint32_t n_edges, uint32_t n_sp, uint32_t rounds) {
+    cg::grid_group g = cg::this_grid();
+    zero64(w.ebid, n_edges);
+    zero64(w.hbid, n_sp);
+    g.sync();
+    bid_step(w, 1);
+    g.sync();
+    for (uint32_t r = 0; r < rounds; ++r) {
+        zero64(w.ebid, n_edges);
+        round_step(w, r == 0);
+        g.sync();
+        bid_step(w, -1);
+        g.sync();
+        reset_step(w);
+        g.sync();
+    }
+    hit_step(T, w);
 }
 
 // gbts_estimate_seed_params (gbts_convert_seeds.ipp:33-67)
@@ -1222,6 +1243,12 @@ struct seedgb_gbts {
     cudaStream_t last = nullptr;
     Work w{};
     uint64_t a_sp = 0, a_e = 0;
+    // single-pass scans: running tile ticket and scan epoch
+    unsigned long long* d_ticket = nullptr;
+    unsigned long long ticket_base = 0;
+    uint32_t epoch = 0;
+    // cooperative launches: blocks that can be co-resident
+    uint32_t coop_cca = 0, coop_bid = 0;
 };
 
 namespace {
@@ -1251,17 +1278,20 @@ uint32_t blocks(uint64_t n, int threads = kThreads) {
     return static_cast<uint32_t>(std::max<uint64_t>(1, (n + threads - 1) / threads));
 }
 
-// exclusive scan helper: n on the device (n_dev + add) or the host; grid for `cap`
-void scan(const uint32_t* in, uint32_t* out, const uint32_t* n_dev, uint32_t n_host, uint32_t add,
-          uint64_t cap, uint32_t* tile, uint32_t* tile_total, uint32_t* total_dst, cudaStream_t s) {
-    if (cap <= kSmallScan) {
-        k_scan_small<<<1, kScanThreads, 0, s>>>(in, out, n_dev, n_host, add, total_dst);
-        return;
-    }
+// exclusive scan of n values (n_dev + add on the device, else n_host) into
+// out[0, n], the total also to *total_dst; one launch sized for `cap`
+void scan(seedgb_gbts* h, const uint32_t* in, uint32_t* out, const uint32_t* n_dev,
+          uint32_t n_host, uint32_t add, uint64_t cap, unsigned long long* state,
+          uint32_t* total_dst, cudaStream_t s);
+
+void scan(seedgb_gbts* h, const uint32_t* in, uint32_t* out, const uint32_t* n_dev,
+          uint32_t n_host, uint32_t add, uint64_t cap, unsigned long long* state,
+          uint32_t* total_dst, cudaStream_t s) {
     const uint32_t tiles = static_cast<uint32_t>(std::max<uint64_t>(1, (cap + kScanTile - 1) / kScanTile));
-    k_scan_tile<<<tiles, kScanThreads, 0, s>>>(in, out, n_dev, n_host, add, tile);
-    k_scan_sums<<<1, kScanThreads, 0, s>>>(tile, tiles, tile_total);
-    k_scan_add<<<tiles, kScanThreads, 0, s>>>(out, n_dev, n_host, add, tile, tile_total, total_dst);
+    if (++h->epoch >= (1u << 30)) h->epoch = 1;
+    k_scan<<<tiles, kScanThreads, 0, s>>>(in, out, n_dev, n_host, add, state, h->d_ticket,
+                                          h->ticket_base, h->epoch, total_dst, h->d_sz);
+    h->ticket_base += tiles;
 }
 
 // carve the spacepoint-sized arena (base == nullptr: measure only)
@@ -1313,7 +1343,7 @@ size_t carve_a(seedgb_gbts* h, char* base, uint64_t n_sp, uint64_t items_cap, Wo
     w.pbase = cv.take<uint32_t>(E + 1);
     w.ebid = cv.take<unsigned long long>(E);
     w.hbid = cv.take<unsigned long long>(N);
-    w.tile = cv.take<uint32_t>(scan_cap / kScanTile + 4);
+    w.tstate = cv.take<unsigned long long>(scan_cap / kScanTile + 4);
     w.ecap = E;
     return cv.off + 256;
 }
@@ -1334,7 +1364,7 @@ size_t carve_b(char* base, uint64_t n_term, uint64_t n_paths, Work& w) {
     w.ecount = cv.take<uint32_t>(P);
     w.eoff = cv.take<uint32_t>(P + 1);
     w.seeds3 = cv.take<uint4>(3 * P);
-    w.tile_b = cv.take<uint32_t>((P + 1) / kScanTile + 4);
+    w.tstate_b = cv.take<unsigned long long>((P + 1) / kScanTile + 4);
     w.pcap = S;
     return cv.off + 256;
 }
@@ -1413,6 +1443,7 @@ void free_tables(seedgb_gbts* h) {
     cudaFree(h->d_lut);
     cudaFree(h->d_vmap);
     cudaFree(h->d_sz);
+    cudaFree(h->d_ticket);
     if (h->h_sz) cudaFreeHost(h->h_sz);
 }
 
@@ -1541,6 +1572,25 @@ extern "C" seedgb_status seedgb_gbts_create(const seedgb_gbts_config* config,
     }
     std::memset(h->h_sz, 0, sizeof(uint32_t) * S_COUNT);
     cudaMemset(h->d_sz, 0, sizeof(uint32_t) * S_COUNT);
+    int dev = 0, sms = 0, coop = 0, nb_cca = 0, nb_bid = 0;
+    if (cudaMalloc(reinterpret_cast<void**>(&h->d_ticket), sizeof(unsigned long long)) != cudaSuccess ||
+        cudaMemset(h->d_ticket, 0, sizeof(unsigned long long)) != cudaSuccess ||
+        cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb_cca, k_cca_all, kThreads, 0) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb_bid, k_bidding, kThreads, 0) != cudaSuccess) {
+        free_tables(h);
+        delete h;
+        return SEEDGB_CUDA_ERROR;
+    }
+    if (!coop || nb_cca < 1 || nb_bid < 1) {
+        free_tables(h);
+        delete h;
+        return SEEDGB_UNSUPPORTED;
+    }
+    h->coop_cca = static_cast<uint32_t>(nb_cca * sms);
+    h->coop_bid = static_cast<uint32_t>(nb_bid * sms);
     *out = h;
     return SEEDGB_OK;
 }
@@ -1595,45 +1645,54 @@ extern "C" seedgb_status seedgb_gbts_run(seedgb_gbts* h, const seedgb_spacepoint
     const uint64_t N = n_sp;
     const uint64_t E = w.ecap;  // edge capacity: max_edges_factor x arena spacepoints
     const uint32_t cells = h->n_eta * h->cfg.n_phi_bins;
-    uint32_t* tile_total = h->d_sz + S_TMP;
+    unsigned long long* st = w.tstate;
+    const uint64_t scan_tiles = (std::max<uint64_t>({E + 1, N + 1, cells + 1ull, h->a_e * kEdgeThreads + 1,
+                                                    h->n_pairs + 1ull}) / kScanTile) + 4;
+    cudaMemsetAsync(st, 0, sizeof(unsigned long long) * scan_tiles, s);
     // nodes
     cudaMemsetAsync(w.cell_cnt, 0, sizeof(uint32_t) * (cells + 1ull), s);
     cudaMemsetAsync(w.cell_cur, 0, sizeof(uint32_t) * (cells + 1ull), s);
     k_classify<<<blocks(N), kThreads, 0, s>>>(T, *sps, surface_link, diameter, n_meas, w);
-    scan(w.cell_cnt, w.cell_off, nullptr, cells, 0, cells + 1ull, w.tile, tile_total, h->d_sz + S_NODES, s);
+    scan(h, w.cell_cnt, w.cell_off, nullptr, cells, 0, cells + 1ull, st, h->d_sz + S_NODES, s);
     k_scatter<<<blocks(N), kThreads, 0, s>>>(n_sp, w);
     k_sort_cells<<<blocks(cells), kThreads, 0, s>>>(cells, w);
     k_node_params<<<blocks(N), kThreads, 0, s>>>(T, w);
     k_eta_bins<<<blocks(32ull * h->n_eta), kThreads, 0, s>>>(h->n_eta, h->cfg.n_phi_bins, w);
     // work items
     k_items_count<<<blocks(h->n_pairs), kThreads, 0, s>>>(T, w);
-    scan(w.item_cnt, w.item_off, nullptr, h->n_pairs, 0, h->n_pairs + 1ull, w.tile, tile_total,
-         h->d_sz + S_ITEMS, s);
+    scan(h, w.item_cnt, w.item_off, nullptr, h->n_pairs, 0, h->n_pairs + 1ull, st, h->d_sz + S_ITEMS, s);
     k_items_fill<<<blocks(h->n_pairs), kThreads, 0, s>>>(T, w);
     // edges: count per (item, thread), scan, write
     const uint32_t edge_grid = 152u * 16u;
     k_edges<false><<<edge_grid, kEdgeThreads, 0, s>>>(T, w);
-    scan(w.item_tcnt, w.item_toff, h->d_sz + S_SLOTS, 0, 0, h->a_e * kEdgeThreads + 1, w.tile,
-         tile_total, h->d_sz + S_EDGES_MADE, s);
+    scan(h, w.item_tcnt, w.item_toff, h->d_sz + S_SLOTS, 0, 0, h->a_e * kEdgeThreads + 1, st,
+         h->d_sz + S_EDGES_MADE, s);
     cudaMemsetAsync(w.out_cnt, 0, sizeof(uint32_t) * (N + 1), s);
     k_edges<true><<<edge_grid, kEdgeThreads, 0, s>>>(T, w);
     // the edges leaving each node: offsets by inner node, lists in ascending
     // edge index; every kernel from here to the path store reads its size
     // from device memory (grid-stride launches), so nothing waits on the host
-    scan(w.out_cnt, w.lstart, h->d_sz + S_NODES, 0, 0, N + 1, w.tile, tile_total, nullptr, s);
+    scan(h, w.out_cnt, w.lstart, h->d_sz + S_NODES, 0, 0, N + 1, st, nullptr, s);
     cudaMemsetAsync(w.lcur, 0, sizeof(uint32_t) * (N + 1), s);
     k_edges_kept<<<1, 1, 0, s>>>(T, w);
     k_link_fill<<<blocks(E), kThreads, 0, s>>>(w);
     k_link_sort<<<kGrid, kThreads, 0, s>>>(w);
     k_match<<<blocks(E), kThreads, 0, s>>>(T, w);
-    scan(w.kept, w.kbase, h->d_sz + S_EDGES, 0, 0, E + 1, w.tile, tile_total, h->d_sz + S_CONNECTED, s);
+    scan(h, w.kept, w.kbase, h->d_sz + S_EDGES, 0, 0, E + 1, st, h->d_sz + S_CONNECTED, s);
     k_compress<<<blocks(E), kThreads, 0, s>>>(T, w);
     // automaton over the connected edges
     cudaMemsetAsync(w.levels, 1, static_cast<size_t>(2 * E), s);
-    for (uint32_t it = 0; it < kMaxCca; ++it) k_cca<<<kGrid, kThreads, 0, s>>>(T, w, it);
+    {
+        Tables Tc = T;
+        Work wc = w;
+        void* args[] = {&Tc, &wc};
+        if (cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(k_cca_all), dim3(h->coop_cca),
+                                        dim3(kThreads), args, 0, s) != cudaSuccess)
+            return SEEDGB_CUDA_ERROR;
+    }
     k_term_flags<<<kGrid, kThreads, 0, s>>>(w);
-    scan(w.tflag, w.tidx, h->d_sz + S_CONNECTED, 0, 0, E + 1, w.tile, tile_total, h->d_sz + S_TERMINUS, s);
-    scan(w.tpaths, w.pbase, h->d_sz + S_CONNECTED, 0, 0, E + 1, w.tile, tile_total, h->d_sz + S_PATHS, s);
+    scan(h, w.tflag, w.tidx, h->d_sz + S_CONNECTED, 0, 0, E + 1, st, h->d_sz + S_TERMINUS, s);
+    scan(h, w.tpaths, w.pbase, h->d_sz + S_CONNECTED, 0, 0, E + 1, st, h->d_sz + S_PATHS, s);
     // the one wait: the path store's size
     if (cudaMemcpyAsync(h->h_sz, h->d_sz, sizeof(uint32_t) * S_COUNT, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
         cudaStreamSynchronize(s) != cudaSuccess)
@@ -1649,25 +1708,25 @@ extern "C" seedgb_status seedgb_gbts_run(seedgb_gbts* h, const seedgb_spacepoint
         const size_t need = carve_b(nullptr, n_term, n_paths, tmp);
         if (!h->arena_b.ensure(need)) return SEEDGB_CUDA_ERROR;
         carve_b(static_cast<char*>(h->arena_b.p), n_term, n_paths, w);
+        cudaMemsetAsync(w.tstate_b, 0, sizeof(unsigned long long) * ((n_paths + 1) / kScanTile + 4), s);
     }
     k_term_fill<<<kGrid, kThreads, 0, s>>>(w);
     k_dfs<<<blocks(n_term), kThreads, 0, s>>>(T, w);
     k_fit<<<blocks(n_paths), kThreads, 0, s>>>(T, w);
-    scan(w.fflag, w.fidx, h->d_sz + S_PATHS, 0, 0, n_paths + 1, w.tile_b, tile_total, h->d_sz + S_PROPS, s);
+    scan(h, w.fflag, w.fidx, h->d_sz + S_PATHS, 0, 0, n_paths + 1, w.tstate_b, h->d_sz + S_PROPS, s);
     k_props<<<blocks(n_paths), kThreads, 0, s>>>(w);
-    // bidding: the fit's one-edge bids, then the rounds
-    cudaMemsetAsync(w.ebid, 0, sizeof(unsigned long long) * n_edges, s);
-    k_bid<<<blocks(n_paths), kThreads, 0, s>>>(w, 1);
-    for (uint32_t r = 0; r < h->cfg.edge_bidding_rounds; ++r) {
-        cudaMemsetAsync(w.ebid, 0, sizeof(unsigned long long) * n_edges, s);
-        k_round<<<blocks(n_paths), kThreads, 0, s>>>(w, r == 0 ? 1 : 0);
-        k_bid<<<blocks(n_paths), kThreads, 0, s>>>(w, -1);
-        k_reset<<<blocks(n_paths), kThreads, 0, s>>>(w);
+    // bidding: the fit's one-edge bids, the rounds, the hit bids
+    {
+        Tables Tc = T;
+        Work wc = w;
+        uint32_t ne = static_cast<uint32_t>(n_edges), nsp = n_sp, rounds = h->cfg.edge_bidding_rounds;
+        void* args[] = {&Tc, &wc, &ne, &nsp, &rounds};
+        if (cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(k_bidding), dim3(h->coop_bid),
+                                        dim3(kThreads), args, 0, s) != cudaSuccess)
+            return SEEDGB_CUDA_ERROR;
     }
-    cudaMemsetAsync(w.hbid, 0, sizeof(unsigned long long) * N, s);
-    k_hit_bids<<<blocks(n_paths), kThreads, 0, s>>>(T, w);
     k_convert<<<blocks(n_paths), kThreads, 0, s>>>(T, w);
-    scan(w.ecount, w.eoff, h->d_sz + S_PROPS, 0, 0, n_paths + 1, w.tile_b, tile_total, h->d_sz + S_SEEDS, s);
+    scan(h, w.ecount, w.eoff, h->d_sz + S_PROPS, 0, 0, n_paths + 1, w.tstate_b, h->d_sz + S_SEEDS, s);
     k_seeds_out<<<blocks(n_paths), kThreads, 0, s>>>(w, *out);
     return cudaGetLastError() == cudaSuccess ? SEEDGB_OK : SEEDGB_CUDA_ERROR;
 }
