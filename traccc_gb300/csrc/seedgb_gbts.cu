@@ -111,6 +111,7 @@ struct Work {
     uint32_t *item_cnt, *item_off;
     uint4* items;
     float* item_dphi;
+    uint32_t* item_eta;  // eta bin of bin 1, top bit: the bin holds a node wrapped to phi bin 0
     uint32_t *item_tcnt, *item_toff;  // edges per (item, thread) and their offsets
     // edges
     uint32_t *e_in, *e_out;
@@ -462,11 +463,17 @@ __global__ void __launch_bounds__(kThreads) k_items_fill(Tables T, Work w) {
     const uint32_t bin1 = T.pairs[2 * p], bin2 = T.pairs[2 * p + 1];
     const uint32_t b1 = w.view[2 * bin1], e1 = w.view[2 * bin1 + 1];
     const uint32_t o = w.item_off[p];
+    // a node whose phi rounds into bin n_phi is wrapped to bin 0, ahead of
+    // nodes of smaller phi: the window walk of such a chunk takes no short cut
+    bool wrapped = false;
+    const uint32_t c0 = bin1 * T.c.n_phi_bins;
+    for (uint32_t k = w.cell_off[c0]; k < w.cell_off[c0 + 1] && !wrapped; ++k) wrapped = w.node_phi[k] > 0.0f;
     for (uint32_t j = 0; j < chunks; ++j) {
         const uint32_t b = b1 + j * kNodeBuffer;
         const uint32_t e = (e1 - b > kNodeBuffer) ? b + kNodeBuffer : e1;
         w.items[o + j] = make_uint4(b, e, w.view[2 * bin2], w.view[2 * bin2 + 1]);
         w.item_dphi[o + j] = dphi;
+        w.item_eta[o + j] = bin1 | (wrapped ? 0x80000000u : 0u);
     }
 }
 
@@ -501,6 +508,9 @@ __device__ __forceinline__ bool edge_test(float4 np1, float4 np2, float phi1, fl
 struct ItemCtx {
     uint32_t b1, n1, b2;
     float dphi, phi0, phiN, pbw, brk;
+    const uint32_t* bin_first;  // first node of each phi bin of the chunk's eta bin, or null
+    float inv_slice;
+    uint32_t n_phi;
 };
 
 // one outer node of a work item: the reference's window walk with the
@@ -526,6 +536,18 @@ __device__ __forceinline__ uint32_t walk(const ItemCtx& it, uint32_t n2Idx, uint
         if (it.phiN < min_phi1) {
             if (it.phi0 > it.brk) done = true;
             return 0;
+        }
+        // every node of a phi bin below the bin of min_phi1 has phi1 <
+        // min_phi1 (the bin is a monotone function of phi), so the walk
+        // would step over it: start at the first node of that bin
+        const float x = (min_phi1 + kPi) * it.inv_slice;
+        if (it.bin_first && x >= 1.0f) {
+            const uint32_t pb = static_cast<uint32_t>(x);
+            if (pb < it.n_phi) {
+                const uint32_t f = it.bin_first[pb];
+                const uint32_t jump = f > it.b1 ? (f - it.b1 < it.n1 ? f - it.b1 : it.n1) : 0u;
+                if (jump > n1Idx) n1Idx = jump;
+            }
         }
     } else {
         if (it.phi0 < max_phi1) {
@@ -562,22 +584,32 @@ __device__ __forceinline__ uint32_t walk(const ItemCtx& it, uint32_t n2Idx, uint
     return cnt;
 }
 
-// Edges of one work item, thread t taking the outer nodes t, t + 128, ...
-// with the reference's sliding-window state; an item's edges in thread order,
-// then outer node, then inner node.  The count pass records each thread's
-// edge count; after one scan over (item, thread) the write pass walks again
-// and writes from the thread's offset, no barrier inside the item.
+// Edges of one work item, thread t (of 128) taking the outer nodes t,
+// t + 128, ... with the reference's sliding-window state; an item's edges in
+// thread order, then outer node, then inner node.  The four warps of a block
+// work independently: a warp takes one quarter of an item (threads 32q ...
+// 32q + 31) and stages its own copy of the item's bin-1 chunk, so only warp
+// barriers remain.  The count pass records each thread's edge count; after
+// one scan over (item, thread) the write pass walks again and writes from the
+// thread's offset.
+constexpr int kEdgeWarps = kEdgeThreads / 32;
+
 template <bool WRITE>
 __global__ void __launch_bounds__(kEdgeThreads) k_edges(Tables T, Work w) {
-    __shared__ float s_phi[kNodeBuffer];
-    __shared__ float4 s_np[kNodeBuffer];
-    __shared__ uint32_t s_cnt[kNodeBuffer];  // edges per inner node of the chunk
-    const uint32_t t = threadIdx.x;
+    __shared__ float s_phi_all[kEdgeWarps][kNodeBuffer];
+    __shared__ float4 s_np_all[kEdgeWarps][kNodeBuffer];
+    __shared__ uint32_t s_cnt_all[kEdgeWarps][kNodeBuffer];  // edges per inner node
+    const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
+    float* s_phi = s_phi_all[wid];
+    float4* s_np = s_np_all[wid];
+    uint32_t* s_cnt = s_cnt_all[wid];
     const uint32_t n_items = w.sz[S_ITEMS];
-    if (!WRITE && blockIdx.x == 0 && t == 0) w.sz[S_SLOTS] = n_items * kEdgeThreads;
+    if (!WRITE && blockIdx.x == 0 && threadIdx.x == 0) w.sz[S_SLOTS] = n_items * kEdgeThreads;
     const uint64_t by_nodes = static_cast<uint64_t>(T.c.max_edges_factor) * w.sz[S_NODES];
     const uint64_t cap = by_nodes < w.ecap ? by_nodes : w.ecap;
-    for (uint32_t item = blockIdx.x; item < n_items; item += gridDim.x) {
+    const uint32_t n_units = n_items * kEdgeWarps;
+    for (uint32_t u = blockIdx.x * kEdgeWarps + wid; u < n_units; u += gridDim.x * kEdgeWarps) {
+        const uint32_t item = u / kEdgeWarps, q = u % kEdgeWarps;
         const uint4 r = w.items[item];
         ItemCtx it;
         it.b1 = r.x;
@@ -585,17 +617,24 @@ __global__ void __launch_bounds__(kEdgeThreads) k_edges(Tables T, Work w) {
         it.b2 = r.z;
         const uint32_t n2 = r.w - r.z;
         it.dphi = w.item_dphi[item];
-        __syncthreads();
-        if (t < it.n1) {
-            s_np[t] = w.node_p[it.b1 + t];
-            s_phi[t] = w.node_phi[it.b1 + t];
+        const uint32_t em = w.item_eta[item];
+        it.bin_first = (em & 0x80000000u) ? nullptr : w.cell_off + (em & 0x7FFFFFFFu) * T.c.n_phi_bins;
+        it.n_phi = T.c.n_phi_bins;
+        it.inv_slice = 1.0f / (kTwoPi / static_cast<float>(T.c.n_phi_bins));
+        __syncwarp();
+        for (uint32_t k = lane; k < kNodeBuffer; k += 32) {
+            if (k < it.n1) {
+                s_np[k] = w.node_p[it.b1 + k];
+                s_phi[k] = w.node_phi[it.b1 + k];
+            }
+            s_cnt[k] = 0;
         }
-        s_cnt[t] = 0;
-        __syncthreads();
+        __syncwarp();
         it.phi0 = s_phi[0];
         it.phiN = s_phi[it.n1 - 1u];
         it.pbw = kTwoPi / static_cast<float>(T.c.n_phi_bins);
         it.brk = it.dphi + it.pbw - kPi;
+        const uint32_t t = 32u * q + lane;
         uint32_t last_n1 = 0u;
         bool done = false;
         const uint64_t slot = static_cast<uint64_t>(item) * kEdgeThreads + t;
@@ -606,8 +645,9 @@ __global__ void __launch_bounds__(kEdgeThreads) k_edges(Tables T, Work w) {
         if (!WRITE) {
             w.item_tcnt[slot] = cnt;
         } else {
-            __syncthreads();
-            if (t < it.n1 && s_cnt[t]) atomicAdd(&w.out_cnt[it.b1 + t], s_cnt[t]);
+            __syncwarp();
+            for (uint32_t k = lane; k < it.n1; k += 32)
+                if (s_cnt[k]) atomicAdd(&w.out_cnt[it.b1 + k], s_cnt[k]);
         }
     }
 }
@@ -1318,6 +1358,7 @@ size_t carve_a(seedgb_gbts* h, char* base, uint64_t n_sp, uint64_t items_cap, Wo
     w.item_off = cv.take<uint32_t>(h->n_pairs + 1ull);
     w.items = cv.take<uint4>(items_cap);
     w.item_dphi = cv.take<float>(items_cap);
+    w.item_eta = cv.take<uint32_t>(items_cap);
     w.item_tcnt = cv.take<uint32_t>(items_cap * kEdgeThreads + 1);
     w.item_toff = cv.take<uint32_t>(items_cap * kEdgeThreads + 1);
     w.e_in = cv.take<uint32_t>(E);
