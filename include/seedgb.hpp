@@ -17,6 +17,15 @@
  *  seedgb::to_ckf   the parameters in the record layout the track finding
  *                   takes (examples/run/cuda/src/full_chain_algorithm.cpp:
  *                   241-247), device-resident
+ *  seedgb::gbts_seeding_algorithm           <- traccc::cuda::gbts_seeding_algorithm
+ *      constructor: gbts_seedfinder_config::setLinkingScheme (core/src/
+ *                   gbts_seeding/gbts_seeding_config.cpp:19-142) + stream
+ *      operator():  device/common/include/traccc/gbts_seeding/device/
+ *                   gbts_seeding_algorithm.hpp:94-96 (spacepoints and the
+ *                   measurements' barcodes and diameters -> seed buffer)
+ *      gbts_seedfinder_config::from_directory: the reference's configuration
+ *                   directory (examples/options/src/track_gbts_seeding.cpp:
+ *                   158-226)
  *  triplet_seeding_algorithm::autotune / train_filter / calibrate_gate /
  *                   set_filter: the library's launch-shape search and learned
  *                   doublet filter (no counterpart in the reference)
@@ -370,6 +379,78 @@ private:
 };
 
 /* traccc::cuda::seed_parameter_estimation_algorithm (constant field). */
+/* traccc::gbts_seedfinder_config before setLinkingScheme: the parameters and
+ * the linking inputs (bin tables unrolled to pairs, layer table, geometry-id
+ * binning, minimum pT in MeV, optional tau table). */
+struct gbts_seedfinder_config {
+    seedgb_gbts_config params{};
+    std::vector<seedgb_gbts_layer> layers;
+    std::vector<uint32_t> bin_pairs;  // (bin1, bin2) per linked pair
+    std::vector<seedgb_gbts_geoid> geoid_binning;
+    float min_pt = 900.0f;
+    std::vector<float> tau_lut;
+
+    gbts_seedfinder_config() { seedgb_gbts_config_default(&params); }
+
+    /* geoidBinning.txt, binTables.txt and layerInfo.txt of `dir`. */
+    static gbts_seedfinder_config from_directory(const std::string& dir, float min_pt = 900.0f) {
+        gbts_seedfinder_config c;
+        c.min_pt = min_pt;
+        uint32_t nl = 0, np = 0, ng = 0;
+        check(seedgb_gbts_read_config_dir(dir.c_str(), nullptr, &nl, nullptr, &np, nullptr, &ng),
+              "gbts_seedfinder_config::from_directory");
+        c.layers.resize(nl);
+        c.bin_pairs.resize(2ull * np);
+        c.geoid_binning.resize(ng);
+        check(seedgb_gbts_read_config_dir(dir.c_str(), c.layers.data(), &nl, c.bin_pairs.data(), &np,
+                                          c.geoid_binning.data(), &ng),
+              "gbts_seedfinder_config::from_directory");
+        return c;
+    }
+};
+
+/* traccc::cuda::gbts_seeding_algorithm.  The measurements enter as their
+ * device columns: surface barcode and cluster diameter. */
+class gbts_seeding_algorithm {
+public:
+    gbts_seeding_algorithm(const gbts_seedfinder_config& cfg, cudaStream_t stream)
+        : stream_(stream) {
+        check(seedgb_gbts_create(&cfg.params, cfg.layers.data(), static_cast<uint32_t>(cfg.layers.size()),
+                                 cfg.bin_pairs.data(), static_cast<uint32_t>(cfg.bin_pairs.size() / 2),
+                                 cfg.geoid_binning.data(),
+                                 static_cast<uint32_t>(cfg.geoid_binning.size()), cfg.min_pt,
+                                 cfg.tau_lut.empty() ? nullptr : cfg.tau_lut.data(),
+                                 static_cast<uint32_t>(cfg.tau_lut.size()), &h_),
+              "gbts_seeding_algorithm");
+    }
+    gbts_seeding_algorithm(const gbts_seeding_algorithm&) = delete;
+    gbts_seeding_algorithm& operator=(const gbts_seeding_algorithm&) = delete;
+    ~gbts_seeding_algorithm() { seedgb_gbts_destroy(h_); }
+
+    seed_collection_buffer operator()(const seedgb_spacepoint_view& spacepoints,
+                                      const uint64_t* surface_link, const float* diameter,
+                                      uint32_t n_measurements) const {
+        seed_collection_buffer out(3u * (spacepoints.size ? spacepoints.size : 1u));
+        seedgb_seed_buffer b = out.view();
+        check(seedgb_gbts_run(h_, &spacepoints, surface_link, diameter, n_measurements, &b, stream_),
+              "gbts_seeding_algorithm()");
+        return out;
+    }
+
+    /* Device status of the last run (synchronises the stream). */
+    seedgb_status status() const { return seedgb_gbts_last_status(h_, stream_); }
+
+    std::array<uint64_t, SEEDGB_GBTS_N_COUNTERS> counters() const {
+        std::array<uint64_t, SEEDGB_GBTS_N_COUNTERS> c{};
+        check(seedgb_gbts_counters(h_, c.data()), "gbts_seeding_algorithm::counters");
+        return c;
+    }
+
+private:
+    seedgb_gbts* h_ = nullptr;
+    cudaStream_t stream_;
+};
+
 class seed_parameter_estimation_algorithm {
 public:
     seed_parameter_estimation_algorithm(const seedgb_track_params_estimation_config& cfg,

@@ -124,3 +124,36 @@ def test_cpp_full_chain(tmp_path):
         assert np.array_equal(got["cov"], rp["cov"]) or np.allclose(got["cov"], rp["cov"],
                                                                      rtol=1e-5, atol=0)
     assert off == len(raw)
+
+
+def test_cpp_gbts_from_config_directory(tmp_path):
+    """GBTS from C++: the configuration directory in the reference's format
+    (written here from the synthetic barrel) read by
+    gbts_seedfinder_config::from_directory, seeds equal to the oracle's."""
+    from traccc_gb300 import gbts, seeding
+    lib = seeding.library_path()
+    exe = str(tmp_path / "gbts_check")
+    subprocess.run([_nvcc(), "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "cpp", "gbts_check.cpp"),
+                    "-L", os.path.dirname(lib), "-lseedgb",
+                    "-Xlinker", "-rpath=" + os.path.dirname(lib), "-o", exe], check=True)
+    layers, pairs, geoid = synth.gbts_geometry()
+    cfgdir = tmp_path / "gbts_config"
+    gbts.write_config_dir(str(cfgdir), layers, pairs, geoid)
+    ev = synth.workload_event("trk1000", 7)
+    link, dia = synth.gbts_measurements(ev, 7)
+    inp = tmp_path / "event.bin"
+    with open(inp, "wb") as f:
+        np.array([len(ev["global"]), len(link)], np.uint32).tofile(f)
+        np.asarray(ev["measurement_index_1"], np.uint32).tofile(f)
+        np.asarray(ev["global"], np.float32).tofile(f)
+        np.asarray(link, np.uint64).tofile(f)
+        np.asarray(dia, np.float32).tofile(f)
+    out = tmp_path / "out.bin"
+    subprocess.run([exe, str(cfgdir), str(inp), str(out)], check=True)
+    raw = out.read_bytes()
+    ns = int(np.frombuffer(raw[:4], np.uint32)[0])
+    got = np.frombuffer(raw[4:4 + 16 * ns], O.SEED_DTYPE)
+    l2, p2, g2 = gbts.read_config_dir(str(cfgdir))
+    ref, _ = O.gbts(ev, link, dia, l2, p2, g2)
+    assert len(ref) > 0 and np.array_equal(got, ref)
