@@ -116,3 +116,49 @@ def test_config_dir_errors_are_statuses(tmp_path):
     (tmp_path / "binTables.txt").write_text("3\n1 2\n3\n")
     with pytest.raises(RuntimeError):
         gbts.read_config_dir(str(tmp_path))
+
+
+def test_create_refuses_bad_tables_before_device_work():
+    """seedgb_gbts_create checks the linking inputs on the host first:
+    setLinkingScheme's own failures and tables the kernels could not index
+    give SEEDGB_BAD_CONFIG, missing arguments SEEDGB_INVALID_ARGUMENT (no
+    GPU is touched on these paths)."""
+    L = gbts.lib()
+    layers, pairs, geoid = synth.gbts_geometry()
+    lay = np.ascontiguousarray(layers.astype(gbts.LAYER_DTYPE))
+    prs = np.ascontiguousarray(pairs, np.uint32)
+    geo = np.zeros(len(geoid), gbts.GEOID_DTYPE)
+    geo["barcode"] = geoid["barcode"]
+    geo["layer"] = geoid["layer"]
+    cfg = gbts.config_default()
+
+    def create(c=cfg, lay=lay, prs=prs, geo=geo, min_pt=900.0, lut=None, nlut=0):
+        h = C.c_void_p()
+        return L.seedgb_gbts_create(C.byref(c), lay.ctypes.data if lay is not None else None,
+                                    0 if lay is None else len(lay), prs.ctypes.data, len(prs),
+                                    geo.ctypes.data, len(geo), min_pt, lut, nlut, C.byref(h))
+
+    BAD, INV = 2, 6
+    bad_layer = geo.copy()
+    bad_layer["layer"][3] = len(lay)           # a layer the table does not have
+    assert create(geo=bad_layer) == BAD
+    bad_pair = prs.copy()
+    bad_pair[0, 1] = 10 ** 6                   # an eta bin past the last layer's
+    assert create(prs=bad_pair) == BAD
+    assert create(lay=lay[:0]) == BAD          # no layers
+    assert create(min_pt=0.0) == BAD
+    c2 = gbts.config_default()                 # decoded volumes >= SHRT_MAX (9 << 12)
+    c2.volume_shift, c2.volume_bits = 40, 20
+    assert create(c=c2) == BAD
+    c3 = gbts.config_default()
+    c3.useTauLUT = 1
+    lut = np.zeros(7, np.float32)              # not a multiple of 5
+    assert create(c=c3, lut=lut.ctypes.data, nlut=7) == BAD
+    assert create(c=c3) == BAD                 # the table is missing
+    assert L.seedgb_gbts_create(None, lay.ctypes.data, len(lay), prs.ctypes.data, len(prs),
+                                geo.ctypes.data, len(geo), 900.0, None, 0,
+                                C.byref(C.c_void_p())) == INV
+    from traccc_gb300 import seeding
+    v = seeding._SpacepointView()
+    b = seeding._SeedBuffer()
+    assert L.seedgb_gbts_run(None, C.byref(v), None, None, 0, C.byref(b), None) == INV
