@@ -789,7 +789,8 @@ typedef struct seedgb_gbts seedgb_gbts;
  * The pT-dependent cuts of the config are scaled by 900 MeV / min_pt (MeV),
  * as setLinkingScheme does.  SEEDGB_BAD_CONFIG where setLinkingScheme returns
  * false, and for tables the kernels cannot index (a layer index outside the
- * layer table, a bin pair outside the eta bins, a malformed tau table). */
+ * layer table, a bin pair outside the eta bins, a malformed tau table) or
+ * more than 49 bidding rounds. */
 seedgb_status seedgb_gbts_create(const seedgb_gbts_config* config,
                                  const seedgb_gbts_layer* layers, uint32_t n_layers,
                                  const uint32_t* bin_pairs, uint32_t n_pairs,

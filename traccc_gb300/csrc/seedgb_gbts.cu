@@ -56,7 +56,8 @@ constexpr float kPi = 3.14159265358979323846f;
 constexpr float kTwoPi = 2.0f * kPi;
 constexpr uint32_t kInvalid = 0xFFFFFFFFu;
 constexpr int32_t kPathCountLimit = 1 << 30;
-constexpr uint32_t kGrid = 152u * 8u;  // grid-stride kernels: 8 blocks per SM
+constexpr uint32_t kGrid = 152u * 8u;
+constexpr uint32_t kFlagSlots = 64u;  // automaton iterations, then bidding rounds  // grid-stride kernels: 8 blocks per SM
 
 #define GRID_STRIDE(i, n) \
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < (n); i += gridDim.x * blockDim.x)
@@ -128,6 +129,7 @@ struct Work {
     uint32_t *tflag, *tidx, *tpaths, *pbase;
     unsigned long long *ebid, *hbid;
     unsigned long long* tstate;  // scan tile states
+    uint32_t* flags;  // per automaton iteration / bidding round: anything left to do
     // path-sized buffers
     int2* store;
     uint32_t *term_edge, *term_pos;
@@ -639,8 +641,11 @@ __global__ void __launch_bounds__(kEdgeThreads) k_edges(Tables T, Work w) {
         bool done = false;
         const uint64_t slot = static_cast<uint64_t>(item) * kEdgeThreads + t;
         uint64_t pos = WRITE ? w.item_toff[slot] : 0;
+        // the write pass knows the thread's edge count: it stops once they
+        // are all written (the rest of its walk would find none)
+        const uint32_t want = WRITE ? w.item_tcnt[slot] : 0xFFFFFFFFu;
         uint32_t cnt = 0;
-        for (uint32_t n2Idx = t; n2Idx < n2 && !done; n2Idx += kEdgeThreads)
+        for (uint32_t n2Idx = t; n2Idx < n2 && !done && cnt < want; n2Idx += kEdgeThreads)
             cnt += walk<WRITE>(it, n2Idx, last_n1, done, s_phi, s_np, w, T.c, pos + cnt, cap, s_cnt);
         if (!WRITE) {
             w.item_tcnt[slot] = cnt;
@@ -703,19 +708,29 @@ __global__ void __launch_bounds__(kThreads) k_match(Tables T, Work w) {
         const float uat_2 = 1.0f / p1.x;
         const float Phi2 = p1.z;
         const float curv2 = p1.y;
-        for (uint32_t k = 0u; k < nLinks; k++) {
-            if (num_nei >= M) break;
-            const uint32_t e2 = w.links[link_begin + k];
-            const float4 p2 = w.e_p[e2];
-            const float tau_ratio = p2.x * uat_2 - 1.0f;
-            if (fabsf(tau_ratio) > c.cut_tau_ratio_max) continue;
-            const float dPhi = wrap_phi(Phi2 - p2.w);
-            if (fabsf(dPhi) > c.cut_dphi_max) continue;
-            const float dcurv = curv2 - p2.y;
-            if (fabsf(dcurv) > c.cut_dcurv_max) continue;
-            w.nei[static_cast<uint64_t>(M) * e + num_nei] = e2;
-            w.kept[e2] = 1u;
-            ++num_nei;
+        // candidates loaded four at a time (loads in flight together), tested
+        // in list order
+        for (uint32_t k0 = 0u; k0 < nLinks && num_nei < M; k0 += 4u) {
+            uint32_t e2s[4];
+            float4 p2s[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) e2s[j] = k0 + j < nLinks ? w.links[link_begin + k0 + j] : 0u;
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                p2s[j] = k0 + j < nLinks ? w.e_p[e2s[j]] : make_float4(0.f, 0.f, 0.f, 0.f);
+            for (int j = 0; j < 4 && k0 + j < nLinks; ++j) {
+                if (num_nei >= M) break;
+                const float4 p2 = p2s[j];
+                const float tau_ratio = p2.x * uat_2 - 1.0f;
+                if (fabsf(tau_ratio) > c.cut_tau_ratio_max) continue;
+                const float dPhi = wrap_phi(Phi2 - p2.w);
+                if (fabsf(dPhi) > c.cut_dphi_max) continue;
+                const float dcurv = curv2 - p2.y;
+                if (fabsf(dcurv) > c.cut_dcurv_max) continue;
+                w.nei[static_cast<uint64_t>(M) * e + num_nei] = e2s[j];
+                w.kept[e2s[j]] = 1u;
+                ++num_nei;
+            }
         }
     }
     w.nnei[e] = static_cast<uint8_t>(num_nei);
@@ -744,7 +759,9 @@ __global__ void __launch_bounds__(kThreads) k_compress(Tables T, Work w) {
 // ---------------------------------------------------------------------------
 // Longest chains: gbts_run_cca_iteration.ipp:23-101 (one launch per iteration)
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void cca_step(const Tables& T, const Work& w, uint32_t iter) {
+// returns whether this thread left an edge active for the next iteration
+__device__ __forceinline__ bool cca_step(const Tables& T, const Work& w, uint32_t iter) {
+    bool more = false;
     GRID_STRIDE(e, w.sz[S_CONNECTED]) {
     if (iter != 0 && w.active[e] != static_cast<int8_t>(iter)) continue;
     const uint32_t esz = 3u + T.c.max_num_neighbours;
@@ -769,6 +786,7 @@ __device__ __forceinline__ void cca_step(const Tables& T, const Work& w, uint32_
             w.active[e] = -1;
         } else {
             w.active[e] = static_cast<int8_t>(iter + 1u);
+            more = true;
         }
     } else {
         w.active[e] = -1;
@@ -787,14 +805,19 @@ __device__ __forceinline__ void cca_step(const Tables& T, const Work& w, uint32_
     }
     lstore[e] = next_level;
     }
+    return more;
 }
 
 // the fifteen iterations in one cooperative launch, a grid barrier between them
+// (an iteration that leaves no edge active ends the automaton: the
+// remaining iterations would change nothing)
 __global__ void __launch_bounds__(kThreads) k_cca_all(Tables T, Work w) {
     cg::grid_group g = cg::this_grid();
     for (uint32_t iter = 0; iter < kMaxCca; ++iter) {
-        cca_step(T, w, iter);
+        const bool more = cca_step(T, w, iter);
+        if (__syncthreads_or(more) && threadIdx.x == 0) w.flags[iter] = 1u;
         g.sync();
+        if (w.flags[iter] == 0u) break;
     }
 }
 
@@ -1040,7 +1063,8 @@ __device__ __forceinline__ void bid_step(const Work& w, int depth) {
 // who bids in this round: the first round every proposal still 0 (best on
 // its outermost edge), later rounds the "maybe" ones (1); value 2 marks a
 // bidder until its round's reset
-__device__ __forceinline__ void round_step(const Work& w, bool first) {
+__device__ __forceinline__ bool round_step(const Work& w, bool first) {
+    bool any = false;
     GRID_STRIDE(P, w.sz[S_PROPS]) {
         const int8_t a = w.ambi[P];
         uint8_t b = 0;
@@ -1056,7 +1080,9 @@ __device__ __forceinline__ void round_step(const Work& w, bool first) {
             b = 1;
         }
         w.bidder[P] = b;
+        any |= b != 0;
     }
+    return any;
 }
 
 __device__ __forceinline__ void reset_step(const Work& w) {
@@ -1116,8 +1142,11 @@ k_bidding(Tables T, Work w, uint32_t n_edges, uint32_t n_sp, uint32_t rounds) {
     g.sync();
     for (uint32_t r = 0; r < rounds; ++r) {
         zero64(w.ebid, n_edges);
-        round_step(w, r == 0);
+        const bool any = round_step(w, r == 0);
+        if (__syncthreads_or(any) && threadIdx.x == 0) w.flags[kMaxCca + r] = 1u;
         g.sync();
+        // a round without bidders leaves nothing to bid on in any later round
+        if (w.flags[kMaxCca + r] == 0u) break;
         bid_step(w, -1);
         g.sync();
         reset_step(w);
@@ -1385,6 +1414,7 @@ size_t carve_a(seedgb_gbts* h, char* base, uint64_t n_sp, uint64_t items_cap, Wo
     w.ebid = cv.take<unsigned long long>(E);
     w.hbid = cv.take<unsigned long long>(N);
     w.tstate = cv.take<unsigned long long>(scan_cap / kScanTile + 4);
+    w.flags = cv.take<uint32_t>(kFlagSlots);
     w.ecap = E;
     return cv.off + 256;
 }
@@ -1555,7 +1585,8 @@ extern "C" seedgb_status seedgb_gbts_create(const seedgb_gbts_config* config,
     *out = nullptr;
     seedgb_gbts_config c = *config;
     if (n_layers == 0 || c.n_phi_bins == 0 || c.max_num_neighbours == 0 ||
-        c.max_num_neighbours > 255 || c.max_edges_factor == 0 || !(min_pt > 0.0f))
+        c.max_num_neighbours > 255 || c.max_edges_factor == 0 || !(min_pt > 0.0f) ||
+        c.edge_bidding_rounds > kFlagSlots - kMaxCca)
         return SEEDGB_BAD_CONFIG;
     if (c.useTauLUT && (!tau_lut || n_tau_lut % 5 != 0 || c.tauLutSize > n_tau_lut))
         return SEEDGB_BAD_CONFIG;
@@ -1630,8 +1661,10 @@ extern "C" seedgb_status seedgb_gbts_create(const seedgb_gbts_config* config,
         delete h;
         return SEEDGB_UNSUPPORTED;
     }
+    // the automaton at full occupancy; the bidding at two blocks per SM (few
+    // arrivals per grid barrier)
     h->coop_cca = static_cast<uint32_t>(nb_cca * sms);
-    h->coop_bid = static_cast<uint32_t>(nb_bid * sms);
+    h->coop_bid = static_cast<uint32_t>(std::min(nb_bid, 2) * sms);
     *out = h;
     return SEEDGB_OK;
 }
@@ -1690,6 +1723,7 @@ extern "C" seedgb_status seedgb_gbts_run(seedgb_gbts* h, const seedgb_spacepoint
     const uint64_t scan_tiles = (std::max<uint64_t>({E + 1, N + 1, cells + 1ull, h->a_e * kEdgeThreads + 1,
                                                     h->n_pairs + 1ull}) / kScanTile) + 4;
     cudaMemsetAsync(st, 0, sizeof(unsigned long long) * scan_tiles, s);
+    cudaMemsetAsync(w.flags, 0, sizeof(uint32_t) * kFlagSlots, s);
     // nodes
     cudaMemsetAsync(w.cell_cnt, 0, sizeof(uint32_t) * (cells + 1ull), s);
     cudaMemsetAsync(w.cell_cur, 0, sizeof(uint32_t) * (cells + 1ull), s);
