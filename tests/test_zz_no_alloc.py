@@ -53,6 +53,57 @@ def test_noalloc_binning_equals_seeding_grid_two_calls():
         assert off[-1] > 0
 
 
+def _padded(ev, n):
+    """The event followed by spacepoints far outside the finder's z range
+    (dropped by every binning), n spacepoints in all."""
+    k = len(ev["global"])
+    pad = n - k
+    g = np.concatenate([np.asarray(ev["global"], np.float32),
+                        np.tile(np.array([[100.0, 0.0, 1.0e6]], np.float32), (pad, 1))])
+    return {"measurement_index_1": np.arange(n, dtype=np.uint32),
+            "measurement_index_2": np.full(n, 0xFFFFFFFF, np.uint32), "global": g,
+            "z_variance": np.zeros(n, np.float32), "radius_variance": np.zeros(n, np.float32),
+            "layer": np.zeros(n, np.uint32)}
+
+
+def test_noalloc_under_stream_capture_replays_on_new_events():
+    """The use the entry point exists for: one eager call (caches the scratch
+    address), then the call captured into a CUDA graph on a side stream and
+    replayed on two events written into the same input buffers; each replay
+    gives the handle path's grid."""
+    import torch
+    f, g, fl, _ = seeding.default_configs()
+    ax = seeding.get_axes(g)
+    nb = ax.phi_bins * ax.z_bins
+    raw = [synth.workload_event("trk1000", 31), synth.workload_event("trk1000", 32)]
+    n = max(len(e["global"]) for e in raw) + 17
+    events = [_padded(e, n) for e in raw]
+    sps = seeding.SpacepointCollection.from_numpy(events[0])
+    off = torch.full((nb + 1,), -1, dtype=torch.int32, device="cuda")
+    bsp = torch.full((n,), -1, dtype=torch.int32, device="cuda")
+    assert seeding.spacepoint_binning_noalloc(f, g, sps, off, bsp) == seeding.OK
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        st = seeding.spacepoint_binning_noalloc(f, g, sps, off, bsp,
+                                                stream=torch.cuda.current_stream())
+    assert st == seeding.OK
+    for ev in events:
+        src = seeding.SpacepointCollection.from_numpy(ev)
+        for col in ("measurement_index_1", "measurement_index_2", "global_", "z_variance",
+                    "radius_variance"):
+            getattr(sps, col).copy_(getattr(src, col))
+        off.fill_(-1)
+        bsp.fill_(-1)
+        graph.replay()
+        torch.cuda.synchronize()
+        o = off.cpu().numpy().view(np.uint32)
+        b = bsp.cpu().numpy().view(np.uint32)[: int(o[-1])]
+        roff, rbsp = _handle_grid(f, g, fl, ev)
+        assert np.array_equal(o, roff) and np.array_equal(b, rbsp)
+        assert o[-1] > 0
+
+
 def test_noalloc_rejects_events_above_its_capacity():
     import torch
     f, g, _, _ = seeding.default_configs()
