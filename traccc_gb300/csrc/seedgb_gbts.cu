@@ -482,11 +482,17 @@ __global__ void __launch_bounds__(kThreads) k_items_fill(Tables T, Work w) {
 // ---------------------------------------------------------------------------
 // Edges (gbts_make_graph_edges.ipp:31-239)
 // ---------------------------------------------------------------------------
+// The cuts are a conjunction of tests on the same inputs, so their order does
+// not change which edges pass: the phi-difference test (no division; the
+// candidate window is wider than deltaPhi by a phi bin on each side) runs
+// before the divisions.
 __device__ __forceinline__ bool edge_test(float4 np1, float4 np2, float phi1, float phi2,
                                           float deltaPhi, const seedgb_gbts_config& ap,
                                           float4& out) {
     const float dr = np2.z - np1.z;
     if (dr < ap.minDeltaRadius) return false;
+    const float dphi = wrap_phi(phi2 - phi1);
+    if (fabsf(dphi) > deltaPhi) return false;
     const float dz = np2.w - np1.w;
     const float tau = dz / dr;
     const float ftau = fabsf(tau);
@@ -496,8 +502,6 @@ __device__ __forceinline__ bool edge_test(float4 np1, float4 np2, float phi1, fl
     if ((z0 < ap.min_z0) || (z0 > ap.max_z0)) return false;
     const float zouter = z0 + ap.maxOuterRadius * tau;
     if (zouter < ap.cut_zMinU || zouter > ap.cut_zMaxU) return false;
-    const float dphi = wrap_phi(phi2 - phi1);
-    if (fabsf(dphi) > deltaPhi) return false;
     const float curv = dphi / dr;
     const float d0_for_max_curv = np1.z * np2.z * (fabsf(curv) - ap.max_Kappa);
     const float d0_max = (ftau < 4.0f) ? ap.low_Kappa_d0 : ap.high_Kappa_d0;
