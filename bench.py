@@ -558,6 +558,14 @@ def run_gbts(args, stream, flush_buf, events):
     t0 = time.perf_counter()
     ref, rctr = oracle.gbts(ev, link, dia, layers, pairs, geoid, cfg=oc, min_pt=900.0)
     cpu_s = time.perf_counter() - t0
+    # one event per host thread (the C call releases the GIL)
+    threads = cpu_threads()
+    sample = [host[i % len(host)] for i in range(threads)]
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+        list(ex.map(lambda h: oracle.gbts(h[0], h[1], h[2], layers, pairs, geoid, cfg=oc,
+                                          min_pt=900.0), sample))
+    cpu_mt_s = time.perf_counter() - t0
     same = bool(len(got) == len(ref) and all(np.array_equal(got[k], ref[k]) for k in
                                              ("bottom", "middle", "top")) and
                 np.array_equal(got["quality"].view(np.uint32), ref["quality"].view(np.uint32)))
@@ -574,6 +582,9 @@ def run_gbts(args, stream, flush_buf, events):
                                                             "the reference has no GBTS tests)"},
             "cpu_oracle": {"s_per_event": cpu_s, "events_per_s": 1.0 / cpu_s, "cores": 1,
                            "sample": "event 0, one host thread"},
+            "cpu_oracle_all_cores": {"events_per_s": len(sample) / cpu_mt_s, "cores": threads,
+                                     "sample": f"{len(sample)} of the step's events, one per "
+                                               f"thread on {threads} threads ({cpu_model()})"},
             "timing": f"median of {steps} steps, each the {n_ev} per-event calls back to back "
                       "on one stream, L2 flushed before each step; CUDA events on the stream"}
 
