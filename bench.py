@@ -550,6 +550,22 @@ def run_gbts(args, stream, flush_buf, events):
         ms.append(e0.elapsed_time(e1))
     counters = alg.counters()  # of the last event
     status = alg.last_status(stream=sptr)
+    # the same events through seedgb_gbts_run_batch (one call per step)
+    sps_l = [d[0] for d in data]
+    meas_l = [d[1] for d in data]
+    for _ in range(max(3, args.warmup)):
+        alg.run_batch(sps_l, meas_l, outs, stream=sptr)
+    torch.cuda.synchronize()
+    ms_b = []
+    for _ in range(steps):
+        flush_buf.fill_(1)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        alg.run_batch(sps_l, meas_l, outs, stream=sptr)
+        e1.record(stream)
+        e1.synchronize()
+        ms_b.append(e0.elapsed_time(e1))
+    status_b = alg.last_status(stream=sptr)
     got = outs[0].to_numpy()
     ev, link, dia = host[0]
     oc = oracle.GbtsConfig()
@@ -576,6 +592,11 @@ def run_gbts(args, stream, flush_buf, events):
                         f"default cuts at min_pt 900 MeV, max_edges_factor {GBTS_EDGES_FACTOR}",
             "value": 1e3 * n_ev / med, "unit": "events/s", "ms_per_step": med,
             "ms_per_event": med / n_ev, "status": int(status),
+            "batch": {"value": 1e3 * n_ev / statistics.median(ms_b), "unit": "events/s",
+                      "ms_per_step": statistics.median(ms_b), "status": int(status_b),
+                      "timing": "one seedgb_gbts_run_batch call per step (event e + 1's kernels "
+                                "queued before the wait for event e's path-store size), same "
+                                "outputs"},
             "last_event_counters": counters,
             "parity": {"event0_seeds_bit_exact": same, "seeds": len(got),
                        "oracle_seeds": len(ref), "against": "the C oracle (parity unpinned: "

@@ -821,10 +821,21 @@ seedgb_status seedgb_gbts_run(seedgb_gbts* h, const seedgb_spacepoint_view* sps,
                               const uint64_t* surface_link, const float* diameter,
                               uint32_t n_meas, seedgb_seed_buffer* out, void* stream);
 
-/* Synchronise `stream` and return the device status of the last run. */
+/* Many events in one call, the same seeds as one seedgb_gbts_run per event:
+ * event e is (events[e], surface_links[e], diameters[e], n_meas[e]) ->
+ * outs[e].  All work stays in order on `stream`; the call enqueues event
+ * e + 1's kernels before it waits for event e's path-store size, so the GPU
+ * keeps working while the host waits (two events' work areas are kept). */
+seedgb_status seedgb_gbts_run_batch(seedgb_gbts* h, const seedgb_spacepoint_view* events,
+                                    const uint64_t* const* surface_links,
+                                    const float* const* diameters, const uint32_t* n_meas,
+                                    uint32_t n_events, seedgb_seed_buffer* outs, void* stream);
+
+/* Synchronise `stream` and return the worst device status of the last call
+ * (over all events of a batch). */
 seedgb_status seedgb_gbts_last_status(seedgb_gbts* h, void* stream);
 
-/* Counters of the last run (synchronises the handle's last stream): nodes,
+/* Counters of the last event (synchronises the handle's last stream): nodes,
  * edges created, edge connections, connected edges, terminus edges, path
  * store entries below the terminus edges, seed proposals, proposals rejected
  * by the bidding, seeds. */

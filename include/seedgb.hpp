@@ -437,7 +437,31 @@ public:
         return out;
     }
 
-    /* Device status of the last run (synchronises the stream). */
+    /* Many events in one call (seedgb_gbts_run_batch); element e of each
+     * vector is event e. */
+    std::vector<seed_collection_buffer> operator()(
+        const std::vector<seedgb_spacepoint_view>& spacepoints,
+        const std::vector<const uint64_t*>& surface_links, const std::vector<const float*>& diameters,
+        const std::vector<uint32_t>& n_measurements) const {
+        const std::size_t n = spacepoints.size();
+        if (surface_links.size() != n || diameters.size() != n || n_measurements.size() != n)
+            throw std::invalid_argument("gbts_seeding_algorithm(batch): sizes");
+        std::vector<seed_collection_buffer> out;
+        std::vector<seedgb_seed_buffer> bufs;
+        out.reserve(n);
+        for (const auto& sp : spacepoints) {
+            out.emplace_back(3u * (sp.size ? sp.size : 1u));
+            bufs.push_back(out.back().view());
+        }
+        if (n)
+            check(seedgb_gbts_run_batch(h_, spacepoints.data(), surface_links.data(), diameters.data(),
+                                        n_measurements.data(), static_cast<uint32_t>(n), bufs.data(),
+                                        stream_),
+                  "gbts_seeding_algorithm(batch)");
+        return out;
+    }
+
+    /* Device status of the last call (synchronises the stream). */
     seedgb_status status() const { return seedgb_gbts_last_status(h_, stream_); }
 
     std::array<uint64_t, SEEDGB_GBTS_N_COUNTERS> counters() const {

@@ -133,3 +133,41 @@ def test_gbts_bad_measurement_index_and_small_buffer():
     ev2["measurement_index_1"] = mi
     alg, out = _run(ev2, link, dia, layers, pairs, geoid)
     assert alg.last_status() == 6  # SEEDGB_INVALID_ARGUMENT
+
+
+def test_gbts_batch_equals_per_event_calls():
+    """seedgb_gbts_run_batch (events alternating over two work areas, each
+    event's kernels queued before the previous event's wait) gives the seeds
+    of one call per event -- on a batch with an empty event, a small and a
+    100k-spacepoint event -- twice in a row."""
+    import torch
+
+    from traccc_gb300 import seeding
+    layers, pairs, geoid = synth.gbts_geometry()
+    cfg = gbts.config_default()
+    cfg.max_edges_factor = 40
+    alg = gbts.GbtsSeedingAlgorithm(cfg, layers, pairs, geoid)
+    evs = [synth.workload_event("trk1000", 11), synth.workload_event("pileup9k", 12),
+           synth.workload_event("trk100", 13), synth.workload_event("pileup9k", 14, 3000)]
+    evs.insert(2, {k: v[:0] for k, v in evs[0].items()})
+    sps, meas = [], []
+    for s, ev in enumerate(evs):
+        link, dia = synth.gbts_measurements(ev, s) if len(ev["global"]) else (
+            np.zeros(0, np.uint64), np.zeros(0, np.float32))
+        sps.append(seeding.SpacepointCollection.from_numpy(ev))
+        meas.append(seeding.MeasurementCollection.from_numpy(dict(surface_link=link, diameter=dia)))
+    single = []
+    for sp, m in zip(sps, meas):
+        single.append(alg(sp, m).to_numpy())
+    assert alg.last_status() == 0
+    for _ in range(2):
+        outs = alg.run_batch(sps, meas)
+        torch.cuda.synchronize()
+        assert alg.last_status() == 0
+        for got, ref in zip(outs, single):
+            g = got.to_numpy()
+            assert len(g) == len(ref)
+            for k in ("bottom", "middle", "top"):
+                assert np.array_equal(g[k], ref[k])
+            assert np.array_equal(g["quality"].view(np.uint32), ref["quality"].view(np.uint32))
+    assert len(single[2]) == 0 and len(single[1]) > 0

@@ -1301,6 +1301,36 @@ struct Carver {
 
 }  // namespace
 
+namespace {
+
+// One event in flight: its work arenas, sizes and scan ticket.  A single call
+// uses slot 0; a batch alternates its events over two slots on the caller's
+// stream and enqueues event e + 1's kernels before it waits for event e's
+// path-store size, so the GPU has work queued while the host waits (the
+// events' kernels stay in stream order: no two cooperative launches can be
+// resident at once).
+constexpr uint32_t kMaxSlots = 2;
+
+struct Slot {
+    DevBlock arena_a, arena_b;
+    uint32_t* d_sz = nullptr;
+    uint32_t* h_sz = nullptr;  // pinned
+    Work w{};
+    uint64_t a_sp = 0, a_e = 0;
+    // single-pass scans: running tile ticket and scan epoch
+    unsigned long long* d_ticket = nullptr;
+    unsigned long long ticket_base = 0;
+    uint32_t epoch = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ready = nullptr;    // sizes copied to h_sz
+    // the event in flight: its tail runs after the path store's size is known
+    bool pending = false;
+    seedgb_seed_buffer out{};
+    uint32_t n_sp = 0;
+};
+
+}  // namespace
+
 struct seedgb_gbts {
     seedgb_gbts_config cfg;
     uint32_t n_layers = 0, n_eta = 0, n_pairs = 0, n_volumes = 0, n_surfaces = 0, n_tau = 0;
@@ -1310,16 +1340,9 @@ struct seedgb_gbts {
     uint32_t *d_bin0 = nullptr, *d_neta = nullptr, *d_pairs = nullptr, *d_smap = nullptr;
     float *d_min_eta = nullptr, *d_width = nullptr, *d_lut = nullptr;
     int16_t* d_vmap = nullptr;
-    DevBlock arena_a, arena_b;
-    uint32_t* d_sz = nullptr;
-    uint32_t* h_sz = nullptr;  // pinned
-    cudaStream_t last = nullptr;
-    Work w{};
-    uint64_t a_sp = 0, a_e = 0;
-    // single-pass scans: running tile ticket and scan epoch
-    unsigned long long* d_ticket = nullptr;
-    unsigned long long ticket_base = 0;
-    uint32_t epoch = 0;
+    Slot slot[kMaxSlots];
+    uint32_t used = 1;       // slots the last call used
+    uint32_t last_slot = 0;  // slot of the last event
     // cooperative launches: blocks that can be co-resident
     uint32_t coop_cca = 0, coop_bid = 0;
 };
@@ -1353,18 +1376,13 @@ uint32_t blocks(uint64_t n, int threads = kThreads) {
 
 // exclusive scan of n values (n_dev + add on the device, else n_host) into
 // out[0, n], the total also to *total_dst; one launch sized for `cap`
-void scan(seedgb_gbts* h, const uint32_t* in, uint32_t* out, const uint32_t* n_dev,
-          uint32_t n_host, uint32_t add, uint64_t cap, unsigned long long* state,
-          uint32_t* total_dst, cudaStream_t s);
-
-void scan(seedgb_gbts* h, const uint32_t* in, uint32_t* out, const uint32_t* n_dev,
-          uint32_t n_host, uint32_t add, uint64_t cap, unsigned long long* state,
-          uint32_t* total_dst, cudaStream_t s) {
+void scan(Slot& sl, const uint32_t* in, uint32_t* out, const uint32_t* n_dev, uint32_t n_host,
+          uint32_t add, uint64_t cap, unsigned long long* state, uint32_t* total_dst) {
     const uint32_t tiles = static_cast<uint32_t>(std::max<uint64_t>(1, (cap + kScanTile - 1) / kScanTile));
-    if (++h->epoch >= (1u << 30)) h->epoch = 1;
-    k_scan<<<tiles, kScanThreads, 0, s>>>(in, out, n_dev, n_host, add, state, h->d_ticket,
-                                          h->ticket_base, h->epoch, total_dst, h->d_sz);
-    h->ticket_base += tiles;
+    if (++sl.epoch >= (1u << 30)) sl.epoch = 1;
+    k_scan<<<tiles, kScanThreads, 0, sl.stream>>>(in, out, n_dev, n_host, add, state, sl.d_ticket,
+                                                  sl.ticket_base, sl.epoch, total_dst, sl.d_sz);
+    sl.ticket_base += tiles;
 }
 
 // carve the spacepoint-sized arena (base == nullptr: measure only)
@@ -1517,9 +1535,25 @@ void free_tables(seedgb_gbts* h) {
     cudaFree(h->d_width);
     cudaFree(h->d_lut);
     cudaFree(h->d_vmap);
-    cudaFree(h->d_sz);
-    cudaFree(h->d_ticket);
-    if (h->h_sz) cudaFreeHost(h->h_sz);
+    for (Slot& sl : h->slot) {
+        cudaFree(sl.d_sz);
+        cudaFree(sl.d_ticket);
+        if (sl.h_sz) cudaFreeHost(sl.h_sz);
+        if (sl.ready) cudaEventDestroy(sl.ready);
+    }
+}
+
+bool slot_init(Slot& sl) {
+    if (sl.d_sz) return true;
+    if (cudaMalloc(reinterpret_cast<void**>(&sl.d_sz), sizeof(uint32_t) * S_COUNT) != cudaSuccess ||
+        cudaMallocHost(reinterpret_cast<void**>(&sl.h_sz), sizeof(uint32_t) * S_COUNT) != cudaSuccess ||
+        cudaMalloc(reinterpret_cast<void**>(&sl.d_ticket), sizeof(unsigned long long)) != cudaSuccess ||
+        cudaMemset(sl.d_ticket, 0, sizeof(unsigned long long)) != cudaSuccess ||
+        cudaMemset(sl.d_sz, 0, sizeof(uint32_t) * S_COUNT) != cudaSuccess ||
+        cudaEventCreateWithFlags(&sl.ready, cudaEventDisableTiming) != cudaSuccess)
+        return false;
+    std::memset(sl.h_sz, 0, sizeof(uint32_t) * S_COUNT);
+    return true;
 }
 
 }  // namespace
@@ -1638,20 +1672,14 @@ extern "C" seedgb_status seedgb_gbts_create(const seedgb_gbts_config* config,
                     upload(&h->d_pairs, bin_pairs, 2ull * n_pairs) &&
                     upload(&h->d_vmap, vmap.data(), vmap.size()) &&
                     upload(&h->d_smap, smap.data(), smap.size()) &&
-                    upload(&h->d_lut, lut.data(), lut.size()) &&
-                    cudaMalloc(reinterpret_cast<void**>(&h->d_sz), sizeof(uint32_t) * S_COUNT) == cudaSuccess &&
-                    cudaMallocHost(reinterpret_cast<void**>(&h->h_sz), sizeof(uint32_t) * S_COUNT) == cudaSuccess;
+                    upload(&h->d_lut, lut.data(), lut.size()) && slot_init(h->slot[0]);
     if (!ok) {
         free_tables(h);
         delete h;
         return SEEDGB_CUDA_ERROR;
     }
-    std::memset(h->h_sz, 0, sizeof(uint32_t) * S_COUNT);
-    cudaMemset(h->d_sz, 0, sizeof(uint32_t) * S_COUNT);
     int dev = 0, sms = 0, coop = 0, nb_cca = 0, nb_bid = 0;
-    if (cudaMalloc(reinterpret_cast<void**>(&h->d_ticket), sizeof(unsigned long long)) != cudaSuccess ||
-        cudaMemset(h->d_ticket, 0, sizeof(unsigned long long)) != cudaSuccess ||
-        cudaGetDevice(&dev) != cudaSuccess ||
+    if (cudaGetDevice(&dev) != cudaSuccess ||
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
         cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess ||
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb_cca, k_cca_all, kThreads, 0) != cudaSuccess ||
@@ -1692,108 +1720,132 @@ extern "C" seedgb_status seedgb_gbts_get_config(const seedgb_gbts* h, seedgb_gbt
     return SEEDGB_OK;
 }
 
-extern "C" seedgb_status seedgb_gbts_run(seedgb_gbts* h, const seedgb_spacepoint_view* sps,
-                                         const uint64_t* surface_link, const float* diameter,
-                                         uint32_t n_meas, seedgb_seed_buffer* out, void* stream) {
-    if (!h || !sps || !out || !out->size || (sps->size && (!sps->global || !sps->measurement_index_1)) ||
+namespace {
+
+seedgb_status check_event(const seedgb_spacepoint_view* sps, const uint64_t* surface_link,
+                          const float* diameter, uint32_t n_meas, const seedgb_seed_buffer* out) {
+    if (!sps || !out || !out->size || (sps->size && (!sps->global || !sps->measurement_index_1)) ||
         (n_meas && (!surface_link || !diameter)) ||
         (out->capacity && (!out->bottom_index || !out->middle_index || !out->top_index || !out->quality)))
         return SEEDGB_INVALID_ARGUMENT;
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
-    h->last = s;
-    if (cudaMemsetAsync(h->d_sz, 0, sizeof(uint32_t) * S_COUNT, s) != cudaSuccess) return SEEDGB_CUDA_ERROR;
+    return SEEDGB_OK;
+}
+
+// the event's kernels up to the path store's size, whose copy to the host
+// the slot's `ready` event marks; the status words of the call stay
+seedgb_status front(seedgb_gbts* h, Slot& sl, const seedgb_spacepoint_view* sps,
+                    const uint64_t* surface_link, const float* diameter, uint32_t n_meas,
+                    const seedgb_seed_buffer* out) {
+    if (cudaMemsetAsync(sl.d_sz, 0, sizeof(uint32_t) * S_STATUS, sl.stream) != cudaSuccess)
+        return SEEDGB_CUDA_ERROR;
+    sl.pending = false;
     const uint32_t n_sp = sps->size;
     if (n_sp == 0) {
-        k_empty_out<<<1, 1, 0, s>>>(*out);
+        k_empty_out<<<1, 1, 0, sl.stream>>>(*out);
         return cudaGetLastError() == cudaSuccess ? SEEDGB_OK : SEEDGB_CUDA_ERROR;
     }
     const uint64_t items_cap = static_cast<uint64_t>(h->n_pairs) +
                                static_cast<uint64_t>(h->max_first_degree) * ((n_sp + kNodeBuffer - 1) / kNodeBuffer);
-    if (n_sp > h->a_sp || items_cap > h->a_e) {
+    if (n_sp > sl.a_sp || items_cap > sl.a_e) {
         Work tmp{};
         const size_t need = carve_a(h, nullptr, n_sp, items_cap, tmp);
-        if (!h->arena_a.ensure(need)) return SEEDGB_CUDA_ERROR;
-        h->a_sp = n_sp;
-        h->a_e = items_cap;
+        if (!sl.arena_a.ensure(need)) return SEEDGB_CUDA_ERROR;
+        sl.a_sp = n_sp;
+        sl.a_e = items_cap;
     }
-    Work& w = h->w;
-    carve_a(h, static_cast<char*>(h->arena_a.p), h->a_sp, h->a_e, w);
-    w.sz = h->d_sz;
+    Work& w = sl.w;
+    carve_a(h, static_cast<char*>(sl.arena_a.p), sl.a_sp, sl.a_e, w);
+    w.sz = sl.d_sz;
     const Tables T = tables_of(h);
     const uint64_t N = n_sp;
     const uint64_t E = w.ecap;  // edge capacity: max_edges_factor x arena spacepoints
     const uint32_t cells = h->n_eta * h->cfg.n_phi_bins;
     unsigned long long* st = w.tstate;
-    const uint64_t scan_tiles = (std::max<uint64_t>({E + 1, N + 1, cells + 1ull, h->a_e * kEdgeThreads + 1,
+    const uint64_t scan_tiles = (std::max<uint64_t>({E + 1, N + 1, cells + 1ull, sl.a_e * kEdgeThreads + 1,
                                                     h->n_pairs + 1ull}) / kScanTile) + 4;
-    cudaMemsetAsync(st, 0, sizeof(unsigned long long) * scan_tiles, s);
-    cudaMemsetAsync(w.flags, 0, sizeof(uint32_t) * kFlagSlots, s);
+    cudaMemsetAsync(st, 0, sizeof(unsigned long long) * scan_tiles, sl.stream);
+    cudaMemsetAsync(w.flags, 0, sizeof(uint32_t) * kFlagSlots, sl.stream);
     // nodes
-    cudaMemsetAsync(w.cell_cnt, 0, sizeof(uint32_t) * (cells + 1ull), s);
-    cudaMemsetAsync(w.cell_cur, 0, sizeof(uint32_t) * (cells + 1ull), s);
-    k_classify<<<blocks(N), kThreads, 0, s>>>(T, *sps, surface_link, diameter, n_meas, w);
-    scan(h, w.cell_cnt, w.cell_off, nullptr, cells, 0, cells + 1ull, st, h->d_sz + S_NODES, s);
-    k_scatter<<<blocks(N), kThreads, 0, s>>>(n_sp, w);
-    k_sort_cells<<<blocks(cells), kThreads, 0, s>>>(cells, w);
-    k_node_params<<<blocks(N), kThreads, 0, s>>>(T, w);
-    k_eta_bins<<<blocks(32ull * h->n_eta), kThreads, 0, s>>>(h->n_eta, h->cfg.n_phi_bins, w);
+    cudaMemsetAsync(w.cell_cnt, 0, sizeof(uint32_t) * (cells + 1ull), sl.stream);
+    cudaMemsetAsync(w.cell_cur, 0, sizeof(uint32_t) * (cells + 1ull), sl.stream);
+    k_classify<<<blocks(N), kThreads, 0, sl.stream>>>(T, *sps, surface_link, diameter, n_meas, w);
+    scan(sl, w.cell_cnt, w.cell_off, nullptr, cells, 0, cells + 1ull, st, sl.d_sz + S_NODES);
+    k_scatter<<<blocks(N), kThreads, 0, sl.stream>>>(n_sp, w);
+    k_sort_cells<<<blocks(cells), kThreads, 0, sl.stream>>>(cells, w);
+    k_node_params<<<blocks(N), kThreads, 0, sl.stream>>>(T, w);
+    k_eta_bins<<<blocks(32ull * h->n_eta), kThreads, 0, sl.stream>>>(h->n_eta, h->cfg.n_phi_bins, w);
     // work items
-    k_items_count<<<blocks(h->n_pairs), kThreads, 0, s>>>(T, w);
-    scan(h, w.item_cnt, w.item_off, nullptr, h->n_pairs, 0, h->n_pairs + 1ull, st, h->d_sz + S_ITEMS, s);
-    k_items_fill<<<blocks(h->n_pairs), kThreads, 0, s>>>(T, w);
+    k_items_count<<<blocks(h->n_pairs), kThreads, 0, sl.stream>>>(T, w);
+    scan(sl, w.item_cnt, w.item_off, nullptr, h->n_pairs, 0, h->n_pairs + 1ull, st, sl.d_sz + S_ITEMS);
+    k_items_fill<<<blocks(h->n_pairs), kThreads, 0, sl.stream>>>(T, w);
     // edges: count per (item, thread), scan, write
     const uint32_t edge_grid = 152u * 16u;
-    k_edges<false><<<edge_grid, kEdgeThreads, 0, s>>>(T, w);
-    scan(h, w.item_tcnt, w.item_toff, h->d_sz + S_SLOTS, 0, 0, h->a_e * kEdgeThreads + 1, st,
-         h->d_sz + S_EDGES_MADE, s);
-    cudaMemsetAsync(w.out_cnt, 0, sizeof(uint32_t) * (N + 1), s);
-    k_edges<true><<<edge_grid, kEdgeThreads, 0, s>>>(T, w);
+    k_edges<false><<<edge_grid, kEdgeThreads, 0, sl.stream>>>(T, w);
+    scan(sl, w.item_tcnt, w.item_toff, sl.d_sz + S_SLOTS, 0, 0, sl.a_e * kEdgeThreads + 1, st,
+         sl.d_sz + S_EDGES_MADE);
+    cudaMemsetAsync(w.out_cnt, 0, sizeof(uint32_t) * (N + 1), sl.stream);
+    k_edges<true><<<edge_grid, kEdgeThreads, 0, sl.stream>>>(T, w);
     // the edges leaving each node: offsets by inner node, lists in ascending
     // edge index; every kernel from here to the path store reads its size
     // from device memory (grid-stride launches), so nothing waits on the host
-    scan(h, w.out_cnt, w.lstart, h->d_sz + S_NODES, 0, 0, N + 1, st, nullptr, s);
-    cudaMemsetAsync(w.lcur, 0, sizeof(uint32_t) * (N + 1), s);
-    k_edges_kept<<<1, 1, 0, s>>>(T, w);
-    k_link_fill<<<blocks(E), kThreads, 0, s>>>(w);
-    k_link_sort<<<kGrid, kThreads, 0, s>>>(w);
-    k_match<<<blocks(E), kThreads, 0, s>>>(T, w);
-    scan(h, w.kept, w.kbase, h->d_sz + S_EDGES, 0, 0, E + 1, st, h->d_sz + S_CONNECTED, s);
-    k_compress<<<blocks(E), kThreads, 0, s>>>(T, w);
+    scan(sl, w.out_cnt, w.lstart, sl.d_sz + S_NODES, 0, 0, N + 1, st, nullptr);
+    cudaMemsetAsync(w.lcur, 0, sizeof(uint32_t) * (N + 1), sl.stream);
+    k_edges_kept<<<1, 1, 0, sl.stream>>>(T, w);
+    k_link_fill<<<blocks(E), kThreads, 0, sl.stream>>>(w);
+    k_link_sort<<<kGrid, kThreads, 0, sl.stream>>>(w);
+    k_match<<<blocks(E), kThreads, 0, sl.stream>>>(T, w);
+    scan(sl, w.kept, w.kbase, sl.d_sz + S_EDGES, 0, 0, E + 1, st, sl.d_sz + S_CONNECTED);
+    k_compress<<<blocks(E), kThreads, 0, sl.stream>>>(T, w);
     // automaton over the connected edges
-    cudaMemsetAsync(w.levels, 1, static_cast<size_t>(2 * E), s);
+    cudaMemsetAsync(w.levels, 1, static_cast<size_t>(2 * E), sl.stream);
     {
         Tables Tc = T;
         Work wc = w;
         void* args[] = {&Tc, &wc};
         if (cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(k_cca_all), dim3(h->coop_cca),
-                                        dim3(kThreads), args, 0, s) != cudaSuccess)
+                                        dim3(kThreads), args, 0, sl.stream) != cudaSuccess)
             return SEEDGB_CUDA_ERROR;
     }
-    k_term_flags<<<kGrid, kThreads, 0, s>>>(w);
-    scan(h, w.tflag, w.tidx, h->d_sz + S_CONNECTED, 0, 0, E + 1, st, h->d_sz + S_TERMINUS, s);
-    scan(h, w.tpaths, w.pbase, h->d_sz + S_CONNECTED, 0, 0, E + 1, st, h->d_sz + S_PATHS, s);
-    // the one wait: the path store's size
-    if (cudaMemcpyAsync(h->h_sz, h->d_sz, sizeof(uint32_t) * S_COUNT, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-        cudaStreamSynchronize(s) != cudaSuccess)
+    k_term_flags<<<kGrid, kThreads, 0, sl.stream>>>(w);
+    scan(sl, w.tflag, w.tidx, sl.d_sz + S_CONNECTED, 0, 0, E + 1, st, sl.d_sz + S_TERMINUS);
+    scan(sl, w.tpaths, w.pbase, sl.d_sz + S_CONNECTED, 0, 0, E + 1, st, sl.d_sz + S_PATHS);
+    if (cudaMemcpyAsync(sl.h_sz, sl.d_sz, sizeof(uint32_t) * S_COUNT, cudaMemcpyDeviceToHost,
+                        sl.stream) != cudaSuccess ||
+        cudaEventRecord(sl.ready, sl.stream) != cudaSuccess)
         return SEEDGB_CUDA_ERROR;
-    const uint64_t n_edges = h->h_sz[S_EDGES];
-    const uint64_t n_term = h->h_sz[S_TERMINUS], n_paths = h->h_sz[S_PATHS];
+    sl.pending = true;
+    sl.out = *out;
+    sl.n_sp = n_sp;
+    return SEEDGB_OK;
+}
+
+// the rest of the event once its path store's size is on the host
+seedgb_status finish(seedgb_gbts* h, Slot& sl) {
+    if (!sl.pending) return SEEDGB_OK;
+    sl.pending = false;
+    if (cudaEventSynchronize(sl.ready) != cudaSuccess) return SEEDGB_CUDA_ERROR;
+    const seedgb_seed_buffer* out = &sl.out;
+    const uint32_t n_sp = sl.n_sp;
+    Work& w = sl.w;
+    const Tables T = tables_of(h);
+    const uint64_t n_edges = sl.h_sz[S_EDGES];
+    const uint64_t n_term = sl.h_sz[S_TERMINUS], n_paths = sl.h_sz[S_PATHS];
     if (n_term == 0 || n_paths == 0) {
-        k_empty_out<<<1, 1, 0, s>>>(*out);
+        k_empty_out<<<1, 1, 0, sl.stream>>>(*out);
         return cudaGetLastError() == cudaSuccess ? SEEDGB_OK : SEEDGB_CUDA_ERROR;
     }
     {
         Work tmp{};
         const size_t need = carve_b(nullptr, n_term, n_paths, tmp);
-        if (!h->arena_b.ensure(need)) return SEEDGB_CUDA_ERROR;
-        carve_b(static_cast<char*>(h->arena_b.p), n_term, n_paths, w);
-        cudaMemsetAsync(w.tstate_b, 0, sizeof(unsigned long long) * ((n_paths + 1) / kScanTile + 4), s);
+        if (!sl.arena_b.ensure(need)) return SEEDGB_CUDA_ERROR;
+        carve_b(static_cast<char*>(sl.arena_b.p), n_term, n_paths, w);
+        cudaMemsetAsync(w.tstate_b, 0, sizeof(unsigned long long) * ((n_paths + 1) / kScanTile + 4), sl.stream);
     }
-    k_term_fill<<<kGrid, kThreads, 0, s>>>(w);
-    k_dfs<<<blocks(n_term), kThreads, 0, s>>>(T, w);
-    k_fit<<<blocks(n_paths), kThreads, 0, s>>>(T, w);
-    scan(h, w.fflag, w.fidx, h->d_sz + S_PATHS, 0, 0, n_paths + 1, w.tstate_b, h->d_sz + S_PROPS, s);
-    k_props<<<blocks(n_paths), kThreads, 0, s>>>(w);
+    k_term_fill<<<kGrid, kThreads, 0, sl.stream>>>(w);
+    k_dfs<<<blocks(n_term), kThreads, 0, sl.stream>>>(T, w);
+    k_fit<<<blocks(n_paths), kThreads, 0, sl.stream>>>(T, w);
+    scan(sl, w.fflag, w.fidx, sl.d_sz + S_PATHS, 0, 0, n_paths + 1, w.tstate_b, sl.d_sz + S_PROPS);
+    k_props<<<blocks(n_paths), kThreads, 0, sl.stream>>>(w);
     // bidding: the fit's one-edge bids, the rounds, the hit bids
     {
         Tables Tc = T;
@@ -1801,31 +1853,103 @@ extern "C" seedgb_status seedgb_gbts_run(seedgb_gbts* h, const seedgb_spacepoint
         uint32_t ne = static_cast<uint32_t>(n_edges), nsp = n_sp, rounds = h->cfg.edge_bidding_rounds;
         void* args[] = {&Tc, &wc, &ne, &nsp, &rounds};
         if (cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(k_bidding), dim3(h->coop_bid),
-                                        dim3(kThreads), args, 0, s) != cudaSuccess)
+                                        dim3(kThreads), args, 0, sl.stream) != cudaSuccess)
             return SEEDGB_CUDA_ERROR;
     }
-    k_convert<<<blocks(n_paths), kThreads, 0, s>>>(T, w);
-    scan(h, w.ecount, w.eoff, h->d_sz + S_PROPS, 0, 0, n_paths + 1, w.tstate_b, h->d_sz + S_SEEDS, s);
-    k_seeds_out<<<blocks(n_paths), kThreads, 0, s>>>(w, *out);
+    k_convert<<<blocks(n_paths), kThreads, 0, sl.stream>>>(T, w);
+    scan(sl, w.ecount, w.eoff, sl.d_sz + S_PROPS, 0, 0, n_paths + 1, w.tstate_b, sl.d_sz + S_SEEDS);
+    k_seeds_out<<<blocks(n_paths), kThreads, 0, sl.stream>>>(w, *out);
     return cudaGetLastError() == cudaSuccess ? SEEDGB_OK : SEEDGB_CUDA_ERROR;
+}
+
+}  // namespace
+
+extern "C" seedgb_status seedgb_gbts_run(seedgb_gbts* h, const seedgb_spacepoint_view* sps,
+                                         const uint64_t* surface_link, const float* diameter,
+                                         uint32_t n_meas, seedgb_seed_buffer* out, void* stream) {
+    if (!h) return SEEDGB_INVALID_ARGUMENT;
+    const seedgb_status chk = check_event(sps, surface_link, diameter, n_meas, out);
+    if (chk != SEEDGB_OK) return chk;
+    Slot& sl = h->slot[0];
+    sl.stream = static_cast<cudaStream_t>(stream);
+    h->used = 1;
+    h->last_slot = 0;
+    if (cudaMemsetAsync(sl.d_sz + S_STATUS, 0, sizeof(uint32_t) * (S_COUNT - S_STATUS), sl.stream) !=
+        cudaSuccess)
+        return SEEDGB_CUDA_ERROR;
+    const seedgb_status st = front(h, sl, sps, surface_link, diameter, n_meas, out);
+    if (st != SEEDGB_OK) return st;
+    return finish(h, sl);
+}
+
+extern "C" seedgb_status seedgb_gbts_run_batch(seedgb_gbts* h, const seedgb_spacepoint_view* events,
+                                               const uint64_t* const* surface_links,
+                                               const float* const* diameters, const uint32_t* n_meas,
+                                               uint32_t n_events, seedgb_seed_buffer* outs,
+                                               void* stream) {
+    if (!h || (n_events && (!events || !surface_links || !diameters || !n_meas || !outs)))
+        return SEEDGB_INVALID_ARGUMENT;
+    for (uint32_t e = 0; e < n_events; ++e) {
+        const seedgb_status chk =
+            check_event(&events[e], surface_links[e], diameters[e], n_meas[e], &outs[e]);
+        if (chk != SEEDGB_OK) return chk;
+    }
+    if (n_events == 0) return SEEDGB_OK;
+    const uint32_t S = std::min<uint32_t>(kMaxSlots, n_events);
+    for (uint32_t k = 0; k < S; ++k) {
+        Slot& sl = h->slot[k];
+        if (!slot_init(sl)) return SEEDGB_CUDA_ERROR;
+        sl.stream = static_cast<cudaStream_t>(stream);
+        if (cudaMemsetAsync(sl.d_sz + S_STATUS, 0, sizeof(uint32_t) * (S_COUNT - S_STATUS),
+                            sl.stream) != cudaSuccess)
+            return SEEDGB_CUDA_ERROR;
+    }
+    h->used = S;
+    seedgb_status st = SEEDGB_OK;
+    for (uint32_t e = 0; e < n_events && st == SEEDGB_OK; ++e) {
+        // the slot's previous event (e - S) gets its tail after event e - 1's
+        // front is queued; then event e's front
+        Slot& sl = h->slot[e % S];
+        st = finish(h, sl);
+        if (st == SEEDGB_OK)
+            st = front(h, sl, &events[e], surface_links[e], diameters[e], n_meas[e], &outs[e]);
+        h->last_slot = e % S;
+    }
+    for (uint32_t k = 0; k < S; ++k) {
+        const uint32_t e = (h->last_slot + 1 + k) % S;  // the older pending event first
+        const seedgb_status f = finish(h, h->slot[e]);
+        if (st == SEEDGB_OK) st = f;
+    }
+    return st;
 }
 
 extern "C" seedgb_status seedgb_gbts_last_status(seedgb_gbts* h, void* stream) {
     if (!h) return SEEDGB_INVALID_ARGUMENT;
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
-    if (cudaMemcpyAsync(h->h_sz, h->d_sz, sizeof(uint32_t) * S_COUNT, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-        cudaStreamSynchronize(s) != cudaSuccess)
+    if (cudaStreamSynchronize(static_cast<cudaStream_t>(stream)) != cudaSuccess)
         return SEEDGB_CUDA_ERROR;
-    if (h->h_sz[S_BAD_INPUT]) return SEEDGB_INVALID_ARGUMENT;
-    return static_cast<seedgb_status>(h->h_sz[S_STATUS]);
+    uint32_t worst = SEEDGB_OK;
+    bool bad_input = false;
+    for (uint32_t k = 0; k < h->used; ++k) {
+        Slot& sl = h->slot[k];
+        if (cudaMemcpyAsync(sl.h_sz, sl.d_sz, sizeof(uint32_t) * S_COUNT, cudaMemcpyDeviceToHost,
+                            sl.stream) != cudaSuccess ||
+            cudaStreamSynchronize(sl.stream) != cudaSuccess)
+            return SEEDGB_CUDA_ERROR;
+        worst = std::max(worst, sl.h_sz[S_STATUS]);
+        bad_input |= sl.h_sz[S_BAD_INPUT] != 0;
+    }
+    if (bad_input) return SEEDGB_INVALID_ARGUMENT;
+    return static_cast<seedgb_status>(worst);
 }
 
 extern "C" seedgb_status seedgb_gbts_counters(seedgb_gbts* h, uint64_t* counters) {
     if (!h || !counters) return SEEDGB_INVALID_ARGUMENT;
-    if (cudaMemcpyAsync(h->h_sz, h->d_sz, sizeof(uint32_t) * S_COUNT, cudaMemcpyDeviceToHost, h->last) != cudaSuccess ||
-        cudaStreamSynchronize(h->last) != cudaSuccess)
+    Slot& sl = h->slot[h->last_slot];
+    if (cudaMemcpyAsync(sl.h_sz, sl.d_sz, sizeof(uint32_t) * S_COUNT, cudaMemcpyDeviceToHost,
+                        sl.stream) != cudaSuccess ||
+        cudaStreamSynchronize(sl.stream) != cudaSuccess)
         return SEEDGB_CUDA_ERROR;
-    const uint32_t* z = h->h_sz;
+    const uint32_t* z = sl.h_sz;
     counters[0] = z[S_NODES];
     counters[1] = z[S_EDGES_MADE];
     counters[2] = z[S_CONN];

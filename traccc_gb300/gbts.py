@@ -81,6 +81,8 @@ def lib():
         L.seedgb_gbts_run.argtypes = [vp, P(_s._SpacepointView), vp, vp, C.c_uint32,
                                       P(_s._SeedBuffer), vp]
         L.seedgb_gbts_run.restype = C.c_int
+        L.seedgb_gbts_run_batch.argtypes = [vp, vp, vp, vp, vp, C.c_uint32, vp, vp]
+        L.seedgb_gbts_run_batch.restype = C.c_int
         L.seedgb_gbts_last_status.argtypes = [vp, vp]
         L.seedgb_gbts_last_status.restype = C.c_int
         L.seedgb_gbts_counters.argtypes = [vp, P(C.c_uint64)]
@@ -188,6 +190,26 @@ class GbtsSeedingAlgorithm:
                                         int(measurements.surface_link.shape[0]), C.byref(b),
                                         _s._stream_ptr(stream)), "seedgb_gbts_run")
         return out
+
+    def run_batch(self, spacepoints, measurements, outs=None, stream=None):
+        """seedgb_gbts_run_batch: the events in one call (same seeds as one
+        call per event)."""
+        n = len(spacepoints)
+        if len(measurements) != n:
+            raise ValueError("run_batch: one measurement collection per event")
+        if any(m.diameter is None for m in measurements):
+            raise ValueError("GBTS seeding needs the measurements' cluster diameters")
+        if outs is None:
+            outs = [_s.SeedBuffer(self.max_seeds(len(sp)), device=sp.global_.device)
+                    for sp in spacepoints]
+        views = (_s._SpacepointView * n)(*[sp.view() for sp in spacepoints])
+        bufs = (_s._SeedBuffer * n)(*[o.buf() for o in outs])
+        links = (C.c_void_p * n)(*[m.surface_link.data_ptr() for m in measurements])
+        dias = (C.c_void_p * n)(*[m.diameter.data_ptr() for m in measurements])
+        nm = (C.c_uint32 * n)(*[int(m.surface_link.shape[0]) for m in measurements])
+        _s._check(lib().seedgb_gbts_run_batch(self._h, views, links, dias, nm, n, bufs,
+                                              _s._stream_ptr(stream)), "seedgb_gbts_run_batch")
+        return outs
 
     def last_status(self, stream=None) -> int:
         return int(lib().seedgb_gbts_last_status(self._h, _s._stream_ptr(stream)))
