@@ -243,34 +243,51 @@ k_scan(const uint32_t* in, uint32_t* out, const uint32_t* n_dev, uint32_t n_host
     }
     uint32_t total;
     uint32_t run = block_exclusive_scan(sum, &total);
-    if (threadIdx.x == 0) {
+    // look-back by the first warp: 32 predecessor states per step, nearest
+    // first; the step stops at the nearest inclusive prefix, else adds the 32
+    // aggregates and moves on; a state not yet published makes the warp
+    // re-read (bounded)
+    if (threadIdx.x < 32) {
+        const uint32_t lane = threadIdx.x;
+        if (tile != 0 && lane == 0) atomicExch(&state[tile], tile_word(epoch, kFlagAggregate, total));
+        const unsigned long long want = epoch & 0x3FFFFFFFu;
         uint32_t prefix = 0;
-        if (tile != 0) {
-            atomicExch(&state[tile], tile_word(epoch, kFlagAggregate, total));
-            const unsigned long long want = epoch & 0x3FFFFFFFu;
-            int j = static_cast<int>(tile) - 1;
-            uint32_t spins = 0;
-            while (j >= 0) {
+        int hi = static_cast<int>(tile) - 1;  // nearest predecessor not yet added
+        uint32_t spins = 0;
+        while (hi >= 0) {
+            const int j = hi - static_cast<int>(lane);
+            uint32_t flag = kFlagPrefix, val = 0;  // lanes before tile 0: a zero prefix
+            if (j >= 0) {
                 const unsigned long long sv = *reinterpret_cast<volatile unsigned long long*>(&state[j]);
-                const uint32_t flag = static_cast<uint32_t>(sv >> 32) & 3u;
-                if ((sv >> 34) != want || flag == 0u) {
-                    if (++spins > kSpinLimit) {
-                        set_status(sz, SEEDGB_TIMEOUT);
-                        break;
-                    }
-                    __nanosleep(64);
-                    continue;
-                }
-                prefix += static_cast<uint32_t>(sv);
-                if (flag == kFlagPrefix) break;
-                --j;
+                flag = ((sv >> 34) == want) ? static_cast<uint32_t>(sv >> 32) & 3u : 0u;
+                val = static_cast<uint32_t>(sv);
             }
+            const unsigned not_ready = __ballot_sync(0xffffffffu, flag == 0u);
+            const unsigned is_prefix = __ballot_sync(0xffffffffu, flag == kFlagPrefix);
+            // lanes up to the nearest prefix (lowest lane with one) count
+            const uint32_t stop = is_prefix ? static_cast<uint32_t>(__ffs(is_prefix) - 1) : 31u;
+            const unsigned needed = stop == 31u ? 0xffffffffu : ((2u << stop) - 1u);
+            if (not_ready & needed) {
+                if (++spins > kSpinLimit) {
+                    if (lane == 0) set_status(sz, SEEDGB_TIMEOUT);
+                    break;
+                }
+                __nanosleep(64);
+                continue;
+            }
+            uint32_t part = lane <= stop ? val : 0u;
+            for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+            prefix += part;
+            if (is_prefix) break;
+            hi -= 32;
         }
-        atomicExch(&state[tile], tile_word(epoch, kFlagPrefix, prefix + total));
-        s_prefix = prefix;
-        if (tile == n_tiles - 1u) {
-            out[n] = prefix + total;
-            if (total_dst) *total_dst = prefix + total;
+        if (lane == 0) {
+            atomicExch(&state[tile], tile_word(epoch, kFlagPrefix, prefix + total));
+            s_prefix = prefix;
+            if (tile == n_tiles - 1u) {
+                out[n] = prefix + total;
+                if (total_dst) *total_dst = prefix + total;
+            }
         }
     }
     __syncthreads();
