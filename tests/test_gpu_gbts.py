@@ -171,3 +171,53 @@ def test_gbts_batch_equals_per_event_calls():
                 assert np.array_equal(g[k], ref[k])
             assert np.array_equal(g["quality"].view(np.uint32), ref["quality"].view(np.uint32))
     assert len(single[2]) == 0 and len(single[1]) > 0
+
+
+def _long_chain_event():
+    """24 barrel layers 30 mm apart and straight tracks from the beam line:
+    chains of up to 23 edges, past the automaton's 15 iterations, plus
+    tracks crossing only the first 12 layers (chains that settle)."""
+    radii = 40.0 + 30.0 * np.arange(24)
+    layers = np.zeros(len(radii), gbts.LAYER_DTYPE)
+    for i in range(len(radii)):
+        layers[i] = (0, i, 1, -5.0, 10.0)          # one eta bin per layer
+    pairs = np.array([(i, i + 1) for i in range(len(radii) - 1)], np.uint32)
+    geoid = np.zeros(len(radii), [("barcode", np.uint64), ("layer", np.int16)])
+    geoid["barcode"] = (np.arange(1, len(radii) + 1, dtype=np.uint64) << np.uint64(52))
+    geoid["layer"] = np.arange(len(radii))
+    pts, lay, part = [], [], []
+    rng = np.random.default_rng(5)
+    for k, phi in enumerate(rng.uniform(-3.0, 3.0, 12)):
+        tau = rng.uniform(0.2, 1.2)
+        z0 = rng.uniform(-50.0, 50.0)
+        n_layers = len(radii) if k % 2 == 0 else 12
+        for i in range(n_layers):
+            r = radii[i]
+            pts.append((r * np.cos(phi), r * np.sin(phi), z0 + tau * r))
+            lay.append(i)
+            part.append(k)
+    g = np.asarray(pts, np.float32)
+    n = len(g)
+    ev = {"measurement_index_1": np.arange(n, dtype=np.uint32),
+          "measurement_index_2": np.full(n, 0xFFFFFFFF, np.uint32), "global": g,
+          "z_variance": np.zeros(n, np.float32), "radius_variance": np.zeros(n, np.float32),
+          "layer": np.asarray(lay, np.uint32), "particle": np.asarray(part, np.int32)}
+    link = (np.asarray(lay, np.uint64) + np.uint64(1)) << np.uint64(52)
+    dia = np.zeros(n, np.float32)      # no cluster width: the full tau window
+    return ev, link, dia, layers, pairs, geoid
+
+
+def test_gbts_chains_longer_than_the_automaton():
+    ev, link, dia, layers, pairs, geoid = _long_chain_event()
+    got, ctr = _compare(ev, link, dia, layers, pairs, geoid)
+    assert ctr["connected_edges"] > 0 and ctr["seeds"] > 0
+    # a 24-layer track's 23-edge chain: its 8 innermost edges would need more
+    # than 15 iterations, are capped and never enter a path, so its seeds
+    # start at layer 8; a 12-layer track's seeds start at layer 0
+    part = ev["particle"]
+    lay = ev["layer"]
+    assert np.all(part[got["bottom"]] == part[got["top"]])
+    for k in range(12):
+        b = lay[got["bottom"][part[got["bottom"]] == k]]
+        assert len(b) > 0
+        assert b.min() == (8 if k % 2 == 0 else 0), (k, b.min())
