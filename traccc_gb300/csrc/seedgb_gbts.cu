@@ -118,6 +118,7 @@ struct Work {
     uint32_t *e_in, *e_out;
     float4* e_p;
     uint32_t *out_cnt, *lstart, *lcur, *links, *links_tmp;
+    uint32_t *in_cnt, *instart, *incur, *in_list;  // the edges entering each node (by outer node)
     uint8_t* nnei;
     uint32_t *nei, *kept, *kbase;
     // graph and automaton
@@ -693,7 +694,17 @@ __global__ void __launch_bounds__(kThreads) k_link_fill(Work w) {
     GRID_STRIDE(e, w.sz[S_EDGES]) {
         const uint32_t n1 = w.e_in[e];
         w.links_tmp[w.lstart[n1] + atomicAdd(&w.lcur[n1], 1u)] = e;
+        atomicAdd(&w.in_cnt[w.e_out[e]], 1u);
         w.kept[e] = 0u;
+    }
+}
+
+// the edges entering each node, in any order (the matching of an edge does
+// not depend on the other edges entering its outer node)
+__global__ void __launch_bounds__(kThreads) k_in_fill(Work w) {
+    GRID_STRIDE(e, w.sz[S_EDGES]) {
+        const uint32_t n2 = w.e_out[e];
+        w.in_list[w.instart[n2] + atomicAdd(&w.incur[n2], 1u)] = e;
     }
 }
 
@@ -715,50 +726,69 @@ __global__ void __launch_bounds__(kThreads) k_link_sort(Work w) {
     }
 }
 
-// gbts_match_graph_edges.ipp:29-118
-__global__ void __launch_bounds__(kThreads) k_match(Tables T, Work w) {
-    GRID_STRIDE(e, w.sz[S_EDGES]) {
+// gbts_match_graph_edges.ipp:29-118: each edge keeps the first max_num_neighbours
+// edges leaving its outer node (in link order) that pass the tau-ratio, phi
+// and curvature cuts.  Done per node: one warp stages the node's outgoing
+// edges (the candidates) in shared memory and its lanes match the edges
+// entering the node against them; lists longer than the stage read the rest
+// from global memory.  Every edge enters exactly one node, so every edge is
+// matched once.
+constexpr uint32_t kMatchStage = 128;
+constexpr int kMatchWarps = kThreads / 32;
+
+__global__ void __launch_bounds__(kThreads) k_match_nodes(Tables T, Work w) {
+    __shared__ uint32_t s_e2_all[kMatchWarps][kMatchStage];
+    __shared__ float4 s_p2_all[kMatchWarps][kMatchStage];
+    const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
+    uint32_t* s_e2 = s_e2_all[wid];
+    float4* s_p2 = s_p2_all[wid];
     const seedgb_gbts_config& c = T.c;
     const uint32_t M = c.max_num_neighbours;
-    const uint32_t shared_node = w.e_out[e];
-    const uint32_t link_begin = w.lstart[shared_node];
-    const uint32_t nLinks = w.lstart[shared_node + 1] - link_begin;
-    uint32_t num_nei = 0;
-    if (nLinks != 0u) {
-        const float4 p1 = w.e_p[e];
-        const float uat_2 = 1.0f / p1.x;
-        const float Phi2 = p1.z;
-        const float curv2 = p1.y;
-        // candidates loaded four at a time (loads in flight together), tested
-        // in list order
-        for (uint32_t k0 = 0u; k0 < nLinks && num_nei < M; k0 += 4u) {
-            uint32_t e2s[4];
-            float4 p2s[4];
-#pragma unroll
-            for (int j = 0; j < 4; ++j) e2s[j] = k0 + j < nLinks ? w.links[link_begin + k0 + j] : 0u;
-#pragma unroll
-            for (int j = 0; j < 4; ++j)
-                p2s[j] = k0 + j < nLinks ? w.e_p[e2s[j]] : make_float4(0.f, 0.f, 0.f, 0.f);
-            for (int j = 0; j < 4 && k0 + j < nLinks; ++j) {
-                if (num_nei >= M) break;
-                const float4 p2 = p2s[j];
-                const float tau_ratio = p2.x * uat_2 - 1.0f;
-                if (fabsf(tau_ratio) > c.cut_tau_ratio_max) continue;
-                const float dPhi = wrap_phi(Phi2 - p2.w);
-                if (fabsf(dPhi) > c.cut_dphi_max) continue;
-                const float dcurv = curv2 - p2.y;
-                if (fabsf(dcurv) > c.cut_dcurv_max) continue;
-                w.nei[static_cast<uint64_t>(M) * e + num_nei] = e2s[j];
-                w.kept[e2s[j]] = 1u;
-                ++num_nei;
+    const uint32_t n_nodes = w.sz[S_NODES];
+    for (uint32_t n = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; n < n_nodes;
+         n += (gridDim.x * blockDim.x) >> 5) {
+        const uint32_t i0 = w.instart[n], ni = w.instart[n + 1] - i0;
+        if (ni == 0) continue;
+        const uint32_t link_begin = w.lstart[n];
+        const uint32_t nLinks = w.lstart[n + 1] - link_begin;
+        const uint32_t staged = nLinks < kMatchStage ? nLinks : kMatchStage;
+        __syncwarp();
+        for (uint32_t k = lane; k < staged; k += 32) {
+            const uint32_t e2 = w.links[link_begin + k];
+            s_e2[k] = e2;
+            s_p2[k] = w.e_p[e2];
+        }
+        __syncwarp();
+        for (uint32_t i = lane; i < ni; i += 32) {
+            const uint32_t e = w.in_list[i0 + i];
+            uint32_t num_nei = 0;
+            if (nLinks != 0u) {
+                const float4 p1 = w.e_p[e];
+                const float uat_2 = 1.0f / p1.x;
+                const float Phi2 = p1.z;
+                const float curv2 = p1.y;
+                for (uint32_t k = 0u; k < nLinks; k++) {
+                    if (num_nei >= M) break;
+                    const bool st = k < kMatchStage;
+                    const uint32_t e2 = st ? s_e2[k] : w.links[link_begin + k];
+                    const float4 p2 = st ? s_p2[k] : w.e_p[e2];
+                    const float tau_ratio = p2.x * uat_2 - 1.0f;
+                    if (fabsf(tau_ratio) > c.cut_tau_ratio_max) continue;
+                    const float dPhi = wrap_phi(Phi2 - p2.w);
+                    if (fabsf(dPhi) > c.cut_dphi_max) continue;
+                    const float dcurv = curv2 - p2.y;
+                    if (fabsf(dcurv) > c.cut_dcurv_max) continue;
+                    w.nei[static_cast<uint64_t>(M) * e + num_nei] = e2;
+                    w.kept[e2] = 1u;
+                    ++num_nei;
+                }
+            }
+            w.nnei[e] = static_cast<uint8_t>(num_nei);
+            if (num_nei != 0) {
+                w.kept[e] = 1u;
+                atomicAdd(&w.sz[S_CONN], num_nei);
             }
         }
-    }
-    w.nnei[e] = static_cast<uint8_t>(num_nei);
-    if (num_nei != 0) {
-        w.kept[e] = 1u;
-        atomicAdd(&w.sz[S_CONN], num_nei);
-    }
     }
 }
 
@@ -1437,6 +1467,10 @@ size_t carve_a(seedgb_gbts* h, char* base, uint64_t n_sp, uint64_t items_cap, Wo
     w.lcur = cv.take<uint32_t>(N + 1);
     w.links = cv.take<uint32_t>(E);
     w.links_tmp = cv.take<uint32_t>(E);
+    w.in_cnt = cv.take<uint32_t>(N + 1);
+    w.instart = cv.take<uint32_t>(N + 1);
+    w.incur = cv.take<uint32_t>(N + 1);
+    w.in_list = cv.take<uint32_t>(E);
     w.nnei = cv.take<uint8_t>(E);
     w.nei = cv.take<uint32_t>(M * E);
     w.kept = cv.take<uint32_t>(E);
@@ -1807,10 +1841,14 @@ seedgb_status front(seedgb_gbts* h, Slot& sl, const seedgb_spacepoint_view* sps,
     // from device memory (grid-stride launches), so nothing waits on the host
     scan(sl, w.out_cnt, w.lstart, sl.d_sz + S_NODES, 0, 0, N + 1, st, nullptr);
     cudaMemsetAsync(w.lcur, 0, sizeof(uint32_t) * (N + 1), sl.stream);
+    cudaMemsetAsync(w.in_cnt, 0, sizeof(uint32_t) * (N + 1), sl.stream);
+    cudaMemsetAsync(w.incur, 0, sizeof(uint32_t) * (N + 1), sl.stream);
     k_edges_kept<<<1, 1, 0, sl.stream>>>(T, w);
     k_link_fill<<<blocks(E), kThreads, 0, sl.stream>>>(w);
     k_link_sort<<<kGrid, kThreads, 0, sl.stream>>>(w);
-    k_match<<<blocks(E), kThreads, 0, sl.stream>>>(T, w);
+    scan(sl, w.in_cnt, w.instart, sl.d_sz + S_NODES, 0, 0, N + 1, st, nullptr);
+    k_in_fill<<<blocks(E), kThreads, 0, sl.stream>>>(w);
+    k_match_nodes<<<kGrid, kThreads, 0, sl.stream>>>(T, w);
     scan(sl, w.kept, w.kbase, sl.d_sz + S_EDGES, 0, 0, E + 1, st, sl.d_sz + S_CONNECTED);
     k_compress<<<blocks(E), kThreads, 0, sl.stream>>>(T, w);
     // automaton over the connected edges
