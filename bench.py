@@ -566,6 +566,47 @@ def run_gbts(args, stream, flush_buf, events):
         e1.synchronize()
         ms_b.append(e0.elapsed_time(e1))
     status_b = alg.last_status(stream=sptr)
+    # end to end through the same call: every step copies the events' columns
+    # in from pinned host memory and the seeds (sizes, then the seeds) out
+    cols = []
+    for sp, m in data:
+        cols.append([(torch.empty_like(t, device="cpu").pin_memory(), t) for t in
+                     (sp.measurement_index_1, sp.measurement_index_2, sp.global_, sp.z_variance,
+                      sp.radius_variance, m.surface_link, m.diameter)])
+    for c_ in cols:
+        for h_, d_ in c_:
+            h_.copy_(d_)
+    h2d = sum(h_.numel() * h_.element_size() for c_ in cols for h_, _ in c_)
+    h_size = torch.zeros(len(outs), dtype=torch.int32).pin_memory()
+    h_out = [torch.empty((4, max(1, o.capacity)), dtype=torch.int32).pin_memory() for o in outs]
+
+    def e2e_step():
+        with torch.cuda.stream(stream):
+            for c_ in cols:
+                for h_, d_ in c_:
+                    d_.copy_(h_, non_blocking=True)
+            alg.run_batch(sps_l, meas_l, outs, stream=sptr)
+            for i, o in enumerate(outs):
+                h_size[i:i + 1].copy_(o.size, non_blocking=True)
+        stream.synchronize()
+        nbytes = 4 * h_size.numel()
+        with torch.cuda.stream(stream):
+            for i, o in enumerate(outs):
+                ns = int(h_size[i])
+                for j, col in enumerate((o.bottom_index, o.middle_index, o.top_index)):
+                    h_out[i][j, :ns].copy_(col[:ns], non_blocking=True)
+                h_out[i][3, :ns].copy_(o.quality[:ns].view(torch.int32), non_blocking=True)
+                nbytes += 16 * ns
+        stream.synchronize()
+        return nbytes
+
+    for _ in range(2):
+        e2e_step()
+    t0 = time.perf_counter()
+    d2h = 0
+    for _ in range(steps):
+        d2h = e2e_step()
+    e2e_s = time.perf_counter() - t0
     got = outs[0].to_numpy()
     ev, link, dia = host[0]
     oc = oracle.GbtsConfig()
@@ -592,6 +633,11 @@ def run_gbts(args, stream, flush_buf, events):
                         f"default cuts at min_pt 900 MeV, max_edges_factor {GBTS_EDGES_FACTOR}",
             "value": 1e3 * n_ev / med, "unit": "events/s", "ms_per_step": med,
             "ms_per_event": med / n_ev, "status": int(status),
+            "e2e": {"value": n_ev * steps / e2e_s, "unit": "events/s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h),
+                    "timing": "wall clock over the steps: the events' spacepoint and measurement "
+                              "columns in from pinned host memory, one seedgb_gbts_run_batch "
+                              "call, the seed counts and then the seeds out"},
             "batch": {"value": 1e3 * n_ev / statistics.median(ms_b), "unit": "events/s",
                       "ms_per_step": statistics.median(ms_b), "status": int(status_b),
                       "timing": "one seedgb_gbts_run_batch call per step (event e + 1's kernels "
