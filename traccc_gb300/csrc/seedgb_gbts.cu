@@ -10,9 +10,10 @@
 // computes the same chain in one fixed order, so results are reproducible and
 // equal to the CPU oracle bit for bit:
 //   - nodes of one (eta, phi) cell in ascending spacepoint index;
-//   - edges by (work item, outer node, inner node), each work item a bin pair
-//     with a bin-1 chunk of at most 128 nodes, 128 threads per item taking the
-//     outer nodes t, t + 128, ... with the reference's sliding-window state;
+//   - edges by (work item, thread, outer node, inner node), each work item a
+//     bin pair with a bin-1 chunk of at most 128 nodes, 128 threads per item
+//     taking the outer nodes t, t + 128, ... with the reference's
+//     sliding-window state;
 //   - every node's outgoing edges in ascending edge index;
 //   - connected edges numbered in ascending edge index (a scan, not atomics);
 //   - terminus edges in ascending connected-edge index, the path store as a
@@ -34,10 +35,7 @@
 #include <climits>
 #include <cmath>
 #include <cstdint>
-#include <cstdio>
 #include <cstring>
-#include <fstream>
-#include <string>
 #include <vector>
 
 #include "seedgb.h"
