@@ -64,7 +64,8 @@ constexpr uint32_t kFlagSlots = 64u;  // automaton iterations, then bidding roun
 enum Size : uint32_t {
     S_NODES = 0,
     S_ITEMS,
-    S_SLOTS,
+    S_UNITS,
+    S_RECS,
     S_EDGES_MADE,
     S_EDGES,
     S_CONN,
@@ -111,7 +112,9 @@ struct Work {
     uint4* items;
     float* item_dphi;
     uint32_t* item_eta;  // eta bin of bin 1, top bit: the bin holds a node wrapped to phi bin 0
-    uint32_t *item_tcnt, *item_toff;  // edges per (item, thread) and their offsets
+    uint32_t *unit_cnt, *unit_off, *unit_pos, *unit_nrec;  // per (item, quarter)
+    uint2* rec_a;        // records: (outer node index, first edge's position in the unit)
+    ulonglong2* rec_m;   // records: inner-node mask
     // edges
     uint32_t *e_in, *e_out;
     float4* e_p;
@@ -606,74 +609,253 @@ __device__ __forceinline__ uint32_t walk(const ItemCtx& it, uint32_t n2Idx, uint
     return cnt;
 }
 
+// The same walk recording which inner nodes pair with the outer node: bit
+// n1Idx of (lo, hi) (the chunk has at most 128 nodes); the candidate loop
+// only sets bits, so it runs without branches on the result.
+__device__ __forceinline__ uint32_t walk_mask(const ItemCtx& it, uint32_t n2Idx, uint32_t& last_n1,
+                                              bool& done, const float* s_phi, const float4* s_np,
+                                              const Work& w, const seedgb_gbts_config& c,
+                                              unsigned long long& lo, unsigned long long& hi) {
+    lo = 0ull;
+    hi = 0ull;
+    const uint32_t g2 = it.b2 + n2Idx;
+    const float phi2 = w.node_phi[g2];
+    uint32_t n1Idx = last_n1;
+    float min_phi1 = phi2 - it.dphi;
+    float max_phi1 = phi2 + it.dphi;
+    if (min_phi1 < -kPi) min_phi1 += kTwoPi;
+    if (max_phi1 > kPi) max_phi1 -= kTwoPi;
+    const bool boundary = max_phi1 < min_phi1;
+    max_phi1 += it.pbw;
+    min_phi1 -= it.pbw;
+    if (!boundary) {
+        if (it.phi0 > max_phi1) return 0;
+        if (it.phiN < min_phi1) {
+            if (it.phi0 > it.brk) done = true;
+            return 0;
+        }
+        const float x = (min_phi1 + kPi) * it.inv_slice;
+        if (it.bin_first && x >= 1.0f) {
+            const uint32_t pb = static_cast<uint32_t>(x);
+            if (pb < it.n_phi) {
+                const uint32_t f = it.bin_first[pb];
+                const uint32_t jump = f > it.b1 ? (f - it.b1 < it.n1 ? f - it.b1 : it.n1) : 0u;
+                if (jump > n1Idx) n1Idx = jump;
+            }
+        }
+    } else {
+        if (it.phi0 < max_phi1) {
+            n1Idx = 0u;
+        } else if (it.phiN < min_phi1) {
+            return 0;
+        }
+    }
+    const float4 np2 = w.node_p[g2];
+    for (; n1Idx < it.n1; n1Idx++) {
+        const float phi1 = s_phi[n1Idx];
+        if (!boundary) {
+            if (phi1 > max_phi1) break;
+            if (phi1 < min_phi1) continue;
+        } else if (phi1 > max_phi1 && phi1 < min_phi1) {
+            continue;
+        }
+        last_n1 = n1Idx;
+        float4 ep;
+        const bool pass = edge_test(s_np[n1Idx], np2, phi1, phi2, it.dphi, c, ep);
+        const unsigned long long bit = pass ? (1ull << (n1Idx & 63u)) : 0ull;
+        lo |= n1Idx < 64u ? bit : 0ull;
+        hi |= n1Idx < 64u ? 0ull : bit;
+    }
+    return static_cast<uint32_t>(__popcll(lo) + __popcll(hi));
+}
+
+// The parameters of an edge that passed (exp(-eta), curvature, phi
+// extrapolated at node 2 and at node 1), the same float operations as in
+// edge_test, so a recomputation gives the same bits.
+__device__ __forceinline__ float4 edge_params(float4 np1, float4 np2, float phi1, float phi2) {
+    const float dr = np2.z - np1.z;
+    const float tau = (np2.w - np1.w) / dr;
+    const float curv = wrap_phi(phi2 - phi1) / dr;
+    return make_float4(sqrtf(1.0f + tau * tau) - tau, curv, phi2 + curv * np2.z, phi1 + curv * np1.z);
+}
+
 // Edges of one work item, thread t (of 128) taking the outer nodes t,
 // t + 128, ... with the reference's sliding-window state; an item's edges in
 // thread order, then outer node, then inner node.  The four warps of a block
 // work independently: a warp takes one quarter of an item (threads 32q ...
-// 32q + 31) and stages its own copy of the item's bin-1 chunk, so only warp
-// barriers remain.  The count pass records each thread's edge count; after
-// one scan over (item, thread) the write pass walks again and writes from the
-// thread's offset.
+// 32q + 31, a "unit") and stages its own copy of the item's bin-1 chunk, so
+// only warp barriers remain.  k_edge_masks walks once and keeps, per outer
+// node with edges, a record (outer node, inner-node bit mask, the position of
+// its first edge within the unit); after a scan over the units' edge counts,
+// k_edge_expand writes one edge per set bit.  A unit with more than
+// kRecStage records is walked again by k_edge_expand (count, then write).
 constexpr int kEdgeWarps = kEdgeThreads / 32;
+constexpr uint32_t kRecStage = 256;
+constexpr uint32_t kUnitOverflow = 0xFFFFFFFFu;
 
-template <bool WRITE>
-__global__ void __launch_bounds__(kEdgeThreads) k_edges(Tables T, Work w) {
+__device__ __forceinline__ void setup_item(const Tables& T, const Work& w, uint32_t item, uint32_t lane,
+                                           ItemCtx& it, uint32_t& n2, float* s_phi, float4* s_np,
+                                           uint32_t* s_cnt) {
+    const uint4 r = w.items[item];
+    it.b1 = r.x;
+    it.n1 = r.y - r.x;
+    it.b2 = r.z;
+    n2 = r.w - r.z;
+    it.dphi = w.item_dphi[item];
+    const uint32_t em = w.item_eta[item];
+    it.bin_first = (em & 0x80000000u) ? nullptr : w.cell_off + (em & 0x7FFFFFFFu) * T.c.n_phi_bins;
+    it.n_phi = T.c.n_phi_bins;
+    it.inv_slice = 1.0f / (kTwoPi / static_cast<float>(T.c.n_phi_bins));
+    __syncwarp();
+    for (uint32_t k = lane; k < kNodeBuffer; k += 32) {
+        if (k < it.n1) {
+            s_np[k] = w.node_p[it.b1 + k];
+            s_phi[k] = w.node_phi[it.b1 + k];
+        }
+        if (s_cnt) s_cnt[k] = 0;
+    }
+    __syncwarp();
+    it.phi0 = s_phi[0];
+    it.phiN = s_phi[it.n1 - 1u];
+    it.pbw = kTwoPi / static_cast<float>(T.c.n_phi_bins);
+    it.brk = it.dphi + it.pbw - kPi;
+}
+
+__device__ __forceinline__ uint32_t warp_exclusive(uint32_t v, uint32_t lane, uint32_t& total) {
+    uint32_t incl = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t x = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= static_cast<uint32_t>(o)) incl += x;
+    }
+    total = __shfl_sync(0xffffffffu, incl, 31);
+    return incl - v;
+}
+
+__global__ void __launch_bounds__(kEdgeThreads) k_edge_masks(Tables T, Work w) {
     __shared__ float s_phi_all[kEdgeWarps][kNodeBuffer];
     __shared__ float4 s_np_all[kEdgeWarps][kNodeBuffer];
-    __shared__ uint32_t s_cnt_all[kEdgeWarps][kNodeBuffer];  // edges per inner node
+    __shared__ uint2 s_ra_all[kEdgeWarps][kRecStage];        // (lane << 27 | n2Idx, lane's edges before)
+    __shared__ ulonglong2 s_rm_all[kEdgeWarps][kRecStage];   // the inner-node mask
+    __shared__ uint32_t s_nrec_all[kEdgeWarps];
+    __shared__ uint32_t s_excl_all[kEdgeWarps][32];
+    const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
+    float* s_phi = s_phi_all[wid];
+    float4* s_np = s_np_all[wid];
+    uint2* s_ra = s_ra_all[wid];
+    ulonglong2* s_rm = s_rm_all[wid];
+    uint32_t* s_excl = s_excl_all[wid];
+    const uint32_t n_items = w.sz[S_ITEMS];
+    if (blockIdx.x == 0 && threadIdx.x == 0) w.sz[S_UNITS] = n_items * kEdgeWarps;
+    const uint32_t n_units = n_items * kEdgeWarps;
+    for (uint32_t u = blockIdx.x * kEdgeWarps + wid; u < n_units; u += gridDim.x * kEdgeWarps) {
+        ItemCtx it;
+        uint32_t n2;
+        setup_item(T, w, u / kEdgeWarps, lane, it, n2, s_phi, s_np, nullptr);
+        if (lane == 0) s_nrec_all[wid] = 0;
+        __syncwarp();
+        const uint32_t t = 32u * (u % kEdgeWarps) + lane;
+        uint32_t last_n1 = 0u, cnt = 0;
+        bool done = false;
+        for (uint32_t n2Idx = t; n2Idx < n2 && !done; n2Idx += kEdgeThreads) {
+            unsigned long long lo, hi;
+            const uint32_t k = walk_mask(it, n2Idx, last_n1, done, s_phi, s_np, w, T.c, lo, hi);
+            if (k) {
+                const uint32_t r = atomicAdd(&s_nrec_all[wid], 1u);
+                if (r < kRecStage) {
+                    s_ra[r] = make_uint2((lane << 27) | n2Idx, cnt);
+                    s_rm[r] = make_ulonglong2(lo, hi);
+                }
+                cnt += k;
+            }
+        }
+        __syncwarp();
+        uint32_t total;
+        s_excl[lane] = warp_exclusive(cnt, lane, total);
+        const uint32_t nrec = s_nrec_all[wid];
+        bool ok = nrec <= kRecStage && n2 < (1u << 27);
+        uint32_t pos0 = 0;
+        if (ok) {
+            if (lane == 0) pos0 = atomicAdd(&w.sz[S_RECS], nrec);
+            pos0 = __shfl_sync(0xffffffffu, pos0, 0);
+            ok = static_cast<uint64_t>(pos0) + nrec <= w.ecap;
+        }
+        __syncwarp();
+        if (ok)
+            for (uint32_t r = lane; r < nrec; r += 32) {
+                const uint2 a = s_ra[r];
+                w.rec_a[pos0 + r] = make_uint2(a.x & ((1u << 27) - 1u), s_excl[a.x >> 27] + a.y);
+                w.rec_m[pos0 + r] = s_rm[r];
+            }
+        if (lane == 0) {
+            w.unit_cnt[u] = total;
+            w.unit_pos[u] = ok ? pos0 : kUnitOverflow;
+            w.unit_nrec[u] = nrec;
+        }
+        __syncwarp();
+    }
+}
+
+__global__ void __launch_bounds__(kEdgeThreads) k_edge_expand(Tables T, Work w) {
+    __shared__ float s_phi_all[kEdgeWarps][kNodeBuffer];
+    __shared__ float4 s_np_all[kEdgeWarps][kNodeBuffer];
+    __shared__ uint32_t s_cnt_all[kEdgeWarps][kNodeBuffer];  // edges per inner node of the chunk
     const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
     float* s_phi = s_phi_all[wid];
     float4* s_np = s_np_all[wid];
     uint32_t* s_cnt = s_cnt_all[wid];
-    const uint32_t n_items = w.sz[S_ITEMS];
-    if (!WRITE && blockIdx.x == 0 && threadIdx.x == 0) w.sz[S_SLOTS] = n_items * kEdgeThreads;
     const uint64_t by_nodes = static_cast<uint64_t>(T.c.max_edges_factor) * w.sz[S_NODES];
     const uint64_t cap = by_nodes < w.ecap ? by_nodes : w.ecap;
-    const uint32_t n_units = n_items * kEdgeWarps;
+    const uint32_t n_units = w.sz[S_UNITS];
     for (uint32_t u = blockIdx.x * kEdgeWarps + wid; u < n_units; u += gridDim.x * kEdgeWarps) {
-        const uint32_t item = u / kEdgeWarps, q = u % kEdgeWarps;
-        const uint4 r = w.items[item];
+        if (w.unit_cnt[u] == 0) continue;
         ItemCtx it;
-        it.b1 = r.x;
-        it.n1 = r.y - r.x;
-        it.b2 = r.z;
-        const uint32_t n2 = r.w - r.z;
-        it.dphi = w.item_dphi[item];
-        const uint32_t em = w.item_eta[item];
-        it.bin_first = (em & 0x80000000u) ? nullptr : w.cell_off + (em & 0x7FFFFFFFu) * T.c.n_phi_bins;
-        it.n_phi = T.c.n_phi_bins;
-        it.inv_slice = 1.0f / (kTwoPi / static_cast<float>(T.c.n_phi_bins));
-        __syncwarp();
-        for (uint32_t k = lane; k < kNodeBuffer; k += 32) {
-            if (k < it.n1) {
-                s_np[k] = w.node_p[it.b1 + k];
-                s_phi[k] = w.node_phi[it.b1 + k];
+        uint32_t n2;
+        setup_item(T, w, u / kEdgeWarps, lane, it, n2, s_phi, s_np, s_cnt);
+        const uint64_t off = w.unit_off[u];
+        const uint32_t pos0 = w.unit_pos[u];
+        if (pos0 != kUnitOverflow) {
+            const uint32_t nrec = w.unit_nrec[u];
+            for (uint32_t r = lane; r < nrec; r += 32) {
+                const uint2 a = w.rec_a[pos0 + r];
+                const ulonglong2 m = w.rec_m[pos0 + r];
+                const uint32_t g2 = it.b2 + a.x;
+                const float4 np2 = w.node_p[g2];
+                const float phi2 = w.node_phi[g2];
+                uint64_t q = off + a.y;
+                for (int half = 0; half < 2; ++half) {
+                    unsigned long long bits = half ? m.y : m.x;
+                    while (bits) {
+                        const uint32_t i1 = (half ? 64u : 0u) + static_cast<uint32_t>(__ffsll(bits) - 1);
+                        bits &= bits - 1ull;
+                        if (q < cap) {
+                            w.e_in[q] = it.b1 + i1;
+                            w.e_out[q] = g2;
+                            w.e_p[q] = edge_params(s_np[i1], np2, s_phi[i1], phi2);
+                            atomicAdd(&s_cnt[i1], 1u);
+                        }
+                        ++q;
+                    }
+                }
             }
-            s_cnt[k] = 0;
+        } else {
+            // more records than the stage held: count per thread, then write
+            const uint32_t t = 32u * (u % kEdgeWarps) + lane;
+            uint32_t last_n1 = 0u, cnt = 0;
+            bool done = false;
+            for (uint32_t n2Idx = t; n2Idx < n2 && !done; n2Idx += kEdgeThreads)
+                cnt += walk<false>(it, n2Idx, last_n1, done, s_phi, s_np, w, T.c, 0, 0, s_cnt);
+            uint32_t total;
+            const uint64_t pos = off + warp_exclusive(cnt, lane, total);
+            const uint32_t want = cnt;
+            last_n1 = 0u;
+            done = false;
+            cnt = 0;
+            for (uint32_t n2Idx = t; n2Idx < n2 && !done && cnt < want; n2Idx += kEdgeThreads)
+                cnt += walk<true>(it, n2Idx, last_n1, done, s_phi, s_np, w, T.c, pos + cnt, cap, s_cnt);
         }
         __syncwarp();
-        it.phi0 = s_phi[0];
-        it.phiN = s_phi[it.n1 - 1u];
-        it.pbw = kTwoPi / static_cast<float>(T.c.n_phi_bins);
-        it.brk = it.dphi + it.pbw - kPi;
-        const uint32_t t = 32u * q + lane;
-        uint32_t last_n1 = 0u;
-        bool done = false;
-        const uint64_t slot = static_cast<uint64_t>(item) * kEdgeThreads + t;
-        uint64_t pos = WRITE ? w.item_toff[slot] : 0;
-        // the write pass knows the thread's edge count: it stops once they
-        // are all written (the rest of its walk would find none)
-        const uint32_t want = WRITE ? w.item_tcnt[slot] : 0xFFFFFFFFu;
-        uint32_t cnt = 0;
-        for (uint32_t n2Idx = t; n2Idx < n2 && !done && cnt < want; n2Idx += kEdgeThreads)
-            cnt += walk<WRITE>(it, n2Idx, last_n1, done, s_phi, s_np, w, T.c, pos + cnt, cap, s_cnt);
-        if (!WRITE) {
-            w.item_tcnt[slot] = cnt;
-        } else {
-            __syncwarp();
-            for (uint32_t k = lane; k < it.n1; k += 32)
-                if (s_cnt[k]) atomicAdd(&w.out_cnt[it.b1 + k], s_cnt[k]);
-        }
+        for (uint32_t k = lane; k < it.n1; k += 32)
+            if (s_cnt[k]) atomicAdd(&w.out_cnt[it.b1 + k], s_cnt[k]);
     }
 }
 
@@ -1437,7 +1619,7 @@ size_t carve_a(seedgb_gbts* h, char* base, uint64_t n_sp, uint64_t items_cap, Wo
     const uint64_t M = h->cfg.max_num_neighbours;
     const uint64_t cells = static_cast<uint64_t>(h->n_eta) * h->cfg.n_phi_bins;
     const uint64_t scan_cap =
-        std::max<uint64_t>({E + 1, N + 1, cells + 1, items_cap * kEdgeThreads + 1, h->n_pairs + 1ull});
+        std::max<uint64_t>({E + 1, N + 1, cells + 1, items_cap * kEdgeWarps + 1, h->n_pairs + 1ull});
     Carver cv{base};
     w.red = cv.take<float4>(N);
     w.sp_phi = cv.take<float>(N);
@@ -1455,8 +1637,12 @@ size_t carve_a(seedgb_gbts* h, char* base, uint64_t n_sp, uint64_t items_cap, Wo
     w.items = cv.take<uint4>(items_cap);
     w.item_dphi = cv.take<float>(items_cap);
     w.item_eta = cv.take<uint32_t>(items_cap);
-    w.item_tcnt = cv.take<uint32_t>(items_cap * kEdgeThreads + 1);
-    w.item_toff = cv.take<uint32_t>(items_cap * kEdgeThreads + 1);
+    w.unit_cnt = cv.take<uint32_t>(items_cap * kEdgeWarps + 1);
+    w.unit_off = cv.take<uint32_t>(items_cap * kEdgeWarps + 1);
+    w.unit_pos = cv.take<uint32_t>(items_cap * kEdgeWarps + 1);
+    w.unit_nrec = cv.take<uint32_t>(items_cap * kEdgeWarps + 1);
+    w.rec_a = cv.take<uint2>(E);
+    w.rec_m = cv.take<ulonglong2>(E);
     w.e_in = cv.take<uint32_t>(E);
     w.e_out = cv.take<uint32_t>(E);
     w.e_p = cv.take<float4>(E);
@@ -1810,7 +1996,7 @@ seedgb_status front(seedgb_gbts* h, Slot& sl, const seedgb_spacepoint_view* sps,
     const uint64_t E = w.ecap;  // edge capacity: max_edges_factor x arena spacepoints
     const uint32_t cells = h->n_eta * h->cfg.n_phi_bins;
     unsigned long long* st = w.tstate;
-    const uint64_t scan_tiles = (std::max<uint64_t>({E + 1, N + 1, cells + 1ull, sl.a_e * kEdgeThreads + 1,
+    const uint64_t scan_tiles = (std::max<uint64_t>({E + 1, N + 1, cells + 1ull, sl.a_e * kEdgeWarps + 1,
                                                     h->n_pairs + 1ull}) / kScanTile) + 4;
     cudaMemsetAsync(st, 0, sizeof(unsigned long long) * scan_tiles, sl.stream);
     cudaMemsetAsync(w.flags, 0, sizeof(uint32_t) * kFlagSlots, sl.stream);
@@ -1827,13 +2013,14 @@ seedgb_status front(seedgb_gbts* h, Slot& sl, const seedgb_spacepoint_view* sps,
     k_items_count<<<blocks(h->n_pairs), kThreads, 0, sl.stream>>>(T, w);
     scan(sl, w.item_cnt, w.item_off, nullptr, h->n_pairs, 0, h->n_pairs + 1ull, st, sl.d_sz + S_ITEMS);
     k_items_fill<<<blocks(h->n_pairs), kThreads, 0, sl.stream>>>(T, w);
-    // edges: count per (item, thread), scan, write
+    // edges: one walk per (item, quarter) keeping inner-node masks, a scan
+    // over the units' edge counts, one edge record per set bit
     const uint32_t edge_grid = 152u * 16u;
-    k_edges<false><<<edge_grid, kEdgeThreads, 0, sl.stream>>>(T, w);
-    scan(sl, w.item_tcnt, w.item_toff, sl.d_sz + S_SLOTS, 0, 0, sl.a_e * kEdgeThreads + 1, st,
+    k_edge_masks<<<edge_grid, kEdgeThreads, 0, sl.stream>>>(T, w);
+    scan(sl, w.unit_cnt, w.unit_off, sl.d_sz + S_UNITS, 0, 0, sl.a_e * kEdgeWarps + 1, st,
          sl.d_sz + S_EDGES_MADE);
     cudaMemsetAsync(w.out_cnt, 0, sizeof(uint32_t) * (N + 1), sl.stream);
-    k_edges<true><<<edge_grid, kEdgeThreads, 0, sl.stream>>>(T, w);
+    k_edge_expand<<<edge_grid, kEdgeThreads, 0, sl.stream>>>(T, w);
     // the edges leaving each node: offsets by inner node, lists in ascending
     // edge index; every kernel from here to the path store reads its size
     // from device memory (grid-stride launches), so nothing waits on the host
