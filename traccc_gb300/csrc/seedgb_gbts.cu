@@ -66,6 +66,7 @@ enum Size : uint32_t {
     S_ITEMS,
     S_UNITS,
     S_RECS,
+    S_UNIT_NEXT,  // next unit for k_edge_masks' warps
     S_EDGES_MADE,
     S_EDGES,
     S_CONN,
@@ -689,8 +690,10 @@ __device__ __forceinline__ float4 edge_params(float4 np1, float4 np2, float phi1
 // its first edge within the unit); after a scan over the units' edge counts,
 // k_edge_expand writes one edge per set bit.  A unit with more than
 // kRecStage records is walked again by k_edge_expand (count, then write).
+// The walk's warps take units from a counter, so a costly unit late in the
+// order holds up only its own warp.
 constexpr int kEdgeWarps = kEdgeThreads / 32;
-constexpr uint32_t kRecStage = 256;
+constexpr uint32_t kRecStage = 128;
 constexpr uint32_t kUnitOverflow = 0xFFFFFFFFu;
 
 __device__ __forceinline__ void setup_item(const Tables& T, const Work& w, uint32_t item, uint32_t lane,
@@ -731,7 +734,7 @@ __device__ __forceinline__ uint32_t warp_exclusive(uint32_t v, uint32_t lane, ui
     return incl - v;
 }
 
-__global__ void __launch_bounds__(kEdgeThreads) k_edge_masks(Tables T, Work w) {
+__global__ void __launch_bounds__(kEdgeThreads, 8) k_edge_masks(Tables T, Work w) {
     __shared__ float s_phi_all[kEdgeWarps][kNodeBuffer];
     __shared__ float4 s_np_all[kEdgeWarps][kNodeBuffer];
     __shared__ uint2 s_ra_all[kEdgeWarps][kRecStage];        // (lane << 27 | n2Idx, lane's edges before)
@@ -747,7 +750,11 @@ __global__ void __launch_bounds__(kEdgeThreads) k_edge_masks(Tables T, Work w) {
     const uint32_t n_items = w.sz[S_ITEMS];
     if (blockIdx.x == 0 && threadIdx.x == 0) w.sz[S_UNITS] = n_items * kEdgeWarps;
     const uint32_t n_units = n_items * kEdgeWarps;
-    for (uint32_t u = blockIdx.x * kEdgeWarps + wid; u < n_units; u += gridDim.x * kEdgeWarps) {
+    for (;;) {
+        uint32_t u = 0;
+        if (lane == 0) u = atomicAdd(&w.sz[S_UNIT_NEXT], 1u);
+        u = __shfl_sync(0xffffffffu, u, 0);
+        if (u >= n_units) break;
         ItemCtx it;
         uint32_t n2;
         setup_item(T, w, u / kEdgeWarps, lane, it, n2, s_phi, s_np, nullptr);
@@ -1571,7 +1578,7 @@ struct seedgb_gbts {
     uint32_t used = 1;       // slots the last call used
     uint32_t last_slot = 0;  // slot of the last event
     // cooperative launches: blocks that can be co-resident
-    uint32_t coop_cca = 0, coop_bid = 0;
+    uint32_t coop_cca = 0, coop_bid = 0, walk_blocks = 0;
 };
 
 namespace {
@@ -1913,12 +1920,14 @@ extern "C" seedgb_status seedgb_gbts_create(const seedgb_gbts_config* config,
         delete h;
         return SEEDGB_CUDA_ERROR;
     }
-    int dev = 0, sms = 0, coop = 0, nb_cca = 0, nb_bid = 0;
+    int dev = 0, sms = 0, coop = 0, nb_cca = 0, nb_bid = 0, nb_walk = 0;
     if (cudaGetDevice(&dev) != cudaSuccess ||
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
         cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess ||
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb_cca, k_cca_all, kThreads, 0) != cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb_bid, k_bidding, kThreads, 0) != cudaSuccess) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb_bid, k_bidding, kThreads, 0) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb_walk, k_edge_masks, kEdgeThreads, 0) !=
+            cudaSuccess) {
         free_tables(h);
         delete h;
         return SEEDGB_CUDA_ERROR;
@@ -1932,6 +1941,8 @@ extern "C" seedgb_status seedgb_gbts_create(const seedgb_gbts_config* config,
     // arrivals per grid barrier)
     h->coop_cca = static_cast<uint32_t>(nb_cca * sms);
     h->coop_bid = static_cast<uint32_t>(std::min(nb_bid, 2) * sms);
+    // the edge walk: every block resident, units handed out by a counter
+    h->walk_blocks = static_cast<uint32_t>(std::max(nb_walk, 1) * sms);
     *out = h;
     return SEEDGB_OK;
 }
@@ -2016,7 +2027,7 @@ seedgb_status front(seedgb_gbts* h, Slot& sl, const seedgb_spacepoint_view* sps,
     // edges: one walk per (item, quarter) keeping inner-node masks, a scan
     // over the units' edge counts, one edge record per set bit
     const uint32_t edge_grid = 152u * 16u;
-    k_edge_masks<<<edge_grid, kEdgeThreads, 0, sl.stream>>>(T, w);
+    k_edge_masks<<<h->walk_blocks, kEdgeThreads, 0, sl.stream>>>(T, w);
     scan(sl, w.unit_cnt, w.unit_off, sl.d_sz + S_UNITS, 0, 0, sl.a_e * kEdgeWarps + 1, st,
          sl.d_sz + S_EDGES_MADE);
     cudaMemsetAsync(w.out_cnt, 0, sizeof(uint32_t) * (N + 1), sl.stream);
