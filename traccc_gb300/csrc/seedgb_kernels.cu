@@ -841,6 +841,15 @@ __device__ __forceinline__ uint32_t scan_runs(const DevConfig& c, const NbViewT<
                                               uint32_t lt) {
     const uint32_t total = pre[ns];
     uint32_t nq = 0;
+    // a lane's flat indices only rise: its run, the flat index where that
+    // run ends and the run's position offset stay in registers and advance
+    // at run boundaries only
+    uint32_t run[2] = {0u, 0u}, end[2], off[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        end[h] = pre[1];
+        off[h] = bnd[TOP ? 2 : 0];  // pre[0] == 0
+    }
     for (uint32_t base = 0; base < total; base += 64) {
         bool ok[2] = {false, false};
         uint32_t p[2] = {0, 0};
@@ -848,9 +857,12 @@ __device__ __forceinline__ uint32_t scan_runs(const DevConfig& c, const NbViewT<
         for (int h = 0; h < 2; ++h) {
             const uint32_t f = base + 32 * h + lane;
             if (f < total) {
-                uint32_t s = 0;
-                while (s + 1 < ns && pre[s + 1] <= f) ++s;
-                p[h] = bnd[4 * s + (TOP ? 2 : 0)] + (f - pre[s]);
+                while (f >= end[h]) {
+                    const uint32_t s = ++run[h];
+                    end[h] = pre[s + 1];
+                    off[h] = bnd[4 * s + (TOP ? 2 : 0)] - pre[s];
+                }
+                p[h] = off[h] + f;
                 const float4 o = nb.staged[p[h]];
                 ok[h] = TOP ? window_top(c, M, o) : window_bottom(c, M, o);
             }
