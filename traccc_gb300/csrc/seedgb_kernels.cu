@@ -610,6 +610,30 @@ __device__ __forceinline__ bool better(float wa, float sa, uint32_t ka, float wb
     return ka < kb;
 }
 
+// An unsigned key in the order of the float values, +0 and -0 equal (as they
+// compare in better); the values are never NaN (finite coordinates give
+// finite weights and tie sums).
+__device__ __forceinline__ uint32_t order_key(float x) {
+    const uint32_t u = __float_as_uint(x + 0.0f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+// The best untaken triplet (weight not -inf) among k = lane, lane + 32, ...
+// in the order of better; ck = 0xffffffff when there is none.
+__device__ __forceinline__ void lane_best(const float* wf, const float* ts, uint32_t n,
+                                          uint32_t lane, float& cw, float& cs, uint32_t& ck) {
+    ck = 0xffffffffu;
+    for (uint32_t k = lane; k < n; k += 32) {
+        const float wk = wf[k];
+        if (wk == -__int_as_float(0x7f800000)) continue;
+        if (ck == 0xffffffffu || better(wk, ts[k], k, cw, cs, ck)) {
+            cw = wk;
+            cs = ts[k];
+            ck = k;
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Radius-sorted copy of every grid bin
 // ---------------------------------------------------------------------------
@@ -1353,8 +1377,13 @@ __device__ MiddleResult process_middle(const DevConfig& c, const Arena& a,
     }
     __syncwarp();
     for (uint32_t i = lane; i < n_mt; i += 32) {
-        const uint32_t slot = atomicAdd(&ws.bcur[cot_bucket(ws.mtd[i].x, cmin, scale)], 1u);
+        const float kt = ws.mtd[i].x;
+        const uint32_t slot = atomicAdd(&ws.bcur[cot_bucket(kt, cmin, scale)], 1u);
         ws.perm[slot] = static_cast<uint16_t>(i);
+        // without variances the error terms are never read again: er holds
+        // the tops' cot(theta) in bucket order, so the window walk below reads
+        // it beside perm instead of through it
+        if constexpr (!any_var) ws.er[slot] = kt;
     }
     __syncwarp();
 
@@ -1430,7 +1459,7 @@ __device__ MiddleResult process_middle(const DevConfig& c, const Arena& a,
                     uint32_t tp = 0;
                     if (j < cnt) {
                         tp = ws.perm[lo + j];
-                        const float kt = ws.mtd[tp].x;
+                        const float kt = any_var ? ws.mtd[tp].x : ws.er[lo + j];
                         ok = kt >= klo && kt <= khi;
                     }
                     const uint32_t mask = __ballot_sync(0xffffffffu, ok);
@@ -1654,39 +1683,41 @@ __device__ MiddleResult process_middle(const DevConfig& c, const Arena& a,
     //    then the final selection (seed_filtering.cpp:87-122).  Index k of
     //    the sorted triplets is their host order (the tie-break).
     const uint32_t K = min(c.maxSeedsPerSpM, static_cast<uint32_t>(kMaxSeedsPerMiddle));
+    // Each lane holds its best untaken triplet among k = lane, lane + 32, ...
+    // A round takes the warp's best by three warp reductions over order-
+    // preserving keys (weight, then tie sum, then host order); only the lane
+    // that held it looks for its next best.
+    float cw = 0.f, cs = 0.f;
+    uint32_t ck = 0xffffffffu;
+    lane_best(ws.wf, ws.ts, n_ct, lane, cw, cs, ck);
     float my_w = 0.f;
-    uint32_t my_p = 0, n_sel = 0;
+    uint32_t my_k = 0, n_sel = 0;
     for (uint32_t r = 0; r < K; ++r) {
-        float cw = -__int_as_float(0x7f800000), cs = 0.f;
-        uint32_t ck = 0xffffffffu;
-        for (uint32_t k = lane; k < n_ct; k += 32) {
-            const float wk = ws.wf[k];
-            if (wk == -__int_as_float(0x7f800000)) continue;
-            if (ck == 0xffffffffu || better(wk, ws.ts[k], k, cw, cs, ck)) {
-                cw = wk; cs = ws.ts[k]; ck = k;
-            }
-        }
-        for (int o = 16; o > 0; o >>= 1) {
-            const float ow = __shfl_xor_sync(0xffffffffu, cw, o);
-            const float os = __shfl_xor_sync(0xffffffffu, cs, o);
-            const uint32_t ok = __shfl_xor_sync(0xffffffffu, ck, o);
-            if (ok != 0xffffffffu && (ck == 0xffffffffu || better(ow, os, ok, cw, cs, ck))) {
-                cw = ow; cs = os; ck = ok;
-            }
-        }
-        if (ck == 0xffffffffu) break;
+        const bool has = ck != 0xffffffffu;
+        if (!__any_sync(0xffffffffu, has)) break;
+        const uint32_t kw = has ? order_key(cw) : 0u;
+        const uint32_t mw = __reduce_max_sync(0xffffffffu, kw);
+        const bool c1 = has && kw == mw;
+        const uint32_t ks = c1 ? order_key(cs) : 0u;
+        const uint32_t ms = __reduce_max_sync(0xffffffffu, ks);
+        const uint32_t mk = __reduce_min_sync(0xffffffffu, (c1 && ks == ms) ? ck : 0xffffffffu);
+        const uint32_t owner = mk & 31u;
+        const float w_sel = __shfl_sync(0xffffffffu, cw, owner);
         if (lane == r) {
-            const TripCand T = ws.ct[ws.sidx[ck]];
-            my_w = cw;
-            my_p = (static_cast<uint32_t>(ws.qb[T.ib]) << 16) | ws.ppt[T.tp];
+            my_w = w_sel;
+            my_k = mk;
         }
-        __syncwarp();
-        if (lane == 0) ws.wf[ck] = -__int_as_float(0x7f800000);  // taken
-        __syncwarp();
+        if (lane == owner) {
+            ws.wf[mk] = -__int_as_float(0x7f800000);  // taken
+            lane_best(ws.wf, ws.ts, n_ct, lane, cw, cs, ck);
+        }
         ++n_sel;
     }
     bool acc = false;
+    uint32_t my_p = 0;
     if (lane < n_sel) {
+        const TripCand T = ws.ct[ws.sidx[my_k]];
+        my_p = (static_cast<uint32_t>(ws.qb[T.ib]) << 16) | ws.ppt[T.tp];
         const float4 Bsel = nb.get(my_p >> 16);
         acc = (lane == 0) || (my_w > c.seed_min_weight) || (Bsel.w > c.spB_min_radius);
     }
