@@ -1392,9 +1392,11 @@ __device__ MiddleResult process_middle(const DevConfig& c, const Arena& a,
     //    buckets and queues those inside its exact cot window (q0, with the
     //    doublet's lin_circle), one entry per lane per step; stage 1 runs on
     //    32 queued candidates at a time, stage 2 on 32 stage-1 survivors at a
-    //    time, so both run with full lanes across doublets and chunks.
+    //    time, so both run with full lanes across doublets and chunks.  The
+    //    stage-1 queue is a ring of 64 entries (head h1, count n1, at most 63
+    //    held), so the survivors that stage 2 leaves stay in place.
     const float sig2 = c.sigmaScattering * c.sigmaScattering;
-    uint32_t n_ct = 0, n0 = 0, n1 = 0;
+    uint32_t n_ct = 0, n0 = 0, n1 = 0, h1 = 0;
     uint32_t c0 = 0, it = 0, maxc = 0;
     bool have_chunk = false;
     LinCircle lbm;
@@ -1518,7 +1520,7 @@ __device__ MiddleResult process_middle(const DevConfig& c, const Arena& a,
                     s1.is2 = iSinTheta2;
                 }
                 const uint32_t mask = __ballot_sync(0xffffffffu, ok);
-                if (ok) ws.q.q1[n1 + __popc(mask & lt)] = s1;
+                if (ok) ws.q.q1[(h1 + n1 + __popc(mask & lt)) & 63u] = s1;
                 n1 += __popc(mask);
             }
             // move the unprocessed tail of q0 (< 64 entries) to the front
@@ -1538,7 +1540,7 @@ __device__ MiddleResult process_middle(const DevConfig& c, const Arena& a,
             bool ok = false;
             TripCand t;
             if (lane < k2) {
-                const Stage1Cand e = ws.q.q1[lane];
+                const Stage1Cand e = ws.q.q1[(h1 + lane) & 63u];
                 LinCircle lb;
                 lb.cot = e.cot;
                 lb.idr = e.idr;
@@ -1560,12 +1562,8 @@ __device__ MiddleResult process_middle(const DevConfig& c, const Arena& a,
                 if (k < CAPCT) ws.ct[k] = t;
             }
             n_ct += __popc(mask);
-            const uint32_t rest = n1 - k2;
-            Stage1Cand t0;
-            if (lane < rest) t0 = ws.q.q1[k2 + lane];
-            __syncwarp();
-            if (lane < rest) ws.q.q1[lane] = t0;
-            n1 = rest;
+            h1 = (h1 + k2) & 63u;
+            n1 -= k2;
             __syncwarp();
         }
         if (!more && n0 == 0 && n1 == 0) break;
