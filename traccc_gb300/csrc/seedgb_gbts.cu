@@ -1049,7 +1049,10 @@ __device__ __forceinline__ bool cca_step(const Tables& T, const Work& w, uint32_
 // the fifteen iterations in one cooperative launch, a grid barrier between them
 // (an iteration that leaves no edge active ends the automaton: the
 // remaining iterations would change nothing)
-__global__ void __launch_bounds__(kThreads) k_cca_all(Tables T, Work w) {
+// 1024-thread blocks: full occupancy with a quarter of the blocks arriving at
+// each grid barrier
+constexpr int kCcaThreads = 1024;
+__global__ void __launch_bounds__(kCcaThreads) k_cca_all(Tables T, Work w) {
     cg::grid_group g = cg::this_grid();
     for (uint32_t iter = 0; iter < kMaxCca; ++iter) {
         const bool more = cca_step(T, w, iter);
@@ -1924,7 +1927,8 @@ extern "C" seedgb_status seedgb_gbts_create(const seedgb_gbts_config* config,
     if (cudaGetDevice(&dev) != cudaSuccess ||
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
         cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb_cca, k_cca_all, kThreads, 0) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb_cca, k_cca_all, kCcaThreads, 0) !=
+            cudaSuccess ||
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb_bid, k_bidding, kThreads, 0) != cudaSuccess ||
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb_walk, k_edge_masks, kEdgeThreads, 0) !=
             cudaSuccess) {
@@ -2054,7 +2058,7 @@ seedgb_status front(seedgb_gbts* h, Slot& sl, const seedgb_spacepoint_view* sps,
         Work wc = w;
         void* args[] = {&Tc, &wc};
         if (cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(k_cca_all), dim3(h->coop_cca),
-                                        dim3(kThreads), args, 0, sl.stream) != cudaSuccess)
+                                        dim3(kCcaThreads), args, 0, sl.stream) != cudaSuccess)
             return SEEDGB_CUDA_ERROR;
     }
     k_term_flags<<<kGrid, kThreads, 0, sl.stream>>>(w);
