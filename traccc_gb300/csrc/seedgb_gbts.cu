@@ -1372,17 +1372,20 @@ __device__ __forceinline__ void zero64(unsigned long long* p, uint64_t n) {
 }
 
 // the fit's bids on each proposal's outermost edge, the rounds of edge
-// bidding and the hit bids, in one cooperative launch
+// bidding and the hit bids, in one cooperative launch.  Bids are indexed by
+// connected edge (the path store's numbering), so only those entries are
+// cleared each round.
 __global__ void __launch_bounds__(kThreads)
-k_bidding(Tables T, Work w, uint32_t n_edges, uint32_t n_sp, uint32_t rounds) {
+k_bidding(Tables T, Work w, uint32_t n_sp, uint32_t rounds) {
     cg::grid_group g = cg::this_grid();
-    zero64(w.ebid, n_edges);
+    const uint32_t n_conn = w.sz[S_CONNECTED];
+    zero64(w.ebid, n_conn);
     zero64(w.hbid, n_sp);
     g.sync();
     bid_step(w, 1);
     g.sync();
     for (uint32_t r = 0; r < rounds; ++r) {
-        zero64(w.ebid, n_edges);
+        zero64(w.ebid, n_conn);
         const bool any = round_step(w, r == 0);
         if (__syncthreads_or(any) && threadIdx.x == 0) w.flags[kMaxCca + r] = 1u;
         g.sync();
@@ -2083,7 +2086,6 @@ seedgb_status finish(seedgb_gbts* h, Slot& sl) {
     const uint32_t n_sp = sl.n_sp;
     Work& w = sl.w;
     const Tables T = tables_of(h);
-    const uint64_t n_edges = sl.h_sz[S_EDGES];
     const uint64_t n_term = sl.h_sz[S_TERMINUS], n_paths = sl.h_sz[S_PATHS];
     if (n_term == 0 || n_paths == 0) {
         k_empty_out<<<1, 1, 0, sl.stream>>>(*out);
@@ -2105,8 +2107,8 @@ seedgb_status finish(seedgb_gbts* h, Slot& sl) {
     {
         Tables Tc = T;
         Work wc = w;
-        uint32_t ne = static_cast<uint32_t>(n_edges), nsp = n_sp, rounds = h->cfg.edge_bidding_rounds;
-        void* args[] = {&Tc, &wc, &ne, &nsp, &rounds};
+        uint32_t nsp = n_sp, rounds = h->cfg.edge_bidding_rounds;
+        void* args[] = {&Tc, &wc, &nsp, &rounds};
         if (cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(k_bidding), dim3(h->coop_bid),
                                         dim3(kThreads), args, 0, sl.stream) != cudaSuccess)
             return SEEDGB_CUDA_ERROR;
