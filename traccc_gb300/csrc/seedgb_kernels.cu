@@ -1626,6 +1626,10 @@ __device__ MiddleResult process_middle(const DevConfig& c, const Arena& a,
         }
     }
 
+    // the lane's best untaken triplet (cw, cs, ck), kept as the weights are
+    // written (the order of better; ck = 0xffffffff: none)
+    float cw = 0.f, cs = 0.f;
+    uint32_t ck = 0xffffffffu;
     // -- weights, one lane per triplet: compatible-seed weights over its
     //    doublet's run (triplet_finding.hpp:107-179), seed_weight and
     //    single_seed_cut (seed_selecting_helper.hpp:27-62)
@@ -1672,8 +1676,16 @@ __device__ MiddleResult process_middle(const DevConfig& c, const Arena& a,
         if (Tp.w < c.good_spT_max_radius) weight = c.good_spT_weight_increase;
         w += weight;
         const bool cut = B.w > c.good_spB_min_radius && w < c.good_spB_min_weight;
-        ws.wf[k] = cut ? -__int_as_float(0x7f800000) : w;
-        ws.ts[k] = B.y * B.y + B.z * B.z + Tp.y * Tp.y + Tp.z * Tp.z;
+        const float wk = cut ? -__int_as_float(0x7f800000) : w;
+        const float tk = B.y * B.y + B.z * B.z + Tp.y * Tp.y + Tp.z * Tp.z;
+        ws.wf[k] = wk;
+        ws.ts[k] = tk;
+        if (wk != -__int_as_float(0x7f800000) &&
+            (ck == 0xffffffffu || better(wk, tk, k, cw, cs, ck))) {
+            cw = wk;
+            cs = tk;
+            ck = k;
+        }
     }
     __syncwarp();
 
@@ -1685,9 +1697,6 @@ __device__ MiddleResult process_middle(const DevConfig& c, const Arena& a,
     // A round takes the warp's best by three warp reductions over order-
     // preserving keys (weight, then tie sum, then host order); only the lane
     // that held it looks for its next best.
-    float cw = 0.f, cs = 0.f;
-    uint32_t ck = 0xffffffffu;
-    lane_best(ws.wf, ws.ts, n_ct, lane, cw, cs, ck);
     float my_w = 0.f;
     uint32_t my_k = 0, n_sel = 0;
     for (uint32_t r = 0; r < K; ++r) {
@@ -1786,6 +1795,9 @@ __device__ __forceinline__ void seed_fast_items(const DevConfig& c, const Arena&
     const uint32_t total_items = static_cast<uint32_t>(
         min(a.counters[kItemTotal], static_cast<unsigned long long>(a.max_items)));
     unsigned long long* fetch = &a.counters[pass ? kItemFetch2 : kItemFetch];
+    // lane 0: this warp's doublet and triplet counts, added to the batch's
+    // counters once per item instead of once per middle
+    uint32_t agg_mb = 0, agg_mt = 0, agg_trip = 0;
 
     for (;;) {
         if (threadIdx.x == 0) {
@@ -1872,9 +1884,18 @@ __device__ __forceinline__ void seed_fast_items(const DevConfig& c, const Arena&
             const MiddleResult r = process_middle<kNbShared, SCORE, VAR, 512, 1024, 216, 128, GATE>(
                 c, a, nb, gm, true, nb_minr, nb_maxr, e, ws);
             if (lane == 0) {
-                if (r.status) push_overflow(a, gm);
-                else count_middle(a, r);
+                if (r.status) {
+                    push_overflow(a, gm);
+                } else {
+                    agg_mb += r.n_mb;
+                    agg_mt += r.n_mt;
+                    agg_trip += r.n_trip;
+                }
             }
+        }
+        if (lane == 0) {
+            count_middle(a, MiddleResult{agg_mb, agg_mt, agg_trip, 0});
+            agg_mb = agg_mt = agg_trip = 0;
         }
         __syncthreads();
     }
