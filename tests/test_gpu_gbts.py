@@ -221,3 +221,45 @@ def test_gbts_chains_longer_than_the_automaton():
         b = lay[got["bottom"][part[got["bottom"]] == k]]
         assert len(b) > 0
         assert b.min() == (8 if k % 2 == 0 else 0), (k, b.min())
+
+
+def _bundle_event(n=600, n_long=30, seed=11):
+    """Four barrel layers 30 mm apart and a bundle of straight tracks 5 mrad
+    wide in phi: 600 tracks cross the first two layers, 30 of them all four.
+    Every outer node of layer 1 pairs with the inner nodes of each 128-node
+    chunk of layer 0, so a quarter of a work item holds 150-160 outer nodes
+    with edges: more than the edge walk's 128-record stage, which sends those
+    units through the two-walk fallback (count, then write)."""
+    radii = np.array([50.0, 80.0, 110.0, 140.0])
+    layers = np.zeros(len(radii), gbts.LAYER_DTYPE)
+    for i in range(len(radii)):
+        layers[i] = (0, i, 1, -5.0, 10.0)          # one eta bin per layer
+    pairs = np.array([(0, 1), (1, 2), (2, 3)], np.uint32)
+    geoid = np.zeros(len(radii), [("barcode", np.uint64), ("layer", np.int16)])
+    geoid["barcode"] = np.arange(1, len(radii) + 1, dtype=np.uint64) << np.uint64(52)
+    geoid["layer"] = np.arange(len(radii))
+    rng = np.random.default_rng(seed)
+    phi = rng.uniform(0.500, 0.505, n)
+    tau = rng.uniform(0.40, 0.42, n)
+    z0 = rng.uniform(-2.0, 2.0, n)
+    pts, lay = [], []
+    for k in range(n):
+        for i in range(len(radii) if k < n_long else 2):
+            r = radii[i]
+            pts.append((r * np.cos(phi[k]), r * np.sin(phi[k]), z0[k] + tau[k] * r))
+            lay.append(i)
+    g = np.asarray(pts, np.float32)
+    m = len(g)
+    ev = {"measurement_index_1": np.arange(m, dtype=np.uint32),
+          "measurement_index_2": np.full(m, 0xFFFFFFFF, np.uint32), "global": g,
+          "z_variance": np.zeros(m, np.float32), "radius_variance": np.zeros(m, np.float32)}
+    link = (np.asarray(lay, np.uint64) + np.uint64(1)) << np.uint64(52)
+    return ev, link, np.zeros(m, np.float32), layers, pairs, geoid
+
+
+def test_gbts_dense_bundle_past_the_edge_record_stage():
+    ev, link, dia, layers, pairs, geoid = _bundle_event()
+    cfg = gbts.config_default()
+    cfg.max_edges_factor = 400      # every edge of the bundle is kept
+    got, ctr = _compare(ev, link, dia, layers, pairs, geoid, cfg=cfg)
+    assert ctr["edges"] > 90000 and ctr["connections"] > 0 and ctr["seeds"] > 0
