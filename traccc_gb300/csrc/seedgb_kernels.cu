@@ -856,7 +856,9 @@ struct MiddleResult {
 };
 
 // Append the positions passing the window cuts of one role to q (in order of
-// the flattened per-bin ranges).  Two candidates per lane per iteration.
+// the flattened per-bin ranges).  One candidate per lane per iteration: two
+// or four in flight per lane measured 8 % and 25 % slower over the whole
+// seeding kernel (code size and registers of the fused routine).
 template <bool TOP, int MODE>
 __device__ __forceinline__ uint32_t scan_runs(const DevConfig& c, const NbViewT<MODE>& nb,
                                               const float4 M, const uint32_t* bnd,
@@ -868,38 +870,27 @@ __device__ __forceinline__ uint32_t scan_runs(const DevConfig& c, const NbViewT<
     // a lane's flat indices only rise: its run, the flat index where that
     // run ends and the run's position offset stay in registers and advance
     // at run boundaries only
-    uint32_t run[2] = {0u, 0u}, end[2], off[2];
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-        end[h] = pre[1];
-        off[h] = bnd[TOP ? 2 : 0];  // pre[0] == 0
-    }
-    for (uint32_t base = 0; base < total; base += 64) {
-        bool ok[2] = {false, false};
-        uint32_t p[2] = {0, 0};
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const uint32_t f = base + 32 * h + lane;
-            if (f < total) {
-                while (f >= end[h]) {
-                    const uint32_t s = ++run[h];
-                    end[h] = pre[s + 1];
-                    off[h] = bnd[4 * s + (TOP ? 2 : 0)] - pre[s];
-                }
-                p[h] = off[h] + f;
-                const float4 o = nb.staged[p[h]];
-                ok[h] = TOP ? window_top(c, M, o) : window_bottom(c, M, o);
+    uint32_t run = 0u, end = pre[1], off = bnd[TOP ? 2 : 0];  // pre[0] == 0
+    for (uint32_t base = 0; base < total; base += 32) {
+        const uint32_t f = base + lane;
+        bool ok = false;
+        uint32_t p = 0;
+        if (f < total) {
+            while (f >= end) {
+                const uint32_t s = ++run;
+                end = pre[s + 1];
+                off = bnd[4 * s + (TOP ? 2 : 0)] - pre[s];
             }
+            p = off + f;
+            const float4 o = nb.staged[p];
+            ok = TOP ? window_top(c, M, o) : window_bottom(c, M, o);
         }
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const uint32_t mask = __ballot_sync(0xffffffffu, ok[h]);
-            if (ok[h]) {
-                const uint32_t k = nq + __popc(mask & lt);
-                if (k < cap) q[k] = static_cast<uint16_t>(p[h]);
-            }
-            nq += __popc(mask);
+        const uint32_t mask = __ballot_sync(0xffffffffu, ok);
+        if (ok) {
+            const uint32_t k = nq + __popc(mask & lt);
+            if (k < cap) q[k] = static_cast<uint16_t>(p);
         }
+        nq += __popc(mask);
     }
     return nq;
 }
