@@ -424,13 +424,13 @@ seedgb_status seedgb_seeding_get_tune(seedgb_seeding* h, seedgb_tune* t);
 
 /* The autotuner (no counterpart in the reference): for the batch `events`
  * (device views; seeds into `outs`), sets each candidate shape (NULL: the
- * default grid of 3 x 4 x 4 x 2 shapes -- warps {8, 12, 16}, middles per item
- * {64, 256, 384, 1024}, neighbourhood {1536, 2048, 2560, 3072}, CTAs per SM
+ * default grid of 3 x 5 x 4 x 2 shapes -- warps {8, 12, 16}, middles per item
+ * {64, 256, 384, 512, 1024}, neighbourhood {1536, 2048, 2560, 3072}, CTAs per SM
  * {1, 2}), captures the graph for the batch and times `reps` launches with
  * CUDA events on `stream` (median, after one warm-up launch).  Shapes that do
  * not fit in shared memory, or that are clamped to a shape already measured,
  * are skipped (times_ms[i] = -1; times_ms may be NULL, else n_candidates --
- * or 96 for the default grid -- entries).  Leaves the fastest shape set (and
+ * or 120 for the default grid -- entries).  Leaves the fastest shape set (and
  * in *best) with the graph captured for the batch.  Every measured launch
  * must end with status OK.  Synchronises `stream`. */
 seedgb_status seedgb_seeding_autotune(seedgb_seeding* h, const seedgb_spacepoint_view* events,

@@ -45,7 +45,7 @@ def test_bucket_and_table(tmp_path):
     assert autotune.lookup(t, 6000) == (8, 64, 2048, 1)
     assert autotune.lookup(t, 100000) == (6, 128, 2560, 1)
     assert autotune.lookup(t, 200) is None
-    assert len(autotune.candidates()) == 3 * 4 * 4 * 2
+    assert len(autotune.candidates()) == 3 * 5 * 4 * 2
 
 
 @pytest.mark.gpu

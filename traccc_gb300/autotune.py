@@ -31,7 +31,7 @@ from . import seeding
 
 # 16 warps: as many as fit in shared memory with the neighbourhood capacity
 WARPS = (8, 12, 16)
-MIDDLES = (64, 256, 384, 1024)
+MIDDLES = (64, 256, 384, 512, 1024)
 NEIGHBOURHOOD = (1536, 2048, 2560, 3072)
 CTAS = (1, 2)
 

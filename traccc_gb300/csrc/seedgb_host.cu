@@ -207,7 +207,7 @@ seedgb_status seedgb_seeding_autotune(seedgb_seeding* h, const seedgb_spacepoint
         grid.assign(candidates, candidates + n_candidates);
     } else {
         for (int w : {8, 12, 16})
-            for (int m : {64, 256, 384, 1024})
+            for (int m : {64, 256, 384, 512, 1024})
                 for (int nb : {1536, 2048, 2560, 3072})
                     for (int c : {1, 2}) grid.push_back(seedgb_tune{w, m, nb, c});
     }

@@ -621,7 +621,7 @@ class TripletSeedingAlgorithm:
         ev = (_SpacepointView * n)(*[e.view() for e in events])
         bufs = (_SeedBuffer * n)(*[o.buf() for o in outs])
         shapes = list(candidates) if candidates is not None else None
-        nc = len(shapes) if shapes is not None else 3 * 4 * 4 * 2  # the library's default grid
+        nc = len(shapes) if shapes is not None else 3 * 5 * 4 * 2  # the library's default grid
         cand = (Tune * nc)(*[Tune(*sh) for sh in shapes]) if shapes is not None else None
         times = (C.c_float * nc)()
         best = Tune()
@@ -629,7 +629,7 @@ class TripletSeedingAlgorithm:
                                              reps, C.byref(best), times, _stream_ptr(stream)),
                "seedgb_seeding_autotune")
         if shapes is None:
-            shapes = [(w, m, nb, c) for w in (8, 12, 16) for m in (64, 256, 384, 1024)
+            shapes = [(w, m, nb, c) for w in (8, 12, 16) for m in (64, 256, 384, 512, 1024)
                       for nb in (1536, 2048, 2560, 3072) for c in (1, 2)]
         return best.astuple(), [(tuple(sh), (float(t) if t >= 0 else None))
                                 for sh, t in zip(shapes, times)]
