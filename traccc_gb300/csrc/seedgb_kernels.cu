@@ -1380,11 +1380,11 @@ __device__ MiddleResult process_middle(const DevConfig& c, const Arena& a,
     //    buckets and queues those inside its exact cot window (q0, with the
     //    doublet's lin_circle), one entry per lane per step; stage 1 runs on
     //    32 queued candidates at a time, stage 2 on 32 stage-1 survivors at a
-    //    time, so both run with full lanes across doublets and chunks.  The
-    //    stage-1 queue is a ring of 64 entries (head h1, count n1, at most 63
-    //    held), so the survivors that stage 2 leaves stay in place.
+    //    time, so both run with full lanes across doublets and chunks.  Both
+    //    queues are rings of 64 entries (heads h0 / h1, counts n0 / n1, at
+    //    most 63 held), so what a stage leaves stays in place.
     const float sig2 = c.sigmaScattering * c.sigmaScattering;
-    uint32_t n_ct = 0, n0 = 0, n1 = 0, h1 = 0;
+    uint32_t n_ct = 0, n0 = 0, n1 = 0, h1 = 0, h0 = 0;
     uint32_t c0 = 0, it = 0, maxc = 0;
     bool have_chunk = false;
     LinCircle lbm;
@@ -1462,7 +1462,7 @@ __device__ MiddleResult process_middle(const DevConfig& c, const Arena& a,
                         e.er = lbm.er;
                         e.u = lbm.u;
                         e.v = lbm.v;
-                        ws.q.q0[n0 + __popc(mask & lt)] = e;
+                        ws.q.q0[(h0 + n0 + __popc(mask & lt)) & 63u] = e;
                     }
                     n0 += __popc(mask);
                 }
@@ -1483,7 +1483,7 @@ __device__ MiddleResult process_middle(const DevConfig& c, const Arena& a,
                 bool ok = false;
                 Stage1Cand s1;
                 if (i < k1) {
-                    const Stage0Cand e = ws.q.q0[i];
+                    const Stage0Cand e = ws.q.q0[(h0 + i) & 63u];
                     LinCircle lb;
                     lb.cot = e.cot;
                     lb.idr = e.idr;
@@ -1511,15 +1511,8 @@ __device__ MiddleResult process_middle(const DevConfig& c, const Arena& a,
                 if (ok) ws.q.q1[(h1 + n1 + __popc(mask & lt)) & 63u] = s1;
                 n1 += __popc(mask);
             }
-            // move the unprocessed tail of q0 (< 64 entries) to the front
-            const uint32_t rest = n0 - k1;
-            Stage0Cand t0, t1;
-            if (lane < rest) t0 = ws.q.q0[k1 + lane];
-            if (lane + 32 < rest) t1 = ws.q.q0[k1 + lane + 32];
-            __syncwarp();
-            if (lane < rest) ws.q.q0[lane] = t0;
-            if (lane + 32 < rest) ws.q.q0[lane + 32] = t1;
-            n0 = rest;
+            h0 = (h0 + k1) & 63u;
+            n0 -= k1;
             __syncwarp();
         }
         while (n1 >= 32 || (!more && n0 == 0 && n1 > 0)) {
@@ -1895,8 +1888,10 @@ __device__ __forceinline__ void seed_fast_items(const DevConfig& c, const Arena&
 // GATE: the learned middle gate inside the plain routine (pass 0 with a filter
 // that only gates middles); a separate instantiation, so that the plain
 // kernel's registers and code stay those of plain seeding.
+// One CTA per SM (shared memory holds one): the explicit minimum keeps ptxas
+// from aiming at two CTAs' 64 registers per thread, which spills this routine.
 template <bool SCORE, bool GATE = false>
-__global__ void __launch_bounds__(SCORE ? kScoreWarps * 32 : 512)
+__global__ void __launch_bounds__(SCORE ? kScoreWarps * 32 : 512, 1)
     k_seed_fast(DevConfig c, Arena a, uint32_t mpi, uint32_t nb_cap, uint32_t pass) {
     if (a.counters[kAnyVariance] != 0) seed_fast_items<SCORE, true, GATE>(c, a, mpi, nb_cap, pass);
     else seed_fast_items<SCORE, false, GATE>(c, a, mpi, nb_cap, pass);
